@@ -1,0 +1,219 @@
+/* pgx.h -- C ABI of libpulsar_gb300.so: the GRAPE fidelity-and-gradient hot
+ * path of Pulsar.jl, GB300-native (sm_103a).
+ *
+ * Conventions
+ *   - Every function returns an int status (PGX_OK = 0); no exception crosses
+ *     the boundary.  pgx_last_error() gives the detail of the last failure on
+ *     a context.
+ *   - Complex matrices are column-major with interleaved (re, im) doubles:
+ *     exactly the memory of a Julia Matrix{ComplexF64}.  Element (r, c) of a
+ *     D x D matrix sits at doubles [2*(r + D*c)], [2*(r + D*c) + 1].
+ *   - Control amplitudes u and gradients G are [n_controls x n_slices]
+ *     column-major (u[j + n_controls*k]): the memory of the reference's
+ *     OptimizationResult.controls / ControlSequence.controls.
+ *   - A context is externally synchronised: calls on one context (and on the
+ *     problems it owns) must not overlap.  Distinct contexts are independent.
+ *
+ * Replaced reference interfaces (paths inside the Pulsar.jl project) are cited
+ * beside each entry point.  The reference has no FFI of its own; its plugin
+ * points are Julia dispatch hooks (GRAPEConfig.backend, the physics-hook
+ * grape_optimize overload, EnsembleObjective.batched_eval, MRControl.backend).
+ */
+#ifndef PGX_H
+#define PGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGX_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  PGX_OK = 0,
+  PGX_ERR_INVALID = 1,     /* bad argument / descriptor (reference: ArgumentError) */
+  PGX_ERR_DIMS = 2,        /* inconsistent sizes (reference: DimensionMismatch)    */
+  PGX_ERR_NOMEM = 3,       /* device allocation failed                              */
+  PGX_ERR_BUDGET = 4,      /* admission refused: HBM budget of the context exceeded */
+  PGX_ERR_CUDA = 5,        /* CUDA runtime error                                    */
+  PGX_ERR_UNSUPPORTED = 6, /* valid request this build does not implement           */
+  PGX_ERR_TIMEOUT = 7,     /* a bounded device wait gave up                         */
+  PGX_ERR_CANCELLED = 8,   /* job cancelled                                          */
+  PGX_ERR_STATE = 9,       /* call not valid in the object's current state          */
+  PGX_ERR_NONFINITE = 10   /* non-finite input or result                            */
+};
+
+/* ---- problem description ----------------------------------------------- */
+enum { PGX_GEN_HERMITIAN = 0,   /* U_k = exp(-i H_k dt_k)   (Propagators.jl:659-674)   */
+       PGX_GEN_LIOUVILLIAN = 1  /* U_k = exp(L_k dt_k)      (GRAPELindblad.jl:146-153) */ };
+enum { PGX_TARGET_GATE = 0,     /* z = Tr(T' U_total)/D    (Objectives.jl:239-246)    */
+       PGX_TARGET_STATES = 1    /* z_s = <t_s|U_total i_s>  (Objectives.jl:221)        */ };
+enum { PGX_FID_SQUARE = 0,      /* f = |z|^2 (gate: the :normalized fidelity)          */
+       PGX_FID_REAL = 1,        /* f = Re z                                            */
+       PGX_FID_MODULUS = 2      /* f = |z|                                             */ };
+enum { PGX_GRAD_REF_GRAPE = 0,  /* first-order formula of Gradients.jl:254-291,357-399 */
+       PGX_GRAD_REF_MR = 1,     /* first-order formula of GRAPEState.jl:220-230 /
+                                   GRAPELindblad.jl:183-195                            */
+       PGX_GRAD_EXACT = 2       /* exact Frechet-derivative gradient                    */ };
+enum { PGX_PREC_FP64 = 0,       /* plain FP64 everywhere                                */
+       PGX_PREC_MIXED = 1       /* FP32 bulk, FP64 norm/overlap/chain (see design doc)  */ };
+
+/* A problem is an ensemble of members.  Member m evolves under
+ *   G_m(u_k) = drifts[member_drift[m]] + member_offset[m] * offset_op
+ *              + member_scale[m] * sum_j u[j,k] controls[j]
+ * and F = sum_m member_weight[m] * sum_s f(z_ms).  One member with scale 1 is
+ * a reference QuantumSystem; members = drifts x pwr_levels is an MRControl
+ * ensemble (GRAPEState.jl:145-146); offsets x B1 scales is a broadband
+ * ensemble without replicating the drift (SystemBuilder.jl:49-87).        */
+typedef struct pgx_problem_desc {
+  uint32_t struct_size;        /* sizeof(pgx_problem_desc)                       */
+  int32_t dim;                 /* D <= 64 (Hilbert d, or N*N for Liouvillians)    */
+  int32_t n_controls;          /* >= 1                                            */
+  int32_t n_slices;            /* >= 1                                            */
+  int32_t generator;           /* PGX_GEN_*                                       */
+  int32_t target;              /* PGX_TARGET_*                                    */
+  int32_t fidelity;            /* PGX_FID_*                                       */
+  int32_t grad_mode;           /* PGX_GRAD_*                                      */
+  int32_t precision;           /* PGX_PREC_*                                      */
+  int32_t n_drifts;            /* >= 1                                            */
+  int32_t n_members;           /* >= 1                                            */
+  int32_t n_pairs;             /* state pairs (PGX_TARGET_STATES), else 0         */
+  const double* dt;            /* [n_slices] slice durations                      */
+  const double* drifts;        /* [n_drifts][D*D] complex                         */
+  const double* controls;      /* [n_controls][D*D] complex                       */
+  const double* offset_op;     /* [D*D] complex, or NULL                          */
+  const int32_t* member_drift; /* [n_members] or NULL (all 0)                     */
+  const double* member_scale;  /* [n_members] or NULL (all 1)                     */
+  const double* member_offset; /* [n_members] or NULL (all 0)                     */
+  const double* member_weight; /* [n_members] or NULL (1/(n_members*max(n_pairs,1))) */
+  const double* target_op;     /* gate: [D*D] complex                             */
+  const double* states_init;   /* states: [n_pairs][D] complex (used for F)       */
+  const double* states_target; /* states: [n_pairs][D] complex                    */
+  const double* grad_states_init; /* states: initial states for the gradient, or
+                                     NULL (= states_init).  grape_optimize passes
+                                     the target here (Gradients.jl:153-157).      */
+} pgx_problem_desc;
+
+typedef struct pgx_eval_stats {
+  double ms_device;            /* device time of the call (CUDA events)           */
+  double ms_host;              /* wall time of the call                           */
+  int64_t units;               /* member-slice units processed                    */
+  int32_t n_launches;          /* kernels launched by the call                    */
+  int32_t max_taylor_degree;   /* largest degree chosen (0 = not recorded)        */
+} pgx_eval_stats;
+
+typedef struct pgx_ctx pgx_ctx;
+typedef struct pgx_problem pgx_problem;
+
+/* ---- library / context ------------------------------------------------- */
+int pgx_abi_version(void);
+const char* pgx_status_string(int status);
+
+/* Context on one device with an HBM budget (0 = no limit).  Owns one stream. */
+int pgx_ctx_create(int device, uint64_t hbm_budget_bytes, pgx_ctx** out);
+int pgx_ctx_destroy(pgx_ctx* ctx);
+int pgx_last_error(const pgx_ctx* ctx, char* buf, size_t len);
+int pgx_ctx_hbm_used(const pgx_ctx* ctx, uint64_t* bytes);
+/* The context's cudaStream_t (as void*), for callers that order their own work. */
+int pgx_ctx_stream(pgx_ctx* ctx, void** stream);
+/* Device-time stopwatch on the context stream (CUDA events). */
+int pgx_ctx_timer_start(pgx_ctx* ctx);
+int pgx_ctx_timer_stop(pgx_ctx* ctx, double* ms);
+int pgx_ctx_synchronize(pgx_ctx* ctx);
+/* Kernels launched on this context since creation (monotone counter). */
+int pgx_ctx_launch_count(const pgx_ctx* ctx, int64_t* count);
+/* Per-stage device timing.  While enabled, every evaluation records CUDA
+ * events around its stages (PGX_STAGE_*).  pgx_ctx_stage_times waits for the
+ * recorded work, writes the summed milliseconds of each stage into
+ * ms[PGX_N_STAGES], the number of recorded evaluations into *count, and
+ * clears the record.                                                        */
+enum { PGX_STAGE_EXPM = 0, PGX_STAGE_CHAIN_FWD = 1, PGX_STAGE_CHAIN_BWD = 2, PGX_STAGE_GRAD = 3,
+       PGX_STAGE_REDUCE = 4, PGX_N_STAGES = 5 };
+int pgx_ctx_set_stage_timing(pgx_ctx* ctx, int enabled);
+int pgx_ctx_stage_times(pgx_ctx* ctx, double* ms, int32_t* count);
+/* Measured peak of this device's FP64 FMA pipe (GFLOP/s), from a timed
+ * dependent-free DFMA loop kernel; the roofline denominator of the FP64 path. */
+int pgx_ctx_measure_fp64_peak(pgx_ctx* ctx, double* gflops);
+
+/* ---- problems ---------------------------------------------------------- */
+/* HBM bytes pgx_problem_create would hold for desc (admission control).    */
+int pgx_problem_footprint(const pgx_problem_desc* desc, uint64_t* bytes);
+/* Validates desc (Hermiticity of H for PGX_GEN_HERMITIAN, 1e-10 as
+ * QuantumSystem.jl:318-341; unitarity of a gate target, 1e-8 as
+ * Targets.jl:131-144), copies every input to device memory and owns it.    */
+int pgx_problem_create(pgx_ctx* ctx, const pgx_problem_desc* desc, pgx_problem** out);
+int pgx_problem_destroy(pgx_problem* prob);
+
+/* ---- evaluation -------------------------------------------------------- */
+/* (F, G) at controls u, host buffers, synchronous.  G may be NULL (forward
+ * only, the line-search evaluation).  Replaces, per member and averaged:
+ *   compute_fidelity + compute_grape_gradient   (Objectives.jl:632-639,
+ *       Gradients.jl:80-163), ensemble_value_and_grad (EnsembleObjective.jl:
+ *       272-307), grape_state_kernel (GRAPEState.jl:73-250),
+ *       grape_lindblad_kernel (GRAPELindblad.jl:83-215), gradient_cuda /
+ *       batch_propagators_cuda / fidelity_cuda (CUDABackend.jl:126-373).  */
+int pgx_eval(pgx_problem* prob, const double* u, double* F, double* G, pgx_eval_stats* stats);
+/* Same on device buffers, asynchronous on the context stream.  d_G may be
+ * NULL.  d_F receives one double.                                           */
+int pgx_eval_device(pgx_problem* prob, const double* d_u, double* d_F, double* d_G);
+/* Per-member objective sum_s f(z_ms) of the last evaluation ([n_members]). */
+int pgx_member_fidelities(pgx_problem* prob, double* F_members);
+/* Total propagator U_total of one member at controls u ([D*D] complex):
+ * compute_total_propagator(compute_propagators(...)) (Propagators.jl:212-238). */
+int pgx_total_propagator(pgx_problem* prob, const double* u, int32_t member, double* U_total);
+/* Single-slice propagator exp(c dt G) of a D x D generator G ([D*D] complex in
+ * and out); the compute_propagator / _expm_neg_i hook (Propagators.jl:64-90,
+ * PropagatorRegistry.jl:138-191).                                           */
+int pgx_propagator(pgx_ctx* ctx, int32_t dim, int32_t generator, const double* gen, double dt,
+                   double* U);
+
+/* ---- optimisation ------------------------------------------------------ */
+enum { PGX_OPT_GRAPE = 0,          /* grape_optimize ascent loop (GRAPE.jl:469-643)       */
+       PGX_OPT_ENSEMBLE_LBFGS = 1, /* grape_optimize_ensemble (GRAPE.jl:1012-1230)        */
+       PGX_OPT_MR_LBFGS = 2,       /* optimcon :lbfgs (OptControl.jl:380-482,565-611)     */
+       PGX_OPT_MR_GRAPE = 3        /* optimcon :grape (OptControl.jl:486-561)             */ };
+
+typedef struct pgx_opt_desc {
+  uint32_t struct_size;
+  int32_t method;              /* PGX_OPT_*                                        */
+  int32_t max_iter;
+  int32_t adapt_step_size;     /* GRAPE only                                       */
+  int32_t lbfgs_memory;
+  int32_t reserved;
+  double convergence_tol;      /* GRAPEConfig defaults: 1e-8                       */
+  double step_size;            /* 0.01                                             */
+  double min_step_size;        /* 1e-10                                            */
+  double max_step_size;        /* 10.0                                             */
+  double gradient_norm_tol;    /* 1e-6 (MR: grad_tol 1e-7)                         */
+  double amplitude_limit;      /* ensemble L-BFGS clip, +inf = none                */
+  double l_bound, u_bound;     /* MR bounds (-1, 1)                                */
+} pgx_opt_desc;
+
+typedef struct pgx_opt_result {
+  double fidelity;             /* best fidelity (GRAPE: re-evaluated at the best controls) */
+  double total_time_s;
+  double step_size_final;
+  int32_t n_iterations;
+  int32_t converged;
+  int32_t n_fidelity_evals;
+  int32_t n_gradient_evals;
+  int32_t history_len;         /* fidelity-history entries (<= history_cap written) */
+  int32_t gnorm_history_len;   /* gradient-norm-history entries                    */
+  char reason[100];
+} pgx_opt_result;
+
+/* Runs the optimiser on the device-resident problem.  u_inout holds the
+ * initial controls and receives the best controls.  Histories (nullable,
+ * capacity history_cap) receive fidelity / gradient-norm traces as the
+ * reference's OptimizationResult does (GRAPE.jl:158-170).                   */
+int pgx_optimize(pgx_problem* prob, const pgx_opt_desc* opt, double* u_inout,
+                 double* fidelity_history, double* gnorm_history, int32_t history_cap,
+                 pgx_opt_result* result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PGX_H */

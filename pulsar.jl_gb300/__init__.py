@@ -1,0 +1,20 @@
+"""pulsar_gb300 -- GB300-native GRAPE fidelity-and-gradient hot path of Pulsar.jl.
+
+The compute lives in ``libpulsar_gb300.so`` (sm_103a CUDA kernels behind the C
+ABI of ``include/pgx.h``).  This package is the host-side mirror of the
+reference's Julia API (``api``) plus thin handles over the C ABI (``engine``).
+The directory is named ``pulsar.jl_gb300``; import it as ``pulsar_gb300``
+through ``__graft_entry__.load_package()``.
+"""
+from . import _abi
+from .engine import Context, Problem, default_context
+from .api import (
+    ControlSequence, EnsembleObjective, GRAPEConfig, LindbladMRControl, MRControl,
+    OptimizationResult, QuantumSystem, QuantumTarget, build_control_liouvillian,
+    build_drift_liouvillian, build_ensemble_from_systems, compute_fidelity,
+    compute_grape_gradient, compute_propagator, fidelity_forward, grape_lindblad_kernel,
+    grape_optimize, grape_optimize_ensemble, grape_state_kernel, mat_rho, optimcon, propagate,
+    pure_state_to_vec_rho, quantum_system, random_controls, state_target, unitary_target, vec_rho,
+)
+
+LIB_PATH = _abi.LIB_PATH

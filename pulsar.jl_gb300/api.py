@@ -1,0 +1,627 @@
+"""Pulsar.jl's GRAPE API surface, served by libpulsar_gb300.so.
+
+Names, argument meanings, defaults and error behaviour follow the reference
+(paths inside the Pulsar.jl project):
+
+  QuantumSystem / quantum_system      src/Types/QuantumSystem.jl:60-66,318-341
+  ControlSequence / random_controls   src/Types/ControlSequence.jl:37-158
+  QuantumTarget / state_target /
+  unitary_target                      src/Types/Targets.jl:37-144
+  compute_propagator                  src/Computation/Propagators.jl:64-90
+  compute_fidelity                    src/Physics/Objectives.jl:609-639
+  compute_grape_gradient              src/Physics/Gradients.jl:80-127
+  GRAPEConfig / OptimizationResult    src/Optimization/GRAPE.jl:60-211
+  grape_optimize                      src/Optimization/GRAPE.jl:469-643
+  grape_optimize_ensemble             src/Optimization/GRAPE.jl:1012-1230
+  build_ensemble_from_systems         src/Optimization/Ensemble/SystemBuilder.jl:49-87
+  MRControl / LindbladMRControl       src/Application/MR/OptControl.jl:137-259,733-885
+  grape_state_kernel                  src/Application/MR/GRAPEState.jl:73-250
+  grape_lindblad_kernel               src/Application/MR/GRAPELindblad.jl:83-215
+  fidelity_forward                    src/Application/MR/GRAPEState.jl:434-566
+  optimcon                            src/Application/MR/OptControl.jl:310-370,913-948
+  build_drift_liouvillian, build_control_liouvillian, vec_rho, mat_rho,
+  pure_state_to_vec_rho               src/Physics/Lindblad.jl:57-197
+
+Every physics evaluation runs on the GPU through the C ABI.  Argument errors
+raise ValueError (the reference's ArgumentError / DimensionMismatch).  There
+is no CPU fallback: without the library every call raises.
+
+Gradient modes: the reference's own first-order formulas are the defaults of
+the reference entry points (``grad_mode="ref_grape"`` for the GRAPE path,
+``"ref_mr"`` for the MR kernels); ``grad_mode="exact"`` gives the exact
+Frechet-derivative gradient of the same objective.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+from .engine import Context, Problem, default_context
+
+C128 = np.complex128
+
+
+# ---------------------------------------------------------------------------
+# Types
+# ---------------------------------------------------------------------------
+
+def _check_hermitian(H: np.ndarray, name: str, tol: float = 1e-10):
+    dev = float(np.max(np.abs(H - H.conj().T))) if H.size else 0.0
+    if dev > tol:
+        raise ValueError(f"{name} is not Hermitian: max|H - H'| = {dev} > tol = {tol}")
+
+
+@dataclass
+class QuantumSystem:
+    H_drift: np.ndarray
+    H_controls: list
+    metadata: dict = field(default_factory=dict)
+
+    @property
+    def dim(self) -> int:
+        return int(self.H_drift.shape[0])
+
+    @property
+    def n_controls(self) -> int:
+        return len(self.H_controls)
+
+
+def quantum_system(H_drift, H_controls, metadata=None) -> QuantumSystem:
+    """Validates Hermiticity (1e-10) and shapes (QuantumSystem.jl:318-341)."""
+    Hd = np.asarray(H_drift, C128)
+    if Hd.ndim != 2 or Hd.shape[0] != Hd.shape[1]:
+        raise ValueError("H_drift must be square")
+    _check_hermitian(Hd, "H_drift")
+    Hcs = []
+    for j, Hc in enumerate(H_controls):
+        Hc = np.asarray(Hc, C128)
+        if Hc.shape != Hd.shape:
+            raise ValueError(f"H_controls[{j}] has size {Hc.shape} but expected {Hd.shape}")
+        _check_hermitian(Hc, f"H_controls[{j}]")
+        Hcs.append(Hc)
+    return QuantumSystem(Hd, Hcs, dict(metadata or {}))
+
+
+class ControlSequence:
+    """amplitudes: [n_steps, n_controls]; .controls is the [n_c, n_t] view."""
+
+    def __init__(self, amplitudes, dt: float, n_steps: Optional[int] = None):
+        a = np.asarray(amplitudes, np.float64)
+        if dt < 0:
+            raise ValueError(f"dt must be non-negative, got {dt}")
+        if n_steps is not None and a.shape[0] != n_steps:
+            raise ValueError(f"amplitudes has {a.shape[0]} rows but n_steps = {n_steps}")
+        self.amplitudes = a
+        self.dt = float(dt)
+
+    @classmethod
+    def from_controls(cls, controls, dt: float, total_time: Optional[float] = None,
+                      n_timesteps: Optional[int] = None) -> "ControlSequence":
+        """The 4-argument constructor of ControlSequence.jl:77-89."""
+        c = np.asarray(controls, np.float64)
+        if n_timesteps is not None and c.shape[1] != n_timesteps:
+            raise ValueError(f"controls has {c.shape[1]} columns but n_timesteps = {n_timesteps}")
+        return cls(np.ascontiguousarray(c.T), dt)
+
+    @property
+    def controls(self) -> np.ndarray:
+        return self.amplitudes.T
+
+    @property
+    def n_steps(self) -> int:
+        return self.amplitudes.shape[0]
+
+    n_timesteps = n_steps
+
+    @property
+    def total_time(self) -> float:
+        return self.dt * self.n_steps
+
+
+def random_controls(system: QuantumSystem, total_time: float, n_timesteps: int, amplitude=1.0,
+                    rng: Optional[np.random.Generator] = None) -> ControlSequence:
+    """U(-amplitude, amplitude) amplitudes (ControlSequence.jl:142-158); the
+    stream is numpy's, not Julia's MersenneTwister."""
+    if total_time <= 0:
+        raise ValueError(f"total_time must be positive, got {total_time}")
+    if n_timesteps <= 0:
+        raise ValueError(f"n_timesteps must be positive, got {n_timesteps}")
+    rng = rng or np.random.default_rng()
+    a = amplitude * (2 * rng.random((n_timesteps, system.n_controls)) - 1)
+    return ControlSequence(a, total_time / n_timesteps)
+
+
+@dataclass
+class QuantumTarget:
+    type: str
+    target_state: Optional[np.ndarray] = None
+    target_unitary: Optional[np.ndarray] = None
+    initial_state: Optional[np.ndarray] = None
+
+    @property
+    def dim(self) -> int:
+        return int((self.target_unitary if self.type == "unitary" else self.target_state).shape[0])
+
+
+def state_target(state, psi_init=None) -> QuantumTarget:
+    """Targets.jl:77-107.  Without psi_init the objective is the fixed-point
+    overlap |<t|U|t>|^2 (Objectives.jl:620-623)."""
+    psi = np.asarray(state, C128).ravel()
+    if psi.size == 0:
+        raise ValueError("Target state vector must be non-empty")
+    if not np.all(np.isfinite(psi)):
+        raise ValueError("Target state contains NaN or Inf values")
+    if np.linalg.norm(psi) < np.finfo(float).eps:
+        raise ValueError("Target state has zero norm")
+    pi = None
+    if psi_init is not None:
+        pi = np.asarray(psi_init, C128).ravel()
+        if pi.size != psi.size:
+            raise ValueError(f"psi_init has length {pi.size}; expected {psi.size}")
+        if not np.all(np.isfinite(pi)):
+            raise ValueError("psi_init contains NaN or Inf values")
+        if np.linalg.norm(pi) < np.finfo(float).eps:
+            raise ValueError("psi_init has zero norm")
+    return QuantumTarget("state", target_state=psi, initial_state=pi)
+
+
+def unitary_target(U) -> QuantumTarget:
+    """Targets.jl:131-144: square and ||U'U - I|| / d <= 1e-8."""
+    U = np.asarray(U, C128)
+    if U.ndim != 2 or U.shape[0] != U.shape[1]:
+        raise ValueError(f"Target unitary must be square, got {U.shape}")
+    dev = np.linalg.norm(U.conj().T @ U - np.eye(U.shape[0])) / U.shape[0]
+    if dev > 1e-8:
+        raise ValueError(f"Target matrix is not unitary: ||U'U - I|| / dim = {dev} > 1e-8")
+    return QuantumTarget("unitary", target_unitary=U)
+
+
+@dataclass
+class GRAPEConfig:
+    """GRAPE.jl:60-127 (defaults and validation kept)."""
+    max_iter: int = 1000
+    convergence_tol: float = 1e-8
+    step_size: float = 0.01
+    adapt_step_size: bool = True
+    min_step_size: float = 1e-10
+    max_step_size: float = 10.0
+    gradient_norm_tol: float = 1e-6
+    verbose: bool = False
+    print_interval: int = 100
+    callback: Optional[Callable] = None
+    use_threads: bool = True
+    backend: str = "gpu"
+    grad_mode: str = "ref_grape"
+    precision: str = "fp64"
+
+    def __post_init__(self):
+        if self.max_iter <= 0:
+            raise ValueError("max_iter must be positive")
+        if self.convergence_tol <= 0:
+            raise ValueError("convergence_tol must be positive")
+        if self.step_size <= 0:
+            raise ValueError("step_size must be positive")
+        if self.min_step_size <= 0:
+            raise ValueError("min_step_size must be positive")
+        if self.max_step_size < self.step_size:
+            raise ValueError("max_step_size must be >= step_size")
+        if self.min_step_size > self.step_size:
+            raise ValueError("min_step_size must be <= step_size")
+        if self.gradient_norm_tol <= 0:
+            raise ValueError("gradient_norm_tol must be positive")
+        if self.print_interval <= 0:
+            raise ValueError("print_interval must be positive")
+        if self.backend not in ("auto", "cpu", "gpu", "hybrid"):
+            raise ValueError("backend must be :auto, :cpu, :gpu, or :hybrid")
+
+
+@dataclass
+class OptimizationResult:
+    """GRAPE.jl:158-170."""
+    controls: np.ndarray
+    fidelity: float
+    fidelity_history: list
+    gradient_norm_history: list
+    n_iterations: int
+    converged: bool
+    termination_reason: str
+    total_time: float
+    n_fidelity_evaluations: int
+    n_gradient_evaluations: int
+    metadata: dict = field(default_factory=dict)
+
+
+# ---------------------------------------------------------------------------
+# Problem construction from reference objects
+# ---------------------------------------------------------------------------
+
+def _dt_vec(dt, n_t: int) -> np.ndarray:
+    return np.broadcast_to(np.asarray(dt, np.float64), (n_t,)).copy()
+
+
+def _normalise(v):
+    v = np.asarray(v, C128)
+    n = np.linalg.norm(v)
+    if n < np.finfo(float).eps:
+        raise ValueError("state has zero norm")
+    return v / n
+
+
+def _system_problem(system: QuantumSystem, target: QuantumTarget, n_t: int, dt, *,
+                    grad_mode: str, precision: str = "fp64", legacy_state_gradient: bool = False,
+                    normalise_states: bool = False, ctx: Optional[Context] = None) -> Problem:
+    kw = dict(ctx=ctx, grad_mode=grad_mode, precision=precision)
+    if target.type == "unitary":
+        return Problem(system.H_drift, np.stack(system.H_controls), _dt_vec(dt, n_t),
+                       target="gate", fidelity="square", target_op=target.target_unitary, **kw)
+    if target.type != "state":
+        raise ValueError(f'Unknown target type "{target.type}"; expected "unitary" or "state"')
+    psi_t = target.target_state
+    psi_i = psi_t if target.initial_state is None else target.initial_state
+    grad_init = psi_t if legacy_state_gradient else psi_i
+    if normalise_states:
+        psi_t, psi_i, grad_init = _normalise(psi_t), _normalise(psi_i), _normalise(grad_init)
+    return Problem(system.H_drift, np.stack(system.H_controls), _dt_vec(dt, n_t), target="states",
+                   fidelity="square", states_init=psi_i, states_target=psi_t,
+                   grad_states_init=grad_init, **kw)
+
+
+# ---------------------------------------------------------------------------
+# Computation / physics entry points
+# ---------------------------------------------------------------------------
+
+def compute_propagator(H, dt: float, ctx: Optional[Context] = None) -> np.ndarray:
+    """exp(-i H dt) on the device; identity for dt = 0 (Propagators.jl:64-90)."""
+    H = np.asarray(H, C128)
+    if H.ndim != 2 or H.shape[0] != H.shape[1]:
+        raise ValueError(f"H must be square, got {H.shape}")
+    if dt == 0.0:
+        return np.eye(H.shape[0], dtype=C128)
+    _check_hermitian(H, "H")
+    return (ctx or default_context()).propagator(H, dt, "hermitian")
+
+
+def propagate(system: QuantumSystem, controls: ControlSequence) -> np.ndarray:
+    """U_total (Propagators.jl:566-571)."""
+    prob = Problem(system.H_drift, np.stack(system.H_controls),
+                   _dt_vec(controls.dt, controls.n_steps), target="gate",
+                   target_op=np.eye(system.dim), grad_mode="ref_grape")
+    try:
+        return prob.total_propagator(controls.controls, 0)
+    finally:
+        prob.close()
+
+
+def compute_fidelity(system: QuantumSystem, controls: ControlSequence, target: QuantumTarget) -> float:
+    """Objectives.jl:632-639: gate |Tr(U_t'U)/d|^2, state |<t|U i>|^2 with
+    i = initial_state or target_state."""
+    if controls.amplitudes.shape[1] != system.n_controls:
+        raise ValueError("controls and system disagree on the number of control fields")
+    prob = _system_problem(system, target, controls.n_steps, controls.dt, grad_mode="ref_grape")
+    try:
+        return prob.eval(controls.controls, want_grad=False)[0]
+    finally:
+        prob.close()
+
+
+def compute_grape_gradient(system: QuantumSystem, controls: ControlSequence, target: QuantumTarget,
+                           grad_mode: str = "ref_grape") -> np.ndarray:
+    """G[n_c, n_t] (Gradients.jl:80-127): honours initial_state; state vectors
+    are normalised as in Gradients.jl:377-381."""
+    prob = _system_problem(system, target, controls.n_steps, controls.dt, grad_mode=grad_mode,
+                           normalise_states=True)
+    try:
+        return prob.eval(controls.controls)[1]
+    finally:
+        prob.close()
+
+
+# ---------------------------------------------------------------------------
+# Optimisation
+# ---------------------------------------------------------------------------
+
+def _result(o, algorithm: str, extra: Optional[dict] = None) -> OptimizationResult:
+    md = {"algorithm": algorithm, "step_size_final": o.step_size_final}
+    md.update(extra or {})
+    return OptimizationResult(o.controls, o.fidelity, o.fidelity_history, o.gradient_norm_history,
+                              o.n_iterations, o.converged, o.termination_reason, o.total_time,
+                              o.n_fidelity_evaluations, o.n_gradient_evaluations, md)
+
+
+def grape_optimize(system: QuantumSystem, target: QuantumTarget, controls_init: ControlSequence,
+                   config: GRAPEConfig = GRAPEConfig()) -> OptimizationResult:
+    """GRAPE ascent (GRAPE.jl:469-643) on the device-resident problem.  As in
+    the reference, F uses initial_state while the in-loop gradient
+    (compute_grape_gradient_with!, Gradients.jl:153-157) uses target_state on
+    both sides."""
+    n_c, n_t = controls_init.controls.shape
+    if n_c != system.n_controls:
+        raise ValueError(f"controls_init.controls size {(n_c, n_t)} does not match system")
+    prob = _system_problem(system, target, n_t, controls_init.dt, grad_mode=config.grad_mode,
+                           precision=config.precision, legacy_state_gradient=True)
+    try:
+        o = prob.optimize(controls_init.controls, "grape", max_iter=config.max_iter,
+                          convergence_tol=config.convergence_tol, step_size=config.step_size,
+                          adapt_step_size=config.adapt_step_size, min_step_size=config.min_step_size,
+                          max_step_size=config.max_step_size,
+                          gradient_norm_tol=config.gradient_norm_tol)
+    finally:
+        prob.close()
+    return _result(o, "GRAPE", {"n_controls": n_c, "n_timesteps": n_t, "dt": controls_init.dt,
+                                "total_time": controls_init.total_time})
+
+
+def _systems_as_members(systems: Sequence[QuantumSystem]):
+    """Ensemble of systems -> (drifts, controls, member_scale).  Members must
+    share their control Hamiltonians up to one real scale per member (B1)."""
+    ref = np.stack(systems[0].H_controls)
+    scales = []
+    for i, s in enumerate(systems):
+        Hc = np.stack(s.H_controls)
+        if Hc.shape != ref.shape:
+            raise ValueError(f"system {i} has a different control set")
+        den = np.vdot(ref.ravel(), ref.ravel()).real
+        sc = np.vdot(ref.ravel(), Hc.ravel()).real / den if den > 0 else 1.0
+        if np.max(np.abs(Hc - sc * ref)) > 1e-12 * max(1.0, np.max(np.abs(Hc))):
+            raise ValueError("systems must share control Hamiltonians up to a common real scale")
+        scales.append(sc)
+    drifts = np.stack([s.H_drift for s in systems])
+    return drifts, ref, np.asarray(scales)
+
+
+class EnsembleObjective:
+    """Mean-aggregated ensemble objective served by one batched GPU
+    evaluation: the ``batched_eval`` plug of EnsembleObjective.jl:145-163."""
+
+    def __init__(self, problem: Problem, n_samples: int, n_c: int, n_t: int):
+        self.problem = problem
+        self.n_samples = n_samples
+        self._shape = (n_c, n_t)
+
+    def batched_eval(self, theta):
+        u = np.asarray(theta, np.float64).reshape(self._shape, order="F")
+        F, G = self.problem.eval(u)
+        return F, G.reshape(-1, order="F")
+
+    def value(self, theta) -> float:
+        u = np.asarray(theta, np.float64).reshape(self._shape, order="F")
+        return self.problem.eval(u, want_grad=False)[0]
+
+    value_and_grad = batched_eval
+
+
+def build_ensemble_from_systems(systems, target: QuantumTarget, controls: ControlSequence,
+                                aggregator: str = "mean", grad_mode: str = "ref_grape",
+                                precision: str = "fp64") -> EnsembleObjective:
+    """SystemBuilder.jl:49-87 with the :mean aggregator (per-system
+    compute_fidelity + compute_grape_gradient, averaged)."""
+    if aggregator != "mean":
+        raise ValueError("only the :mean aggregator runs batched on the device")
+    if not systems:
+        raise ValueError("systems must be non-empty")
+    drifts, ctrls, scales = _systems_as_members(systems)
+    n = len(systems)
+    n_t = controls.n_steps
+    kw = dict(member_drift=np.arange(n), member_scale=scales, member_weight=np.full(n, 1.0 / n),
+              grad_mode=grad_mode, precision=precision)
+    if target.type == "unitary":
+        prob = Problem(drifts, ctrls, _dt_vec(controls.dt, n_t), target="gate",
+                       target_op=target.target_unitary, **kw)
+    else:
+        psi_t = target.target_state
+        psi_i = psi_t if target.initial_state is None else target.initial_state
+        # compute_fidelity uses raw states; compute_grape_gradient normalises
+        prob = Problem(drifts, ctrls, _dt_vec(controls.dt, n_t), target="states",
+                       states_init=psi_i, states_target=psi_t, **kw)
+    return EnsembleObjective(prob, n, ctrls.shape[0], n_t)
+
+
+def grape_optimize_ensemble(systems, target: QuantumTarget, controls_init: ControlSequence,
+                            config: GRAPEConfig = GRAPEConfig(), lbfgs_memory: int = 10,
+                            amplitude_limit: float = math.inf) -> OptimizationResult:
+    """Ensemble L-BFGS-GRAPE (GRAPE.jl:1012-1230) on the device."""
+    if len(systems) == 0:
+        raise ValueError("systems must be non-empty")
+    if lbfgs_memory <= 0:
+        raise ValueError("lbfgs_memory must be positive")
+    obj = build_ensemble_from_systems(systems, target, controls_init, grad_mode=config.grad_mode,
+                                      precision=config.precision)
+    try:
+        o = obj.problem.optimize(controls_init.controls, "ensemble_lbfgs", max_iter=config.max_iter,
+                                 convergence_tol=config.convergence_tol, step_size=config.step_size,
+                                 min_step_size=config.min_step_size,
+                                 max_step_size=config.max_step_size,
+                                 gradient_norm_tol=config.gradient_norm_tol,
+                                 lbfgs_memory=lbfgs_memory, amplitude_limit=amplitude_limit)
+    finally:
+        obj.problem.close()
+    return _result(o, "Ensemble L-BFGS-GRAPE", {"n_systems": len(systems), "lbfgs_memory": lbfgs_memory})
+
+
+# ---------------------------------------------------------------------------
+# Lindblad builders (src/Physics/Lindblad.jl) -- problem set-up, host side
+# ---------------------------------------------------------------------------
+
+def vec_rho(rho) -> np.ndarray:
+    return np.asarray(rho, C128).reshape(-1, order="F")
+
+
+def mat_rho(v, N: int) -> np.ndarray:
+    return np.asarray(v, C128).reshape((N, N), order="F")
+
+
+def pure_state_to_vec_rho(psi) -> np.ndarray:
+    c = np.asarray(psi, C128)
+    return vec_rho(np.outer(c, c.conj()))
+
+
+def build_drift_liouvillian(H_drift, jump_ops, decay_rates) -> np.ndarray:
+    """-i(I(x)H - H^T(x)I) + sum_k g_k [conj(L)(x)L - 1/2 I(x)L'L - 1/2 conj(L'L)(x)I]."""
+    H = np.asarray(H_drift, C128)
+    N = H.shape[0]
+    IN = np.eye(N, dtype=C128)
+    L = -1j * np.kron(IN, H) + 1j * np.kron(H.T, IN)
+    for Lk, g in zip(jump_ops, decay_rates):
+        if g == 0.0 or not math.isfinite(g):
+            continue
+        if g < 0.0:
+            raise ValueError(f"Lindblad decay rate must be non-negative; got {g}")
+        Lk = np.asarray(Lk, C128)
+        Ak = Lk.conj().T @ Lk
+        L = L + g * (np.kron(Lk.conj(), Lk) - 0.5 * np.kron(IN, Ak) - 0.5 * np.kron(Ak.conj(), IN))
+    return L
+
+
+def build_control_liouvillian(H_ctrl) -> np.ndarray:
+    Hc = np.asarray(H_ctrl, C128)
+    IN = np.eye(Hc.shape[0], dtype=C128)
+    return -1j * np.kron(IN, Hc) + 1j * np.kron(Hc.T, IN)
+
+
+# ---------------------------------------------------------------------------
+# MR contexts and kernels
+# ---------------------------------------------------------------------------
+
+def _wrap_states(x):
+    a = np.asarray(x, C128)
+    return [a] if a.ndim == 1 else [np.asarray(v, C128) for v in x]
+
+
+@dataclass
+class MRControl:
+    """OptControl.jl:137-259 (fields the GRAPE path uses; defaults kept)."""
+    drifts: list
+    operators: list
+    rho_init: list
+    rho_targ: list
+    pwr_levels: list
+    pulse_dt: np.ndarray
+    l_bound: float = -1.0
+    u_bound: float = 1.0
+    method: str = "lbfgs"
+    max_iter: int = 500
+    grad_tol: float = 1e-7
+    fidelity: str = "real"
+    lbfgs_memory: int = 10
+    backend: str = "cuda"
+    grad_mode: str = "ref_mr"
+    precision: str = "fp64"
+
+    def __post_init__(self):
+        self.rho_init = _wrap_states(self.rho_init)
+        self.rho_targ = _wrap_states(self.rho_targ)
+        if len(self.rho_init) != len(self.rho_targ):
+            raise ValueError("rho_init and rho_targ must have the same length")
+        self.pulse_dt = np.asarray(self.pulse_dt, np.float64)
+        self._prob = None
+
+    def problem(self) -> Problem:
+        if self._prob is None:
+            n_d, n_p = len(self.drifts), len(self.pwr_levels)
+            md = np.repeat(np.arange(n_d), n_p)
+            ms = np.tile(np.asarray(self.pwr_levels, np.float64), n_d)
+            self._prob = Problem(np.stack(self.drifts), np.stack(self.operators), self.pulse_dt,
+                                 member_drift=md, member_scale=ms, target="states",
+                                 fidelity=self.fidelity, states_init=np.stack(self.rho_init),
+                                 states_target=np.stack(self.rho_targ), grad_mode=self.grad_mode,
+                                 precision=self.precision)
+        return self._prob
+
+
+@dataclass
+class LindbladMRControl:
+    """OptControl.jl:733-885: Liouvillians precomputed at construction."""
+    drifts: list
+    operators: list
+    rho_init: list
+    rho_targ: list
+    pwr_levels: list
+    pulse_dt: np.ndarray
+    jump_ops: list = field(default_factory=list)
+    decay_rates: list = field(default_factory=list)
+    l_bound: float = -1.0
+    u_bound: float = 1.0
+    method: str = "lbfgs"
+    max_iter: int = 500
+    grad_tol: float = 1e-7
+    fidelity: str = "square"
+    lbfgs_memory: int = 10
+    backend: str = "cuda"
+    precision: str = "fp64"
+    grad_mode: str = "ref_mr"
+
+    def __post_init__(self):
+        if len(self.jump_ops) != len(self.decay_rates):
+            raise ValueError("jump_ops and decay_rates must have the same length")
+        if self.fidelity not in ("real", "square"):
+            raise ValueError("LindbladMRControl fidelity must be :square or :real")
+        if not self.l_bound < self.u_bound:
+            raise ValueError("l_bound must be < u_bound")
+        N = np.asarray(self.drifts[0]).shape[0]
+        self._N = N
+        self._L_drifts = [build_drift_liouvillian(H, self.jump_ops, self.decay_rates)
+                          for H in self.drifts]
+        self._L_controls = [build_control_liouvillian(op) for op in self.operators]
+
+        def to_sigma(psi):
+            psi = np.asarray(psi, C128)
+            if psi.size == N:
+                return pure_state_to_vec_rho(psi)
+            if psi.size == N * N:
+                return psi
+            raise ValueError(f"State vector has length {psi.size}; expected N={N} or N^2={N * N}")
+
+        self.rho_init = _wrap_states(self.rho_init)
+        self.rho_targ = _wrap_states(self.rho_targ)
+        if len(self.rho_init) != len(self.rho_targ):
+            raise ValueError("rho_init and rho_targ must have the same length")
+        self._sigma_init = [to_sigma(s) for s in self.rho_init]
+        self._sigma_targ = [to_sigma(s) for s in self.rho_targ]
+        self.pulse_dt = np.asarray(self.pulse_dt, np.float64)
+        self._prob = None
+
+    def problem(self) -> Problem:
+        if self._prob is None:
+            n_d, n_p = len(self._L_drifts), len(self.pwr_levels)
+            self._prob = Problem(np.stack(self._L_drifts), np.stack(self._L_controls), self.pulse_dt,
+                                 generator="liouvillian", member_drift=np.repeat(np.arange(n_d), n_p),
+                                 member_scale=np.tile(np.asarray(self.pwr_levels, np.float64), n_d),
+                                 target="states", fidelity=self.fidelity,
+                                 states_init=np.stack(self._sigma_init),
+                                 states_target=np.stack(self._sigma_targ), grad_mode=self.grad_mode,
+                                 precision=self.precision)
+        return self._prob
+
+
+def grape_state_kernel(waveform, ctrl: MRControl):
+    """(fidelity, grad) averaged over drifts x pwr_levels x state pairs."""
+    return ctrl.problem().eval(np.asarray(waveform, np.float64))
+
+
+def grape_lindblad_kernel(waveform, ctrl: LindbladMRControl):
+    return ctrl.problem().eval(np.asarray(waveform, np.float64))
+
+
+def fidelity_forward(waveform, ctrl) -> float:
+    """Forward-only ensemble fidelity (GRAPEState.jl:434-566)."""
+    return ctrl.problem().eval(np.asarray(waveform, np.float64), want_grad=False)[0]
+
+
+def optimcon(ctrl, guess) -> OptimizationResult:
+    """optimcon(::MRControl | ::LindbladMRControl, guess) with :lbfgs or :grape."""
+    guess = np.asarray(guess, np.float64)
+    n_c, n_t = guess.shape
+    if n_c != len(ctrl.operators):
+        raise ValueError(f"guess rows {n_c} != length(ctrl.operators) {len(ctrl.operators)}")
+    if n_t != len(ctrl.pulse_dt):
+        raise ValueError(f"guess columns {n_t} != length(ctrl.pulse_dt) {len(ctrl.pulse_dt)}")
+    if ctrl.method not in ("lbfgs", "grape"):
+        raise ValueError(f"method :{ctrl.method} is not served on the device (:lbfgs, :grape)")
+    o = ctrl.problem().optimize(guess, "mr_lbfgs" if ctrl.method == "lbfgs" else "mr_grape",
+                                max_iter=ctrl.max_iter, gradient_norm_tol=ctrl.grad_tol,
+                                lbfgs_memory=ctrl.lbfgs_memory, l_bound=ctrl.l_bound,
+                                u_bound=ctrl.u_bound)
+    return _result(o, "L-BFGS" if ctrl.method == "lbfgs" else "GRAPE")

@@ -1,0 +1,267 @@
+// Device building blocks for the GRAPE hot path on sm_103a.
+//
+// A "team" of T threads owns one D x D complex matrix problem.  T = 32 (one
+// warp, __syncwarp) for D <= 8 and T = 256 (one CTA, __syncthreads) for
+// D >= 16.  Matrices are column-major, element (r, c) at r + D*c, stored as
+// interleaved complex (double2 / float2) -- the layout of Julia's
+// Matrix{ComplexF64} and of the C-ABI buffers.
+//
+// Products stage every lane's outputs in registers before a team barrier and
+// only then write, so an output may alias an input (Y = B4 * Y in place).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "taylor_table.h"
+
+namespace pgx {
+
+template <class R> struct CxOf;
+template <> struct CxOf<double> { using type = double2; };
+template <> struct CxOf<float> { using type = float2; };
+
+template <class C> __device__ __forceinline__ C czero() { C z; z.x = 0; z.y = 0; return z; }
+template <class C, class R> __device__ __forceinline__ C cmake(R x, R y) { C z; z.x = x; z.y = y; return z; }
+
+// acc += a * b
+template <class C> __device__ __forceinline__ C cmac(C acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}
+// acc += conj(a) * b
+template <class C> __device__ __forceinline__ C cmac_cj(C acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+template <class C> __device__ __forceinline__ C cmul(C a, C b) { return cmac(czero<C>(), a, b); }
+template <class C, class R> __device__ __forceinline__ C cscale(C a, R s) { a.x *= s; a.y *= s; return a; }
+template <class C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+
+template <int T> struct Team {
+  int lane;
+  __device__ __forceinline__ void sync() const {
+    if constexpr (T <= 32) __syncwarp(); else __syncthreads();
+  }
+};
+
+struct EpiNone {
+  template <class C> __device__ __forceinline__ C operator()(int, int, int, C s) const { return s; }
+};
+
+// out = A1*B1 (+ A2*B2 when TWO) then epi(e, r, c, value).
+template <int D, int T, bool TWO, class C, class Epi>
+__device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const C* B1,
+                                   const C* A2, const C* B2, Epi epi) {
+  constexpr int NE = (D * D + T - 1) / T;
+  C acc[NE];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = tm.lane + i * T;
+    C s = czero<C>();
+    if (e < D * D) {
+      const int r = e % D, c = e / D;
+#pragma unroll 8
+      for (int k = 0; k < D; ++k) s = cmac(s, A1[r + D * k], B1[k + D * c]);
+      if constexpr (TWO) {
+#pragma unroll 8
+        for (int k = 0; k < D; ++k) s = cmac(s, A2[r + D * k], B2[k + D * c]);
+      }
+      s = epi(e, r, c, s);
+    }
+    acc[i] = s;
+  }
+  tm.sync();
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = tm.lane + i * T;
+    if (e < D * D) out[e] = acc[i];
+  }
+  tm.sync();
+}
+
+template <int D, int T, class C>
+__device__ __forceinline__ void mm1(const Team<T>& tm, C* out, const C* A, const C* B) {
+  mm<D, T, false>(tm, out, A, B, (const C*)nullptr, (const C*)nullptr, EpiNone{});
+}
+
+template <int D, int T, class C>
+__device__ __forceinline__ void copy_mat(const Team<T>& tm, C* dst, const C* src) {
+  for (int e = tm.lane; e < D * D; e += T) dst[e] = src[e];
+}
+
+// Team-wide sum of per-lane complex partials (scratch: T complex entries).
+template <int T, class C>
+__device__ __forceinline__ C team_sum(const Team<T>& tm, C v, C* scratch) {
+  if constexpr (T <= 32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+  } else {
+    scratch[tm.lane] = v;
+    __syncthreads();
+    for (int w = T / 2; w > 0; w >>= 1) {
+      if (tm.lane < w) scratch[tm.lane] = cadd(scratch[tm.lane], scratch[tm.lane + w]);
+      __syncthreads();
+    }
+    C r = scratch[0];
+    __syncthreads();
+    return r;
+  }
+}
+
+template <int T>
+__device__ __forceinline__ double team_max(const Team<T>& tm, double v, double* scratch) {
+  if constexpr (T <= 32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+  } else {
+    scratch[tm.lane] = v;
+    __syncthreads();
+    for (int w = T / 2; w > 0; w >>= 1) {
+      if (tm.lane < w) scratch[tm.lane] = fmax(scratch[tm.lane], scratch[tm.lane + w]);
+      __syncthreads();
+    }
+    double r = scratch[0];
+    __syncthreads();
+    return r;
+  }
+}
+
+// 1-norm (max column abs sum) of a D x D matrix; computed in FP64 whatever the
+// storage type, because it selects the Taylor degree and the squarings.
+template <int D, int T, class C>
+__device__ __forceinline__ double norm1(const Team<T>& tm, const C* A, double* scratch) {
+  double best = 0.0;
+  for (int c = tm.lane; c < D; c += T) {
+    double s = 0.0;
+    for (int r = 0; r < D; ++r) {
+      C a = A[r + D * c];
+      s += hypot((double)a.x, (double)a.y);
+    }
+    best = fmax(best, s);
+  }
+  return team_max<T>(tm, best, scratch);
+}
+
+// Degree m in {4,...,20} and squarings s minimising products for ||A||_1.
+__device__ __forceinline__ void choose_degree(double nrm, const double* theta, int& m, int& s) {
+  int best_cost = 1 << 30;
+  m = 4;
+  s = 0;
+#pragma unroll
+  for (int i = 0; i < PGX_N_DEGREES; ++i) {
+    int si = 0;
+    double x = nrm;
+    while (x > theta[i] && si < 60) { x *= 0.5; ++si; }
+    const int mi = 4 * (i + 1);
+    const int cost = (3 + mi / 4 - 1) + si;
+    if (cost < best_cost) { best_cost = cost; m = mi; s = si; }
+  }
+}
+
+// Taylor block C_i = c_{4i} I + c_{4i+1} B + c_{4i+2} B2 + c_{4i+3} B3 at element e.
+template <class C, class R>
+__device__ __forceinline__ C block_val(int i, int r, int c, C b1, C b2, C b3, const R* invf) {
+  C v = cscale(b1, invf[4 * i + 1]);
+  v = cadd(v, cscale(b2, invf[4 * i + 2]));
+  v = cadd(v, cscale(b3, invf[4 * i + 3]));
+  if (r == c) v.x += invf[4 * i];
+  return v;
+}
+template <class C, class R>
+__device__ __forceinline__ C block_der(int i, C d1, C d2, C d3, const R* invf) {
+  C v = cscale(d1, invf[4 * i + 1]);
+  v = cadd(v, cscale(d2, invf[4 * i + 2]));
+  return cadd(v, cscale(d3, invf[4 * i + 3]));
+}
+
+// Workspace layout (10 matrices) used by the Taylor routines.
+template <class C, int D> struct Work {
+  C* B; C* B2; C* B3; C* B4; C* Y;
+  C* dB; C* dB2; C* dB3; C* dB4; C* dY;
+  __device__ __forceinline__ static Work at(C* base) {
+    Work w;
+    constexpr int S = D * D;
+    w.B = base; w.B2 = base + S; w.B3 = base + 2 * S; w.B4 = base + 3 * S; w.Y = base + 4 * S;
+    w.dB = base + 5 * S; w.dB2 = base + 6 * S; w.dB3 = base + 7 * S; w.dB4 = base + 8 * S;
+    w.dY = base + 9 * S;
+    return w;
+  }
+};
+
+// Y = T_m(B)^(2^s).  B holds A / 2^s on entry (destroyed: B..B4 are scratch).
+// Paterson-Stockmeyer with q = 4: powers B2, B3, B4, then Horner in B4 over
+// blocks of four coefficients.  m = 4L costs 3 + (L - 1) products.
+template <int D, int T, class C, class R>
+__device__ void taylor_exp(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
+  mm1<D, T>(tm, w.B2, w.B, w.B);
+  mm1<D, T>(tm, w.B3, w.B2, w.B);
+  mm1<D, T>(tm, w.B4, w.B2, w.B2);
+  const int L = m / 4;
+  for (int e = tm.lane; e < D * D; e += T) {
+    const int r = e % D, c = e / D;
+    C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
+    w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
+  }
+  tm.sync();
+  for (int i = L - 2; i >= 0; --i) {
+    const C* B = w.B; const C* B2 = w.B2; const C* B3 = w.B3;
+    mm<D, T, false>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
+                    [=](int e, int r, int c, C v) {
+                      return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
+                    });
+  }
+  for (int k = 0; k < s; ++k) mm1<D, T>(tm, w.Y, w.Y, w.Y);
+}
+
+// (Y, dY) = (f(A), L_f(A, M)) for f(A) = T_m(A/2^s)^(2^s).  On entry B = A/2^s
+// and dB = M/2^s.  The derivative is exact for the polynomial f actually
+// evaluated, so Tr(L_f(A, M) E) equals Tr(M L_f(A, E)) to rounding.
+template <int D, int T, class C, class R>
+__device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
+  mm1<D, T>(tm, w.B2, w.B, w.B);
+  mm<D, T, true>(tm, w.dB2, w.dB, w.B, w.B, w.dB, EpiNone{});
+  mm1<D, T>(tm, w.B3, w.B2, w.B);
+  mm<D, T, true>(tm, w.dB3, w.dB2, w.B, w.B2, w.dB, EpiNone{});
+  mm1<D, T>(tm, w.B4, w.B2, w.B2);
+  mm<D, T, true>(tm, w.dB4, w.dB2, w.B2, w.B2, w.dB2, EpiNone{});
+  const int L = m / 4;
+  for (int e = tm.lane; e < D * D; e += T) {
+    const int r = e % D, c = e / D;
+    C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
+    w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
+    C dv = block_der(L - 1, w.dB[e], w.dB2[e], w.dB3[e], invf);
+    w.dY[e] = cadd(dv, cscale(w.dB4[e], invf[4 * L]));
+  }
+  tm.sync();
+  for (int i = L - 2; i >= 0; --i) {
+    const C* B = w.B; const C* B2 = w.B2; const C* B3 = w.B3;
+    const C* dB = w.dB; const C* dB2 = w.dB2; const C* dB3 = w.dB3;
+    // dY <- dB4*Y + B4*dY + dC_i   (uses the old Y)
+    mm<D, T, true>(tm, w.dY, w.dB4, w.Y, w.B4, w.dY,
+                   [=](int e, int, int, C v) {
+                     return cadd(v, block_der(i, dB[e], dB2[e], dB3[e], invf));
+                   });
+    // Y <- B4*Y + C_i
+    mm<D, T, false>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
+                    [=](int e, int r, int c, C v) {
+                      return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
+                    });
+  }
+  for (int k = 0; k < s; ++k) {
+    mm<D, T, true>(tm, w.dY, w.Y, w.dY, w.dY, w.Y, EpiNone{});
+    mm1<D, T>(tm, w.Y, w.Y, w.Y);
+  }
+}
+
+}  // namespace pgx

@@ -1,0 +1,77 @@
+// Internal types shared by the kernels and the host runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pgx {
+
+constexpr int kMaxDim = 64;
+
+// Device view of a problem.  Matrices are padded to Dp (the kernel's
+// compile-time size, a power of two >= the true dimension D); padding rows
+// and columns of every generator, target and state are zero, so exp() acts as
+// the identity there and no padded entry reaches F or G.
+struct ProbDev {
+  int D;          // true dimension (normalises the gate overlap)
+  int Dp;         // padded dimension
+  int n_c, n_t, n_members, n_pairs;
+  int gen;        // PGX_GEN_*
+  int target;     // PGX_TARGET_*
+  int fid;        // PGX_FID_*
+  int grad_mode;  // PGX_GRAD_*
+  const double* dt;          // [n_t]
+  const double2* drifts;     // [n_drifts][Dp*Dp]
+  const double2* ctrls;      // [n_c][Dp*Dp]
+  const double2* offset_op;  // [Dp*Dp] (zeros when absent)
+  const int* m_drift;        // [n_members]
+  const double* m_scale;     // [n_members]
+  const double* m_offset;    // [n_members]
+  const double* m_weight;    // [n_members]
+  const double2* target_op;  // gate: [Dp*Dp]
+  const double2* psi_init;   // states: [n_pairs][Dp]
+  const double2* psi_targ;   // states: [n_pairs][Dp]
+};
+
+// Device work buffers of one evaluation.
+struct WorkDev {
+  double2* U;       // [n_members][n_t][Dp*Dp] slice propagators
+  double2* P;       // gate: [n_members][n_t][Dp*Dp] forward chain, then M_k
+  double2* Utot;    // [n_members][Dp*Dp]
+  double2* psi;     // states: [n_members][n_t+1][n_pairs][Dp]
+  double2* lam;     // states: [n_members][n_t+1][n_pairs][Dp]
+  double2* z;       // [n_members][max(n_pairs,1)] overlaps
+  double2* kap;     // [n_members][max(n_pairs,1)] weighted chain-rule coefficients
+  double* Fm;       // [n_members] sum_s f(z_ms)
+  double* Gm;       // [n_members][n_t][n_c] per-member weighted gradient
+  double2* slab;    // global Taylor workspace for Dp = 64: [slab_teams][10][Dp*Dp]
+  int slab_teams;
+  const double* u;  // [n_t][n_c]  (column-major [n_c x n_t])
+  double* G;        // [n_t][n_c]
+  double* F;        // [1]
+};
+
+struct LaunchInfo {
+  int num_sms;
+  cudaStream_t stream;
+  int64_t* launches;   // counter incremented per kernel launch
+};
+
+// Stage launchers (pgx_kernels.cu).  Each returns cudaGetLastError() after
+// launching on li.stream.
+cudaError_t launch_expm(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+cudaError_t launch_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li,
+                             bool store_history);
+cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad);
+// Global slab size (in double2 elements) the Dp = 64 path needs.
+size_t slab_elems(int Dp, int num_sms);
+int slab_team_count(int Dp, int num_sms);
+// Independent-DFMA loop used to measure the device's FP64 FMA rate; *flops
+// receives the floating-point operations it performs.
+cudaError_t launch_fp64_peak(double* sink, const LaunchInfo& li, double* flops);
+// One propagator exp(c dt G) of a padded Dp x Dp generator (device buffers).
+cudaError_t launch_single_expm(int Dp, int gen, const double2* G, double dt, double2* U,
+                               double2* slab, const LaunchInfo& li);
+
+}  // namespace pgx

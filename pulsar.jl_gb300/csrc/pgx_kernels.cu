@@ -1,0 +1,682 @@
+// FP64 kernels of the GRAPE hot path (sm_103a).
+//
+// One evaluation (F, dF/du) of an ensemble problem runs five stages:
+//   expm       slice-parallel   U_mk = exp(A_mk), A_mk = c dt_k G_m(u_k)
+//                               (replaces Propagators.jl:166-184,659-674 and the
+//                                per-slice exp of GRAPELindblad.jl:146-153)
+//   chain_fwd  member-parallel  P_{k+1} = U_k P_k  or  psi_{k+1} = U_k psi_k,
+//                               overlap z, f(z) and the chain-rule coefficient
+//                               (Propagators.jl:309-325, Objectives.jl:609-630)
+//   chain_bwd  member-parallel  Lambda_{k-1} = Lambda_k U_k, M_k = P_k Lambda_k
+//                               or lambda_k = U_k' lambda_{k+1}
+//                               (Propagators.jl:390-406, GRAPEState.jl:214-217)
+//   grad       slice-parallel   g_jk = Re Tr(X_k E_jk), X_k = L_exp(A_k, M_k)
+//                               (exact) or M_k (first-order reference formulas,
+//                               Gradients.jl:254-291,357-399, GRAPEState.jl:220-230)
+//   reduce     deterministic    G = sum_m G_m in member order, F = sum_m w_m F_m
+//                               (EnsembleObjective.jl:169-217, GRAPEState.jl:238-244)
+//
+// The exact gradient uses Tr(M L(A,E)) = Tr(L(A,M) E), valid for any
+// polynomial in A with scalar coefficients, so ONE Frechet derivative per
+// slice serves all n_c controls.
+#include "pgx_device.cuh"
+#include "pgx_internal.h"
+
+namespace pgx {
+
+__constant__ double c_invf[PGX_N_INVFACT] = PGX_INVFACT_INIT;
+__constant__ double c_theta64[PGX_N_DEGREES] = PGX_THETA64_INIT;
+
+enum { GEN_HERM = 0, GEN_LIOUV = 1 };
+enum { TGT_GATE = 0, TGT_STATES = 1 };
+enum { FID_SQUARE = 0, FID_REAL = 1, FID_MODULUS = 2 };
+enum { GRAD_REF_GRAPE = 0, GRAD_REF_MR = 1, GRAD_EXACT = 2 };
+
+template <int D> struct Cfg {
+  static constexpr int T = (D <= 8) ? 32 : 256;    // threads per team
+  static constexpr int TPC = (D <= 8) ? 4 : 1;     // teams per CTA
+  static constexpr bool SLAB = (D >= 64);          // Taylor workspace in global memory
+  static constexpr int NBUF = 10;                  // matrices of Taylor workspace
+  static constexpr int THREADS = T * TPC;
+};
+
+template <int D> constexpr size_t taylor_smem_bytes() {
+  using G = Cfg<D>;
+  return (G::SLAB ? 0 : (size_t)G::TPC * G::NBUF * D * D * sizeof(double2)) +
+         (size_t)G::TPC * G::T * sizeof(double2);
+}
+template <int D> constexpr size_t chain_smem_bytes(int n_pairs) {
+  using G = Cfg<D>;
+  // gate: two matrices; states: two n_pairs x D panels.  Plus reduction scratch.
+  const size_t mats = (size_t)2 * D * D;
+  const size_t vecs = (size_t)2 * (n_pairs > 0 ? n_pairs : 1) * D;
+  return (size_t)G::TPC * ((mats > vecs ? mats : vecs) + G::T) * sizeof(double2);
+}
+
+__device__ __forceinline__ double2 times_c(double2 v, int gen) {
+  // c = -i for a Hermitian generator, 1 for a Liouvillian.
+  if (gen == GEN_HERM) return make_double2(v.y, -v.x);
+  return v;
+}
+
+// A = c dt_k (drift + off O + scale sum_j u_jk C_j)
+template <int D, int T>
+__device__ __forceinline__ void build_A(const Team<T>& tm, const ProbDev& p, const double* u, int m,
+                                        int k, double2* A) {
+  const double dt = p.dt[k];
+  const double sc = p.m_scale[m], off = p.m_offset[m];
+  const double2* Gd = p.drifts + (size_t)p.m_drift[m] * D * D;
+  const double* uk = u + (size_t)k * p.n_c;
+  for (int e = tm.lane; e < D * D; e += T) {
+    double2 v = Gd[e];
+    const double2 o = p.offset_op[e];
+    v.x = fma(off, o.x, v.x);
+    v.y = fma(off, o.y, v.y);
+    for (int j = 0; j < p.n_c; ++j) {
+      const double a = sc * uk[j];
+      const double2 c = p.ctrls[(size_t)j * D * D + e];
+      v.x = fma(a, c.x, v.x);
+      v.y = fma(a, c.y, v.y);
+    }
+    v.x *= dt;
+    v.y *= dt;
+    A[e] = times_c(v, p.gen);
+  }
+}
+
+// f(z) and the chain-rule coefficient kappa with dF = Re(kappa dz).
+__device__ __forceinline__ void fid_kappa(double2 z, int fid, int mode, double& f, double2& kap) {
+  const double az = hypot(z.x, z.y);
+  if (fid == FID_SQUARE) {
+    f = z.x * z.x + z.y * z.y;
+    kap = make_double2(2.0 * z.x, -2.0 * z.y);
+  } else if (fid == FID_REAL) {
+    f = z.x;
+    kap = make_double2(1.0, 0.0);
+  } else {
+    f = az;
+    if (az < 1e-14) kap = make_double2(0.0, 0.0);
+    else if (mode == GRAD_EXACT) kap = make_double2(z.x / az, -z.y / az);
+    else kap = make_double2(1.0 / az, 0.0);  // Objectives.jl:356-361 uses Im(inner/|z|)
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void team_slot(double2* smem, int per_team_elems, int team, double2*& base,
+                                          double2*& red) {
+  base = smem + (size_t)team * per_team_elems;
+  red = base + (per_team_elems - Cfg<D>::T);
+}
+
+// --------------------------------------------------------------------------
+// Stage 1: slice propagators
+// --------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_expm(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  double2* base;
+  double2* red;
+  if constexpr (G::SLAB) {
+    base = w.slab + (size_t)blockIdx.x * G::NBUF * D * D;
+    red = smem + (size_t)team * T;
+  } else {
+    base = smem + (size_t)team * G::NBUF * D * D;
+    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * T;
+  }
+  const Work<double2, D> W = Work<double2, D>::at(base);
+  const long items = (long)p.n_members * p.n_t;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
+    build_A<D, T>(tm, p, w.u, m, k, W.B);
+    tm.sync();
+    const double nrm = norm1<D, T>(tm, W.B, reinterpret_cast<double*>(red));
+    int deg, s;
+    choose_degree(nrm, c_theta64, deg, s);
+    const double sc = ldexp(1.0, -s);
+    for (int e = tm.lane; e < D * D; e += T) W.B[e] = cscale(W.B[e], sc);
+    tm.sync();
+    taylor_exp<D, T>(tm, W, deg, s, c_invf);
+    double2* out = w.U + ((size_t)m * p.n_t + k) * D * D;
+    for (int e = tm.lane; e < D * D; e += T) out[e] = W.Y[e];
+    tm.sync();
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_single_expm(int gen, const double2* Gin, double dt,
+                                                                 double2* U, double2* slab) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  if (threadIdx.x >= T) return;  // one team
+  const Team<T> tm{(int)threadIdx.x};
+  double2* base = G::SLAB ? slab : smem;
+  double2* red = G::SLAB ? smem : smem + (size_t)G::TPC * G::NBUF * D * D;
+  const Work<double2, D> W = Work<double2, D>::at(base);
+  for (int e = tm.lane; e < D * D; e += T) {
+    double2 v = Gin[e];
+    v.x *= dt;
+    v.y *= dt;
+    W.B[e] = times_c(v, gen);
+  }
+  tm.sync();
+  const double nrm = norm1<D, T>(tm, W.B, reinterpret_cast<double*>(red));
+  int deg, s;
+  choose_degree(nrm, c_theta64, deg, s);
+  const double sc = ldexp(1.0, -s);
+  for (int e = tm.lane; e < D * D; e += T) W.B[e] = cscale(W.B[e], sc);
+  tm.sync();
+  taylor_exp<D, T>(tm, W, deg, s, c_invf);
+  for (int e = tm.lane; e < D * D; e += T) U[e] = W.Y[e];
+}
+
+// --------------------------------------------------------------------------
+// Stage 2: forward chains
+// --------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_fwd(ProbDev p, WorkDev w, int store) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  constexpr int NE = (D * D + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;  // whole team leaves together
+  double2 *base, *red;
+  team_slot<D>(smem, 2 * D * D + T, team, base, red);
+  double2* Pc = base;
+  double2* Ub = base + D * D;
+  for (int e = tm.lane; e < D * D; e += T)
+    Pc[e] = make_double2((e % D) == (e / D) ? 1.0 : 0.0, 0.0);
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  double2 pre[NE];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = tm.lane + i * T;
+    if (e < D * D) pre[i] = Um[e];
+  }
+  tm.sync();
+  for (int k = 0; k < p.n_t; ++k) {
+    if (store) {
+      double2* dst = w.P + ((size_t)m * p.n_t + k) * D * D;
+      for (int e = tm.lane; e < D * D; e += T) dst[e] = Pc[e];
+    }
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      const int e = tm.lane + i * T;
+      if (e < D * D) Ub[e] = pre[i];
+    }
+    if (k + 1 < p.n_t) {  // prefetch U_{k+1} while U_k P_k is formed
+      const double2* nx = Um + (size_t)(k + 1) * D * D;
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        const int e = tm.lane + i * T;
+        if (e < D * D) pre[i] = nx[e];
+      }
+    }
+    tm.sync();
+    mm1<D, T>(tm, Pc, Ub, Pc);
+  }
+  double2* Ut = w.Utot + (size_t)m * D * D;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int e = tm.lane; e < D * D; e += T) {
+    Ut[e] = Pc[e];
+    acc = cmac_cj(acc, p.target_op[e], Pc[e]);
+  }
+  double2 z = team_sum<T>(tm, acc, red);
+  if (tm.lane == 0) {
+    z.x /= p.D;
+    z.y /= p.D;
+    double f;
+    double2 kap;
+    fid_kappa(z, p.fid, p.grad_mode, f, kap);
+    const double sc = p.m_weight[m] / p.D;
+    w.z[m] = z;
+    w.kap[m] = make_double2(kap.x * sc, kap.y * sc);
+    w.Fm[m] = f;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_states_fwd(ProbDev p, WorkDev w, int store) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  const int np = p.n_pairs;
+  const int pan = np * D;
+  const int per_team = (2 * D * D > 2 * pan ? 2 * D * D : 2 * pan) + T;
+  double2 *base, *red;
+  team_slot<D>(smem, per_team, team, base, red);
+  double2* Ps = base;  // [np][D]
+  for (int e = tm.lane; e < pan; e += T) Ps[e] = p.psi_init[e];
+  tm.sync();
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  for (int k = 0; k < p.n_t; ++k) {
+    if (store) {
+      double2* dst = w.psi + ((size_t)m * (p.n_t + 1) + k) * pan;
+      for (int e = tm.lane; e < pan; e += T) dst[e] = Ps[e];
+    }
+    const double2* Uk = Um + (size_t)k * D * D;
+    // Each lane forms its outputs in registers, then the team writes.
+    double2 outv[(D * 8 + T - 1) / T > 0 ? (D * 8 + T - 1) / T : 1];
+    int cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      const int s = e / D, r = e % D;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int q = 0; q < D; ++q) acc = cmac(acc, Uk[r + D * q], Ps[s * D + q]);
+      if (cnt < (int)(sizeof(outv) / sizeof(outv[0]))) outv[cnt] = acc;
+    }
+    tm.sync();
+    cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) Ps[e] = outv[cnt];
+    tm.sync();
+  }
+  if (store) {
+    double2* dst = w.psi + ((size_t)m * (p.n_t + 1) + p.n_t) * pan;
+    for (int e = tm.lane; e < pan; e += T) dst[e] = Ps[e];
+  }
+  double Fm = 0.0;
+  for (int s = 0; s < np; ++s) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int r = tm.lane; r < D; r += T) acc = cmac_cj(acc, p.psi_targ[s * D + r], Ps[s * D + r]);
+    const double2 z = team_sum<T>(tm, acc, red);
+    double f;
+    double2 kap;
+    fid_kappa(z, p.fid, p.grad_mode, f, kap);
+    Fm += f;
+    if (tm.lane == 0) {
+      const double wgt = p.m_weight[m];
+      w.z[(size_t)m * np + s] = z;
+      w.kap[(size_t)m * np + s] = make_double2(kap.x * wgt, kap.y * wgt);
+    }
+  }
+  if (tm.lane == 0) w.Fm[m] = Fm;
+}
+
+// --------------------------------------------------------------------------
+// Stage 3: backward chains
+// --------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  double2 *base, *red;
+  team_slot<D>(smem, 2 * D * D + T, team, base, red);
+  double2* Lam = base;
+  double2* Buf = base + D * D;
+  const double2 kap = w.kap[m];
+  // Lambda_{n-1} = kappa T'   (kappa carries the member weight and 1/D)
+  for (int e = tm.lane; e < D * D; e += T) {
+    const int r = e % D, c = e / D;
+    const double2 t = p.target_op[c + D * r];
+    Lam[e] = cmul(kap, make_double2(t.x, -t.y));
+  }
+  tm.sync();
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  double2* Pm = w.P + (size_t)m * p.n_t * D * D;
+  const bool grape = (p.grad_mode == GRAD_REF_GRAPE);
+  for (int k = p.n_t - 1; k >= 0; --k) {
+    if (grape) {  // Gradients.jl: the costate includes the slice's own U_k
+      for (int e = tm.lane; e < D * D; e += T) Buf[e] = Um[(size_t)k * D * D + e];
+      tm.sync();
+      mm1<D, T>(tm, Lam, Lam, Buf);
+    }
+    for (int e = tm.lane; e < D * D; e += T) Buf[e] = Pm[(size_t)k * D * D + e];
+    tm.sync();
+    mm1<D, T>(tm, Pm + (size_t)k * D * D, Buf, Lam);  // M_k = P_k Lambda
+    if (!grape) {
+      for (int e = tm.lane; e < D * D; e += T) Buf[e] = Um[(size_t)k * D * D + e];
+      tm.sync();
+      mm1<D, T>(tm, Lam, Lam, Buf);
+    }
+  }
+  (void)red;
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_states_bwd(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  const int np = p.n_pairs;
+  const int pan = np * D;
+  const int per_team = (2 * D * D > 2 * pan ? 2 * D * D : 2 * pan) + T;
+  double2 *base, *red;
+  team_slot<D>(smem, per_team, team, base, red);
+  double2* Ls = base;
+  // lambda_n = conj(kappa_s) t_s, so that lambda' E psi = kappa_s <t_s|...>
+  for (int e = tm.lane; e < pan; e += T) {
+    const double2 kp = w.kap[(size_t)m * np + e / D];
+    Ls[e] = cmul(make_double2(kp.x, -kp.y), p.psi_targ[e]);
+  }
+  tm.sync();
+  double2* Lm = w.lam + (size_t)m * (p.n_t + 1) * pan;
+  for (int e = tm.lane; e < pan; e += T) Lm[(size_t)p.n_t * pan + e] = Ls[e];
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  for (int k = p.n_t - 1; k >= 0; --k) {
+    const double2* Uk = Um + (size_t)k * D * D;
+    double2 outv[(D * 8 + T - 1) / T > 0 ? (D * 8 + T - 1) / T : 1];
+    int cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      const int s = e / D, r = e % D;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int q = 0; q < D; ++q) acc = cmac_cj(acc, Uk[q + D * r], Ls[s * D + q]);
+      if (cnt < (int)(sizeof(outv) / sizeof(outv[0]))) outv[cnt] = acc;
+    }
+    tm.sync();
+    cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      Ls[e] = outv[cnt];
+      Lm[(size_t)k * pan + e] = outv[cnt];
+    }
+    tm.sync();
+  }
+  (void)red;
+}
+
+// --------------------------------------------------------------------------
+// Stage 4: per-slice gradient contributions
+// --------------------------------------------------------------------------
+// g_j = Re(c dt scale Tr(X C_j)), X in the team's reach (smem or global).
+template <int D, int T>
+__device__ __forceinline__ void trace_controls(const Team<T>& tm, const ProbDev& p, const double2* X,
+                                               int m, int k, double* Gout, double2* red) {
+  const double cds = p.dt[k] * p.m_scale[m];
+  for (int j = 0; j < p.n_c; ++j) {
+    const double2* Cj = p.ctrls + (size_t)j * D * D;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int e = tm.lane; e < D * D; e += T) {
+      const int r = e % D, c = e / D;
+      acc = cmac(acc, X[e], Cj[c + D * r]);
+    }
+    const double2 t = team_sum<T>(tm, acc, red);
+    if (tm.lane == 0) Gout[j] = cds * (p.gen == GEN_HERM ? t.y : t.x);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_grad(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  double2* base;
+  double2* red;
+  if constexpr (G::SLAB) {
+    base = w.slab + (size_t)blockIdx.x * G::NBUF * D * D;
+    red = smem + (size_t)team * T;
+  } else {
+    base = smem + (size_t)team * G::NBUF * D * D;
+    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * T;
+  }
+  const Work<double2, D> W = Work<double2, D>::at(base);
+  const int np = p.n_pairs;
+  const int pan = np * D;
+  const bool exact = (p.grad_mode == GRAD_EXACT);
+  const long items = (long)p.n_members * p.n_t;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
+    double* Gout = w.Gm + ((size_t)m * p.n_t + k) * p.n_c;
+    const double2* X;
+    if (p.target == TGT_GATE) {
+      const double2* Mk = w.P + ((size_t)m * p.n_t + k) * D * D;
+      if (!exact) {
+        trace_controls<D, T>(tm, p, Mk, m, k, Gout, red);
+        continue;
+      }
+      for (int e = tm.lane; e < D * D; e += T) W.dB[e] = Mk[e];
+    } else {
+      const double2* psi = w.psi + ((size_t)m * (p.n_t + 1) + k) * pan;
+      const int li = (p.grad_mode == GRAD_REF_GRAPE) ? k : k + 1;
+      const double2* lam = w.lam + ((size_t)m * (p.n_t + 1) + li) * pan;
+      if (!exact) {
+        // g_j = Re(c dt scale sum_s lambda_s' C_j psi_s)
+        const double cds = p.dt[k] * p.m_scale[m];
+        for (int j = 0; j < p.n_c; ++j) {
+          const double2* Cj = p.ctrls + (size_t)j * D * D;
+          double2 acc = make_double2(0.0, 0.0);
+          for (int e = tm.lane; e < D * D; e += T) {
+            const int r = e % D, c = e / D;
+            double2 lp = make_double2(0.0, 0.0);
+            for (int s = 0; s < np; ++s) lp = cmac_cj(lp, lam[s * D + r], psi[s * D + c]);
+            acc = cmac(acc, lp, Cj[e]);
+          }
+          const double2 t = team_sum<T>(tm, acc, red);
+          if (tm.lane == 0) Gout[j] = cds * (p.gen == GEN_HERM ? t.y : t.x);
+        }
+        continue;
+      }
+      // M = sum_s psi_s lambda_s'
+      for (int e = tm.lane; e < D * D; e += T) {
+        const int r = e % D, c = e / D;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int s = 0; s < np; ++s) {
+          const double2 l = lam[s * D + c];
+          acc = cmac(acc, psi[s * D + r], make_double2(l.x, -l.y));
+        }
+        W.dB[e] = acc;
+      }
+    }
+    // Exact: X = L_f(A_k, M_k) with the same degree/squarings as stage 1.
+    build_A<D, T>(tm, p, w.u, m, k, W.B);
+    tm.sync();
+    const double nrm = norm1<D, T>(tm, W.B, reinterpret_cast<double*>(red));
+    int deg, s;
+    choose_degree(nrm, c_theta64, deg, s);
+    const double sc = ldexp(1.0, -s);
+    for (int e = tm.lane; e < D * D; e += T) {
+      W.B[e] = cscale(W.B[e], sc);
+      W.dB[e] = cscale(W.dB[e], sc);
+    }
+    tm.sync();
+    taylor_exp_frechet<D, T>(tm, W, deg, s, c_invf);
+    X = W.dY;
+    trace_controls<D, T>(tm, p, X, m, k, Gout, red);
+    tm.sync();
+  }
+}
+
+// --------------------------------------------------------------------------
+// Stage 5: deterministic ensemble reduction
+// --------------------------------------------------------------------------
+__global__ void k_reduce(ProbDev p, WorkDev w, int want_grad) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = p.n_t * p.n_c;
+  if (want_grad && idx < n) {
+    double s = 0.0;
+    for (int m = 0; m < p.n_members; ++m) s += w.Gm[(size_t)m * n + idx];
+    w.G[idx] = s;
+  }
+  if (idx == 0) {
+    double f = 0.0;
+    for (int m = 0; m < p.n_members; ++m) f += p.m_weight[m] * w.Fm[m];
+    w.F[0] = f;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Launchers
+// --------------------------------------------------------------------------
+template <class K>
+static void ensure_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class K>
+static int item_grid(K kernel, int threads, size_t smem, long teams_needed, int tpc, int num_sms,
+                     int cap) {
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  long blocks = (teams_needed + tpc - 1) / tpc;
+  long maxb = (long)num_sms * per_sm;
+  if (blocks > maxb) blocks = maxb;
+  if (cap > 0 && blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+int slab_team_count(int Dp, int num_sms) { return Dp >= 64 ? 2 * num_sms : 0; }
+size_t slab_elems(int Dp, int num_sms) {
+  return Dp >= 64 ? (size_t)slab_team_count(Dp, num_sms) * 10 * Dp * Dp : 0;
+}
+
+#define PGX_DISPATCH(DP, CALL)                      \
+  switch (DP) {                                     \
+    case 2: { constexpr int D_ = 2; CALL; } break;  \
+    case 4: { constexpr int D_ = 4; CALL; } break;  \
+    case 8: { constexpr int D_ = 8; CALL; } break;  \
+    case 16: { constexpr int D_ = 16; CALL; } break; \
+    case 32: { constexpr int D_ = 32; CALL; } break; \
+    case 64: { constexpr int D_ = 64; CALL; } break; \
+    default: return cudaErrorInvalidValue;          \
+  }
+
+template <int D>
+static cudaError_t do_expm(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = taylor_smem_bytes<D>();
+  ensure_smem(k_expm<D>, smem);
+  const int grid = item_grid(k_expm<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
+                             li.num_sms, G::SLAB ? w.slab_teams : 0);
+  k_expm<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_expm(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH(p.Dp, return do_expm<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
+  using G = Cfg<D>;
+  const size_t smem = chain_smem_bytes<D>(p.n_pairs);
+  const int grid = (p.n_members + G::TPC - 1) / G::TPC;
+  if (p.target == TGT_GATE) {
+    ensure_smem(k_chain_gate_fwd<D>, smem);
+    k_chain_gate_fwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w, store ? 1 : 0);
+  } else {
+    ensure_smem(k_chain_states_fwd<D>, smem);
+    k_chain_states_fwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w, store ? 1 : 0);
+  }
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
+  PGX_DISPATCH(p.Dp, return do_chain_fwd<D_>(p, w, li, store));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = chain_smem_bytes<D>(p.n_pairs);
+  const int grid = (p.n_members + G::TPC - 1) / G::TPC;
+  if (p.target == TGT_GATE) {
+    ensure_smem(k_chain_gate_bwd<D>, smem);
+    k_chain_gate_bwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  } else {
+    ensure_smem(k_chain_states_bwd<D>, smem);
+    k_chain_states_bwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  }
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH(p.Dp, return do_chain_bwd<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = taylor_smem_bytes<D>();
+  ensure_smem(k_grad<D>, smem);
+  const int grid = item_grid(k_grad<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
+                             li.num_sms, G::SLAB ? w.slab_teams : 0);
+  k_grad<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH(p.Dp, return do_grad<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad) {
+  const int n = p.n_t * p.n_c;
+  const int grid = want_grad ? (n + 255) / 256 : 1;
+  k_reduce<<<grid, 256, 0, li.stream>>>(p, w, want_grad ? 1 : 0);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
+// 8 independent FMA chains per thread; the result is stored only when it is
+// impossible (all-zero inputs keep it finite), which keeps the loop alive.
+__global__ void __launch_bounds__(256) k_fp64_peak(double* sink, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = threadIdx.x * 1e-9 + i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += x[i];
+  if (s == 12345.678) sink[threadIdx.x & 63] = s;
+}
+
+cudaError_t launch_fp64_peak(double* sink, const LaunchInfo& li, double* flops) {
+  const int blocks = li.num_sms * 8, threads = 256, iters = 8192;
+  k_fp64_peak<<<blocks, threads, 0, li.stream>>>(sink, iters, 0.999999, 1e-7);
+  ++*li.launches;
+  *flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  return cudaGetLastError();
+}
+
+template <int D>
+static cudaError_t do_single(int gen, const double2* Gm, double dt, double2* U, double2* slab,
+                             const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = taylor_smem_bytes<D>();
+  ensure_smem(k_single_expm<D>, smem);
+  k_single_expm<D><<<1, G::THREADS, smem, li.stream>>>(gen, Gm, dt, U, slab);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_single_expm(int Dp, int gen, const double2* Gm, double dt, double2* U,
+                               double2* slab, const LaunchInfo& li) {
+  PGX_DISPATCH(Dp, return do_single<D_>(gen, Gm, dt, U, slab, li));
+  return cudaSuccess;
+}
+
+}  // namespace pgx

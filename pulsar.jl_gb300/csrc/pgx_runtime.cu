@@ -1,0 +1,741 @@
+// Host runtime behind include/pgx.h: contexts, problems, evaluation.
+//
+// The reference keeps everything in Julia arrays and, on its CUDA path,
+// uploads CPU-built propagators every call (GRAPEState.jl:329-330,
+// GRAPELindblad.jl:369-410).  Here every input is copied to HBM once at
+// pgx_problem_create; an evaluation moves only u (n_c*n_t doubles) in and
+// (F, G) out.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pgx.h"
+#include "pgx_internal.h"
+#include "pgx_runtime.h"
+
+using pgx::ProbDev;
+using pgx::WorkDev;
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+int ctx_fail(pgx_ctx* c, int status, const std::string& msg) {
+  if (c) c->err = msg;
+  return status;
+}
+
+int ctx_cuda(pgx_ctx* c, cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return PGX_OK;
+  const int st = (e == cudaErrorMemoryAllocation) ? PGX_ERR_NOMEM : PGX_ERR_CUDA;
+  return ctx_fail(c, st, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int ctx_alloc(pgx_ctx* c, void** p, size_t bytes, std::vector<void*>& owned, uint64_t& acct) {
+  *p = nullptr;
+  if (bytes == 0) return PGX_OK;
+  if (c->budget && c->used + bytes > c->budget)
+    return ctx_fail(c, PGX_ERR_BUDGET, "HBM budget exceeded: " + std::to_string(c->used + bytes) +
+                                           " > " + std::to_string(c->budget) + " bytes");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return ctx_cuda(c, e, "cudaMalloc");
+  }
+  owned.push_back(*p);
+  c->used += bytes;
+  acct += bytes;
+  return PGX_OK;
+}
+
+extern "C" int pgx_abi_version(void) { return PGX_ABI_VERSION; }
+
+extern "C" const char* pgx_status_string(int s) {
+  switch (s) {
+    case PGX_OK: return "ok";
+    case PGX_ERR_INVALID: return "invalid argument";
+    case PGX_ERR_DIMS: return "dimension mismatch";
+    case PGX_ERR_NOMEM: return "out of device memory";
+    case PGX_ERR_BUDGET: return "HBM budget exceeded";
+    case PGX_ERR_CUDA: return "CUDA error";
+    case PGX_ERR_UNSUPPORTED: return "unsupported";
+    case PGX_ERR_TIMEOUT: return "timeout";
+    case PGX_ERR_CANCELLED: return "cancelled";
+    case PGX_ERR_STATE: return "invalid state";
+    case PGX_ERR_NONFINITE: return "non-finite value";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int pgx_ctx_create(int device, uint64_t hbm_budget_bytes, pgx_ctx** out) {
+  if (!out) return PGX_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return PGX_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return PGX_ERR_CUDA;
+  pgx_ctx* c = new (std::nothrow) pgx_ctx();
+  if (!c) return PGX_ERR_NOMEM;
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreate(&c->tev0) != cudaSuccess || cudaEventCreate(&c->tev1) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return PGX_ERR_CUDA;
+  }
+  *out = c;
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_destroy(pgx_ctx* c) {
+  if (!c) return PGX_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaEventDestroy(c->ev0);
+  cudaEventDestroy(c->ev1);
+  cudaEventDestroy(c->tev0);
+  cudaEventDestroy(c->tev1);
+  for (auto& ev : c->stage_marks)
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return PGX_OK;
+}
+
+extern "C" int pgx_last_error(const pgx_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return PGX_ERR_INVALID;
+  std::snprintf(buf, len, "%s", c->err.c_str());
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_hbm_used(const pgx_ctx* c, uint64_t* bytes) {
+  if (!c || !bytes) return PGX_ERR_INVALID;
+  *bytes = c->used;
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_stream(pgx_ctx* c, void** stream) {
+  if (!c || !stream) return PGX_ERR_INVALID;
+  *stream = (void*)c->stream;
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_timer_start(pgx_ctx* c) {
+  if (!c) return PGX_ERR_INVALID;
+  return ctx_cuda(c, cudaEventRecord(c->tev0, c->stream), "timer_start");
+}
+
+extern "C" int pgx_ctx_timer_stop(pgx_ctx* c, double* ms) {
+  if (!c || !ms) return PGX_ERR_INVALID;
+  int st = ctx_cuda(c, cudaEventRecord(c->tev1, c->stream), "timer_stop");
+  if (st) return st;
+  st = ctx_cuda(c, cudaEventSynchronize(c->tev1), "timer_stop sync");
+  if (st) return st;
+  float f = 0.f;
+  st = ctx_cuda(c, cudaEventElapsedTime(&f, c->tev0, c->tev1), "timer elapsed");
+  *ms = f;
+  return st;
+}
+
+extern "C" int pgx_ctx_synchronize(pgx_ctx* c) {
+  if (!c) return PGX_ERR_INVALID;
+  return ctx_cuda(c, cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+extern "C" int pgx_ctx_launch_count(const pgx_ctx* c, int64_t* count) {
+  if (!c || !count) return PGX_ERR_INVALID;
+  *count = c->launches;
+  return PGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// problem validation / sizing
+// ---------------------------------------------------------------------------
+static int pad_dim(int d) {
+  int p = 2;
+  while (p < d) p *= 2;
+  return p;
+}
+
+static bool finite_all(const double* x, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(x[i])) return false;
+  return true;
+}
+
+static double herm_dev(const double* m, int D) {
+  double dev = 0.0;
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c) {
+      const cplx a(m[2 * (r + D * c)], m[2 * (r + D * c) + 1]);
+      const cplx b(m[2 * (c + D * r)], -m[2 * (c + D * r) + 1]);
+      dev = std::max(dev, std::abs(a - b));
+    }
+  return dev;
+}
+
+static double unitarity_dev(const double* m, int D) {
+  // ||U'U - I||_F / D  (Targets.jl:135-137)
+  double s = 0.0;
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) {
+      cplx acc = 0.0;
+      for (int k = 0; k < D; ++k)
+        acc += std::conj(cplx(m[2 * (k + D * i)], m[2 * (k + D * i) + 1])) *
+               cplx(m[2 * (k + D * j)], m[2 * (k + D * j) + 1]);
+      if (i == j) acc -= 1.0;
+      s += std::norm(acc);
+    }
+  return std::sqrt(s) / D;
+}
+
+static int validate(pgx_ctx* c, const pgx_problem_desc* d) {
+  if (!d) return ctx_fail(c, PGX_ERR_INVALID, "descriptor is NULL");
+  if (d->struct_size < sizeof(pgx_problem_desc))
+    return ctx_fail(c, PGX_ERR_INVALID, "descriptor struct_size too small");
+  if (d->dim < 1 || d->dim > pgx::kMaxDim)
+    return ctx_fail(c, PGX_ERR_DIMS, "dim must be in [1, 64]");
+  if (d->n_controls < 1 || d->n_slices < 1 || d->n_drifts < 1 || d->n_members < 1)
+    return ctx_fail(c, PGX_ERR_DIMS, "n_controls, n_slices, n_drifts, n_members must be >= 1");
+  if (d->generator != PGX_GEN_HERMITIAN && d->generator != PGX_GEN_LIOUVILLIAN)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown generator kind");
+  if (d->target != PGX_TARGET_GATE && d->target != PGX_TARGET_STATES)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown target kind");
+  if (d->fidelity < PGX_FID_SQUARE || d->fidelity > PGX_FID_MODULUS)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown fidelity type");
+  if (d->generator == PGX_GEN_LIOUVILLIAN && d->fidelity == PGX_FID_MODULUS)
+    return ctx_fail(c, PGX_ERR_INVALID,
+                    "modulus fidelity is not supported in Liouville space (OptControl.jl:813-816)");
+  if (d->grad_mode < PGX_GRAD_REF_GRAPE || d->grad_mode > PGX_GRAD_EXACT)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown gradient mode");
+  if (d->precision != PGX_PREC_FP64 && d->precision != PGX_PREC_MIXED)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown precision mode");
+  if (!d->dt || !d->drifts || !d->controls)
+    return ctx_fail(c, PGX_ERR_INVALID, "dt, drifts and controls are required");
+  const size_t DD = (size_t)d->dim * d->dim;
+  if (!finite_all(d->dt, d->n_slices)) return ctx_fail(c, PGX_ERR_NONFINITE, "dt not finite");
+  for (int k = 0; k < d->n_slices; ++k)
+    if (d->dt[k] < 0.0) return ctx_fail(c, PGX_ERR_INVALID, "dt must be non-negative");
+  if (!finite_all(d->drifts, 2 * DD * d->n_drifts) || !finite_all(d->controls, 2 * DD * d->n_controls))
+    return ctx_fail(c, PGX_ERR_NONFINITE, "generator entries must be finite");
+  if (d->offset_op && !finite_all(d->offset_op, 2 * DD))
+    return ctx_fail(c, PGX_ERR_NONFINITE, "offset_op entries must be finite");
+  if (d->generator == PGX_GEN_HERMITIAN) {
+    for (int i = 0; i < d->n_drifts; ++i)
+      if (herm_dev(d->drifts + 2 * DD * i, d->dim) > 1e-10)
+        return ctx_fail(c, PGX_ERR_INVALID, "drift " + std::to_string(i) + " is not Hermitian");
+    for (int j = 0; j < d->n_controls; ++j)
+      if (herm_dev(d->controls + 2 * DD * j, d->dim) > 1e-10)
+        return ctx_fail(c, PGX_ERR_INVALID, "control " + std::to_string(j) + " is not Hermitian");
+    if (d->offset_op && herm_dev(d->offset_op, d->dim) > 1e-10)
+      return ctx_fail(c, PGX_ERR_INVALID, "offset_op is not Hermitian");
+  }
+  if (d->member_drift)
+    for (int m = 0; m < d->n_members; ++m)
+      if (d->member_drift[m] < 0 || d->member_drift[m] >= d->n_drifts)
+        return ctx_fail(c, PGX_ERR_INVALID, "member_drift out of range");
+  for (const double* v : {d->member_scale, d->member_offset, d->member_weight})
+    if (v && !finite_all(v, d->n_members))
+      return ctx_fail(c, PGX_ERR_NONFINITE, "member table entries must be finite");
+  if (d->target == PGX_TARGET_GATE) {
+    if (d->n_pairs != 0) return ctx_fail(c, PGX_ERR_INVALID, "gate target takes n_pairs = 0");
+    if (!d->target_op) return ctx_fail(c, PGX_ERR_INVALID, "gate target needs target_op");
+    if (!finite_all(d->target_op, 2 * DD)) return ctx_fail(c, PGX_ERR_NONFINITE, "target not finite");
+    if (unitarity_dev(d->target_op, d->dim) > 1e-8)
+      return ctx_fail(c, PGX_ERR_INVALID, "target matrix is not unitary (Targets.jl:135-140)");
+  } else {
+    if (d->n_pairs < 1 || d->n_pairs > pgx_problem::kMaxPairs)
+      return ctx_fail(c, PGX_ERR_DIMS, "n_pairs must be in [1, 8]");
+    if (!d->states_init || !d->states_target)
+      return ctx_fail(c, PGX_ERR_INVALID, "state target needs states_init and states_target");
+    const size_t n = 2 * (size_t)d->n_pairs * d->dim;
+    if (!finite_all(d->states_init, n) || !finite_all(d->states_target, n) ||
+        (d->grad_states_init && !finite_all(d->grad_states_init, n)))
+      return ctx_fail(c, PGX_ERR_NONFINITE, "states not finite");
+    for (int s = 0; s < d->n_pairs; ++s) {
+      double ni = 0, nt = 0;
+      for (int i = 0; i < 2 * d->dim; ++i) {
+        ni += d->states_init[2 * (size_t)s * d->dim + i] * d->states_init[2 * (size_t)s * d->dim + i];
+        nt += d->states_target[2 * (size_t)s * d->dim + i] * d->states_target[2 * (size_t)s * d->dim + i];
+      }
+      if (std::sqrt(ni) < 2.220446049250313e-16 || std::sqrt(nt) < 2.220446049250313e-16)
+        return ctx_fail(c, PGX_ERR_INVALID, "state has zero norm (Targets.jl:85-96)");
+    }
+  }
+  return PGX_OK;
+}
+
+struct Sizes {
+  size_t U, P, Utot, psi, z, Fm, Gm, slab, u, G;
+};
+
+static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
+  Sizes s{};
+  const size_t DD = (size_t)Dp * Dp;
+  const size_t nm = d->n_members, nt = d->n_slices;
+  const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
+  s.U = nm * nt * DD * sizeof(double2);
+  s.P = d->target == PGX_TARGET_GATE ? nm * nt * DD * sizeof(double2) : 0;
+  s.Utot = nm * DD * sizeof(double2);
+  s.psi = np ? nm * (nt + 1) * np * Dp * sizeof(double2) : 0;
+  s.z = nm * std::max<size_t>(np, 1) * sizeof(double2);
+  s.Fm = nm * sizeof(double);
+  s.Gm = nm * nt * d->n_controls * sizeof(double);
+  s.slab = pgx::slab_elems(Dp, num_sms) * sizeof(double2);
+  s.u = nt * d->n_controls * sizeof(double);
+  s.G = s.u;
+  return s;
+}
+
+static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
+  const int Dp = pad_dim(d->dim);
+  const Sizes s = sizes_of(d, Dp, num_sms);
+  const size_t DD = (size_t)Dp * Dp * sizeof(double2);
+  const size_t consts = DD * (d->n_drifts + d->n_controls + 3) +
+                        2 * (size_t)std::max(d->n_pairs, 0) * Dp * sizeof(double2) * 2 +
+                        (size_t)d->n_members * (sizeof(int) + 3 * sizeof(double)) +
+                        (size_t)d->n_slices * sizeof(double);
+  return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
+         2 * sizeof(double) + consts;
+}
+
+extern "C" int pgx_problem_footprint(const pgx_problem_desc* d, uint64_t* bytes) {
+  if (!d || !bytes) return PGX_ERR_INVALID;
+  if (d->struct_size < sizeof(pgx_problem_desc) || d->dim < 1 || d->dim > pgx::kMaxDim ||
+      d->n_controls < 1 || d->n_slices < 1 || d->n_drifts < 1 || d->n_members < 1)
+    return PGX_ERR_DIMS;
+  *bytes = footprint(d, 152);
+  return PGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// problem create / destroy
+// ---------------------------------------------------------------------------
+static std::vector<double> pad_mats(const double* src, int n, int D, int Dp) {
+  std::vector<double> out((size_t)n * Dp * Dp * 2, 0.0);
+  if (!src) return out;
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < D; ++c)
+      for (int r = 0; r < D; ++r) {
+        const size_t si = 2 * ((size_t)i * D * D + r + (size_t)D * c);
+        const size_t di = 2 * ((size_t)i * Dp * Dp + r + (size_t)Dp * c);
+        out[di] = src[si];
+        out[di + 1] = src[si + 1];
+      }
+  return out;
+}
+
+static std::vector<double> pad_vecs(const double* src, int n, int D, int Dp) {
+  std::vector<double> out((size_t)n * Dp * 2, 0.0);
+  if (!src) return out;
+  for (int i = 0; i < n; ++i)
+    for (int r = 0; r < D; ++r) {
+      out[2 * ((size_t)i * Dp + r)] = src[2 * ((size_t)i * D + r)];
+      out[2 * ((size_t)i * Dp + r) + 1] = src[2 * ((size_t)i * D + r) + 1];
+    }
+  return out;
+}
+
+template <class T>
+static int upload(pgx_problem* p, T** dptr, const std::vector<T>& host) {
+  int st = ctx_alloc(p->ctx, (void**)dptr, host.size() * sizeof(T), p->owned, p->bytes);
+  if (st) return st;
+  if (host.empty()) return PGX_OK;
+  return ctx_cuda(p->ctx, cudaMemcpy(*dptr, host.data(), host.size() * sizeof(T),
+                                     cudaMemcpyHostToDevice), "upload");
+}
+
+extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_problem** out) {
+  if (!c || !out) return PGX_ERR_INVALID;
+  *out = nullptr;
+  int st = validate(c, d);
+  if (st) return st;
+  cudaSetDevice(c->device);
+  if (c->budget && c->used + footprint(d, c->num_sms) > c->budget)
+    return ctx_fail(c, PGX_ERR_BUDGET, "problem footprint exceeds the context HBM budget");
+  pgx_problem* p = new (std::nothrow) pgx_problem();
+  if (!p) return ctx_fail(c, PGX_ERR_NOMEM, "host allocation failed");
+  p->ctx = c;
+  p->desc = *d;
+  const int D = d->dim, Dp = pad_dim(D);
+  p->Dp = Dp;
+  const int nm = d->n_members, nt = d->n_slices, nc = d->n_controls;
+  const int np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
+
+  // ---- constant inputs, padded ----
+  std::vector<double> drifts = pad_mats(d->drifts, d->n_drifts, D, Dp);
+  std::vector<double> ctrls = pad_mats(d->controls, nc, D, Dp);
+  std::vector<double> offs = pad_mats(d->offset_op, 1, D, Dp);
+  std::vector<double> tgt = pad_mats(d->target_op, 1, D, Dp);
+  std::vector<double> dt(d->dt, d->dt + nt);
+  std::vector<int> mdrift(nm, 0);
+  std::vector<double> mscale(nm, 1.0), moff(nm, 0.0), mw(nm, 1.0 / ((double)nm * std::max(np, 1)));
+  for (int m = 0; m < nm; ++m) {
+    if (d->member_drift) mdrift[m] = d->member_drift[m];
+    if (d->member_scale) mscale[m] = d->member_scale[m];
+    if (d->member_offset) moff[m] = d->member_offset[m];
+    if (d->member_weight) mw[m] = d->member_weight[m];
+  }
+  p->h_weight = mw;
+  std::vector<double> psi_i = pad_vecs(d->states_init, np, D, Dp);
+  std::vector<double> psi_t = pad_vecs(d->states_target, np, D, Dp);
+  std::vector<double> psi_g = pad_vecs(d->grad_states_init ? d->grad_states_init : d->states_init, np, D, Dp);
+  p->split_grad_states = np > 0 && d->grad_states_init &&
+                         std::memcmp(d->grad_states_init, d->states_init,
+                                     sizeof(double) * 2 * (size_t)np * D) != 0;
+
+  double *g_dr, *g_ct, *g_of, *g_tg, *g_dt, *g_ms, *g_mo, *g_mw, *g_pi, *g_pt, *g_pg;
+  int* g_md;
+  if ((st = upload(p, &g_dr, drifts)) || (st = upload(p, &g_ct, ctrls)) || (st = upload(p, &g_of, offs)) ||
+      (st = upload(p, &g_tg, tgt)) || (st = upload(p, &g_dt, dt)) || (st = upload(p, &g_md, mdrift)) ||
+      (st = upload(p, &g_ms, mscale)) || (st = upload(p, &g_mo, moff)) || (st = upload(p, &g_mw, mw)) ||
+      (st = upload(p, &g_pi, psi_i)) || (st = upload(p, &g_pt, psi_t)) || (st = upload(p, &g_pg, psi_g))) {
+    pgx_problem_destroy(p);
+    return st;
+  }
+  ProbDev& pd = p->pd;
+  pd.D = D;
+  pd.Dp = Dp;
+  pd.n_c = nc;
+  pd.n_t = nt;
+  pd.n_members = nm;
+  pd.n_pairs = np;
+  pd.gen = d->generator;
+  pd.target = d->target;
+  pd.fid = d->fidelity;
+  pd.grad_mode = d->grad_mode;
+  pd.dt = g_dt;
+  pd.drifts = (const double2*)g_dr;
+  pd.ctrls = (const double2*)g_ct;
+  pd.offset_op = (const double2*)g_of;
+  pd.m_drift = g_md;
+  pd.m_scale = g_ms;
+  pd.m_offset = g_mo;
+  pd.m_weight = g_mw;
+  pd.target_op = (const double2*)g_tg;
+  pd.psi_init = (const double2*)g_pi;
+  pd.psi_targ = (const double2*)g_pt;
+  p->pd_grad = pd;
+  p->pd_grad.psi_init = (const double2*)g_pg;
+
+  // ---- workspace ----
+  const Sizes s = sizes_of(d, Dp, c->num_sms);
+  WorkDev& w = p->w;
+  void* ptr;
+  auto A = [&](size_t bytes) -> void* {
+    if (st) return nullptr;
+    st = ctx_alloc(c, &ptr, bytes, p->owned, p->bytes);
+    return st ? nullptr : ptr;
+  };
+  w.U = (double2*)A(s.U);
+  w.P = (double2*)A(s.P);
+  w.Utot = (double2*)A(s.Utot);
+  w.psi = (double2*)A(s.psi);
+  w.lam = (double2*)A(s.psi);
+  w.z = (double2*)A(s.z);
+  w.kap = (double2*)A(s.z);
+  w.Fm = (double*)A(s.Fm);
+  w.Gm = (double*)A(s.Gm);
+  w.slab = (double2*)A(s.slab);
+  w.slab_teams = pgx::slab_team_count(Dp, c->num_sms);
+  p->d_u = (double*)A(s.u);
+  p->d_G = (double*)A(s.G);
+  p->d_F = (double*)A(2 * sizeof(double));
+  if (st) {
+    pgx_problem_destroy(p);
+    return st;
+  }
+  if (cudaMallocHost((void**)&p->h_stage, 2 * s.u + 2 * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    pgx_problem_destroy(p);
+    return ctx_fail(c, PGX_ERR_NOMEM, "pinned staging allocation failed");
+  }
+  *out = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_problem_destroy(pgx_problem* p) {
+  if (!p) return PGX_ERR_INVALID;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  for (void* q : p->owned) cudaFree(q);
+  if (p->h_stage) cudaFreeHost(p->h_stage);
+  p->ctx->used -= p->bytes;
+  delete p;
+  return PGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// evaluation
+// ---------------------------------------------------------------------------
+// Stage marks: event i is recorded before stage i (i = 0..4) and event 5 after
+// the last stage, so stage i lasts ev[i] -> ev[i+1].
+struct Marks {
+  pgx_ctx* c;
+  std::vector<cudaEvent_t> ev;
+  explicit Marks(pgx_ctx* ctx) : c(ctx) {
+    if (!c->stage_timing) return;
+    for (int i = 0; i <= PGX_N_STAGES; ++i) {
+      cudaEvent_t e;
+      if (!c->ev_pool.empty()) { e = c->ev_pool.back(); c->ev_pool.pop_back(); }
+      else if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); ev.clear(); return; }
+      ev.push_back(e);
+    }
+  }
+  void mark(int i) {
+    if (!ev.empty()) cudaEventRecord(ev[i], c->stream);
+  }
+  void commit() {
+    if (!ev.empty()) c->stage_marks.push_back(ev);
+  }
+};
+
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
+  pgx_ctx* c = p->ctx;
+  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  WorkDev w = p->w;
+  w.u = d_u;
+  w.G = d_G ? d_G : p->d_G;
+  w.F = d_F;
+  const bool want_grad = d_G != nullptr;
+  Marks mk(c);
+  int st;
+  mk.mark(PGX_STAGE_EXPM);
+  if ((st = ctx_cuda(c, pgx::launch_expm(p->pd, w, li), "expm"))) return st;
+  mk.mark(PGX_STAGE_CHAIN_FWD);
+  if (want_grad && p->split_grad_states) {
+    // F from states_init; gradient from grad_states_init (Gradients.jl:153-157).
+    if ((st = ctx_cuda(c, pgx::launch_chain_fwd(p->pd, w, li, false), "chain_fwd(F)"))) return st;
+    if ((st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, false), "reduce(F)"))) return st;
+    WorkDev w2 = w;
+    w2.F = p->d_F + 1;  // scratch: the gradient pass's own objective
+    if ((st = ctx_cuda(c, pgx::launch_chain_fwd(p->pd_grad, w2, li, true), "chain_fwd"))) return st;
+    mk.mark(PGX_STAGE_CHAIN_BWD);
+    if ((st = ctx_cuda(c, pgx::launch_chain_bwd(p->pd_grad, w2, li), "chain_bwd"))) return st;
+    mk.mark(PGX_STAGE_GRAD);
+    if ((st = ctx_cuda(c, pgx::launch_grad(p->pd_grad, w2, li), "grad"))) return st;
+    mk.mark(PGX_STAGE_REDUCE);
+    st = ctx_cuda(c, pgx::launch_reduce(p->pd_grad, w2, li, true), "reduce");
+    mk.mark(PGX_N_STAGES);
+    mk.commit();
+    return st;
+  }
+  if ((st = ctx_cuda(c, pgx::launch_chain_fwd(p->pd, w, li, want_grad), "chain_fwd"))) return st;
+  mk.mark(PGX_STAGE_CHAIN_BWD);
+  if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd(p->pd, w, li), "chain_bwd"))) return st;
+  mk.mark(PGX_STAGE_GRAD);
+  if (want_grad && (st = ctx_cuda(c, pgx::launch_grad(p->pd, w, li), "grad"))) return st;
+  mk.mark(PGX_STAGE_REDUCE);
+  st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, want_grad), "reduce");
+  mk.mark(PGX_N_STAGES);
+  mk.commit();
+  return st;
+}
+
+extern "C" int pgx_ctx_set_stage_timing(pgx_ctx* c, int enabled) {
+  if (!c) return PGX_ERR_INVALID;
+  c->stage_timing = enabled != 0;
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_stage_times(pgx_ctx* c, double* ms, int32_t* count) {
+  if (!c || !ms || !count) return PGX_ERR_INVALID;
+  for (int i = 0; i < PGX_N_STAGES; ++i) ms[i] = 0.0;
+  int st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "stage sync");
+  if (st) return st;
+  for (auto& ev : c->stage_marks) {
+    for (int i = 0; i < PGX_N_STAGES; ++i) {
+      float f = 0.f;
+      if (cudaEventElapsedTime(&f, ev[i], ev[i + 1]) == cudaSuccess) ms[i] += f;
+      else cudaGetLastError();
+    }
+    for (cudaEvent_t e : ev) c->ev_pool.push_back(e);
+  }
+  *count = (int32_t)c->stage_marks.size();
+  c->stage_marks.clear();
+  return PGX_OK;
+}
+
+extern "C" int pgx_ctx_measure_fp64_peak(pgx_ctx* c, double* gflops) {
+  if (!c || !gflops) return PGX_ERR_INVALID;
+  cudaSetDevice(c->device);
+  double* sink = nullptr;
+  int st = ctx_cuda(c, cudaMallocAsync((void**)&sink, sizeof(double) * 64, c->stream), "alloc");
+  if (st) return st;
+  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  double best = 0.0;
+  for (int rep = 0; rep < 4 && !st; ++rep) {
+    double flops = 0.0;
+    cudaEventRecord(c->tev0, c->stream);
+    st = ctx_cuda(c, pgx::launch_fp64_peak(sink, li, &flops), "fp64 peak");
+    cudaEventRecord(c->tev1, c->stream);
+    if (!st) st = ctx_cuda(c, cudaEventSynchronize(c->tev1), "sync");
+    float ms = 0.f;
+    if (!st) cudaEventElapsedTime(&ms, c->tev0, c->tev1);
+    if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e9);
+  }
+  cudaFreeAsync(sink, c->stream);
+  cudaStreamSynchronize(c->stream);
+  *gflops = best;
+  return st;
+}
+
+int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats) {
+  pgx_ctx* c = p->ctx;
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t n = (size_t)p->desc.n_controls * p->desc.n_slices;
+  if (!finite_all(u, n)) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
+  cudaSetDevice(c->device);
+  const int64_t l0 = c->launches;
+  std::memcpy(p->h_stage, u, n * sizeof(double));
+  int st;
+  if ((st = ctx_cuda(c, cudaEventRecord(c->ev0, c->stream), "event"))) return st;
+  if ((st = ctx_cuda(c, cudaMemcpyAsync(p->d_u, p->h_stage, n * sizeof(double), cudaMemcpyHostToDevice,
+                                        c->stream), "H2D u")))
+    return st;
+  if ((st = run_pipeline(p, p->d_u, p->d_F, G ? p->d_G : nullptr))) return st;
+  double* hG = p->h_stage + n;
+  double* hF = p->h_stage + 2 * n;
+  if (G && (st = ctx_cuda(c, cudaMemcpyAsync(hG, p->d_G, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                             c->stream), "D2H G")))
+    return st;
+  if ((st = ctx_cuda(c, cudaMemcpyAsync(hF, p->d_F, sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                     "D2H F")))
+    return st;
+  if ((st = ctx_cuda(c, cudaEventRecord(c->ev1, c->stream), "event"))) return st;
+  if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "eval sync"))) return st;
+  if (G) std::memcpy(G, hG, n * sizeof(double));
+  if (F) *F = *hF;
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->ms_device = ms;
+    stats->ms_host = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    stats->units = (int64_t)p->desc.n_members * p->desc.n_slices;
+    stats->n_launches = (int32_t)(c->launches - l0);
+    stats->max_taylor_degree = 0;
+  }
+  if (!std::isfinite(*hF)) return ctx_fail(c, PGX_ERR_NONFINITE, "objective is not finite");
+  return PGX_OK;
+}
+
+extern "C" int pgx_eval(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats) {
+  if (!p || !u || !F) return PGX_ERR_INVALID;
+  return eval_host(p, u, F, G, stats);
+}
+
+extern "C" int pgx_eval_device(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
+  if (!p || !d_u || !d_F) return PGX_ERR_INVALID;
+  cudaSetDevice(p->ctx->device);
+  return run_pipeline(p, d_u, d_F, d_G);
+}
+
+extern "C" int pgx_member_fidelities(pgx_problem* p, double* F_members) {
+  if (!p || !F_members) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  int st = ctx_cuda(c, cudaMemcpyAsync(F_members, p->w.Fm, sizeof(double) * p->desc.n_members,
+                                       cudaMemcpyDeviceToHost, c->stream), "D2H Fm");
+  if (st) return st;
+  return ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+extern "C" int pgx_total_propagator(pgx_problem* p, const double* u, int32_t member, double* U_total) {
+  if (!p || !u || !U_total) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  if (member < 0 || member >= p->desc.n_members) return ctx_fail(c, PGX_ERR_INVALID, "member out of range");
+  const size_t n = (size_t)p->desc.n_controls * p->desc.n_slices;
+  if (!finite_all(u, n)) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
+  cudaSetDevice(c->device);
+  std::memcpy(p->h_stage, u, n * sizeof(double));
+  int st = ctx_cuda(c, cudaMemcpyAsync(p->d_u, p->h_stage, n * sizeof(double), cudaMemcpyHostToDevice,
+                                       c->stream), "H2D u");
+  if (st) return st;
+  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  ProbDev pd = p->pd;
+  pd.target = PGX_TARGET_GATE;  // the gate chain forms U_total for any target kind
+  pd.n_pairs = 0;
+  WorkDev w = p->w;
+  w.u = p->d_u;
+  w.F = p->d_F + 1;
+  // The gate chain writes z/kap/Fm for every member; keep those of the last
+  // evaluation intact by pointing them at scratch that is large enough.
+  if (!w.P) w.P = nullptr;
+  double2* zsave = nullptr;
+  double* fsave = nullptr;
+  const size_t zbytes = (size_t)p->desc.n_members * std::max(p->pd.n_pairs, 1) * sizeof(double2);
+  if ((st = ctx_cuda(c, cudaMallocAsync((void**)&zsave, 2 * zbytes, c->stream), "alloc scratch")) ||
+      (st = ctx_cuda(c, cudaMallocAsync((void**)&fsave, sizeof(double) * p->desc.n_members, c->stream),
+                     "alloc scratch")))
+    return st;
+  w.z = zsave;
+  w.kap = zsave + zbytes / sizeof(double2);
+  w.Fm = fsave;
+  if ((st = ctx_cuda(c, pgx::launch_expm(pd, w, li), "expm")) ||
+      (st = ctx_cuda(c, pgx::launch_chain_fwd(pd, w, li, false), "chain")))
+    return st;
+  const int D = p->desc.dim, Dp = p->Dp;
+  std::vector<double> buf((size_t)Dp * Dp * 2);
+  st = ctx_cuda(c, cudaMemcpyAsync(buf.data(), p->w.Utot + (size_t)member * Dp * Dp,
+                                   buf.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+  cudaFreeAsync(zsave, c->stream);
+  cudaFreeAsync(fsave, c->stream);
+  if (st) return st;
+  if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync"))) return st;
+  for (int col = 0; col < D; ++col)
+    for (int r = 0; r < D; ++r) {
+      U_total[2 * (r + (size_t)D * col)] = buf[2 * (r + (size_t)Dp * col)];
+      U_total[2 * (r + (size_t)D * col) + 1] = buf[2 * (r + (size_t)Dp * col) + 1];
+    }
+  return PGX_OK;
+}
+
+extern "C" int pgx_propagator(pgx_ctx* c, int32_t dim, int32_t generator, const double* gen, double dt,
+                              double* U) {
+  if (!c || !gen || !U) return PGX_ERR_INVALID;
+  if (dim < 1 || dim > pgx::kMaxDim) return ctx_fail(c, PGX_ERR_DIMS, "dim must be in [1, 64]");
+  if (generator != PGX_GEN_HERMITIAN && generator != PGX_GEN_LIOUVILLIAN)
+    return ctx_fail(c, PGX_ERR_INVALID, "unknown generator kind");
+  if (!std::isfinite(dt) || !finite_all(gen, 2 * (size_t)dim * dim))
+    return ctx_fail(c, PGX_ERR_NONFINITE, "generator and dt must be finite");
+  if (generator == PGX_GEN_HERMITIAN && herm_dev(gen, dim) > 1e-10)
+    return ctx_fail(c, PGX_ERR_INVALID, "H is not Hermitian (Propagators.jl:617-624)");
+  cudaSetDevice(c->device);
+  const int Dp = pad_dim(dim);
+  std::vector<double> g = pad_mats(gen, 1, dim, Dp);
+  const size_t mb = (size_t)Dp * Dp * sizeof(double2);
+  const size_t slab = pgx::slab_elems(Dp, c->num_sms) ? (size_t)10 * Dp * Dp * sizeof(double2) : 0;
+  double2* dbuf = nullptr;
+  int st = ctx_cuda(c, cudaMallocAsync((void**)&dbuf, 2 * mb + slab, c->stream), "alloc");
+  if (st) return st;
+  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  std::vector<double> out((size_t)Dp * Dp * 2);
+  if (!(st = ctx_cuda(c, cudaMemcpyAsync(dbuf, g.data(), mb, cudaMemcpyHostToDevice, c->stream), "H2D")) &&
+      !(st = ctx_cuda(c, pgx::launch_single_expm(Dp, generator, dbuf, dt, dbuf + Dp * Dp,
+                                                 slab ? dbuf + 2 * Dp * Dp : nullptr, li), "expm")))
+    st = ctx_cuda(c, cudaMemcpyAsync(out.data(), dbuf + Dp * Dp, mb, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  cudaFreeAsync(dbuf, c->stream);
+  int st2 = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st) return st;
+  if (st2) return st2;
+  for (int col = 0; col < dim; ++col)
+    for (int r = 0; r < dim; ++r) {
+      U[2 * (r + (size_t)dim * col)] = out[2 * (r + (size_t)Dp * col)];
+      U[2 * (r + (size_t)dim * col) + 1] = out[2 * (r + (size_t)Dp * col) + 1];
+    }
+  return PGX_OK;
+}

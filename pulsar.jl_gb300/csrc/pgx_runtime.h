@@ -1,0 +1,48 @@
+// Host-side object layouts behind the opaque handles of pgx.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "pgx.h"
+#include "pgx_internal.h"
+
+struct pgx_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;    // per-evaluation timing
+  cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // caller stopwatch
+  uint64_t budget = 0;                         // bytes, 0 = unlimited
+  uint64_t used = 0;                           // bytes held by live problems
+  int64_t launches = 0;
+  std::string err;
+  // per-stage timing (pgx_ctx_set_stage_timing)
+  bool stage_timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::vector<cudaEvent_t>> stage_marks;  // one vector of 6 events per evaluation
+};
+
+struct pgx_problem {
+  static constexpr int kMaxPairs = 8;
+  pgx_ctx* ctx = nullptr;
+  pgx_problem_desc desc{};
+  int Dp = 0;
+  pgx::ProbDev pd{};       // F pass (states_init)
+  pgx::ProbDev pd_grad{};  // gradient pass (grad_states_init)
+  bool split_grad_states = false;
+  pgx::WorkDev w{};
+  double* d_u = nullptr;
+  double* d_G = nullptr;
+  double* d_F = nullptr;   // [2]: objective, scratch
+  double* h_stage = nullptr;  // pinned: u | G | F
+  std::vector<double> h_weight;
+  std::vector<void*> owned;
+  uint64_t bytes = 0;
+};
+
+int ctx_fail(pgx_ctx* c, int status, const std::string& msg);
+int ctx_cuda(pgx_ctx* c, cudaError_t e, const char* where);
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G);
+int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats);

@@ -1,0 +1,261 @@
+"""Thin Python handles over the C ABI: ``Context`` and ``Problem``.
+
+Everything computes inside libpulsar_gb300.so; this module only marshals
+numpy arrays into the column-major interleaved buffers of include/pgx.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _abi as A
+
+
+class Context:
+    """One device, one stream, an HBM budget (0 = unlimited)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._h = C.c_void_p()
+        st = A.lib().pgx_ctx_create(int(device), int(hbm_budget), C.byref(self._h))
+        A.check(st)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            A.lib().pgx_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def hbm_used(self) -> int:
+        v = C.c_uint64()
+        A.check(A.lib().pgx_ctx_hbm_used(self._h, C.byref(v)), self._h)
+        return int(v.value)
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        A.check(A.lib().pgx_ctx_launch_count(self._h, C.byref(v)), self._h)
+        return int(v.value)
+
+    def stream(self) -> int:
+        v = C.c_void_p()
+        A.check(A.lib().pgx_ctx_stream(self._h, C.byref(v)), self._h)
+        return int(v.value or 0)
+
+    def timer_start(self):
+        A.check(A.lib().pgx_ctx_timer_start(self._h), self._h)
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        A.check(A.lib().pgx_ctx_timer_stop(self._h, C.byref(ms)), self._h)
+        return float(ms.value)
+
+    def synchronize(self):
+        A.check(A.lib().pgx_ctx_synchronize(self._h), self._h)
+
+    STAGES = ("expm", "chain_fwd", "chain_bwd", "grad", "reduce")
+
+    def set_stage_timing(self, on: bool):
+        A.check(A.lib().pgx_ctx_set_stage_timing(self._h, int(bool(on))), self._h)
+
+    def stage_times(self):
+        """({stage: summed ms}, evaluations recorded) since the last call."""
+        ms = np.zeros(len(self.STAGES))
+        n = C.c_int32()
+        A.check(A.lib().pgx_ctx_stage_times(self._h, A.as_dptr(ms), C.byref(n)), self._h)
+        return dict(zip(self.STAGES, ms.tolist())), int(n.value)
+
+    def measure_fp64_peak(self) -> float:
+        g = C.c_double()
+        A.check(A.lib().pgx_ctx_measure_fp64_peak(self._h, C.byref(g)), self._h)
+        return float(g.value)
+
+    def propagator(self, G: np.ndarray, dt: float, generator: str = "hermitian") -> np.ndarray:
+        """exp(-i G dt) (Hermitian) or exp(G dt) (Liouvillian) on the device."""
+        G = np.asarray(G, np.complex128)
+        D = G.shape[0]
+        gb = A.cmat_buf(G)
+        out = np.zeros(2 * D * D)
+        A.check(A.lib().pgx_propagator(self._h, D, A.GEN[generator], A.as_dptr(gb), float(dt),
+                                       A.as_dptr(out)), self._h)
+        return A.cmat_from_buf(out, D)
+
+
+_DEFAULT: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+@dataclass
+class OptOutcome:
+    controls: np.ndarray
+    fidelity: float
+    fidelity_history: list
+    gradient_norm_history: list
+    n_iterations: int
+    converged: bool
+    termination_reason: str
+    total_time: float
+    n_fidelity_evaluations: int
+    n_gradient_evaluations: int
+    step_size_final: float
+
+
+class Problem:
+    """An ensemble GRAPE problem resident in device memory (pgx_problem)."""
+
+    def __init__(self, drifts, controls, dt, *, ctx: Optional[Context] = None,
+                 generator: str = "hermitian", offset_op=None, member_drift=None,
+                 member_scale=None, member_offset=None, member_weight=None,
+                 target: str = "gate", fidelity: str = "square", grad_mode: str = "exact",
+                 precision: str = "fp64", target_op=None, states_init=None, states_target=None,
+                 grad_states_init=None, n_members: Optional[int] = None):
+        self.ctx = ctx or default_context()
+        drifts = np.asarray(drifts, np.complex128)
+        if drifts.ndim == 2:
+            drifts = drifts[None]
+        controls = np.asarray(controls, np.complex128)
+        dt = np.ascontiguousarray(np.asarray(dt, np.float64).ravel())
+        D = drifts.shape[-1]
+        self.D, self.n_c, self.n_t = D, controls.shape[0], dt.size
+        nm = n_members
+        for arr in (member_drift, member_scale, member_offset, member_weight):
+            if arr is not None:
+                nm = len(arr) if nm is None else nm
+        self.n_members = nm if nm is not None else 1
+        keep = {}
+
+        def buf(name, val):
+            keep[name] = val
+            return A.as_dptr(val) if val is not None else None
+
+        d = A.ProblemDesc()
+        d.struct_size = C.sizeof(A.ProblemDesc)
+        d.dim, d.n_controls, d.n_slices = D, self.n_c, self.n_t
+        d.generator, d.target = A.GEN[generator], A.TARGET[target]
+        d.fidelity, d.grad_mode, d.precision = A.FID[fidelity], A.GRAD[grad_mode], A.PREC[precision]
+        d.n_drifts, d.n_members = drifts.shape[0], self.n_members
+        d.dt = buf("dt", dt)
+        d.drifts = buf("drifts", A.cmat_buf(drifts))
+        d.controls = buf("controls", A.cmat_buf(controls))
+        d.offset_op = buf("off", None if offset_op is None else A.cmat_buf(offset_op))
+        if member_drift is not None:
+            md = np.ascontiguousarray(np.asarray(member_drift, np.int32))
+            keep["md"] = md
+            d.member_drift = md.ctypes.data_as(A.iptr)
+        for field, name, arr in (("member_scale", "ms", member_scale),
+                                 ("member_offset", "mo", member_offset),
+                                 ("member_weight", "mw", member_weight)):
+            if arr is not None:
+                setattr(d, field, buf(name, np.ascontiguousarray(np.asarray(arr, np.float64))))
+        if target == "gate":
+            d.n_pairs = 0
+            d.target_op = buf("tgt", A.cmat_buf(target_op))
+        else:
+            si = np.atleast_2d(np.asarray(states_init, np.complex128))
+            stt = np.atleast_2d(np.asarray(states_target, np.complex128))
+            d.n_pairs = si.shape[0]
+            d.states_init = buf("si", A.cvec_buf(si))
+            d.states_target = buf("st", A.cvec_buf(stt))
+            if grad_states_init is not None:
+                d.grad_states_init = buf("sg", A.cvec_buf(np.atleast_2d(
+                    np.asarray(grad_states_init, np.complex128))))
+        self.n_pairs = d.n_pairs
+        self._h = C.c_void_p()
+        A.check(A.lib().pgx_problem_create(self.ctx.handle, C.byref(d), C.byref(self._h)),
+                self.ctx.handle)
+        self._desc = d
+        self._u = np.zeros(self.n_c * self.n_t)
+        self._G = np.zeros(self.n_c * self.n_t)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            A.lib().pgx_problem_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _load_u(self, u) -> np.ndarray:
+        u = np.asarray(u, np.float64)
+        if u.shape != (self.n_c, self.n_t):
+            raise ValueError(f"controls have shape {u.shape}, expected {(self.n_c, self.n_t)}")
+        self._u[:] = u.T.ravel()   # column-major [n_c x n_t]
+        return self._u
+
+    def eval(self, u, want_grad: bool = True, stats: bool = False):
+        """(F, G[n_c, n_t]) at controls u[n_c, n_t]; G is None when not wanted."""
+        ub = self._load_u(u)
+        F = C.c_double()
+        st = A.EvalStats()
+        A.check(A.lib().pgx_eval(self._h, A.as_dptr(ub), C.byref(F),
+                                 A.as_dptr(self._G) if want_grad else None, C.byref(st)),
+                self.ctx.handle)
+        G = self._G.reshape(self.n_t, self.n_c).T.copy() if want_grad else None
+        if stats:
+            return float(F.value), G, {"ms_device": st.ms_device, "ms_host": st.ms_host,
+                                       "units": int(st.units), "n_launches": int(st.n_launches)}
+        return float(F.value), G
+
+    def eval_device(self, d_u: int, d_F: int, d_G: Optional[int]):
+        A.check(A.lib().pgx_eval_device(self._h, C.c_void_p(d_u), C.c_void_p(d_F),
+                                        C.c_void_p(d_G) if d_G else None), self.ctx.handle)
+
+    def member_fidelities(self) -> np.ndarray:
+        out = np.zeros(self.n_members)
+        A.check(A.lib().pgx_member_fidelities(self._h, A.as_dptr(out)), self.ctx.handle)
+        return out
+
+    def total_propagator(self, u, member: int = 0) -> np.ndarray:
+        ub = self._load_u(u)
+        out = np.zeros(2 * self.D * self.D)
+        A.check(A.lib().pgx_total_propagator(self._h, A.as_dptr(ub), int(member), A.as_dptr(out)),
+                self.ctx.handle)
+        return A.cmat_from_buf(out, self.D)
+
+    def optimize(self, u0, method: str, *, max_iter: int = 1000, convergence_tol: float = 1e-8,
+                 step_size: float = 0.01, adapt_step_size: bool = True, min_step_size: float = 1e-10,
+                 max_step_size: float = 10.0, gradient_norm_tol: float = 1e-6,
+                 lbfgs_memory: int = 10, amplitude_limit: float = math.inf,
+                 l_bound: float = -1.0, u_bound: float = 1.0, history_cap: int = 0) -> OptOutcome:
+        o = A.OptDesc()
+        o.struct_size = C.sizeof(A.OptDesc)
+        o.method = A.OPT[method]
+        o.max_iter, o.adapt_step_size, o.lbfgs_memory = int(max_iter), int(bool(adapt_step_size)), \
+            int(lbfgs_memory)
+        o.convergence_tol, o.step_size = float(convergence_tol), float(step_size)
+        o.min_step_size, o.max_step_size = float(min_step_size), float(max_step_size)
+        o.gradient_norm_tol, o.amplitude_limit = float(gradient_norm_tol), float(amplitude_limit)
+        o.l_bound, o.u_bound = float(l_bound), float(u_bound)
+        ub = self._load_u(u0).copy()
+        cap = history_cap or (4 * max_iter + 8)
+        fh, gh = np.zeros(cap), np.zeros(cap)
+        r = A.OptResult()
+        A.check(A.lib().pgx_optimize(self._h, C.byref(o), A.as_dptr(ub), A.as_dptr(fh),
+                                     A.as_dptr(gh), cap, C.byref(r)), self.ctx.handle)
+        n = min(r.history_len, cap)
+        n_g = min(r.gnorm_history_len, cap)
+        return OptOutcome(ub.reshape(self.n_t, self.n_c).T.copy(), float(r.fidelity),
+                          fh[:n].tolist(), gh[:n_g].tolist(),
+                          int(r.n_iterations), bool(r.converged), r.reason.decode(),
+                          float(r.total_time_s), int(r.n_fidelity_evals), int(r.n_gradient_evals),
+                          float(r.step_size_final))

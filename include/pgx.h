@@ -170,6 +170,31 @@ int pgx_total_propagator(pgx_problem* prob, const double* u, int32_t member, dou
 int pgx_propagator(pgx_ctx* ctx, int32_t dim, int32_t generator, const double* gen, double dt,
                    double* U);
 
+/* ---- allocation-free total propagator ----------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need a propagator (during CUDA-graph capture, in real-time
+ * loops that forbid allocation after start-up, or inside hosts whose device
+ * memory comes from their own pool): computes
+ *   U_total = exp(c dt_{n-1} G_{n-1}) ... exp(c dt_0 G_0),
+ * c = -i (PGX_GEN_HERMITIAN) or 1 (PGX_GEN_LIOUVILLIAN), with every piece of
+ * working memory in one static device array of PGX_NOALLOC_SCRATCH_BYTES that
+ * each GPU loading the library holds until the process exits.  It calls no
+ * cudaMalloc/cudaFree.  d_gens ([n_slices][dim*dim] complex), d_dt
+ * ([n_slices]) and d_U_total ([dim*dim] complex) are device pointers the
+ * caller owns; the work is enqueued on `stream` (cudaStream_t, NULL = legacy
+ * default stream) and is asynchronous.  Sizes whose propagator stack
+ * (n_slices * Dp^2 * 16 bytes, Dp = next power of two >= dim, plus 5 MiB of
+ * Taylor workspace when Dp = 64) exceeds the array are rejected with
+ * PGX_ERR_BUDGET and a message in err (err may be NULL).  The first call on a
+ * device sets that device up (resolves the array's address); make it before
+ * any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps race and must be serialised by the caller.  Input contents are not
+ * validated (Hermiticity, finiteness are the caller's responsibility).     */
+#define PGX_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slices,
+                                 const double* d_gens, const double* d_dt, double* d_U_total,
+                                 void* stream, char* err, size_t err_len);
+
 /* ---- optimisation ------------------------------------------------------ */
 enum { PGX_OPT_GRAPE = 0,          /* grape_optimize ascent loop (GRAPE.jl:469-643)       */
        PGX_OPT_ENSEMBLE_LBFGS = 1, /* grape_optimize_ensemble (GRAPE.jl:1012-1230)        */

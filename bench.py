@@ -59,9 +59,9 @@ def flops_per_unit(stage: str, grad_mode: str) -> float:
     return 0.0
 
 
-def workload():
+def workload(slices: int = 1000):
     from oracle import members as mb  # seeded generator of the synthetic inputs
-    return mb.spin4_ensemble()
+    return mb.spin4_ensemble(n_t=slices)
 
 
 class ClockSampler:
@@ -138,7 +138,7 @@ def cpu_baseline(prob, u0, grad_mode: str, budget_s: float = 20.0):
 def run_reference(args, rank: int):
     if rank != 0:
         return 0
-    prob, u0 = workload()
+    prob, u0 = workload(args.slices)
     from oracle import cpu_port
     cp = cpu_port.CpuProblem(prob, "ref_grape")
     threads = os.cpu_count() or 1
@@ -175,6 +175,8 @@ def main():
     ap.add_argument("--grad-mode", default="exact", choices=["exact", "ref_grape", "ref_mr"])
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slices", type=int, default=1000,
+                    help="slices per member (1000 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -195,7 +197,7 @@ def main():
     import __graft_entry__ as ge
     ge._load_builder().build()
     pg = ge.load_package()
-    prob, u0 = workload()
+    prob, u0 = workload(args.slices)
     ctx = pg.Context(local)
     di, sc, of, w = prob.members()
     p = pg.Problem(prob.drifts, prob.controls, prob.dt, ctx=ctx, offset_op=prob.offset_op,
@@ -270,7 +272,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision == "fp64" else "f32+f64",
                 "data": "synthetic (seeded)",
-                "config": {"workload": "spin4_d16_231members_1000slices", "grad_mode": args.grad_mode,
+                "config": {"workload": f"spin4_d16_231members_{prob.n_t}slices", "grad_mode": args.grad_mode,
                            "precision": args.precision, "members": prob.n_members, "slices": prob.n_t,
                            "d": D, "n_controls": N_C, "parallelism": f"replicas x{world}",
                            "l2": "working set ~1.9 GB per step >> 129 MB L2 (no flush needed)"},

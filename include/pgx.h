@@ -134,9 +134,11 @@ enum { PGX_STAGE_EXPM = 0, PGX_STAGE_CHAIN_FWD = 1, PGX_STAGE_CHAIN_BWD = 2, PGX
        PGX_STAGE_REDUCE = 4, PGX_N_STAGES = 5 };
 int pgx_ctx_set_stage_timing(pgx_ctx* ctx, int enabled);
 int pgx_ctx_stage_times(pgx_ctx* ctx, double* ms, int32_t* count);
-/* Measured peak of this device's FP64 FMA pipe (GFLOP/s), from a timed
- * dependent-free DFMA loop kernel; the roofline denominator of the FP64 path. */
-int pgx_ctx_measure_fp64_peak(pgx_ctx* ctx, double* gflops);
+/* Measured FMA peak (GFLOP/s) of one pipe of this device, from a timed loop
+ * of independent FMAs: PGX_PIPE_FP64 (the FP64 path's roofline denominator)
+ * or PGX_PIPE_FP32 (the mixed path's).                                      */
+enum { PGX_PIPE_FP64 = 0, PGX_PIPE_FP32 = 1 };
+int pgx_ctx_measure_peak(pgx_ctx* ctx, int32_t pipe, double* gflops);
 
 /* ---- problems ---------------------------------------------------------- */
 /* HBM bytes pgx_problem_create would hold for desc (admission control).    */

@@ -81,7 +81,7 @@ SIGNATURES = {
     "pgx_ctx_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "pgx_ctx_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "pgx_ctx_stage_times": (C.c_int, [C.c_void_p, dptr, C.POINTER(C.c_int32)]),
-    "pgx_ctx_measure_fp64_peak": (C.c_int, [C.c_void_p, dptr]),
+    "pgx_ctx_measure_peak": (C.c_int, [C.c_void_p, C.c_int32, dptr]),
     "pgx_problem_footprint": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(C.c_uint64)]),
     "pgx_problem_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)]),
     "pgx_problem_destroy": (C.c_int, [C.c_void_p]),

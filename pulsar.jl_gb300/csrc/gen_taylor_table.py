@@ -50,6 +50,17 @@ def main(out=sys.stdout):
     inv = ", ".join(f"{1.0 / math.factorial(k):.17g}" for k in range(max(DEGREES) + 1))
     print(f"#define PGX_N_INVFACT {max(DEGREES) + 1}", file=out)
     print(f"#define PGX_INVFACT_INIT {{{inv}}}", file=out)
+    # 1/k! as a float (FP32 Taylor) and as a double-float pair hi + lo (df Taylor)
+    import numpy as np
+    his, pairs = [], []
+    for k in range(max(DEGREES) + 1):
+        x = 1.0 / math.factorial(k)
+        hi = np.float32(x)
+        lo = np.float32(x - float(hi))
+        his.append(f"{float(hi):.9e}f")
+        pairs.append(f"{{{float(hi):.9e}f, {float(lo):.9e}f}}")
+    print(f"#define PGX_INVFACT32_INIT {{{', '.join(his)}}}", file=out)
+    print(f"#define PGX_INVFACT_DF_INIT {{{', '.join(pairs)}}}", file=out)
 
 
 if __name__ == "__main__":

@@ -64,12 +64,20 @@ cudaError_t launch_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInf
 cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad);
+// Mixed-precision stages (pgx_mixed.cu), gate targets: df expm and forward
+// chain, FP32 backward chain and gradient.  U stack holds df (float4), the P
+// stack float2.
+cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store);
+cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 // Global slab size (in double2 elements) the Dp = 64 path needs.
 size_t slab_elems(int Dp, int num_sms);
 int slab_team_count(int Dp, int num_sms);
 // Independent-DFMA loop used to measure the device's FP64 FMA rate; *flops
 // receives the floating-point operations it performs.
 cudaError_t launch_fp64_peak(double* sink, const LaunchInfo& li, double* flops);
+cudaError_t launch_fp32_peak(float* sink, const LaunchInfo& li, double* flops);
 // One propagator exp(c dt G) of a padded Dp x Dp generator (device buffers).
 cudaError_t launch_single_expm(int Dp, int gen, const double2* G, double dt, double2* U,
                                double2* slab, const LaunchInfo& li);

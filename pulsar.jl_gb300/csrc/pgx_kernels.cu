@@ -19,94 +19,9 @@
 // The exact gradient uses Tr(M L(A,E)) = Tr(L(A,M) E), valid for any
 // polynomial in A with scalar coefficients, so ONE Frechet derivative per
 // slice serves all n_c controls.
-#include "pgx_device.cuh"
-#include "pgx_internal.h"
+#include "pgx_stages.cuh"
 
 namespace pgx {
-
-__constant__ double c_invf[PGX_N_INVFACT] = PGX_INVFACT_INIT;
-__constant__ double c_theta64[PGX_N_DEGREES] = PGX_THETA64_INIT;
-
-enum { GEN_HERM = 0, GEN_LIOUV = 1 };
-enum { TGT_GATE = 0, TGT_STATES = 1 };
-enum { FID_SQUARE = 0, FID_REAL = 1, FID_MODULUS = 2 };
-enum { GRAD_REF_GRAPE = 0, GRAD_REF_MR = 1, GRAD_EXACT = 2 };
-
-template <int D> struct Cfg {
-  static constexpr int T = (D <= 8) ? 32 : 256;    // threads per team
-  static constexpr int TPC = (D <= 8) ? 4 : 1;     // teams per CTA
-  static constexpr bool SLAB = (D >= 64);          // Taylor workspace in global memory
-  static constexpr int NBUF = 10;                  // matrices of Taylor workspace
-  static constexpr int THREADS = T * TPC;
-};
-
-template <int D> constexpr size_t taylor_smem_bytes() {
-  using G = Cfg<D>;
-  return (G::SLAB ? 0 : (size_t)G::TPC * G::NBUF * D * D * sizeof(double2)) +
-         (size_t)G::TPC * G::T * sizeof(double2);
-}
-template <int D> constexpr size_t chain_smem_bytes(int n_pairs) {
-  using G = Cfg<D>;
-  // gate: two matrices; states: two n_pairs x D panels.  Plus reduction scratch.
-  const size_t mats = (size_t)2 * D * D;
-  const size_t vecs = (size_t)2 * (n_pairs > 0 ? n_pairs : 1) * D;
-  return (size_t)G::TPC * ((mats > vecs ? mats : vecs) + G::T) * sizeof(double2);
-}
-
-__device__ __forceinline__ double2 times_c(double2 v, int gen) {
-  // c = -i for a Hermitian generator, 1 for a Liouvillian.
-  if (gen == GEN_HERM) return make_double2(v.y, -v.x);
-  return v;
-}
-
-// A = c dt_k (drift + off O + scale sum_j u_jk C_j)
-template <int D, int T>
-__device__ __forceinline__ void build_A(const Team<T>& tm, const ProbDev& p, const double* u, int m,
-                                        int k, double2* A) {
-  const double dt = p.dt[k];
-  const double sc = p.m_scale[m], off = p.m_offset[m];
-  const double2* Gd = p.drifts + (size_t)p.m_drift[m] * D * D;
-  const double* uk = u + (size_t)k * p.n_c;
-  for (int e = tm.lane; e < D * D; e += T) {
-    double2 v = Gd[e];
-    const double2 o = p.offset_op[e];
-    v.x = fma(off, o.x, v.x);
-    v.y = fma(off, o.y, v.y);
-    for (int j = 0; j < p.n_c; ++j) {
-      const double a = sc * uk[j];
-      const double2 c = p.ctrls[(size_t)j * D * D + e];
-      v.x = fma(a, c.x, v.x);
-      v.y = fma(a, c.y, v.y);
-    }
-    v.x *= dt;
-    v.y *= dt;
-    A[e] = times_c(v, p.gen);
-  }
-}
-
-// f(z) and the chain-rule coefficient kappa with dF = Re(kappa dz).
-__device__ __forceinline__ void fid_kappa(double2 z, int fid, int mode, double& f, double2& kap) {
-  const double az = hypot(z.x, z.y);
-  if (fid == FID_SQUARE) {
-    f = z.x * z.x + z.y * z.y;
-    kap = make_double2(2.0 * z.x, -2.0 * z.y);
-  } else if (fid == FID_REAL) {
-    f = z.x;
-    kap = make_double2(1.0, 0.0);
-  } else {
-    f = az;
-    if (az < 1e-14) kap = make_double2(0.0, 0.0);
-    else if (mode == GRAD_EXACT) kap = make_double2(z.x / az, -z.y / az);
-    else kap = make_double2(1.0 / az, 0.0);  // Objectives.jl:356-361 uses Im(inner/|z|)
-  }
-}
-
-template <int D>
-__device__ __forceinline__ void team_slot(double2* smem, int per_team_elems, int team, double2*& base,
-                                          double2*& red) {
-  base = smem + (size_t)team * per_team_elems;
-  red = base + (per_team_elems - Cfg<D>::T);
-}
 
 // --------------------------------------------------------------------------
 // Stage 1: slice propagators
@@ -653,6 +568,28 @@ __global__ void __launch_bounds__(256) k_fp64_peak(double* sink, int iters, doub
 #pragma unroll
   for (int i = 0; i < 8; ++i) s += x[i];
   if (s == 12345.678) sink[threadIdx.x & 63] = s;
+}
+
+__global__ void __launch_bounds__(256) k_fp32_peak(float* sink, int iters, float a, float b) {
+  float x[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) x[i] = threadIdx.x * 1e-6f + i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = fmaf(x[i], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) s += x[i];
+  if (s == 12345.678f) sink[threadIdx.x & 63] = s;
+}
+
+cudaError_t launch_fp32_peak(float* sink, const LaunchInfo& li, double* flops) {
+  const int blocks = li.num_sms * 8, threads = 256, iters = 65536;
+  k_fp32_peak<<<blocks, threads, 0, li.stream>>>(sink, iters, 0.9999f, 1e-4f);
+  ++*li.launches;
+  *flops = 2.0 * 16.0 * iters * (double)blocks * threads;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fp64_peak(double* sink, const LaunchInfo& li, double* flops) {

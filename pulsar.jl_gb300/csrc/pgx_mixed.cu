@@ -1,0 +1,336 @@
+// Mixed-precision kernels (PGX_PREC_MIXED), gate targets.
+//
+// GB300 issues FP32 at 64x its FP64 rate, so the FP64 pipeline is replaced
+// stage by stage with the cheapest arithmetic that keeps the objective at
+// near-FP64 accuracy:
+//   expm       df (double-float) Paterson-Stockmeyer Taylor; degree and
+//              squarings from the FP64 1-norm and the FP64 theta table, so the
+//              truncation error stays at the FP64 level.  U stack = df (float4).
+//   chain_fwd  df products P_{k+1} = U_k P_k; the total propagator and the
+//              overlap Tr(T'U)/D are formed in FP64 from the df chain; the
+//              float rounding of P_k is stored for the gradient.
+//   chain_bwd  FP32: Lambda <- Lambda U_k, M_k = P_k Lambda (only the
+//              gradient depends on it).
+//   grad       FP32 Frechet derivative L(A_k, M_k) (degree from the FP32 theta
+//              table) and traces; results accumulated as FP64.
+// F therefore carries df (~1e-13 per product) rounding; G carries FP32
+// (~1e-6 relative) rounding.
+#include "pgx_df.cuh"
+#include "pgx_stages.cuh"
+
+namespace pgx {
+
+static __constant__ df c_dfcoef[PGX_N_INVFACT] = PGX_INVFACT_DF_INIT;
+
+// ---- expm in df --------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* smem = reinterpret_cast<float4*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  float4 *base, *red;
+  if constexpr (G::SLAB) {
+    base = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * G::NBUF * D * D;
+    red = smem + (size_t)team * T;
+  } else {
+    base = smem + (size_t)team * G::NBUF * D * D;
+    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * T;
+  }
+  float4* B = base;
+  float4* B2 = base + D * D;
+  float4* B3 = base + 2 * D * D;
+  float4* B4 = base + 3 * D * D;
+  float4* Y = base + 4 * D * D;
+  const long items = (long)p.n_members * p.n_t;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
+    double2* Ad = reinterpret_cast<double2*>(B);  // FP64 assembly in the same bytes
+    build_A<D, T>(tm, p, w.u, m, k, Ad);
+    tm.sync();
+    const double nrm = norm1<D, T>(tm, Ad, reinterpret_cast<double*>(red));
+    int deg, s;
+    choose_degree(nrm, c_theta64, deg, s);
+    const double sc = ldexp(1.0, -s);
+    for (int e = tm.lane; e < D * D; e += T) {  // each lane converts the entries it built
+      const double2 a = Ad[e];
+      B[e] = dfc_store(dfc_from(make_double2(a.x * sc, a.y * sc)));
+    }
+    tm.sync();
+    taylor_exp_df<D, T>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
+    float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
+    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[e];
+    tm.sync();
+  }
+}
+
+// ---- forward chain in df -------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_fwd_mx(ProbDev p, WorkDev w, int store) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  constexpr int NE = (D * D + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* smem = reinterpret_cast<float4*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  float4* Pc = smem + (size_t)team * (2 * D * D + T);
+  float4* Ub = Pc + D * D;
+  double2* red = reinterpret_cast<double2*>(Ub + D * D);
+  for (int e = tm.lane; e < D * D; e += T)
+    Pc[e] = make_float4((e % D) == (e / D) ? 1.f : 0.f, 0.f, 0.f, 0.f);
+  const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+  float2* Pst = reinterpret_cast<float2*>(w.P) + (size_t)m * p.n_t * D * D;
+  float4 pre[NE];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = tm.lane + i * T;
+    if (e < D * D) pre[i] = Um[e];
+  }
+  tm.sync();
+  for (int k = 0; k < p.n_t; ++k) {
+    if (store)
+      for (int e = tm.lane; e < D * D; e += T) Pst[(size_t)k * D * D + e] = make_float2(Pc[e].x, Pc[e].y);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      const int e = tm.lane + i * T;
+      if (e < D * D) Ub[e] = pre[i];
+    }
+    if (k + 1 < p.n_t) {
+      const float4* nx = Um + (size_t)(k + 1) * D * D;
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        const int e = tm.lane + i * T;
+        if (e < D * D) pre[i] = nx[e];
+      }
+    }
+    tm.sync();
+    mm1_df<D, T>(tm, Pc, Ub, Pc);
+  }
+  double2* Ut = w.Utot + (size_t)m * D * D;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int e = tm.lane; e < D * D; e += T) {
+    const double2 v = dfc_to(dfc_load(Pc[e]));
+    Ut[e] = v;
+    acc = cmac_cj(acc, p.target_op[e], v);
+  }
+  double2 z = team_sum<T>(tm, acc, red);
+  if (tm.lane == 0) {
+    z.x /= p.D;
+    z.y /= p.D;
+    double f;
+    double2 kap;
+    fid_kappa(z, p.fid, p.grad_mode, f, kap);
+    const double sc = p.m_weight[m] / p.D;
+    w.z[m] = z;
+    w.kap[m] = make_double2(kap.x * sc, kap.y * sc);
+    w.Fm[m] = f;
+  }
+}
+
+// ---- backward chain in FP32 -------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* smem = reinterpret_cast<float2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  float2* Lam = smem + (size_t)team * 2 * D * D;
+  float2* Buf = Lam + D * D;
+  const double2 kap = w.kap[m];
+  for (int e = tm.lane; e < D * D; e += T) {
+    const int r = e % D, c = e / D;
+    const double2 t = p.target_op[c + D * r];
+    const double2 v = cmul(kap, make_double2(t.x, -t.y));
+    Lam[e] = make_float2((float)v.x, (float)v.y);
+  }
+  tm.sync();
+  const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+  float2* Pm = reinterpret_cast<float2*>(w.P) + (size_t)m * p.n_t * D * D;
+  const bool grape = (p.grad_mode == GRAD_REF_GRAPE);
+  for (int k = p.n_t - 1; k >= 0; --k) {
+    if (grape) {
+      for (int e = tm.lane; e < D * D; e += T) {
+        const float4 u = Um[(size_t)k * D * D + e];
+        Buf[e] = make_float2(u.x, u.y);
+      }
+      tm.sync();
+      mm1<D, T>(tm, Lam, Lam, Buf);
+    }
+    for (int e = tm.lane; e < D * D; e += T) Buf[e] = Pm[(size_t)k * D * D + e];
+    tm.sync();
+    mm1<D, T>(tm, Pm + (size_t)k * D * D, Buf, Lam);
+    if (!grape) {
+      for (int e = tm.lane; e < D * D; e += T) {
+        const float4 u = Um[(size_t)k * D * D + e];
+        Buf[e] = make_float2(u.x, u.y);
+      }
+      tm.sync();
+      mm1<D, T>(tm, Lam, Lam, Buf);
+    }
+  }
+}
+
+// ---- gradient in FP32 -----------------------------------------------------------
+template <int D, int T>
+__device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDev& p, const float2* X,
+                                                 int m, int k, double* Gout, float2* red) {
+  const double cds = p.dt[k] * p.m_scale[m];
+  for (int j = 0; j < p.n_c; ++j) {
+    const double2* Cj = p.ctrls + (size_t)j * D * D;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int e = tm.lane; e < D * D; e += T) {
+      const int r = e % D, c = e / D;
+      const double2 cv = Cj[c + D * r];
+      acc = cmac(acc, X[e], make_float2((float)cv.x, (float)cv.y));
+    }
+    const float2 t = team_sum<T>(tm, acc, red);
+    if (tm.lane == 0) Gout[j] = cds * (double)(p.gen == GEN_HERM ? t.y : t.x);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_grad_gate_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* smem = reinterpret_cast<float2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  float2 *base, *red;
+  if constexpr (G::SLAB) {
+    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * G::NBUF * D * D;
+    red = smem + (size_t)team * 2 * T;
+  } else {
+    base = smem + (size_t)team * G::NBUF * D * D;
+    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * 2 * T;
+  }
+  const Work<float2, D> W = Work<float2, D>::at(base);
+  const bool exact = (p.grad_mode == GRAD_EXACT);
+  const long items = (long)p.n_members * p.n_t;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
+    double* Gout = w.Gm + ((size_t)m * p.n_t + k) * p.n_c;
+    const float2* Mk = reinterpret_cast<const float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
+    if (!exact) {
+      trace_controls32<D, T>(tm, p, Mk, m, k, Gout, red);
+      continue;
+    }
+    for (int e = tm.lane; e < D * D; e += T) W.dB[e] = Mk[e];
+    build_A<D, T>(tm, p, w.u, m, k, W.B);
+    tm.sync();
+    const double nrm = norm1<D, T>(tm, W.B, reinterpret_cast<double*>(red));
+    int deg, s;
+    choose_degree(nrm, c_theta32, deg, s);
+    const float sc = ldexpf(1.f, -s);
+    for (int e = tm.lane; e < D * D; e += T) {
+      W.B[e] = cscale(W.B[e], sc);
+      W.dB[e] = cscale(W.dB[e], sc);
+    }
+    tm.sync();
+    taylor_exp_frechet<D, T>(tm, W, deg, s, c_invf32);
+    trace_controls32<D, T>(tm, p, W.dY, m, k, Gout, red);
+    tm.sync();
+  }
+}
+
+// ---- launchers ---------------------------------------------------------------------
+template <class K>
+static void ensure_smem_mx(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class K>
+static int grid_for(K kernel, int threads, size_t smem, long teams, int tpc, int num_sms, int cap) {
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  long blocks = (teams + tpc - 1) / tpc;
+  const long maxb = (long)num_sms * per_sm;
+  if (blocks > maxb) blocks = maxb;
+  if (cap > 0 && blocks > cap) blocks = cap;
+  return blocks < 1 ? 1 : (int)blocks;
+}
+
+#define PGX_DISPATCH_MX(DP, CALL)                     \
+  switch (DP) {                                       \
+    case 2: { constexpr int D_ = 2; CALL; } break;    \
+    case 4: { constexpr int D_ = 4; CALL; } break;    \
+    case 8: { constexpr int D_ = 8; CALL; } break;    \
+    case 16: { constexpr int D_ = 16; CALL; } break;  \
+    case 32: { constexpr int D_ = 32; CALL; } break;  \
+    case 64: { constexpr int D_ = 64; CALL; } break;  \
+    default: return cudaErrorInvalidValue;            \
+  }
+
+template <int D>
+static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = taylor_smem_bytes<D>();  // float4 and double2 are both 16 B
+  ensure_smem_mx(k_expm_mx<D>, smem);
+  const int grid = grid_for(k_expm_mx<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC, li.num_sms,
+                            G::SLAB ? w.slab_teams : 0);
+  k_expm_mx<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH_MX(p.Dp, return do_expm_mx<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
+  using G = Cfg<D>;
+  const size_t smem = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
+  ensure_smem_mx(k_chain_gate_fwd_mx<D>, smem);
+  k_chain_gate_fwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w, store);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
+  PGX_DISPATCH_MX(p.Dp, return do_chain_fwd_mx<D_>(p, w, li, store));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = (size_t)G::TPC * 2 * D * D * sizeof(float2);
+  ensure_smem_mx(k_chain_gate_bwd_mx<D>, smem);
+  k_chain_gate_bwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH_MX(p.Dp, return do_chain_bwd_mx<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+template <int D>
+static cudaError_t do_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem = (G::SLAB ? 0 : (size_t)G::TPC * G::NBUF * D * D * sizeof(float2)) +
+                      (size_t)G::TPC * 2 * G::T * sizeof(float2);
+  ensure_smem_mx(k_grad_gate_mx<D>, smem);
+  const int grid = grid_for(k_grad_gate_mx<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
+                            li.num_sms, G::SLAB ? w.slab_teams : 0);
+  k_grad_gate_mx<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  PGX_DISPATCH_MX(p.Dp, return do_grad_mx<D_>(p, w, li));
+  return cudaSuccess;
+}
+
+}  // namespace pgx

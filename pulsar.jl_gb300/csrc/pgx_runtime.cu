@@ -225,6 +225,8 @@ static int validate(pgx_ctx* c, const pgx_problem_desc* d) {
     return ctx_fail(c, PGX_ERR_INVALID, "unknown gradient mode");
   if (d->precision != PGX_PREC_FP64 && d->precision != PGX_PREC_MIXED)
     return ctx_fail(c, PGX_ERR_INVALID, "unknown precision mode");
+  if (d->precision == PGX_PREC_MIXED && d->target != PGX_TARGET_GATE)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "mixed precision serves gate targets; use FP64 for state targets");
   if (!d->dt || !d->drifts || !d->controls)
     return ctx_fail(c, PGX_ERR_INVALID, "dt, drifts and controls are required");
   const size_t DD = (size_t)d->dim * d->dim;
@@ -515,6 +517,21 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
   const bool want_grad = d_G != nullptr;
   Marks mk(c);
   int st;
+  if (p->desc.precision == PGX_PREC_MIXED) {  // gate targets (validated at create)
+    mk.mark(PGX_STAGE_EXPM);
+    if ((st = ctx_cuda(c, pgx::launch_expm_mx(p->pd, w, li), "expm_mx"))) return st;
+    mk.mark(PGX_STAGE_CHAIN_FWD);
+    if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, want_grad), "chain_fwd_mx"))) return st;
+    mk.mark(PGX_STAGE_CHAIN_BWD);
+    if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd, w, li), "chain_bwd_mx"))) return st;
+    mk.mark(PGX_STAGE_GRAD);
+    if (want_grad && (st = ctx_cuda(c, pgx::launch_grad_mx(p->pd, w, li), "grad_mx"))) return st;
+    mk.mark(PGX_STAGE_REDUCE);
+    st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, want_grad), "reduce");
+    mk.mark(PGX_N_STAGES);
+    mk.commit();
+    return st;
+  }
   mk.mark(PGX_STAGE_EXPM);
   if ((st = ctx_cuda(c, pgx::launch_expm(p->pd, w, li), "expm"))) return st;
   mk.mark(PGX_STAGE_CHAIN_FWD);
@@ -571,8 +588,8 @@ extern "C" int pgx_ctx_stage_times(pgx_ctx* c, double* ms, int32_t* count) {
   return PGX_OK;
 }
 
-extern "C" int pgx_ctx_measure_fp64_peak(pgx_ctx* c, double* gflops) {
-  if (!c || !gflops) return PGX_ERR_INVALID;
+extern "C" int pgx_ctx_measure_peak(pgx_ctx* c, int32_t pipe, double* gflops) {
+  if (!c || !gflops || (pipe != PGX_PIPE_FP64 && pipe != PGX_PIPE_FP32)) return PGX_ERR_INVALID;
   cudaSetDevice(c->device);
   double* sink = nullptr;
   int st = ctx_cuda(c, cudaMallocAsync((void**)&sink, sizeof(double) * 64, c->stream), "alloc");
@@ -582,7 +599,8 @@ extern "C" int pgx_ctx_measure_fp64_peak(pgx_ctx* c, double* gflops) {
   for (int rep = 0; rep < 4 && !st; ++rep) {
     double flops = 0.0;
     cudaEventRecord(c->tev0, c->stream);
-    st = ctx_cuda(c, pgx::launch_fp64_peak(sink, li, &flops), "fp64 peak");
+    st = ctx_cuda(c, pipe == PGX_PIPE_FP64 ? pgx::launch_fp64_peak(sink, li, &flops)
+                                           : pgx::launch_fp32_peak((float*)sink, li, &flops), "peak");
     cudaEventRecord(c->tev1, c->stream);
     if (!st) st = ctx_cuda(c, cudaEventSynchronize(c->tev1), "sync");
     float ms = 0.f;

@@ -76,9 +76,10 @@ class Context:
         A.check(A.lib().pgx_ctx_stage_times(self._h, A.as_dptr(ms), C.byref(n)), self._h)
         return dict(zip(self.STAGES, ms.tolist())), int(n.value)
 
-    def measure_fp64_peak(self) -> float:
+    def measure_peak(self, pipe: str = "fp64") -> float:
+        """Measured FMA peak of the FP64 or FP32 pipe, GFLOP/s."""
         g = C.c_double()
-        A.check(A.lib().pgx_ctx_measure_fp64_peak(self._h, C.byref(g)), self._h)
+        A.check(A.lib().pgx_ctx_measure_peak(self._h, {"fp64": 0, "fp32": 1}[pipe], C.byref(g)), self._h)
         return float(g.value)
 
     def propagator(self, G: np.ndarray, dt: float, generator: str = "hermitian") -> np.ndarray:

@@ -172,6 +172,15 @@ int pgx_total_propagator(pgx_problem* prob, const double* u, int32_t member, dou
 int pgx_propagator(pgx_ctx* ctx, int32_t dim, int32_t generator, const double* gen, double dt,
                    double* U);
 
+/* ---- autotuning --------------------------------------------------------- */
+/* Times every team-size variant (threads per matrix problem, with the
+ * matching register blocking) of the problem's slice-parallel mixed-precision
+ * kernels at controls u, `reps` launches each, keeps the fastest for this
+ * problem and writes a one-line report (nullable).  Variants only re-map work
+ * to threads; every dot product is summed in the same order, so results are
+ * bit-identical whatever is chosen.  The FP64 path has no variants.         */
+int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report, size_t report_len);
+
 /* ---- allocation-free total propagator ----------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need a propagator (during CUDA-graph capture, in real-time

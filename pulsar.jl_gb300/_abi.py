@@ -90,6 +90,7 @@ SIGNATURES = {
     "pgx_member_fidelities": (C.c_int, [C.c_void_p, dptr]),
     "pgx_total_propagator": (C.c_int, [C.c_void_p, dptr, C.c_int32, dptr]),
     "pgx_propagator": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.c_double, dptr]),
+    "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
     "pgx_total_propagator_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
                                                C.c_size_t]),

@@ -43,10 +43,18 @@ template <class C> __device__ __forceinline__ C cmul(C a, C b) { return cmac(cze
 template <class C, class R> __device__ __forceinline__ C cscale(C a, R s) { a.x *= s; a.y *= s; return a; }
 template <class C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
 
+// A team synchronises with __syncwarp (T <= 32) or with hardware barrier
+// `bar` over its T threads (bar = 0 and T = blockDim is __syncthreads; several
+// multi-warp teams in one CTA use barriers 1, 2, ...).
 template <int T> struct Team {
   int lane;
+  int bar = 0;
   __device__ __forceinline__ void sync() const {
-    if constexpr (T <= 32) __syncwarp(); else __syncthreads();
+    if constexpr (T <= 32) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(T) : "memory");
+    }
   }
 };
 
@@ -54,33 +62,74 @@ struct EpiNone {
   template <class C> __device__ __forceinline__ C operator()(int, int, int, C s) const { return s; }
 };
 
-// out = A1*B1 (+ A2*B2 when TWO) then epi(e, r, c, value).
+// Register blocking of a D x D product over T lanes: each lane owns an RB x CB
+// block of outputs (rows rb*RB.., columns cb*CB..).  With one output per lane
+// (RB = CB = 1) lanes beyond D*D idle.
+template <int D, int T> struct Blocking {
+  static constexpr int NE = (D * D >= T) ? D * D / T : 1;
+  static constexpr int RB = (NE >= 2 && D % 2 == 0) ? 2 : 1;
+  static constexpr int CB = NE / RB;
+  static constexpr int NR = D / RB;               // row blocks
+  static constexpr int ACTIVE = NR * (D / CB);    // lanes with work
+  static_assert(RB * CB == NE, "blocking");
+  static_assert(D * D >= T ? ACTIVE == T : ACTIVE == D * D, "blocking covers the matrix");
+};
+
+// out = A1*B1 (+ A2*B2 when TWO) then epi(e, r, c, value); out may alias any
+// input (outputs are staged in registers across a team barrier).
 template <int D, int T, bool TWO, class C, class Epi>
 __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const C* B1,
                                    const C* A2, const C* B2, Epi epi) {
-  constexpr int NE = (D * D + T - 1) / T;
-  C acc[NE];
+  using BK = Blocking<D, T>;
+  constexpr int RB = BK::RB, CB = BK::CB;
+  const bool active = tm.lane < BK::ACTIVE;
+  const int r0 = (tm.lane % BK::NR) * RB, c0 = (tm.lane / BK::NR) * CB;
+  C acc[RB][CB];
 #pragma unroll
-  for (int i = 0; i < NE; ++i) {
-    const int e = tm.lane + i * T;
-    C s = czero<C>();
-    if (e < D * D) {
-      const int r = e % D, c = e / D;
-#pragma unroll 8
-      for (int k = 0; k < D; ++k) s = cmac(s, A1[r + D * k], B1[k + D * c]);
-      if constexpr (TWO) {
-#pragma unroll 8
-        for (int k = 0; k < D; ++k) s = cmac(s, A2[r + D * k], B2[k + D * c]);
-      }
-      s = epi(e, r, c, s);
+  for (int i = 0; i < RB; ++i)
+#pragma unroll
+    for (int j = 0; j < CB; ++j) acc[i][j] = czero<C>();
+  if (active) {
+#pragma unroll 4
+    for (int k = 0; k < D; ++k) {
+      C a[RB], b[CB];
+#pragma unroll
+      for (int i = 0; i < RB; ++i) a[i] = A1[r0 + i + D * k];
+#pragma unroll
+      for (int j = 0; j < CB; ++j) b[j] = B1[k + D * (c0 + j)];
+#pragma unroll
+      for (int i = 0; i < RB; ++i)
+#pragma unroll
+        for (int j = 0; j < CB; ++j) acc[i][j] = cmac(acc[i][j], a[i], b[j]);
     }
-    acc[i] = s;
+    if constexpr (TWO) {
+#pragma unroll 4
+      for (int k = 0; k < D; ++k) {
+        C a[RB], b[CB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) a[i] = A2[r0 + i + D * k];
+#pragma unroll
+        for (int j = 0; j < CB; ++j) b[j] = B2[k + D * (c0 + j)];
+#pragma unroll
+        for (int i = 0; i < RB; ++i)
+#pragma unroll
+          for (int j = 0; j < CB; ++j) acc[i][j] = cmac(acc[i][j], a[i], b[j]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int r = r0 + i, c = c0 + j;
+        acc[i][j] = epi(r + D * c, r, c, acc[i][j]);
+      }
   }
   tm.sync();
+  if (active) {
 #pragma unroll
-  for (int i = 0; i < NE; ++i) {
-    const int e = tm.lane + i * T;
-    if (e < D * D) out[e] = acc[i];
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) out[r0 + i + D * (c0 + j)] = acc[i][j];
   }
   tm.sync();
 }
@@ -107,13 +156,13 @@ __device__ __forceinline__ C team_sum(const Team<T>& tm, C v, C* scratch) {
     return v;
   } else {
     scratch[tm.lane] = v;
-    __syncthreads();
+    tm.sync();
     for (int w = T / 2; w > 0; w >>= 1) {
       if (tm.lane < w) scratch[tm.lane] = cadd(scratch[tm.lane], scratch[tm.lane + w]);
-      __syncthreads();
+      tm.sync();
     }
     C r = scratch[0];
-    __syncthreads();
+    tm.sync();
     return r;
   }
 }
@@ -126,13 +175,13 @@ __device__ __forceinline__ double team_max(const Team<T>& tm, double v, double* 
     return v;
   } else {
     scratch[tm.lane] = v;
-    __syncthreads();
+    tm.sync();
     for (int w = T / 2; w > 0; w >>= 1) {
       if (tm.lane < w) scratch[tm.lane] = fmax(scratch[tm.lane], scratch[tm.lane + w]);
-      __syncthreads();
+      tm.sync();
     }
     double r = scratch[0];
-    __syncthreads();
+    tm.sync();
     return r;
   }
 }

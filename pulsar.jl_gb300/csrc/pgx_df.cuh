@@ -95,8 +95,8 @@ struct DfAcc {
   }
   __device__ __forceinline__ dfc result() const {
     dfc r;
-    fast_two_sum(sr, cr, r.re.hi, r.re.lo);
-    fast_two_sum(si, ci, r.im.hi, r.im.lo);
+    two_sum(sr, cr, r.re.hi, r.re.lo);
+    two_sum(si, ci, r.im.hi, r.im.lo);
     return r;
   }
 };
@@ -109,30 +109,53 @@ struct DfEpiNone {
 template <int D, int T, bool TWO, class Epi>
 __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const float4* A1, const float4* B1,
                                       const float4* A2, const float4* B2, Epi epi) {
-  constexpr int NE = (D * D + T - 1) / T;
-  float4 acc[NE];
+  using BK = Blocking<D, T>;
+  constexpr int RB = BK::RB, CB = BK::CB;
+  const bool active = tm.lane < BK::ACTIVE;
+  const int r0 = (tm.lane % BK::NR) * RB, c0 = (tm.lane / BK::NR) * CB;
+  DfAcc acc[RB][CB];
+  float4 res[RB][CB];
+  if (active) {
+#pragma unroll 2
+    for (int k = 0; k < D; ++k) {
+      float4 a[RB], b[CB];
 #pragma unroll
-  for (int i = 0; i < NE; ++i) {
-    const int e = tm.lane + i * T;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (e < D * D) {
-      const int r = e % D, c = e / D;
-      DfAcc a;
-#pragma unroll 4
-      for (int k = 0; k < D; ++k) a.mac(A1[r + D * k], B1[k + D * c]);
-      if constexpr (TWO) {
-#pragma unroll 4
-        for (int k = 0; k < D; ++k) a.mac(A2[r + D * k], B2[k + D * c]);
-      }
-      v = dfc_store(epi(e, r, c, a.result()));
+      for (int i = 0; i < RB; ++i) a[i] = A1[r0 + i + D * k];
+#pragma unroll
+      for (int j = 0; j < CB; ++j) b[j] = B1[k + D * (c0 + j)];
+#pragma unroll
+      for (int i = 0; i < RB; ++i)
+#pragma unroll
+        for (int j = 0; j < CB; ++j) acc[i][j].mac(a[i], b[j]);
     }
-    acc[i] = v;
+    if constexpr (TWO) {
+#pragma unroll 2
+      for (int k = 0; k < D; ++k) {
+        float4 a[RB], b[CB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) a[i] = A2[r0 + i + D * k];
+#pragma unroll
+        for (int j = 0; j < CB; ++j) b[j] = B2[k + D * (c0 + j)];
+#pragma unroll
+        for (int i = 0; i < RB; ++i)
+#pragma unroll
+          for (int j = 0; j < CB; ++j) acc[i][j].mac(a[i], b[j]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int r = r0 + i, c = c0 + j;
+        res[i][j] = dfc_store(epi(r + D * c, r, c, acc[i][j].result()));
+      }
   }
   tm.sync();
+  if (active) {
 #pragma unroll
-  for (int i = 0; i < NE; ++i) {
-    const int e = tm.lane + i * T;
-    if (e < D * D) out[e] = acc[i];
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) out[r0 + i + D * (c0 + j)] = res[i][j];
   }
   tm.sync();
 }

@@ -50,11 +50,21 @@ struct WorkDev {
   double* F;        // [1]
 };
 
+// Tunable kernels: their team size (threads per matrix problem) is chosen per
+// problem by pgx_autotune; 0 = the built-in default for the dimension.
+enum { kTuneExpmMx = 0, kTuneGradMx = 1, kNumTunable = 2 };
+
 struct LaunchInfo {
   int num_sms;
   cudaStream_t stream;
   int64_t* launches;   // counter incremented per kernel launch
+  int team[kNumTunable] = {0, 0};
 };
+
+// Team sizes the mixed slice-parallel kernels admit at padded dimension Dp
+// (writes up to 4 values, returns the count), and the default choice.
+int mixed_variants(int Dp, int* out);
+int mixed_default_team(int Dp, int kernel);
 
 // Stage launchers (pgx_kernels.cu).  Each returns cudaGetLastError() after
 // launching on li.stream.

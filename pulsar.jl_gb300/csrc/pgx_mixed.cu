@@ -22,23 +22,44 @@ namespace pgx {
 
 static __constant__ df c_dfcoef[PGX_N_INVFACT] = PGX_INVFACT_DF_INIT;
 
+// Teams of the slice-parallel mixed kernels.  A team of T threads owns one
+// matrix problem; a CTA holds 256 / T teams (T = 32: independent warps on
+// __syncwarp; 64 and 128: hardware barriers 1..; 256: the whole CTA).  Each
+// lane owns an RB x CB block of every product (Blocking<D, T>).  The
+// workspace is 80 bytes x D^2 per team (five df matrices for the propagator,
+// ten complex-float ones for the gradient), in shared memory up to D = 32 and
+// in a per-CTA global slab at D = 64.  The best T depends on the kernel and on
+// D (occupancy against barrier waits); pgx_autotune picks it per problem.  All
+// variants sum every dot product in the same order: results are identical.
+template <int D, int T> struct CfgM {
+  static constexpr bool SLAB = (D >= 64);
+  static constexpr int TPC = (T >= 256) ? 1 : 256 / T;
+  static constexpr int THREADS = T * TPC;
+  static constexpr size_t WS = (size_t)80 * D * D;                 // workspace bytes per team
+  static constexpr size_t RED = (size_t)2 * T * sizeof(float2);    // reduction scratch per team
+  static constexpr size_t SMEM = (SLAB ? 0 : TPC * WS) + TPC * RED;
+};
+
+template <int D, int T>
+__device__ __forceinline__ Team<T> team_of() {
+  Team<T> tm{(int)(threadIdx.x % T)};
+  tm.bar = (T > 32 && CfgM<D, T>::TPC > 1) ? 1 + (int)(threadIdx.x / T) : 0;
+  return tm;
+}
+
 // ---- expm in df --------------------------------------------------------------
-template <int D>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
-  using G = Cfg<D>;
-  constexpr int T = G::T;
+template <int D, int T>
+__global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
+  using G = CfgM<D, T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float4* smem = reinterpret_cast<float4*>(smem_raw);
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
-  float4 *base, *red;
-  if constexpr (G::SLAB) {
-    base = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * G::NBUF * D * D;
-    red = smem + (size_t)team * T;
-  } else {
-    base = smem + (size_t)team * G::NBUF * D * D;
-    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * T;
-  }
+  const Team<T> tm = team_of<D, T>();
+  float4* base;
+  if constexpr (G::SLAB)
+    base = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * 10 * D * D;
+  else
+    base = reinterpret_cast<float4*>(smem_raw + (size_t)team * G::WS);
+  float4* red = reinterpret_cast<float4*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WS) + (size_t)team * G::RED);
   float4* B = base;
   float4* B2 = base + D * D;
   float4* B3 = base + 2 * D * D;
@@ -180,39 +201,45 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd_mx(ProbDev p
 }
 
 // ---- gradient in FP32 -----------------------------------------------------------
+// g_j = Re(c dt scale Tr(X C_j)).  The team's first warp sums in a fixed order
+// (stride-32 partial sums, then a fixed shuffle tree) so that the result does
+// not depend on the team size the autotuner picks.
 template <int D, int T>
 __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDev& p, const float2* X,
-                                                 int m, int k, double* Gout, float2* red) {
+                                                 int m, int k, double* Gout, float2*) {
   const double cds = p.dt[k] * p.m_scale[m];
-  for (int j = 0; j < p.n_c; ++j) {
-    const double2* Cj = p.ctrls + (size_t)j * D * D;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int e = tm.lane; e < D * D; e += T) {
-      const int r = e % D, c = e / D;
-      const double2 cv = Cj[c + D * r];
-      acc = cmac(acc, X[e], make_float2((float)cv.x, (float)cv.y));
+  if (tm.lane < 32) {
+    for (int j = 0; j < p.n_c; ++j) {
+      const double2* Cj = p.ctrls + (size_t)j * D * D;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int e = tm.lane; e < D * D; e += 32) {
+        const int r = e % D, c = e / D;
+        const double2 cv = Cj[c + D * r];
+        acc = cmac(acc, X[e], make_float2((float)cv.x, (float)cv.y));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      }
+      if (tm.lane == 0) Gout[j] = cds * (double)(p.gen == GEN_HERM ? acc.y : acc.x);
     }
-    const float2 t = team_sum<T>(tm, acc, red);
-    if (tm.lane == 0) Gout[j] = cds * (double)(p.gen == GEN_HERM ? t.y : t.x);
   }
+  tm.sync();
 }
 
-template <int D>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_grad_gate_mx(ProbDev p, WorkDev w) {
-  using G = Cfg<D>;
-  constexpr int T = G::T;
+template <int D, int T>
+__global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p, WorkDev w) {
+  using G = CfgM<D, T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* smem = reinterpret_cast<float2*>(smem_raw);
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
-  float2 *base, *red;
-  if constexpr (G::SLAB) {
-    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * G::NBUF * D * D;
-    red = smem + (size_t)team * 2 * T;
-  } else {
-    base = smem + (size_t)team * G::NBUF * D * D;
-    red = smem + (size_t)G::TPC * G::NBUF * D * D + (size_t)team * 2 * T;
-  }
+  const Team<T> tm = team_of<D, T>();
+  float2* base;
+  if constexpr (G::SLAB)
+    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * 10 * D * D;
+  else
+    base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WS);
+  float2* red = reinterpret_cast<float2*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WS) + (size_t)team * G::RED);
   const Work<float2, D> W = Work<float2, D>::at(base);
   const bool exact = (p.grad_mode == GRAD_EXACT);
   const long items = (long)p.n_members * p.n_t;
@@ -272,19 +299,57 @@ static int grid_for(K kernel, int threads, size_t smem, long teams, int tpc, int
     default: return cudaErrorInvalidValue;            \
   }
 
-template <int D>
+// Team sizes each D admits (register budget of the blocked df products).
+static int variants_for(int Dp, int* out) {
+  int n = 0;
+  if (Dp <= 8) out[n++] = 32;
+  else if (Dp == 16) { out[n++] = 32; out[n++] = 64; out[n++] = 128; out[n++] = 256; }
+  else if (Dp == 32) { out[n++] = 128; out[n++] = 256; }
+  else out[n++] = 256;
+  return n;
+}
+int mixed_variants(int Dp, int* out) { return variants_for(Dp, out); }
+int mixed_default_team(int Dp, int kernel) {
+  if (Dp == 16) return kernel == kTuneExpmMx ? 256 : 32;
+  if (Dp == 32) return 256;
+  return Dp <= 8 ? 32 : 256;
+}
+
+#define PGX_DISPATCH_MX_T(DP, TT, CALL)                                                        \
+  switch (DP) {                                                                                \
+    case 2: { constexpr int D_ = 2, T_ = 32; CALL; } break;                                   \
+    case 4: { constexpr int D_ = 4, T_ = 32; CALL; } break;                                   \
+    case 8: { constexpr int D_ = 8, T_ = 32; CALL; } break;                                   \
+    case 16:                                                                                   \
+      switch (TT) {                                                                            \
+        case 32: { constexpr int D_ = 16, T_ = 32; CALL; } break;                             \
+        case 64: { constexpr int D_ = 16, T_ = 64; CALL; } break;                             \
+        case 128: { constexpr int D_ = 16, T_ = 128; CALL; } break;                           \
+        default: { constexpr int D_ = 16, T_ = 256; CALL; } break;                            \
+      }                                                                                        \
+      break;                                                                                   \
+    case 32:                                                                                   \
+      if (TT == 128) { constexpr int D_ = 32, T_ = 128; CALL; }                               \
+      else { constexpr int D_ = 32, T_ = 256; CALL; }                                         \
+      break;                                                                                   \
+    case 64: { constexpr int D_ = 64, T_ = 256; CALL; } break;                                \
+    default: return cudaErrorInvalidValue;                                                     \
+  }
+
+template <int D, int T>
 static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  using G = Cfg<D>;
-  const size_t smem = taylor_smem_bytes<D>();  // float4 and double2 are both 16 B
-  ensure_smem_mx(k_expm_mx<D>, smem);
-  const int grid = grid_for(k_expm_mx<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC, li.num_sms,
-                            G::SLAB ? w.slab_teams : 0);
-  k_expm_mx<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  using G = CfgM<D, T>;
+  const size_t smem = G::SMEM;
+  ensure_smem_mx(k_expm_mx<D, T>, smem);
+  const int grid = grid_for(k_expm_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
+                            li.num_sms, G::SLAB ? w.slab_teams : 0);
+  k_expm_mx<D, T><<<grid, G::THREADS, smem, li.stream>>>(p, w);
   ++*li.launches;
   return cudaGetLastError();
 }
 cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  PGX_DISPATCH_MX(p.Dp, return do_expm_mx<D_>(p, w, li));
+  const int t = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p.Dp, kTuneExpmMx);
+  PGX_DISPATCH_MX_T(p.Dp, t, return (do_expm_mx<D_, T_>(p, w, li)));
   return cudaSuccess;
 }
 
@@ -316,20 +381,20 @@ cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Launch
   return cudaSuccess;
 }
 
-template <int D>
+template <int D, int T>
 static cudaError_t do_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  using G = Cfg<D>;
-  const size_t smem = (G::SLAB ? 0 : (size_t)G::TPC * G::NBUF * D * D * sizeof(float2)) +
-                      (size_t)G::TPC * 2 * G::T * sizeof(float2);
-  ensure_smem_mx(k_grad_gate_mx<D>, smem);
-  const int grid = grid_for(k_grad_gate_mx<D>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
+  using G = CfgM<D, T>;
+  const size_t smem = G::SMEM;
+  ensure_smem_mx(k_grad_gate_mx<D, T>, smem);
+  const int grid = grid_for(k_grad_gate_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
                             li.num_sms, G::SLAB ? w.slab_teams : 0);
-  k_grad_gate_mx<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  k_grad_gate_mx<D, T><<<grid, G::THREADS, smem, li.stream>>>(p, w);
   ++*li.launches;
   return cudaGetLastError();
 }
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  PGX_DISPATCH_MX(p.Dp, return do_grad_mx<D_>(p, w, li));
+  const int t = li.team[kTuneGradMx] ? li.team[kTuneGradMx] : mixed_default_team(p.Dp, kTuneGradMx);
+  PGX_DISPATCH_MX_T(p.Dp, t, return (do_grad_mx<D_, T_>(p, w, li)));
   return cudaSuccess;
 }
 

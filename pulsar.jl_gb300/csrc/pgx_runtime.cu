@@ -509,7 +509,7 @@ struct Marks {
 
 int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
   pgx_ctx* c = p->ctx;
-  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  const pgx::LaunchInfo li = p->launch_info();
   WorkDev w = p->w;
   w.u = d_u;
   w.G = d_G ? d_G : p->d_G;
@@ -562,6 +562,62 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
   mk.mark(PGX_N_STAGES);
   mk.commit();
   return st;
+}
+
+extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char* report, size_t len) {
+  if (!p || !u) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  if (report && len) report[0] = '\0';
+  if (reps < 1) reps = 1;
+  const size_t n = (size_t)p->desc.n_controls * p->desc.n_slices;
+  if (!finite_all(u, n)) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
+  if (p->desc.precision != PGX_PREC_MIXED) {
+    if (report && len) std::snprintf(report, len, "FP64 path: no tunable kernels");
+    return PGX_OK;
+  }
+  cudaSetDevice(c->device);
+  std::memcpy(p->h_stage, u, n * sizeof(double));
+  int st = ctx_cuda(c, cudaMemcpyAsync(p->d_u, p->h_stage, n * sizeof(double), cudaMemcpyHostToDevice,
+                                       c->stream), "H2D u");
+  if (st || (st = run_pipeline(p, p->d_u, p->d_F, p->d_G))) return st;
+  WorkDev w = p->w;
+  w.u = p->d_u;
+  w.G = p->d_G;
+  w.F = p->d_F;
+  std::string rep;
+  const char* names[pgx::kNumTunable] = {"expm_mx", "grad_mx"};
+  for (int kern = 0; kern < pgx::kNumTunable; ++kern) {
+    if (kern == pgx::kTuneGradMx && p->desc.grad_mode != PGX_GRAD_EXACT) continue;
+    int vs[4];
+    const int nv = pgx::mixed_variants(p->Dp, vs);
+    double best_ms = 1e300;
+    int best = vs[0];
+    rep += std::string(rep.empty() ? "" : " | ") + names[kern] + "<" + std::to_string(p->Dp) + ">:";
+    for (int i = 0; i < nv; ++i) {
+      pgx::LaunchInfo li = p->launch_info();
+      li.team[kern] = vs[i];
+      auto launch = [&]() {
+        return kern == pgx::kTuneExpmMx ? pgx::launch_expm_mx(p->pd, w, li) : pgx::launch_grad_mx(p->pd, w, li);
+      };
+      if ((st = ctx_cuda(c, launch(), "autotune warm-up"))) return st;
+      cudaEventRecord(c->tev0, c->stream);
+      for (int r = 0; r < reps; ++r)
+        if ((st = ctx_cuda(c, launch(), "autotune"))) return st;
+      cudaEventRecord(c->tev1, c->stream);
+      if ((st = ctx_cuda(c, cudaEventSynchronize(c->tev1), "autotune sync"))) return st;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->tev0, c->tev1);
+      const double per = ms / reps;
+      char buf[48];
+      std::snprintf(buf, sizeof buf, " T=%d %.3fms", vs[i], per);
+      rep += buf;
+      if (per < best_ms) { best_ms = per; best = vs[i]; }
+    }
+    p->team[kern] = best;
+    rep += " -> T=" + std::to_string(best);
+  }
+  if (report && len) std::snprintf(report, len, "%s", rep.c_str());
+  return run_pipeline(p, p->d_u, p->d_F, p->d_G);
 }
 
 extern "C" int pgx_ctx_set_stage_timing(pgx_ctx* c, int enabled) {

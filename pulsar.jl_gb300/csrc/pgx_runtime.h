@@ -40,6 +40,12 @@ struct pgx_problem {
   std::vector<double> h_weight;
   std::vector<void*> owned;
   uint64_t bytes = 0;
+  int team[pgx::kNumTunable] = {0, 0};  // tuned team sizes (0 = default)
+  pgx::LaunchInfo launch_info() const {
+    pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};
+    for (int i = 0; i < pgx::kNumTunable; ++i) li.team[i] = team[i];
+    return li;
+  }
 };
 
 int ctx_fail(pgx_ctx* c, int status, const std::string& msg);

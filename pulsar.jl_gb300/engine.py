@@ -221,6 +221,14 @@ class Problem:
         A.check(A.lib().pgx_eval_device(self._h, C.c_void_p(d_u), C.c_void_p(d_F),
                                         C.c_void_p(d_G) if d_G else None), self.ctx.handle)
 
+    def autotune(self, u, reps: int = 3) -> str:
+        """Pick the fastest team size of each tunable kernel for this problem
+        (results are identical for every choice); returns the timing report."""
+        ub = self._load_u(u)
+        buf = C.create_string_buffer(1024)
+        A.check(A.lib().pgx_autotune(self._h, A.as_dptr(ub), int(reps), buf, 1024), self.ctx.handle)
+        return buf.value.decode()
+
     def member_fidelities(self) -> np.ndarray:
         out = np.zeros(self.n_members)
         A.check(A.lib().pgx_member_fidelities(self._h, A.as_dptr(out)), self.ctx.handle)

@@ -66,6 +66,19 @@ def test_mixed_full_size_bench_workload(pg):
     pm.close()
 
 
+@pytest.mark.parametrize("d", [4, 16, 32])
+def test_autotune_keeps_results_bit_identical(pg, d):
+    rng = np.random.default_rng(500 + d)
+    prob, u0 = random_gate_problem(rng, d, n_t=12, n_members=5, dt=0.3 / np.sqrt(d))
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F1, G1 = p.eval(u0)
+    report = p.autotune(u0, reps=2)
+    assert "expm_mx" in report and "grad_mx" in report and "-> T=" in report
+    F2, G2 = p.eval(u0)
+    assert F1 == F2 and np.array_equal(G1, G2)
+    p.close()
+
+
 def test_mixed_states_target_is_refused(pg):
     prob, u0 = mb.single_qubit_transfer()
     with pytest.raises(pg._abi.PgxError) as ei:

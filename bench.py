@@ -1,18 +1,24 @@
 """Benchmark: ensemble-slice gradients per second of the GRAPE hot path.
 
-Workload (default): the broadband robust-gate ensemble -- 4 coupled spin-1/2
-(d = 16), 231 members (21 offsets x 11 B1 scales), 1000 slices of 1 us, two
-controls, exact Frechet gradient.  One step = one evaluation (F, dF/du) of the
-whole ensemble = 231,000 member-slice units.  Seeded synthetic inputs.
-
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed]
+                  [--workload spin4|uneven512|lindblad3q] [--precision mixed|fp64]
 
-value : units/s with u, F and G resident in HBM (pgx_eval_device), CUDA events
-        on the library's stream; the per-evaluation working set (propagator and
-        chain stacks, ~1.9 GB) is far larger than L2, so no flush is needed.
-e2e   : the same metric through the reference-facing call pgx_eval with host
-        buffers: H2D of u from pinned memory and D2H of (F, G) inside the
+Workloads (seeded synthetic inputs with the configurations' shapes):
+  spin4 (default)  broadband robust gate: 4 coupled spin-1/2 (d = 16), 231
+                   members (21 offsets x 11 B1 scales), 1000 slices of 1 us, two
+                   controls, exact Frechet gradient.  Step = one evaluation
+                   (F, dF/du) = 231,000 member-slice units.
+  uneven512        512 independent problems, d in {2,4,8,16,32}, 50-2000 slices,
+                   1-128 members, 2-6 controls; step = one batched GRAPE
+                   iteration (one CUDA graph).
+  lindblad3q       3-qubit Lindblad gate (superoperator D = 64), 32 detuning
+                   draws, 500 slices, exact gradient.
+
+value : units/s with controls and results resident in HBM, CUDA events on the
+        library's stream; each step's working set (propagator and chain stacks)
+        is far larger than the 129 MB L2, so no flush is needed.
+e2e   : the same metric through the reference-facing calls with host buffers:
+        H2D of the controls from pinned memory and D2H of (F, G) inside the
         timed region, wall clock.
 --impl reference : the reference's CPU algorithm (eigendecomposition
         propagators, first-order gradient) as the oracle's multi-threaded C
@@ -38,11 +44,14 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "ensemble-slice grads/s"
 UNIT = "units/s"
-D, N_C = 16, 2
 K_EXP = 8  # conventional matrix-product count of one expm in the FLOP model
 
+# DRAM bytes per launch of the dominant kernel from ncu captures, scaled from
+# the captured 200-slice case to 1000 slices (one M_k read per unit: linear).
+TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6)}
 
-def flops_per_unit(stage: str, grad_mode: str) -> float:
+
+def flops_per_unit(stage: str, D: int, n_c: int, grad_mode: str) -> float:
     """Algorithmic FLOPs per member-slice unit (complex MAC = 8 FLOPs), the
     conventional model W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 split by
     stage: expm K_exp products, forward chain 1, backward chain + costate 2,
@@ -55,19 +64,10 @@ def flops_per_unit(stage: str, grad_mode: str) -> float:
     if stage == "chain_bwd":
         return 2 * d3
     if stage == "grad":
-        return (d3 * K_EXP * 2 * N_C if grad_mode == "exact" else 0.0) + 8.0 * N_C * D ** 2
+        return (d3 * K_EXP * 2 * n_c if grad_mode == "exact" else 0.0) + 8.0 * n_c * D ** 2
+    if stage == "all":
+        return sum(flops_per_unit(s, D, n_c, grad_mode) for s in ("expm", "chain_fwd", "chain_bwd", "grad"))
     return 0.0
-
-
-# DRAM bytes per launch of the dominant kernel from ncu captures (profiles/),
-# scaled from the captured 200-slice case to 1000 slices (traffic is linear in
-# the slices processed: one M_k read per member-slice unit).
-TRAFFIC = {("fp64", "grad"): 5 * (190.615296e6 + 4.743936e6)}
-
-
-def workload(slices: int = 1000):
-    from oracle import members as mb  # seeded generator of the synthetic inputs
-    return mb.spin4_ensemble(n_t=slices)
 
 
 class ClockSampler:
@@ -121,55 +121,228 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(prob, u0, grad_mode: str, budget_s: float = 20.0):
-    """The oracle's C restatement on all host cores; repeats full-workload
-    evaluations until ~budget_s of wall time is spent."""
-    from oracle import cpu_port
-    cp = cpu_port.CpuProblem(prob, grad_mode)
-    threads = os.cpu_count() or 1
-    cp.eval(u0, True, threads)  # warm-up
-    n, t0 = 0, time.perf_counter()
-    while True:
-        cp.eval(u0, True, threads)
-        n += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or n >= 50:
-            break
-    units = n * prob.n_members * prob.n_t
-    return {"value": units / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} full evaluations ({prob.n_members} members x {prob.n_t} slices, "
-                      f"grad_mode={grad_mode}) in {el:.1f} s, OpenMP over members"}
+def gpu_problem(pg, ctx, prob, grad_mode: str, precision: str):
+    di, sc, of, w = prob.members()
+    kw = dict(ctx=ctx, generator=prob.generator, offset_op=prob.offset_op, member_drift=di,
+              member_scale=sc, member_offset=of, member_weight=w, target=prob.target,
+              fidelity=prob.fidelity, grad_mode=grad_mode, precision=precision)
+    if prob.target == "gate":
+        kw["target_op"] = prob.target_op
+    else:
+        kw["states_init"], kw["states_target"] = prob.states_init, prob.states_target
+    return pg.Problem(prob.drifts, prob.controls, prob.dt, **kw)
 
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+class Single:
+    """One ensemble problem; step = one (F, G) evaluation."""
+
+    def __init__(self, name, prob, u0, pg, ctx, grad_mode, precision, torch, dev):
+        self.name, self.prob, self.u0, self.grad_mode, self.precision = name, prob, u0, grad_mode, precision
+        self.p = gpu_problem(pg, ctx, prob, grad_mode, precision)
+        self.units_per_step = prob.n_members * prob.n_t
+        self.tune = self.p.autotune(u0, reps=2) if precision == "mixed" else "FP64 path: no tunable kernels"
+        self.d_u = torch.tensor(np.ascontiguousarray(u0.T).ravel(), dtype=torch.float64, device=dev)
+        self.d_F = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.d_G = torch.zeros(u0.size, dtype=torch.float64, device=dev)
+        self.h2d, self.d2h = int(u0.size * 8), int(u0.size * 8 + 8)
+
+    def step_device(self):
+        self.p.eval_device(self.d_u.data_ptr(), self.d_F.data_ptr(), self.d_G.data_ptr())
+
+    def step_e2e(self):
+        self.F, self.G = self.p.eval(self.u0)
+
+    def run_device(self, K):
+        for _ in range(K):
+            self.step_device()
+        return K * self.units_per_step
+
+    def stage_flops(self, stage):
+        return flops_per_unit(stage, self.prob.D, self.prob.n_c, self.grad_mode) * self.units_per_step
+
+    def config(self):
+        return {"workload": self.name, "members": self.prob.n_members, "slices": self.prob.n_t,
+                "d": self.prob.D, "n_controls": self.prob.n_c, "generator": self.prob.generator}
+
+    def cpu_sample(self, budget_s):
+        return cpu_baseline_single(self.prob, self.u0, budget_s)
+
+    def objective(self):
+        return float(self.p.eval(self.u0, want_grad=False)[0])
+
+    def close(self):
+        self.p.close()
+
+
+class Uneven:
+    """512 uneven problems; step = one batched GRAPE iteration (CUDA graph)."""
+
+    def __init__(self, name, cases, pg, ctx, grad_mode, precision):
+        self.name, self.cases, self.grad_mode, self.precision = name, cases, grad_mode, precision
+        self.probs = [gpu_problem(pg, ctx, pr, grad_mode, precision) for pr, _ in cases]
+        self.batch = pg.Batch(self.probs, n_streams=16)
+        for i, (_, u0) in enumerate(cases):
+            self.batch.set_controls(i, u0)
+        self.units_per_step = self.batch.units
+        self.tune = "defaults (per-problem autotuning skipped for the batch)"
+        self.h2d = int(sum(u0.size * 8 for _, u0 in cases))
+        self.d2h = int(sum(u0.size * 8 + 8 for _, u0 in cases))
+
+    def run_device(self, K):
+        # iterate(K) performs one extra evaluation at the start (the initial history entry)
+        self.batch.iterate(K, trace=False, step_size=0.01)
+        return (K + 1) * self.units_per_step
+
+    def step_e2e(self):
+        for i, (_, u0) in enumerate(self.cases):
+            self.batch.set_controls(i, u0)
+        self.trace = self.batch.iterate(1, trace=True, step_size=0.01)
+        for i in range(len(self.cases)):
+            self.batch.get_controls(i)
+
+    def e2e_units(self):
+        return 2 * self.units_per_step
+
+    def total_flops(self):
+        return sum(flops_per_unit("all", pr.D, pr.n_c, self.grad_mode) * pr.n_members * pr.n_t
+                   for pr, _ in self.cases)
+
+    def config(self):
+        ds = [pr.D for pr, _ in self.cases]
+        return {"workload": self.name, "problems": len(self.cases), "d_values": sorted(set(ds)),
+                "units_per_iteration": self.units_per_step, "execution": "one CUDA graph per iteration"}
+
+    def cpu_sample(self, budget_s):
+        sample = [c for c in self.cases if c[0].D <= 16][:16]
+        return cpu_baseline_multi(sample, budget_s)
+
+    def objective(self):
+        return float(np.mean(self.batch.eval()))
+
+    def close(self):
+        self.batch.close()
+        for p in self.probs:
+            p.close()
+
+
+def cpu_baseline_single(prob, u0, budget_s: float):
+    """The oracle's C restatement of the reference algorithm on all host cores
+    (Hermitian generators), or the numpy oracle on a bounded sample otherwise."""
+    threads = os.cpu_count() or 1
+    if prob.generator == "hermitian":
+        from oracle import cpu_port
+        cp = cpu_port.CpuProblem(prob, "ref_grape")
+        cp.eval(u0, True, threads)
+        n, t0 = 0, time.perf_counter()
+        while True:
+            cp.eval(u0, True, threads)
+            n += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or n >= 50:
+                break
+        return {"value": n * prob.n_members * prob.n_t / el, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{n} full evaluations ({prob.n_members} members x {prob.n_t} slices), reference "
+                          f"algorithm (eigendecomposition propagators, first-order gradient), OpenMP over "
+                          f"members, {el:.1f} s"}
+    from oracle import members as mb
+    sub = mb.Problem(drifts=prob.drifts[:1], controls=prob.controls, dt=prob.dt[:25], generator=prob.generator,
+                     target=prob.target, fidelity=prob.fidelity, target_op=prob.target_op, n_members=1)
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < budget_s:
+        mb.eval_problem(sub, u0[:, :25], "ref_mr")
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": n * 25 / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} evaluations of 1 member x 25 slices with the numpy oracle (scipy Pade expm, "
+                      f"first-order gradient), {el:.1f} s"}
+
+
+def cpu_baseline_multi(cases, budget_s: float):
+    from oracle import cpu_port
+    threads = os.cpu_count() or 1
+    cps = [(cpu_port.CpuProblem(pr, "ref_grape"), u0, pr.n_members * pr.n_t) for pr, u0 in cases]
+    units, t0 = 0, time.perf_counter()
+    while True:
+        for cp, u0, un in cps:
+            cp.eval(u0, True, threads)
+            units += un
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return {"value": units / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(cps)} problems of the batch with d <= 16 evaluated repeatedly, reference algorithm, "
+                      f"OpenMP over members, {el:.1f} s"}
+
+
+def make_workload(args, pg, ctx, torch, dev):
+    from oracle import members as mb
+    if args.workload == "spin4":
+        prob, u0 = mb.spin4_ensemble(n_t=args.slices)
+        return Single(f"spin4_d16_231members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
+                      args.precision, torch, dev)
+    if args.workload == "lindblad3q":
+        prob, u0 = mb.lindblad_3q()
+        return Single("lindblad3q_D64_32members_500slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
+                      torch, dev)
+    if args.workload == "uneven512":
+        return Uneven("uneven512", mb.uneven_batch(512), pg, ctx, args.grad_mode, args.precision)
+    raise ValueError(args.workload)
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
 
 def run_reference(args, rank: int):
     if rank != 0:
         return 0
-    prob, u0 = workload(args.slices)
+    from oracle import members as mb
+    if args.workload == "spin4":
+        prob, u0 = mb.spin4_ensemble(n_t=args.slices)
+        cases = [(prob, u0)]
+        name = f"spin4_d16_231members_{prob.n_t}slices"
+    elif args.workload == "uneven512":
+        cases = [c for c in mb.uneven_batch(512) if c[0].D <= 16][:16]
+        name = "uneven512 (sample: first 16 problems with d <= 16)"
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": "the oracle's C restatement covers Hermitian "
+                          "generators; the Liouvillian workload has no multi-core CPU port"}), flush=True)
+        return 0
     from oracle import cpu_port
-    cp = cpu_port.CpuProblem(prob, "ref_grape")
     threads = os.cpu_count() or 1
+    cps = [(cpu_port.CpuProblem(pr, "ref_grape"), u0, pr.n_members * pr.n_t) for pr, u0 in cases]
     for _ in range(args.warmup):
-        cp.eval(u0, True, threads)
-    t0 = time.perf_counter()
+        for cp, u0, _ in cps:
+            cp.eval(u0, True, threads)
+    units, t0 = 0, time.perf_counter()
     for _ in range(args.steps):
-        cp.eval(u0, True, threads)
+        for cp, u0, un in cps:
+            cp.eval(u0, True, threads)
+            units += un
     el = time.perf_counter() - t0
-    units = args.steps * prob.n_members * prob.n_t
     v = units / el
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": "spin4_d16_231members_1000slices", "grad_mode": "ref_grape",
-                       "members": prob.n_members, "slices": prob.n_t, "d": D, "n_controls": N_C},
+            "config": {"workload": name, "grad_mode": "ref_grape"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} full evaluations, reference algorithm "
-                                       "(Hermitian eigendecomposition propagators, first-order "
-                                       "gradient of Gradients.jl:254-291), OpenMP over members"},
+                             "sample": f"{args.steps} evaluations of the workload, reference algorithm "
+                                       "(Hermitian eigendecomposition propagators, first-order gradient of "
+                                       "Gradients.jl:254-291), OpenMP over members"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
 
 def main():
     ap = argparse.ArgumentParser()
@@ -177,15 +350,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="spin4", choices=["spin4", "uneven512", "lindblad3q"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--grad-mode", default="exact", choices=["exact", "ref_grape", "ref_mr"])
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true",
+                    help="skip timing the plain FP64 GPU form beside the mixed one")
     ap.add_argument("--slices", type=int, default=1000,
-                    help="slices per member (1000 = the benchmark workload; smaller for profiling)")
+                    help="spin4 slices per member (1000 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -203,37 +378,28 @@ def main():
     import __graft_entry__ as ge
     ge._load_builder().build()
     pg = ge.load_package()
-    prob, u0 = workload(args.slices)
     ctx = pg.Context(local)
-    di, sc, of, w = prob.members()
-    p = pg.Problem(prob.drifts, prob.controls, prob.dt, ctx=ctx, offset_op=prob.offset_op,
-                   member_drift=di, member_scale=sc, member_offset=of, member_weight=w,
-                   target="gate", target_op=prob.target_op, grad_mode=args.grad_mode,
-                   precision=args.precision)
-    units_per_step = prob.n_members * prob.n_t
-    # team sizes of the tunable kernels, chosen before any timing (results are
-    # identical for every choice)
-    tune_report = p.autotune(u0, reps=2) if args.precision == "mixed" else "FP64 path: no tunable kernels"
     dev = torch.device(f"cuda:{local}")
-    d_u = torch.tensor(np.ascontiguousarray(u0.T).ravel(), dtype=torch.float64, device=dev)
-    d_F = torch.zeros(2, dtype=torch.float64, device=dev)
-    d_G = torch.zeros(u0.size, dtype=torch.float64, device=dev)
+    wl = make_workload(args, pg, ctx, torch, dev)
     torch.cuda.synchronize(dev)
 
     # ---- device-resident throughput (value) ----
-    for _ in range(args.warmup):
-        p.eval_device(d_u.data_ptr(), d_F.data_ptr(), d_G.data_ptr())
+    single = isinstance(wl, Single)
+    if single:
+        for _ in range(args.warmup):
+            wl.step_device()
+    else:
+        wl.run_device(args.warmup)
     ctx.synchronize()
     if dist:
         dist.barrier()
-    ctx.set_stage_timing(True)
+    ctx.set_stage_timing(single)
     ctx.stage_times()  # clear
     l0 = ctx.launch_count()
     with ClockSampler(local) as clk:
         ctx.synchronize()
         ctx.timer_start()
-        for _ in range(args.steps):
-            p.eval_device(d_u.data_ptr(), d_F.data_ptr(), d_G.data_ptr())
+        units = wl.run_device(args.steps)
         ms = ctx.timer_stop()
     launches = ctx.launch_count() - l0
     stages, n_rec = ctx.stage_times()
@@ -242,62 +408,81 @@ def main():
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * units_per_step * args.steps / (ms * 1e-3)
+    value = world * units / (ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
-    for _ in range(2):
-        p.eval(u0)
+    wl.step_e2e()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        F_host, G_host = p.eval(u0)
+        wl.step_e2e()
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e = world * units_per_step * args.steps / e2e_s
+    e2e_units = wl.e2e_units() if hasattr(wl, "e2e_units") else wl.units_per_step
+    e2e = world * e2e_units * args.steps / e2e_s
 
     if rank == 0:
-        # ---- roofline of the dominant kernel ----
-        dom = max(stages, key=stages.get)
-        dom_ms = stages[dom] / max(n_rec, 1)
-        alg = flops_per_unit(dom, args.grad_mode) * units_per_step
         pipe = "fp64" if args.precision == "fp64" else "fp32"
         peak = ctx.measure_peak(pipe) * 1e9
-        achieved = alg / (dom_ms * 1e-3)
-        share = {k: round(v / max(sum(stages.values()), 1e-30), 4) for k, v in stages.items()}
-        kname = {"fp64": "k_{}", "fp32": "k_{}_mx"}[pipe].format(
-            dom if dom != "grad" or pipe == "fp64" else "grad_gate")
-        roof = {"bound": pipe, "achieved": achieved / 1e12, "peak": peak / 1e12,
-                "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                "traffic": TRAFFIC.get((pipe, dom)), "kernel": kname, "ms_per_launch": dom_ms,
-                "stage_share": share,
-                "peak_source": f"measured in this run: independent-FMA loop kernel on the {pipe.upper()} "
-                               "pipe (MEASURED_PEAKS.json holds only HBM copy and bf16 GEMM figures)",
-                "flop_model": "conventional per-unit W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 "
-                              "(K_exp = 8) split by stage; the exact gradient executes one Frechet "
-                              "derivative per slice where the model counts 2 n_c"}
+        if single:
+            dom = max(stages, key=stages.get)
+            dom_ms = stages[dom] / max(n_rec, 1)
+            achieved = wl.stage_flops(dom) / (dom_ms * 1e-3)
+            share = {k: round(v / max(sum(stages.values()), 1e-30), 4) for k, v in stages.items()}
+            kname = ("k_" + dom) if pipe == "fp64" else {"expm": "k_expm_mx", "chain_fwd": "k_chain_gate_fwd_mx",
+                                                         "chain_bwd": "k_chain_gate_bwd_mx",
+                                                         "grad": "k_grad_gate_mx", "reduce": "k_reduce"}[dom]
+            roof = {"kernel": kname, "ms_per_launch": dom_ms, "stage_share": share,
+                    "traffic": TRAFFIC.get((args.workload, args.precision, dom))}
+        else:
+            achieved = wl.total_flops() * (units / wl.units_per_step) / (ms * 1e-3)
+            roof = {"kernel": "whole batched iteration (CUDA graph)", "ms_per_launch": ms / (args.steps + 1),
+                    "traffic": None}
+        roof.update({"bound": pipe, "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None,
+                     "peak_source": f"measured in this run: independent-FMA loop kernel on the "
+                                    f"{pipe.upper()} pipe (MEASURED_PEAKS.json holds only HBM copy and bf16 "
+                                    "GEMM figures)",
+                     "flop_model": "conventional per-unit W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 "
+                                   "(K_exp = 8) split by stage; the exact gradient executes one Frechet "
+                                   "derivative per slice where the model counts 2 n_c"})
+        extra = {}
+        if args.precision == "mixed" and single and not args.no_fp64_compare:
+            # the plain FP64 GPU form of the same workload, timed in the same run
+            ref = Single(wl.name, wl.prob, wl.u0, pg, ctx, args.grad_mode, "fp64", torch, dev)
+            for _ in range(2):
+                ref.step_device()
+            ctx.synchronize()
+            ctx.timer_start()
+            n_ref = max(2, args.steps // 3)
+            u_ref = ref.run_device(n_ref)
+            ms_ref = ctx.timer_stop()
+            v_ref = u_ref / (ms_ref * 1e-3)
+            F64, Fmx = ref.objective(), wl.objective()
+            extra = {"fp64_gpu_value": v_ref, "vs_fp64_gpu": value / v_ref, "abs_dF_vs_fp64": abs(Fmx - F64)}
+            ref.close()
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            cpu = cpu_baseline(prob, u0, "ref_grape", args.cpu_budget_s)
+            cpu = wl.cpu_sample(args.cpu_budget_s)
+        cfg = wl.config()
+        cfg.update({"autotune": wl.tune, "grad_mode": args.grad_mode, "precision": args.precision,
+                    "parallelism": f"replicas x{world}",
+                    "l2": "per-step working set >> 129 MB L2 (no flush needed)"})
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-                "data": "synthetic (seeded)",
-                "config": {"workload": f"spin4_d16_231members_{prob.n_t}slices", "autotune": tune_report,
-                           "grad_mode": args.grad_mode,
-                           "precision": args.precision, "members": prob.n_members, "slices": prob.n_t,
-                           "d": D, "n_controls": N_C, "parallelism": f"replicas x{world}",
-                           "l2": "working set ~1.9 GB per step >> 129 MB L2 (no flush needed)"},
-                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(u0.size * 8),
-                        "d2h_bytes_per_step": int(u0.size * 8 + 8)},
+                "dtype": "f64" if args.precision == "fp64" else "f32+df32(f64 overlap)",
+                "data": "synthetic (seeded)", "config": cfg,
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": wl.h2d, "d2h_bytes_per_step": wl.d2h},
                 "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary(),
-                "cpu_baseline": cpu, "F": F_host}
+                "cpu_baseline": cpu}
+        line.update(extra)
         print(json.dumps(line), flush=True)
-    p.close()
+    wl.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -249,6 +249,34 @@ int pgx_optimize(pgx_problem* prob, const pgx_opt_desc* opt, double* u_inout,
                  double* fidelity_history, double* gnorm_history, int32_t history_cap,
                  pgx_opt_result* result);
 
+/* ---- batches of uneven problems ----------------------------------------- */
+/* A batch groups problems of any dimensions, slice counts and ensemble sizes
+ * on one context.  pgx_batch_eval / pgx_batch_iterate enqueue every problem's
+ * pipeline -- fanned out over n_streams streams, largest problems first --
+ * as ONE CUDA graph per call / per iteration, captured on first use.  Each
+ * problem runs the kernels of its solo evaluation, so batched results are
+ * bit-identical to solo results.  No reference counterpart: Pulsar.jl runs
+ * problems one after another (grape_multistart, GRAPE.jl:745-768).          */
+typedef struct pgx_batch pgx_batch;
+int pgx_batch_create(pgx_ctx* ctx, int32_t n, pgx_problem* const* problems, int32_t n_streams,
+                     pgx_batch** out);
+int pgx_batch_destroy(pgx_batch* batch);
+/* Controls of problem i (host buffer, [n_c x n_t]); they stay on the device. */
+int pgx_batch_set_controls(pgx_batch* batch, int32_t i, const double* u);
+/* Device-resident controls and last gradient of problem i (either nullable). */
+int pgx_batch_get_controls(pgx_batch* batch, int32_t i, double* u, double* G);
+/* Member-slice units one evaluation of the whole batch processes. */
+int pgx_batch_units(const pgx_batch* batch, int64_t* units);
+/* (F, G) of every problem at its device-resident controls; F[n] (nullable)
+ * receives the objectives, gradients stay on the device.                    */
+int pgx_batch_eval(pgx_batch* batch, double* F);
+/* n_iter iterations of the grape_optimize ascent (GRAPE.jl:536-610: evaluate,
+ * adapt_grape_step_size, u += step G) for every problem, one graph launch per
+ * iteration, controls / gradients / step state device-resident.  Uses
+ * step_size, adapt_step_size, min_step_size and max_step_size of opt.
+ * F_trace ([n_iter][n], nullable) receives the objective of every iteration. */
+int pgx_batch_iterate(pgx_batch* batch, int32_t n_iter, const pgx_opt_desc* opt, double* F_trace);
+
 #ifdef __cplusplus
 }
 #endif

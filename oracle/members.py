@@ -289,6 +289,38 @@ def spin4_ensemble(seed: int = 7, n_t: int = 1000, n_off: int = 21, n_b1: int = 
     return prob, u0
 
 
+def _rand_herm(rng, d, sigma):
+    A = rng.normal(0.0, sigma, (d, d)) + 1j * rng.normal(0.0, sigma, (d, d))
+    return (A + A.conj().T) / 2
+
+
+def uneven_problem(rng: np.random.Generator, d: int = None, n_t: int = None, n_members: int = None):
+    """One problem of the uneven batch: d uniform in {2,4,8,16,32}, n_t
+    log-uniform in [50, 2000], ensemble size log-uniform in [1, 128]; drift a
+    random Hermitian with Gaussian entries (sigma = 2 pi 1 MHz), 2-6 random
+    Hermitian controls of the same scale, members spread by a B1 scale
+    U[0.9, 1.1] and a detuning U[-0.1, 0.1] sigma along a random diagonal;
+    Haar-random gate target; dt = 0.2 / (2 sigma sqrt(d)) so ||H dt|| ~ 0.2."""
+    sigma = 2 * np.pi * 1e6
+    d = int(rng.choice([2, 4, 8, 16, 32])) if d is None else d
+    n_t = int(np.round(np.exp(rng.uniform(np.log(50), np.log(2000))))) if n_t is None else n_t
+    nm = int(np.round(np.exp(rng.uniform(0.0, np.log(128))))) if n_members is None else n_members
+    n_c = int(rng.integers(2, 7))
+    H = _rand_herm(rng, d, sigma)
+    C = np.stack([_rand_herm(rng, d, sigma) for _ in range(n_c)])
+    O = np.diag(rng.uniform(-1, 1, d)).astype(C128)
+    dt = 0.2 / (2 * sigma * np.sqrt(d))
+    prob = Problem(drifts=H[None], controls=C, dt=np.full(n_t, dt), offset_op=O,
+                   member_scale=rng.uniform(0.9, 1.1, nm), member_offset=rng.uniform(-0.1, 0.1, nm) * sigma,
+                   target="gate", fidelity="square", target_op=haar_unitary(rng, d), n_members=nm)
+    return prob, rng.uniform(-1, 1, (n_c, n_t))
+
+
+def uneven_batch(n_problems: int = 512, seed: int = 4):
+    rng = np.random.default_rng(seed)
+    return [uneven_problem(rng) for _ in range(n_problems)]
+
+
 def lindblad_3q(seed: int = 11, n_t: int = 500, n_draws: int = 32):
     """Three qubits, ZZ U[0.1,1] MHz on 3 pairs, detuning U[-0.5,0.5] MHz per
     qubit (redrawn per ensemble member), T1 U[20,100] us, T2 = T1 U(0.5,1);

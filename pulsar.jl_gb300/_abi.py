@@ -91,6 +91,14 @@ SIGNATURES = {
     "pgx_total_propagator": (C.c_int, [C.c_void_p, dptr, C.c_int32, dptr]),
     "pgx_propagator": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.c_double, dptr]),
     "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
+    "pgx_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
+                                   C.POINTER(C.c_void_p)]),
+    "pgx_batch_destroy": (C.c_int, [C.c_void_p]),
+    "pgx_batch_set_controls": (C.c_int, [C.c_void_p, C.c_int32, dptr]),
+    "pgx_batch_get_controls": (C.c_int, [C.c_void_p, C.c_int32, dptr, dptr]),
+    "pgx_batch_units": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "pgx_batch_eval": (C.c_int, [C.c_void_p, dptr]),
+    "pgx_batch_iterate": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(OptDesc), dptr]),
     "pgx_total_propagator_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
                                                C.c_size_t]),

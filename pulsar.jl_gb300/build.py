@@ -20,7 +20,8 @@ INCLUDE = ROOT / "include"
 BUILD = ROOT / "_build"
 LIB = PKG / "libpulsar_gb300.so"
 
-SOURCES = ["pgx_kernels.cu", "pgx_mixed.cu", "pgx_runtime.cu", "pgx_optimize.cu", "pgx_noalloc.cu"]
+SOURCES = ["pgx_kernels.cu", "pgx_mixed.cu", "pgx_runtime.cu", "pgx_optimize.cu", "pgx_batch.cu",
+           "pgx_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -62,28 +62,45 @@ struct EpiNone {
   template <class C> __device__ __forceinline__ C operator()(int, int, int, C s) const { return s; }
 };
 
+// Storage of a D x D matrix in a team's shared memory.  SW = 0: column-major,
+// (r, c) at r + D c.  SW = 1: XOR-swizzled column-major, (r, c) at
+// (r ^ c) + D c (D a power of two): every column is still one contiguous
+// block, but the same row of different columns lands in different banks, so
+// the row-wise operand loads of a product are conflict-free.
+template <int D, int SW> struct Lay {
+  __device__ __forceinline__ static int idx(int r, int c) { return (SW ? (r ^ (c & (D - 1))) : r) + D * c; }
+  __device__ __forceinline__ static int row(int e) {
+    const int c = e / D;
+    return SW ? ((e % D) ^ (c & (D - 1))) : e % D;
+  }
+};
+
 // Register blocking of a D x D product over T lanes: each lane owns an RB x CB
-// block of outputs (rows rb*RB.., columns cb*CB..).  With one output per lane
-// (RB = CB = 1) lanes beyond D*D idle.
+// block of outputs, interleaved (rows rb + NR*i, columns cb + NCB*j) so the
+// lanes of one load instruction touch consecutive rows / columns.  With one
+// output per lane (RB = CB = 1) lanes beyond D*D idle.
 template <int D, int T> struct Blocking {
   static constexpr int NE = (D * D >= T) ? D * D / T : 1;
   static constexpr int RB = (NE >= 2 && D % 2 == 0) ? 2 : 1;
   static constexpr int CB = NE / RB;
   static constexpr int NR = D / RB;               // row blocks
-  static constexpr int ACTIVE = NR * (D / CB);    // lanes with work
+  static constexpr int NCB = D / CB;              // column blocks
+  static constexpr int ACTIVE = NR * NCB;         // lanes with work
   static_assert(RB * CB == NE, "blocking");
   static_assert(D * D >= T ? ACTIVE == T : ACTIVE == D * D, "blocking covers the matrix");
 };
 
-// out = A1*B1 (+ A2*B2 when TWO) then epi(e, r, c, value); out may alias any
-// input (outputs are staged in registers across a team barrier).
-template <int D, int T, bool TWO, class C, class Epi>
+// out = A1*B1 (+ A2*B2 when TWO) then epi(e, r, c, value) with e the storage
+// index of (r, c); out may alias any input (outputs are staged in registers
+// across a team barrier).  Each output's dot product runs over k in order.
+template <int D, int T, bool TWO, int SW = 0, class C, class Epi>
 __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const C* B1,
                                    const C* A2, const C* B2, Epi epi) {
   using BK = Blocking<D, T>;
+  using L = Lay<D, SW>;
   constexpr int RB = BK::RB, CB = BK::CB;
   const bool active = tm.lane < BK::ACTIVE;
-  const int r0 = (tm.lane % BK::NR) * RB, c0 = (tm.lane / BK::NR) * CB;
+  const int rb = tm.lane % BK::NR, cb = tm.lane / BK::NR;
   C acc[RB][CB];
 #pragma unroll
   for (int i = 0; i < RB; ++i)
@@ -94,9 +111,9 @@ __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const
     for (int k = 0; k < D; ++k) {
       C a[RB], b[CB];
 #pragma unroll
-      for (int i = 0; i < RB; ++i) a[i] = A1[r0 + i + D * k];
+      for (int i = 0; i < RB; ++i) a[i] = A1[L::idx(rb + BK::NR * i, k)];
 #pragma unroll
-      for (int j = 0; j < CB; ++j) b[j] = B1[k + D * (c0 + j)];
+      for (int j = 0; j < CB; ++j) b[j] = B1[L::idx(k, cb + BK::NCB * j)];
 #pragma unroll
       for (int i = 0; i < RB; ++i)
 #pragma unroll
@@ -107,9 +124,9 @@ __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const
       for (int k = 0; k < D; ++k) {
         C a[RB], b[CB];
 #pragma unroll
-        for (int i = 0; i < RB; ++i) a[i] = A2[r0 + i + D * k];
+        for (int i = 0; i < RB; ++i) a[i] = A2[L::idx(rb + BK::NR * i, k)];
 #pragma unroll
-        for (int j = 0; j < CB; ++j) b[j] = B2[k + D * (c0 + j)];
+        for (int j = 0; j < CB; ++j) b[j] = B2[L::idx(k, cb + BK::NCB * j)];
 #pragma unroll
         for (int i = 0; i < RB; ++i)
 #pragma unroll
@@ -120,8 +137,8 @@ __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const
     for (int i = 0; i < RB; ++i)
 #pragma unroll
       for (int j = 0; j < CB; ++j) {
-        const int r = r0 + i, c = c0 + j;
-        acc[i][j] = epi(r + D * c, r, c, acc[i][j]);
+        const int r = rb + BK::NR * i, c = cb + BK::NCB * j;
+        acc[i][j] = epi(L::idx(r, c), r, c, acc[i][j]);
       }
   }
   tm.sync();
@@ -129,14 +146,14 @@ __device__ __forceinline__ void mm(const Team<T>& tm, C* out, const C* A1, const
 #pragma unroll
     for (int i = 0; i < RB; ++i)
 #pragma unroll
-      for (int j = 0; j < CB; ++j) out[r0 + i + D * (c0 + j)] = acc[i][j];
+      for (int j = 0; j < CB; ++j) out[L::idx(rb + BK::NR * i, cb + BK::NCB * j)] = acc[i][j];
   }
   tm.sync();
 }
 
-template <int D, int T, class C>
+template <int D, int T, int SW = 0, class C>
 __device__ __forceinline__ void mm1(const Team<T>& tm, C* out, const C* A, const C* B) {
-  mm<D, T, false>(tm, out, A, B, (const C*)nullptr, (const C*)nullptr, EpiNone{});
+  mm<D, T, false, SW>(tm, out, A, B, (const C*)nullptr, (const C*)nullptr, EpiNone{});
 }
 
 template <int D, int T, class C>
@@ -188,13 +205,13 @@ __device__ __forceinline__ double team_max(const Team<T>& tm, double v, double* 
 
 // 1-norm (max column abs sum) of a D x D matrix; computed in FP64 whatever the
 // storage type, because it selects the Taylor degree and the squarings.
-template <int D, int T, class C>
+template <int D, int T, int SW = 0, class C>
 __device__ __forceinline__ double norm1(const Team<T>& tm, const C* A, double* scratch) {
   double best = 0.0;
   for (int c = tm.lane; c < D; c += T) {
     double s = 0.0;
     for (int r = 0; r < D; ++r) {
-      C a = A[r + D * c];
+      C a = A[Lay<D, SW>::idx(r, c)];
       s += hypot((double)a.x, (double)a.y);
     }
     best = fmax(best, s);
@@ -251,42 +268,42 @@ template <class C, int D> struct Work {
 // Y = T_m(B)^(2^s).  B holds A / 2^s on entry (destroyed: B..B4 are scratch).
 // Paterson-Stockmeyer with q = 4: powers B2, B3, B4, then Horner in B4 over
 // blocks of four coefficients.  m = 4L costs 3 + (L - 1) products.
-template <int D, int T, class C, class R>
+template <int D, int T, int SW = 0, class C, class R>
 __device__ void taylor_exp(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
-  mm1<D, T>(tm, w.B2, w.B, w.B);
-  mm1<D, T>(tm, w.B3, w.B2, w.B);
-  mm1<D, T>(tm, w.B4, w.B2, w.B2);
+  mm1<D, T, SW>(tm, w.B2, w.B, w.B);
+  mm1<D, T, SW>(tm, w.B3, w.B2, w.B);
+  mm1<D, T, SW>(tm, w.B4, w.B2, w.B2);
   const int L = m / 4;
   for (int e = tm.lane; e < D * D; e += T) {
-    const int r = e % D, c = e / D;
+    const int r = Lay<D, SW>::row(e), c = e / D;
     C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
     w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
   }
   tm.sync();
   for (int i = L - 2; i >= 0; --i) {
     const C* B = w.B; const C* B2 = w.B2; const C* B3 = w.B3;
-    mm<D, T, false>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
-                    [=](int e, int r, int c, C v) {
-                      return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
-                    });
+    mm<D, T, false, SW>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
+                        [=](int e, int r, int c, C v) {
+                          return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
+                        });
   }
-  for (int k = 0; k < s; ++k) mm1<D, T>(tm, w.Y, w.Y, w.Y);
+  for (int k = 0; k < s; ++k) mm1<D, T, SW>(tm, w.Y, w.Y, w.Y);
 }
 
 // (Y, dY) = (f(A), L_f(A, M)) for f(A) = T_m(A/2^s)^(2^s).  On entry B = A/2^s
 // and dB = M/2^s.  The derivative is exact for the polynomial f actually
 // evaluated, so Tr(L_f(A, M) E) equals Tr(M L_f(A, E)) to rounding.
-template <int D, int T, class C, class R>
+template <int D, int T, int SW = 0, class C, class R>
 __device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
-  mm1<D, T>(tm, w.B2, w.B, w.B);
-  mm<D, T, true>(tm, w.dB2, w.dB, w.B, w.B, w.dB, EpiNone{});
-  mm1<D, T>(tm, w.B3, w.B2, w.B);
-  mm<D, T, true>(tm, w.dB3, w.dB2, w.B, w.B2, w.dB, EpiNone{});
-  mm1<D, T>(tm, w.B4, w.B2, w.B2);
-  mm<D, T, true>(tm, w.dB4, w.dB2, w.B2, w.B2, w.dB2, EpiNone{});
+  mm1<D, T, SW>(tm, w.B2, w.B, w.B);
+  mm<D, T, true, SW>(tm, w.dB2, w.dB, w.B, w.B, w.dB, EpiNone{});
+  mm1<D, T, SW>(tm, w.B3, w.B2, w.B);
+  mm<D, T, true, SW>(tm, w.dB3, w.dB2, w.B, w.B2, w.dB, EpiNone{});
+  mm1<D, T, SW>(tm, w.B4, w.B2, w.B2);
+  mm<D, T, true, SW>(tm, w.dB4, w.dB2, w.B2, w.B2, w.dB2, EpiNone{});
   const int L = m / 4;
   for (int e = tm.lane; e < D * D; e += T) {
-    const int r = e % D, c = e / D;
+    const int r = Lay<D, SW>::row(e), c = e / D;
     C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
     w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
     C dv = block_der(L - 1, w.dB[e], w.dB2[e], w.dB3[e], invf);
@@ -297,19 +314,19 @@ __device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D>& w, int m
     const C* B = w.B; const C* B2 = w.B2; const C* B3 = w.B3;
     const C* dB = w.dB; const C* dB2 = w.dB2; const C* dB3 = w.dB3;
     // dY <- dB4*Y + B4*dY + dC_i   (uses the old Y)
-    mm<D, T, true>(tm, w.dY, w.dB4, w.Y, w.B4, w.dY,
-                   [=](int e, int, int, C v) {
-                     return cadd(v, block_der(i, dB[e], dB2[e], dB3[e], invf));
-                   });
+    mm<D, T, true, SW>(tm, w.dY, w.dB4, w.Y, w.B4, w.dY,
+                       [=](int e, int, int, C v) {
+                         return cadd(v, block_der(i, dB[e], dB2[e], dB3[e], invf));
+                       });
     // Y <- B4*Y + C_i
-    mm<D, T, false>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
-                    [=](int e, int r, int c, C v) {
-                      return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
-                    });
+    mm<D, T, false, SW>(tm, w.Y, w.B4, w.Y, (const C*)nullptr, (const C*)nullptr,
+                        [=](int e, int r, int c, C v) {
+                          return cadd(v, block_val(i, r, c, B[e], B2[e], B3[e], invf));
+                        });
   }
   for (int k = 0; k < s; ++k) {
-    mm<D, T, true>(tm, w.dY, w.Y, w.dY, w.dY, w.Y, EpiNone{});
-    mm1<D, T>(tm, w.Y, w.Y, w.Y);
+    mm<D, T, true, SW>(tm, w.dY, w.Y, w.dY, w.dY, w.Y, EpiNone{});
+    mm1<D, T, SW>(tm, w.Y, w.Y, w.Y);
   }
 }
 

@@ -106,13 +106,14 @@ struct DfEpiNone {
 };
 
 // out = A1*B1 (+ A2*B2) in df, then epi(e, r, c, value); out may alias inputs.
-template <int D, int T, bool TWO, class Epi>
+template <int D, int T, bool TWO, int SW = 0, class Epi>
 __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const float4* A1, const float4* B1,
                                       const float4* A2, const float4* B2, Epi epi) {
   using BK = Blocking<D, T>;
+  using L = Lay<D, SW>;
   constexpr int RB = BK::RB, CB = BK::CB;
   const bool active = tm.lane < BK::ACTIVE;
-  const int r0 = (tm.lane % BK::NR) * RB, c0 = (tm.lane / BK::NR) * CB;
+  const int rb = tm.lane % BK::NR, cb = tm.lane / BK::NR;
   DfAcc acc[RB][CB];
   float4 res[RB][CB];
   if (active) {
@@ -120,9 +121,9 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
     for (int k = 0; k < D; ++k) {
       float4 a[RB], b[CB];
 #pragma unroll
-      for (int i = 0; i < RB; ++i) a[i] = A1[r0 + i + D * k];
+      for (int i = 0; i < RB; ++i) a[i] = A1[L::idx(rb + BK::NR * i, k)];
 #pragma unroll
-      for (int j = 0; j < CB; ++j) b[j] = B1[k + D * (c0 + j)];
+      for (int j = 0; j < CB; ++j) b[j] = B1[L::idx(k, cb + BK::NCB * j)];
 #pragma unroll
       for (int i = 0; i < RB; ++i)
 #pragma unroll
@@ -133,9 +134,9 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
       for (int k = 0; k < D; ++k) {
         float4 a[RB], b[CB];
 #pragma unroll
-        for (int i = 0; i < RB; ++i) a[i] = A2[r0 + i + D * k];
+        for (int i = 0; i < RB; ++i) a[i] = A2[L::idx(rb + BK::NR * i, k)];
 #pragma unroll
-        for (int j = 0; j < CB; ++j) b[j] = B2[k + D * (c0 + j)];
+        for (int j = 0; j < CB; ++j) b[j] = B2[L::idx(k, cb + BK::NCB * j)];
 #pragma unroll
         for (int i = 0; i < RB; ++i)
 #pragma unroll
@@ -146,8 +147,8 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
     for (int i = 0; i < RB; ++i)
 #pragma unroll
       for (int j = 0; j < CB; ++j) {
-        const int r = r0 + i, c = c0 + j;
-        res[i][j] = dfc_store(epi(r + D * c, r, c, acc[i][j].result()));
+        const int r = rb + BK::NR * i, c = cb + BK::NCB * j;
+        res[i][j] = dfc_store(epi(L::idx(r, c), r, c, acc[i][j].result()));
       }
   }
   tm.sync();
@@ -155,14 +156,14 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
 #pragma unroll
     for (int i = 0; i < RB; ++i)
 #pragma unroll
-      for (int j = 0; j < CB; ++j) out[r0 + i + D * (c0 + j)] = res[i][j];
+      for (int j = 0; j < CB; ++j) out[L::idx(rb + BK::NR * i, cb + BK::NCB * j)] = res[i][j];
   }
   tm.sync();
 }
 
-template <int D, int T>
+template <int D, int T, int SW = 0>
 __device__ __forceinline__ void mm1_df(const Team<T>& tm, float4* out, const float4* A, const float4* B) {
-  mm_df<D, T, false>(tm, out, A, B, (const float4*)nullptr, (const float4*)nullptr, DfEpiNone{});
+  mm_df<D, T, false, SW>(tm, out, A, B, (const float4*)nullptr, (const float4*)nullptr, DfEpiNone{});
 }
 
 // Taylor block C_i = c_{4i} I + c_{4i+1} B + c_{4i+2} B2 + c_{4i+3} B3 in df;
@@ -178,26 +179,26 @@ __device__ __forceinline__ dfc df_block(int i, int r, int c, const float4& b1, c
 
 // Y = T_m(B)^(2^s) in df (B = A / 2^s on entry).  Same Paterson-Stockmeyer
 // schedule as taylor_exp: m = 4L costs 3 + (L - 1) products, then s squarings.
-template <int D, int T>
+template <int D, int T, int SW = 0>
 __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* B3, float4* B4, float4* Y,
                               int m, int s, const df* coef) {
-  mm1_df<D, T>(tm, B2, B, B);
-  mm1_df<D, T>(tm, B3, B2, B);
-  mm1_df<D, T>(tm, B4, B2, B2);
+  mm1_df<D, T, SW>(tm, B2, B, B);
+  mm1_df<D, T, SW>(tm, B3, B2, B);
+  mm1_df<D, T, SW>(tm, B4, B2, B2);
   const int L = m / 4;
   for (int e = tm.lane; e < D * D; e += T) {
-    const int r = e % D, c = e / D;
+    const int r = Lay<D, SW>::row(e), c = e / D;
     dfc v = df_block(L - 1, r, c, B[e], B2[e], B3[e], coef);
     Y[e] = dfc_store(dfc_add(v, dfc_scale(dfc_load(B4[e]), coef[4 * L])));
   }
   tm.sync();
   for (int i = L - 2; i >= 0; --i) {
-    mm_df<D, T, false>(tm, Y, B4, Y, (const float4*)nullptr, (const float4*)nullptr,
-                       [=](int e, int r, int c, dfc v) {
-                         return dfc_add(v, df_block(i, r, c, B[e], B2[e], B3[e], coef));
-                       });
+    mm_df<D, T, false, SW>(tm, Y, B4, Y, (const float4*)nullptr, (const float4*)nullptr,
+                           [=](int e, int r, int c, dfc v) {
+                             return dfc_add(v, df_block(i, r, c, B[e], B2[e], B3[e], coef));
+                           });
   }
-  for (int k = 0; k < s; ++k) mm1_df<D, T>(tm, Y, Y, Y);
+  for (int k = 0; k < s; ++k) mm1_df<D, T, SW>(tm, Y, Y, Y);
 }
 
 }  // namespace pgx

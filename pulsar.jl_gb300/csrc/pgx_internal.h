@@ -61,6 +61,9 @@ struct LaunchInfo {
   int team[kNumTunable] = {0, 0};
 };
 
+// Raises a kernel's dynamic shared-memory limit (once per kernel and device).
+void set_smem_once(const void* fn, size_t bytes);
+
 // Team sizes the mixed slice-parallel kernels admit at padded dimension Dp
 // (writes up to 4 values, returns the count), and the default choice.
 int mixed_variants(int Dp, int* out);

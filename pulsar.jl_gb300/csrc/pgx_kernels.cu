@@ -19,6 +19,10 @@
 // The exact gradient uses Tr(M L(A,E)) = Tr(L(A,M) E), valid for any
 // polynomial in A with scalar coefficients, so ONE Frechet derivative per
 // slice serves all n_c controls.
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "pgx_stages.cuh"
 
 namespace pgx {
@@ -440,8 +444,20 @@ __global__ void k_reduce(ProbDev p, WorkDev w, int want_grad) {
 // --------------------------------------------------------------------------
 template <class K>
 static void ensure_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  set_smem_once((const void*)kernel, bytes);
+}
+
+// The dynamic shared-memory limit is set once per kernel and device, so that
+// launches recorded into a CUDA graph never need to change function attributes.
+void set_smem_once(const void* fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.insert({fn, dev}).second)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 template <class K>

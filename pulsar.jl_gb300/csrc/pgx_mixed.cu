@@ -22,6 +22,11 @@ namespace pgx {
 
 static __constant__ df c_dfcoef[PGX_N_INVFACT] = PGX_INVFACT_DF_INIT;
 
+// Shared-memory layout of the team matrices (Lay<D, SW>).  Measured on GB300:
+// the XOR swizzle removes bank conflicts but its index arithmetic costs more
+// than the conflicts do, so the plain column-major layout is used.
+constexpr int kSwz = 0;
+
 // Teams of the slice-parallel mixed kernels.  A team of T threads owns one
 // matrix problem; a CTA holds 256 / T teams (T = 32: independent warps on
 // __syncwarp; 64 and 128: hardware barriers 1..; 256: the whole CTA).  Each
@@ -69,20 +74,20 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
   for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
     double2* Ad = reinterpret_cast<double2*>(B);  // FP64 assembly in the same bytes
-    build_A<D, T>(tm, p, w.u, m, k, Ad);
+    build_A<D, T, kSwz>(tm, p, w.u, m, k, Ad);
     tm.sync();
-    const double nrm = norm1<D, T>(tm, Ad, reinterpret_cast<double*>(red));
+    const double nrm = norm1<D, T, kSwz>(tm, Ad, reinterpret_cast<double*>(red));
     int deg, s;
     choose_degree(nrm, c_theta64, deg, s);
     const double sc = ldexp(1.0, -s);
-    for (int e = tm.lane; e < D * D; e += T) {  // each lane converts the entries it built
+    for (int e = tm.lane; e < D * D; e += T) {  // in place: same bytes, same lane (after the barriers above)
       const double2 a = Ad[e];
       B[e] = dfc_store(dfc_from(make_double2(a.x * sc, a.y * sc)));
     }
     tm.sync();
-    taylor_exp_df<D, T>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
+    taylor_exp_df<D, T, kSwz>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
-    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[e];
+    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[Lay<D, kSwz>::idx(e % D, e / D)];
     tm.sync();
   }
 }
@@ -204,7 +209,7 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd_mx(ProbDev p
 // g_j = Re(c dt scale Tr(X C_j)).  The team's first warp sums in a fixed order
 // (stride-32 partial sums, then a fixed shuffle tree) so that the result does
 // not depend on the team size the autotuner picks.
-template <int D, int T>
+template <int D, int T, int SW>
 __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDev& p, const float2* X,
                                                  int m, int k, double* Gout, float2*) {
   const double cds = p.dt[k] * p.m_scale[m];
@@ -213,7 +218,7 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
       const double2* Cj = p.ctrls + (size_t)j * D * D;
       float2 acc = make_float2(0.f, 0.f);
       for (int e = tm.lane; e < D * D; e += 32) {
-        const int r = e % D, c = e / D;
+        const int r = Lay<D, SW>::row(e), c = e / D;
         const double2 cv = Cj[c + D * r];
         acc = cmac(acc, X[e], make_float2((float)cv.x, (float)cv.y));
       }
@@ -248,13 +253,13 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
     double* Gout = w.Gm + ((size_t)m * p.n_t + k) * p.n_c;
     const float2* Mk = reinterpret_cast<const float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
     if (!exact) {
-      trace_controls32<D, T>(tm, p, Mk, m, k, Gout, red);
+      trace_controls32<D, T, 0>(tm, p, Mk, m, k, Gout, red);
       continue;
     }
-    for (int e = tm.lane; e < D * D; e += T) W.dB[e] = Mk[e];
-    build_A<D, T>(tm, p, w.u, m, k, W.B);
+    for (int e = tm.lane; e < D * D; e += T) W.dB[Lay<D, kSwz>::idx(e % D, e / D)] = Mk[e];
+    build_A<D, T, kSwz>(tm, p, w.u, m, k, W.B);
     tm.sync();
-    const double nrm = norm1<D, T>(tm, W.B, reinterpret_cast<double*>(red));
+    const double nrm = norm1<D, T, kSwz>(tm, W.B, reinterpret_cast<double*>(red));
     int deg, s;
     choose_degree(nrm, c_theta32, deg, s);
     const float sc = ldexpf(1.f, -s);
@@ -263,8 +268,8 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
       W.dB[e] = cscale(W.dB[e], sc);
     }
     tm.sync();
-    taylor_exp_frechet<D, T>(tm, W, deg, s, c_invf32);
-    trace_controls32<D, T>(tm, p, W.dY, m, k, Gout, red);
+    taylor_exp_frechet<D, T, kSwz>(tm, W, deg, s, c_invf32);
+    trace_controls32<D, T, kSwz>(tm, p, W.dY, m, k, Gout, red);
     tm.sync();
   }
 }
@@ -272,8 +277,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
 // ---- launchers ---------------------------------------------------------------------
 template <class K>
 static void ensure_smem_mx(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  set_smem_once((const void*)kernel, bytes);
 }
 
 template <class K>

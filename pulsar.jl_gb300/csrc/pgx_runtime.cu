@@ -490,8 +490,8 @@ extern "C" int pgx_problem_destroy(pgx_problem* p) {
 struct Marks {
   pgx_ctx* c;
   std::vector<cudaEvent_t> ev;
-  explicit Marks(pgx_ctx* ctx) : c(ctx) {
-    if (!c->stage_timing) return;
+  explicit Marks(pgx_ctx* ctx, bool enabled = true) : c(ctx) {
+    if (!c->stage_timing || !enabled) return;
     for (int i = 0; i <= PGX_N_STAGES; ++i) {
       cudaEvent_t e;
       if (!c->ev_pool.empty()) { e = c->ev_pool.back(); c->ev_pool.pop_back(); }
@@ -507,15 +507,16 @@ struct Marks {
   }
 };
 
-int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G) {
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream) {
   pgx_ctx* c = p->ctx;
-  const pgx::LaunchInfo li = p->launch_info();
+  pgx::LaunchInfo li = p->launch_info();
+  if (stream) li.stream = stream;  // batches enqueue on their own (captured) streams
   WorkDev w = p->w;
   w.u = d_u;
   w.G = d_G ? d_G : p->d_G;
   w.F = d_F;
   const bool want_grad = d_G != nullptr;
-  Marks mk(c);
+  Marks mk(c, stream == nullptr);
   int st;
   if (p->desc.precision == PGX_PREC_MIXED) {  // gate targets (validated at create)
     mk.mark(PGX_STAGE_EXPM);

@@ -50,5 +50,6 @@ struct pgx_problem {
 
 int ctx_fail(pgx_ctx* c, int status, const std::string& msg);
 int ctx_cuda(pgx_ctx* c, cudaError_t e, const char* where);
-int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G);
+// Enqueues one evaluation; stream = nullptr means the context stream.
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream = nullptr);
 int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats);

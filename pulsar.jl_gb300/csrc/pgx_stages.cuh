@@ -44,7 +44,7 @@ __device__ __forceinline__ double2 times_c(double2 v, int gen) {
 
 // A = c dt_k (drift + off O + scale sum_j u_jk C_j), assembled in FP64 and
 // stored as C (double2, or float2 for the FP32 stages).
-template <int D, int T, class C>
+template <int D, int T, int SW = 0, class C>
 __device__ __forceinline__ void build_A(const Team<T>& tm, const ProbDev& p, const double* u, int m,
                                         int k, C* A) {
   const double dt = p.dt[k];
@@ -68,7 +68,7 @@ __device__ __forceinline__ void build_A(const Team<T>& tm, const ProbDev& p, con
     C out;
     out.x = a.x;
     out.y = a.y;
-    A[e] = out;
+    A[Lay<D, SW>::idx(e % D, e / D)] = out;
   }
 }
 

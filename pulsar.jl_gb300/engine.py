@@ -103,6 +103,77 @@ def default_context() -> Context:
     return _DEFAULT
 
 
+def opt_desc(method: str = "grape", *, max_iter: int = 1000, convergence_tol: float = 1e-8,
+             step_size: float = 0.01, adapt_step_size: bool = True, min_step_size: float = 1e-10,
+             max_step_size: float = 10.0, gradient_norm_tol: float = 1e-6, lbfgs_memory: int = 10,
+             amplitude_limit: float = math.inf, l_bound: float = -1.0, u_bound: float = 1.0) -> "A.OptDesc":
+    """pgx_opt_desc with GRAPEConfig's defaults (GRAPE.jl:94-127)."""
+    o = A.OptDesc()
+    o.struct_size = C.sizeof(A.OptDesc)
+    o.method = A.OPT[method]
+    o.max_iter, o.adapt_step_size, o.lbfgs_memory = int(max_iter), int(bool(adapt_step_size)), int(lbfgs_memory)
+    o.convergence_tol, o.step_size = float(convergence_tol), float(step_size)
+    o.min_step_size, o.max_step_size = float(min_step_size), float(max_step_size)
+    o.gradient_norm_tol, o.amplitude_limit = float(gradient_norm_tol), float(amplitude_limit)
+    o.l_bound, o.u_bound = float(l_bound), float(u_bound)
+    return o
+
+
+class Batch:
+    """Uneven problems evaluated / iterated together, one CUDA graph per call."""
+
+    def __init__(self, problems, n_streams: int = 8):
+        if not problems:
+            raise ValueError("a batch needs at least one problem")
+        self.problems = list(problems)
+        self.ctx = self.problems[0].ctx
+        arr = (C.c_void_p * len(self.problems))(*[p._h for p in self.problems])
+        self._h = C.c_void_p()
+        A.check(A.lib().pgx_batch_create(self.ctx.handle, len(self.problems), arr, int(n_streams),
+                                         C.byref(self._h)), self.ctx.handle)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            A.lib().pgx_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def units(self) -> int:
+        v = C.c_int64()
+        A.check(A.lib().pgx_batch_units(self._h, C.byref(v)), self.ctx.handle)
+        return int(v.value)
+
+    def set_controls(self, i: int, u):
+        p = self.problems[i]
+        ub = p._load_u(u)
+        A.check(A.lib().pgx_batch_set_controls(self._h, int(i), A.as_dptr(ub)), self.ctx.handle)
+
+    def get_controls(self, i: int):
+        p = self.problems[i]
+        u = np.zeros(p.n_c * p.n_t)
+        G = np.zeros(p.n_c * p.n_t)
+        A.check(A.lib().pgx_batch_get_controls(self._h, int(i), A.as_dptr(u), A.as_dptr(G)), self.ctx.handle)
+        return u.reshape(p.n_t, p.n_c).T.copy(), G.reshape(p.n_t, p.n_c).T.copy()
+
+    def eval(self) -> np.ndarray:
+        F = np.zeros(len(self.problems))
+        A.check(A.lib().pgx_batch_eval(self._h, A.as_dptr(F)), self.ctx.handle)
+        return F
+
+    def iterate(self, n_iter: int, trace: bool = True, **opt):
+        o = opt_desc("grape", **opt)
+        tr = np.zeros((n_iter, len(self.problems))) if trace else None
+        A.check(A.lib().pgx_batch_iterate(self._h, int(n_iter), C.byref(o),
+                                          A.as_dptr(tr) if trace else None), self.ctx.handle)
+        return tr
+
+
 @dataclass
 class OptOutcome:
     controls: np.ndarray
@@ -246,15 +317,11 @@ class Problem:
                  max_step_size: float = 10.0, gradient_norm_tol: float = 1e-6,
                  lbfgs_memory: int = 10, amplitude_limit: float = math.inf,
                  l_bound: float = -1.0, u_bound: float = 1.0, history_cap: int = 0) -> OptOutcome:
-        o = A.OptDesc()
-        o.struct_size = C.sizeof(A.OptDesc)
-        o.method = A.OPT[method]
-        o.max_iter, o.adapt_step_size, o.lbfgs_memory = int(max_iter), int(bool(adapt_step_size)), \
-            int(lbfgs_memory)
-        o.convergence_tol, o.step_size = float(convergence_tol), float(step_size)
-        o.min_step_size, o.max_step_size = float(min_step_size), float(max_step_size)
-        o.gradient_norm_tol, o.amplitude_limit = float(gradient_norm_tol), float(amplitude_limit)
-        o.l_bound, o.u_bound = float(l_bound), float(u_bound)
+        o = opt_desc(method, max_iter=max_iter, convergence_tol=convergence_tol, step_size=step_size,
+                     adapt_step_size=adapt_step_size, min_step_size=min_step_size,
+                     max_step_size=max_step_size, gradient_norm_tol=gradient_norm_tol,
+                     lbfgs_memory=lbfgs_memory, amplitude_limit=amplitude_limit, l_bound=l_bound,
+                     u_bound=u_bound)
         ub = self._load_u(u0).copy()
         cap = history_cap or (4 * max_iter + 8)
         fh, gh = np.zeros(cap), np.zeros(cap)

@@ -1,7 +1,7 @@
 """Benchmark: ensemble-slice gradients per second of the GRAPE hot path.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload spin4|uneven512|lindblad3q] [--precision mixed|fp64]
+                  [--workload spin4|uneven512|lindblad3q|serve] [--precision mixed|fp64]
 
 Workloads (seeded synthetic inputs with the configurations' shapes):
   spin4 (default)  broadband robust gate: 4 coupled spin-1/2 (d = 16), 231
@@ -13,6 +13,11 @@ Workloads (seeded synthetic inputs with the configurations' shapes):
                    iteration (one CUDA graph).
   lindblad3q       3-qubit Lindblad gate (superoperator D = 64), 32 detuning
                    draws, 500 slices, exact gradient.
+  serve            Poisson job stream through the continuous-batching server
+                   (pgx_server): uneven-distribution jobs plus 20 % Lindblad
+                   gate jobs on 2-3 qubits, submitted in real time; reports
+                   served units/s, jobs/s, p50/p99 time-to-converged-pulse and
+                   |dF| of the served results against the FP64 GPU path.
 
 value : units/s with controls and results resident in HBM, CUDA events on the
         library's stream; each step's working set (propagator and chain stacks)
@@ -121,16 +126,8 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def gpu_problem(pg, ctx, prob, grad_mode: str, precision: str):
-    di, sc, of, w = prob.members()
-    kw = dict(ctx=ctx, generator=prob.generator, offset_op=prob.offset_op, member_drift=di,
-              member_scale=sc, member_offset=of, member_weight=w, target=prob.target,
-              fidelity=prob.fidelity, grad_mode=grad_mode, precision=precision)
-    if prob.target == "gate":
-        kw["target_op"] = prob.target_op
-    else:
-        kw["states_init"], kw["states_target"] = prob.states_init, prob.states_target
-    return pg.Problem(prob.drifts, prob.controls, prob.dt, **kw)
+def gpu_problem(pg, ctx, spec, grad_mode: str, precision: str):
+    return pg.Problem(ctx=ctx, **spec.problem_kwargs(grad_mode, precision))
 
 
 # ---------------------------------------------------------------------------
@@ -229,10 +226,109 @@ class Uneven:
             p.close()
 
 
+def run_serve(args, pg, ctx, rank: int, world: int):
+    """Served optimisation stream: Poisson arrivals submitted in real time
+    through the public server API (host buffers in, best controls out), then a
+    drain; the timed region is first submission -> drain."""
+    from pulsar_gb300 import workloads as W
+    warm = W.serve_stream(seed=1, rate=50.0, duration_s=0.08, lindblad_frac=0.5, max_slices=60,
+                          max_members=4, lindblad_slices=20, lindblad_draws=2)
+    jobs = W.serve_stream(seed=args.serve_seed, rate=args.serve_rate, duration_s=args.serve_seconds,
+                          max_slices=args.serve_max_slices, max_members=args.serve_max_members,
+                          lindblad_slices=args.serve_lindblad_slices, lindblad_draws=args.serve_lindblad_draws)
+    opt = dict(max_iter=args.serve_max_iter, step_size=args.serve_step)
+    budget = int(args.serve_budget_gb * 1e9)
+    kw = [j.spec.problem_kwargs("exact", args.precision) for j in jobs]
+    srv = pg.Server(ctx, max_inflight=args.serve_slots, hbm_budget_bytes=budget, target_fidelity=0.999)
+    for j in warm:  # first-use costs (module load, shared-memory limits) stay out of the timed region
+        srv.submit(u0=j.u0, opt=dict(max_iter=3, step_size=args.serve_step),
+                   **j.spec.problem_kwargs("exact", args.precision))
+    srv.drain()
+    s0 = srv.stats()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        t0 = time.perf_counter()
+        ids = []
+        for j, k in zip(jobs, kw):
+            dt = t0 + j.arrival_s - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(u0=j.u0, opt=opt, **k))
+        srv.drain()
+        el = time.perf_counter() - t0
+    st = srv.stats()
+    res = [srv.fetch(i) for i in ids]
+    srv.close()
+    units = st["units"] - s0["units"]
+    launches = st["kernel_launches"] - s0["kernel_launches"]
+    lat = np.array([r.latency_s for r in res if r.state == "done"])
+    # |dF| of the served (mixed) result against the plain FP64 GPU path at the returned controls
+    rng = np.random.default_rng(0)
+    pick = rng.choice(len(jobs), size=min(args.serve_check, len(jobs)), replace=False)
+    dF = []
+    for i in pick:
+        if res[i].state != "done":
+            continue
+        p = pg.Problem(ctx=ctx, **jobs[i].spec.problem_kwargs("exact", "fp64"))
+        F64 = p.eval(res[i].controls, want_grad=False)[0]
+        p.close()
+        dF.append(abs(F64 - res[i].fidelity))
+    kinds = {}
+    for j in jobs:
+        kinds[j.kind] = kinds.get(j.kind, 0) + 1
+    flops = sum(flops_per_unit("all", j.spec.D, j.spec.n_c, "exact") * j.spec.n_members * j.spec.n_t *
+                (r.n_iterations + 1) for j, r in zip(jobs, res))
+    pipe = "fp64" if args.precision == "fp64" else "fp32"
+    peak = ctx.measure_peak(pipe) * 1e9
+    h2d = sum(8 * (k["drifts"].size * 2 + k["controls"].size * 2 + j.u0.size) for j, k in zip(jobs, kw))
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        herm = [(j.spec, j.u0) for j in jobs if j.spec.generator == "hermitian" and j.spec.D <= 16][:16]
+        cpu = cpu_baseline_multi(herm, args.cpu_budget_s)
+    value = units / el
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": len(warm),
+            "ms_per_step": el * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+df32(f64 overlap)",
+            "data": "synthetic (seeded Poisson job stream)",
+            "config": {"workload": "serve", "offered_rate_jobs_s": args.serve_rate,
+                       "arrival_window_s": args.serve_seconds, "jobs": len(jobs), "job_kinds": kinds,
+                       "max_slices": args.serve_max_slices, "max_members": args.serve_max_members,
+                       "lindblad": f"2-3 qubits, {args.serve_lindblad_slices} slices, "
+                                   f"{args.serve_lindblad_draws} draws",
+                       "stop": f"F >= 0.999 or {args.serve_max_iter} iterations or grape_optimize's rules",
+                       "slots": args.serve_slots, "hbm_budget_gb": args.serve_budget_gb,
+                       "precision": args.precision, "grad_mode": "exact",
+                       "l2": "many concurrent jobs; working set of the stream >> 129 MB L2",
+                       "timed_region": "first submission -> drain (wall clock)"},
+            "serve": {"completed": int(st["completed"] - s0["completed"]), "failed": int(st["failed"]),
+                      "jobs_per_s": len(lat) / el,
+                      "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                      "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                      "mean_iterations": float(np.mean([r.n_iterations for r in res])),
+                      "converged_frac": float(np.mean([r.converged for r in res])),
+                      "hbm_peak_gb": st["hbm_peak"] / 1e9,
+                      "max_abs_dF_vs_fp64_gpu": max(dF) if dF else None,
+                      "median_abs_dF_vs_fp64_gpu": float(np.median(dF)) if dF else None,
+                      "dF_sample": len(dF)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(sum(8 * j.u0.size for j in jobs))},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "whole served stream", "bound": pipe, "achieved": flops / el / 1e12,
+                         "peak": peak / 1e12, "unit": "TFLOP/s", "frac": flops / el / peak if peak else None,
+                         "traffic": None,
+                         "peak_source": f"measured in this run: independent-FMA loop kernel on the "
+                                        f"{pipe.upper()} pipe"},
+            "clocks": clk.summary(), "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def cpu_baseline_single(prob, u0, budget_s: float):
     """The oracle's C restatement of the reference algorithm on all host cores
     (Hermitian generators), or the numpy oracle on a bounded sample otherwise."""
     threads = os.cpu_count() or 1
+    from oracle import members as mb
+    prob = mb.Problem.from_spec(prob)
     if prob.generator == "hermitian":
         from oracle import cpu_port
         cp = cpu_port.CpuProblem(prob, "ref_grape")
@@ -248,7 +344,6 @@ def cpu_baseline_single(prob, u0, budget_s: float):
                 "sample": f"{n} full evaluations ({prob.n_members} members x {prob.n_t} slices), reference "
                           f"algorithm (eigendecomposition propagators, first-order gradient), OpenMP over "
                           f"members, {el:.1f} s"}
-    from oracle import members as mb
     sub = mb.Problem(drifts=prob.drifts[:1], controls=prob.controls, dt=prob.dt[:25], generator=prob.generator,
                      target=prob.target, fidelity=prob.fidelity, target_op=prob.target_op, n_members=1)
     t0 = time.perf_counter()
@@ -264,8 +359,10 @@ def cpu_baseline_single(prob, u0, budget_s: float):
 
 def cpu_baseline_multi(cases, budget_s: float):
     from oracle import cpu_port
+    from oracle import members as mb
     threads = os.cpu_count() or 1
-    cps = [(cpu_port.CpuProblem(pr, "ref_grape"), u0, pr.n_members * pr.n_t) for pr, u0 in cases]
+    cps = [(cpu_port.CpuProblem(mb.Problem.from_spec(pr), "ref_grape"), u0, pr.n_members * pr.n_t)
+           for pr, u0 in cases]
     units, t0 = 0, time.perf_counter()
     while True:
         for cp, u0, un in cps:
@@ -280,17 +377,17 @@ def cpu_baseline_multi(cases, budget_s: float):
 
 
 def make_workload(args, pg, ctx, torch, dev):
-    from oracle import members as mb
+    from pulsar_gb300 import workloads as W
     if args.workload == "spin4":
-        prob, u0 = mb.spin4_ensemble(n_t=args.slices)
+        prob, u0 = W.spin4_ensemble(n_t=args.slices)
         return Single(f"spin4_d16_231members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
                       args.precision, torch, dev)
     if args.workload == "lindblad3q":
-        prob, u0 = mb.lindblad_3q()
+        prob, u0 = W.lindblad_3q()
         return Single("lindblad3q_D64_32members_500slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
                       torch, dev)
     if args.workload == "uneven512":
-        return Uneven("uneven512", mb.uneven_batch(512), pg, ctx, args.grad_mode, args.precision)
+        return Uneven("uneven512", W.uneven_batch(512), pg, ctx, args.grad_mode, args.precision)
     raise ValueError(args.workload)
 
 
@@ -301,13 +398,16 @@ def make_workload(args, pg, ctx, torch, dev):
 def run_reference(args, rank: int):
     if rank != 0:
         return 0
+    import __graft_entry__ as ge
+    ge.load_package()
+    from pulsar_gb300 import workloads as W
     from oracle import members as mb
     if args.workload == "spin4":
-        prob, u0 = mb.spin4_ensemble(n_t=args.slices)
+        prob, u0 = W.spin4_ensemble(n_t=args.slices)
         cases = [(prob, u0)]
         name = f"spin4_d16_231members_{prob.n_t}slices"
     elif args.workload == "uneven512":
-        cases = [c for c in mb.uneven_batch(512) if c[0].D <= 16][:16]
+        cases = [c for c in W.uneven_batch(512) if c[0].D <= 16][:16]
         name = "uneven512 (sample: first 16 problems with d <= 16)"
     else:
         print(json.dumps({"impl": "reference", "unavailable": "the oracle's C restatement covers Hermitian "
@@ -315,7 +415,8 @@ def run_reference(args, rank: int):
         return 0
     from oracle import cpu_port
     threads = os.cpu_count() or 1
-    cps = [(cpu_port.CpuProblem(pr, "ref_grape"), u0, pr.n_members * pr.n_t) for pr, u0 in cases]
+    cps = [(cpu_port.CpuProblem(mb.Problem.from_spec(pr), "ref_grape"), u0, pr.n_members * pr.n_t)
+           for pr, u0 in cases]
     for _ in range(args.warmup):
         for cp, u0, _ in cps:
             cp.eval(u0, True, threads)
@@ -350,7 +451,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spin4", choices=["spin4", "uneven512", "lindblad3q"])
+    ap.add_argument("--workload", default="spin4", choices=["spin4", "uneven512", "lindblad3q", "serve"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--grad-mode", default="exact", choices=["exact", "ref_grape", "ref_mr"])
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
@@ -359,6 +460,19 @@ def main():
                     help="skip timing the plain FP64 GPU form beside the mixed one")
     ap.add_argument("--slices", type=int, default=1000,
                     help="spin4 slices per member (1000 = the benchmark workload; smaller for profiling)")
+    sv = ap.add_argument_group("serve workload (Poisson job stream through pgx_server)")
+    sv.add_argument("--serve-rate", type=float, default=200.0, help="offered jobs/s")
+    sv.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window")
+    sv.add_argument("--serve-seed", type=int, default=5)
+    sv.add_argument("--serve-max-slices", type=int, default=200)
+    sv.add_argument("--serve-max-members", type=int, default=16)
+    sv.add_argument("--serve-lindblad-slices", type=int, default=50)
+    sv.add_argument("--serve-lindblad-draws", type=int, default=4)
+    sv.add_argument("--serve-max-iter", type=int, default=100)
+    sv.add_argument("--serve-step", type=float, default=0.01)
+    sv.add_argument("--serve-slots", type=int, default=128)
+    sv.add_argument("--serve-budget-gb", type=float, default=80.0)
+    sv.add_argument("--serve-check", type=int, default=48, help="jobs re-evaluated in FP64 for |dF|")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -380,6 +494,12 @@ def main():
     pg = ge.load_package()
     ctx = pg.Context(local)
     dev = torch.device(f"cuda:{local}")
+    if args.workload == "serve":
+        rc = run_serve(args, pg, ctx, rank, world)
+        ctx.close()
+        if dist:
+            dist.destroy_process_group()
+        return rc
     wl = make_workload(args, pg, ctx, torch, dev)
     torch.cuda.synchronize(dev)
 

@@ -277,6 +277,77 @@ int pgx_batch_eval(pgx_batch* batch, double* F);
  * F_trace ([n_iter][n], nullable) receives the objective of every iteration. */
 int pgx_batch_iterate(pgx_batch* batch, int32_t n_iter, const pgx_opt_desc* opt, double* F_trace);
 
+/* ---- serving -------------------------------------------------------------
+ * A continuous-batching optimisation server.  Jobs (a problem descriptor,
+ * grape_optimize settings and initial controls) are queued by pgx_submit and
+ * admitted, oldest first, while their HBM footprint fits the server budget
+ * and a slot is free.  Every admitted job runs the grape_optimize ascent
+ * (GRAPE.jl:536-610) with controls, gradient, step state and best controls
+ * device-resident; each job advances one iteration (one CUDA graph: ascent
+ * step, evaluation, 24-byte read-back) as soon as its previous one finished,
+ * so jobs of different sizes overlap on the device and a job that arrives
+ * while others run starts as soon as memory and a slot free up.  A job stops
+ * under check_grape_convergence (GRAPE.jl:371-402), at max_iter, or once its
+ * fidelity reaches the server's target_fidelity; its result is the best
+ * controls seen, as grape_optimize returns them.  A job runs the kernels of a
+ * solo run, so its result is bit-identical alone and in any mix.  Only
+ * PGX_OPT_GRAPE jobs are served.  The server uses a private context on the
+ * device of ctx; errors of pgx_submit are recorded on ctx.  No reference
+ * counterpart: Pulsar.jl optimises one problem per call.                   */
+enum { PGX_JOB_QUEUED = 0, PGX_JOB_RUNNING = 1, PGX_JOB_DONE = 2, PGX_JOB_FAILED = 3,
+       PGX_JOB_CANCELLED = 4 };
+
+typedef struct pgx_server_desc {
+  uint32_t struct_size;
+  int32_t max_inflight;        /* slots: jobs on the device at once (one stream each)  */
+  uint64_t hbm_budget_bytes;   /* admission budget over the jobs' footprints, 0 = none */
+  double target_fidelity;      /* serving stop rule F >= target; > 1 disables it       */
+} pgx_server_desc;
+
+typedef struct pgx_job_status {
+  int32_t state;               /* PGX_JOB_*                                             */
+  int32_t status;              /* PGX_OK or the error that failed the job               */
+  int32_t iterations;          /* ascent steps applied                                  */
+  int32_t reserved;
+  double fidelity;             /* objective at the current controls                     */
+  double best_fidelity;
+  double queue_s;              /* submit -> admission (so far, while queued)            */
+  double latency_s;            /* submit -> finish (so far, while unfinished)           */
+  char reason[96];
+} pgx_job_status;
+
+typedef struct pgx_serve_stats {
+  int64_t submitted, completed, failed, cancelled, running, queued;
+  int64_t kernel_launches;     /* kernels the server launched (graph nodes counted)     */
+  int64_t units;               /* member-slice gradient units evaluated                 */
+  uint64_t hbm_in_use, hbm_peak;
+  double elapsed_s;            /* since pgx_server_create                               */
+  double jobs_per_s;           /* completed / elapsed                                   */
+  double p50_latency_s, p99_latency_s;  /* submit -> converged pulse, completed jobs    */
+  double mean_iterations;
+} pgx_serve_stats;
+
+typedef struct pgx_server pgx_server;
+int pgx_server_create(pgx_ctx* ctx, const pgx_server_desc* desc, pgx_server** out);
+/* Cancels queued and running jobs, then frees the server. */
+int pgx_server_destroy(pgx_server* server);
+/* Deep-copies desc, opt and u0 ([n_c x n_t]); PGX_ERR_BUDGET when the job's
+ * footprint alone exceeds the server budget.                                */
+int pgx_submit(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_desc* opt,
+               const double* u0, uint64_t* job_id);
+int pgx_poll(pgx_server* server, uint64_t job_id, pgx_job_status* status);
+/* Result of a finished job: best controls u ([n_c x n_t], nullable) and the
+ * grape_optimize summary (nullable; histories are not kept).  Returns
+ * PGX_ERR_STATE while the job is queued or running, the job's error when it
+ * failed, PGX_ERR_CANCELLED when cancelled.  A fetched job is forgotten.    */
+int pgx_fetch(pgx_server* server, uint64_t job_id, double* u, pgx_opt_result* result);
+/* Queued jobs are dropped at once; running ones stop after their current
+ * iteration (their controls so far stay fetchable).                         */
+int pgx_cancel(pgx_server* server, uint64_t job_id);
+/* Waits until no job is queued or running; timeout_s <= 0 waits forever.   */
+int pgx_server_drain(pgx_server* server, double timeout_s);
+int pgx_server_stats(pgx_server* server, pgx_serve_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,19 @@ class Problem:
     def c(self) -> complex:
         return -1j if self.generator == "hermitian" else 1.0
 
+    @classmethod
+    def from_spec(cls, spec) -> "Problem":
+        """Copy of any object with the pgx_problem_desc fields (the package's
+        seeded workload specs): the oracle keeps its own reading of them."""
+        names = ("drifts", "controls", "dt", "generator", "offset_op", "member_drift", "member_scale",
+                 "member_offset", "member_weight", "target", "fidelity", "target_op", "states_init",
+                 "states_target", "n_members")
+        kw = {}
+        for n in names:
+            v = getattr(spec, n)
+            kw[n] = np.array(v) if isinstance(v, np.ndarray) else v
+        return cls(**kw)
+
 
 def _propagator(prob: Problem, G: np.ndarray, dt: float) -> np.ndarray:
     if prob.generator == "hermitian":
@@ -216,144 +229,3 @@ def eval_problem(prob: Problem, u: np.ndarray, grad_mode: str = "exact", want_gr
         return F, G, np.array(Fm_list)
     return F, G
 
-
-# ----------------------------------------------------------------------------
-# Builders for the benchmark workloads (seeded synthetic inputs)
-# ----------------------------------------------------------------------------
-
-SX = np.array([[0, 1], [1, 0]], C128)
-SY = np.array([[0, -1j], [1j, 0]], C128)
-SZ = np.array([[1, 0], [0, -1]], C128)
-I2 = np.eye(2, dtype=C128)
-
-
-def embed(op: np.ndarray, n: int, q: int) -> np.ndarray:
-    out = np.array([[1.0 + 0j]])
-    for i in range(n):
-        out = np.kron(out, op if i == q else I2)
-    return out
-
-
-def haar_unitary(rng: np.random.Generator, d: int) -> np.ndarray:
-    """QR of a complex Gaussian with the phase fix diag(sign(diag R))
-    (test/fixtures/ProblemLibrary.jl:742-746)."""
-    Z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / np.sqrt(2)
-    Qm, R = np.linalg.qr(Z)
-    ph = np.diag(R) / np.abs(np.diag(R))
-    return Qm * ph[None, :]
-
-
-def single_qubit_transfer(seed: int = 42, explicit_init: bool = False):
-    """Quickstart problem: H_d = (2 pi 10 / 2) sz, H_c = [0.5 sx, 0.5 sy],
-    100 slices over T = pi, |1> fixed-point target (legacy semantics) or the
-    explicit |0> -> |1> transfer.  Amplitudes U[-0.5, 0.5] from this repo's
-    seeded generator (the Julia MersenneTwister stream is not reproducible)."""
-    rng = np.random.default_rng(seed)
-    n_t = 100
-    dt = np.pi / n_t
-    u0 = 0.5 * (2 * rng.random((2, n_t)) - 1)
-    psi_t = np.array([0, 1], C128)
-    psi_i = np.array([1, 0], C128) if explicit_init else psi_t
-    prob = Problem(drifts=(2 * np.pi * 10 / 2 * SZ)[None], controls=np.stack([0.5 * SX, 0.5 * SY]),
-                   dt=np.full(n_t, dt), target="states", fidelity="square",
-                   states_init=psi_i[None], states_target=psi_t[None])
-    return prob, u0
-
-
-def spin4_ensemble(seed: int = 7, n_t: int = 1000, n_off: int = 21, n_b1: int = 11):
-    """Four coupled spin-1/2 (d=16): shifts U[-2,2] kHz, isotropic J U[5,200] Hz
-    on all 6 pairs (QuantumSystem.jl:425-433), controls 2 pi sum Ix / sum Iy,
-    Haar target (seed 7), dt = 1 us, amplitudes U[-10,10] kHz; ensemble of
-    n_off offsets over +-1 kHz (2 pi off sum Iz) x n_b1 B1 scales 0.9..1.1."""
-    rng = np.random.default_rng(seed)
-    n = 4
-    Ix = [embed(SX / 2, n, q) for q in range(n)]
-    Iy = [embed(SY / 2, n, q) for q in range(n)]
-    Iz = [embed(SZ / 2, n, q) for q in range(n)]
-    shifts = rng.uniform(-2e3, 2e3, n)
-    H = sum(2 * np.pi * shifts[q] * Iz[q] for q in range(n))
-    for a in range(n):
-        for b in range(a + 1, n):
-            J = rng.uniform(5.0, 200.0)
-            H = H + 2 * np.pi * J * (Ix[a] @ Ix[b] + Iy[a] @ Iy[b] + Iz[a] @ Iz[b])
-    Hc = np.stack([2 * np.pi * sum(Ix), 2 * np.pi * sum(Iy)])
-    T = haar_unitary(rng, 16)
-    u0 = rng.uniform(-1e4, 1e4, (2, n_t))
-    offs = np.linspace(-1e3, 1e3, n_off) if n_off > 1 else np.zeros(1)
-    b1 = np.linspace(0.9, 1.1, n_b1) if n_b1 > 1 else np.ones(1)
-    mo = np.repeat(2 * np.pi * offs, n_b1)
-    ms = np.tile(b1, n_off)
-    prob = Problem(drifts=H[None], controls=Hc, dt=np.full(n_t, 1e-6), offset_op=sum(Iz),
-                   member_offset=mo, member_scale=ms, target="gate", fidelity="square",
-                   target_op=T, n_members=n_off * n_b1)
-    return prob, u0
-
-
-def _rand_herm(rng, d, sigma):
-    A = rng.normal(0.0, sigma, (d, d)) + 1j * rng.normal(0.0, sigma, (d, d))
-    return (A + A.conj().T) / 2
-
-
-def uneven_problem(rng: np.random.Generator, d: int = None, n_t: int = None, n_members: int = None):
-    """One problem of the uneven batch: d uniform in {2,4,8,16,32}, n_t
-    log-uniform in [50, 2000], ensemble size log-uniform in [1, 128]; drift a
-    random Hermitian with Gaussian entries (sigma = 2 pi 1 MHz), 2-6 random
-    Hermitian controls of the same scale, members spread by a B1 scale
-    U[0.9, 1.1] and a detuning U[-0.1, 0.1] sigma along a random diagonal;
-    Haar-random gate target; dt = 0.2 / (2 sigma sqrt(d)) so ||H dt|| ~ 0.2."""
-    sigma = 2 * np.pi * 1e6
-    d = int(rng.choice([2, 4, 8, 16, 32])) if d is None else d
-    n_t = int(np.round(np.exp(rng.uniform(np.log(50), np.log(2000))))) if n_t is None else n_t
-    nm = int(np.round(np.exp(rng.uniform(0.0, np.log(128))))) if n_members is None else n_members
-    n_c = int(rng.integers(2, 7))
-    H = _rand_herm(rng, d, sigma)
-    C = np.stack([_rand_herm(rng, d, sigma) for _ in range(n_c)])
-    O = np.diag(rng.uniform(-1, 1, d)).astype(C128)
-    dt = 0.2 / (2 * sigma * np.sqrt(d))
-    prob = Problem(drifts=H[None], controls=C, dt=np.full(n_t, dt), offset_op=O,
-                   member_scale=rng.uniform(0.9, 1.1, nm), member_offset=rng.uniform(-0.1, 0.1, nm) * sigma,
-                   target="gate", fidelity="square", target_op=haar_unitary(rng, d), n_members=nm)
-    return prob, rng.uniform(-1, 1, (n_c, n_t))
-
-
-def uneven_batch(n_problems: int = 512, seed: int = 4):
-    rng = np.random.default_rng(seed)
-    return [uneven_problem(rng) for _ in range(n_problems)]
-
-
-def lindblad_3q(seed: int = 11, n_t: int = 500, n_draws: int = 32):
-    """Three qubits, ZZ U[0.1,1] MHz on 3 pairs, detuning U[-0.5,0.5] MHz per
-    qubit (redrawn per ensemble member), T1 U[20,100] us, T2 = T1 U(0.5,1);
-    jumps sqrt(1/T1) s-  and sqrt(g_phi/2) sz with g_phi = 1/T2 - 1/(2 T1);
-    controls sx_q, sy_q (x 2 pi 1 MHz); CCZ gate target as the superoperator
-    conj(U) (x) U; 500 slices over 2 us."""
-    rng = np.random.default_rng(seed)
-    n = 3
-    sm = np.array([[0, 1], [0, 0]], C128)
-    ZZ = sum(2 * np.pi * rng.uniform(0.1e6, 1e6) * embed(SZ, n, a) @ embed(SZ, n, b)
-             for a in range(n) for b in range(a + 1, n))
-    T1 = rng.uniform(20e-6, 100e-6, n)
-    T2 = T1 * rng.uniform(0.5, 1.0, n)
-    jumps, rates = [], []
-    for q in range(n):
-        jumps.append(embed(sm, n, q))
-        rates.append(1.0 / T1[q])
-        gphi = 1.0 / T2[q] - 1.0 / (2 * T1[q])
-        jumps.append(embed(SZ, n, q))
-        rates.append(max(gphi, 0.0) / 2.0)
-    drifts = []
-    for _ in range(n_draws):
-        det = rng.uniform(-0.5e6, 0.5e6, n)
-        Hd = ZZ + sum(2 * np.pi * det[q] * embed(SZ, n, q) / 2 for q in range(n))
-        drifts.append(rs.build_drift_liouvillian(Hd, jumps, rates))
-    ctrls = []
-    for q in range(n):
-        ctrls.append(rs.build_control_liouvillian(2 * np.pi * 1e6 * embed(SX, n, q) / 2))
-        ctrls.append(rs.build_control_liouvillian(2 * np.pi * 1e6 * embed(SY, n, q) / 2))
-    ccz = np.diag([1, 1, 1, 1, 1, 1, 1, -1]).astype(C128)
-    S = np.kron(ccz.conj(), ccz)
-    u0 = rng.uniform(-0.5, 0.5, (2 * n, n_t))
-    prob = Problem(drifts=np.stack(drifts), controls=np.stack(ctrls), dt=np.full(n_t, 2e-6 / n_t),
-                   generator="liouvillian", member_drift=np.arange(n_draws), target="gate",
-                   fidelity="square", target_op=S, n_members=n_draws)
-    return prob, u0

@@ -7,7 +7,7 @@ The directory is named ``pulsar.jl_gb300``; import it as ``pulsar_gb300``
 through ``__graft_entry__.load_package()``.
 """
 from . import _abi
-from .engine import Batch, Context, Problem, default_context, opt_desc
+from .engine import Batch, Context, Problem, Server, default_context, opt_desc, problem_desc
 from .api import (
     ControlSequence, EnsembleObjective, GRAPEConfig, LindbladMRControl, MRControl,
     OptimizationResult, QuantumSystem, QuantumTarget, build_control_liouvillian,

@@ -66,6 +66,33 @@ class OptResult(C.Structure):
     ]
 
 
+JOB_STATE = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("max_inflight", C.c_int32),
+                ("hbm_budget_bytes", C.c_uint64), ("target_fidelity", C.c_double)]
+
+
+class JobStatus(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32), ("status", C.c_int32), ("iterations", C.c_int32),
+        ("reserved", C.c_int32), ("fidelity", C.c_double), ("best_fidelity", C.c_double),
+        ("queue_s", C.c_double), ("latency_s", C.c_double), ("reason", C.c_char * 96),
+    ]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+        ("cancelled", C.c_int64), ("running", C.c_int64), ("queued", C.c_int64),
+        ("kernel_launches", C.c_int64), ("units", C.c_int64), ("hbm_in_use", C.c_uint64),
+        ("hbm_peak", C.c_uint64), ("elapsed_s", C.c_double), ("jobs_per_s", C.c_double),
+        ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double),
+        ("mean_iterations", C.c_double),
+    ]
+
+
 # name -> (restype, argtypes); every symbol declared in include/pgx.h
 SIGNATURES = {
     "pgx_abi_version": (C.c_int, []),
@@ -104,6 +131,15 @@ SIGNATURES = {
                                                C.c_size_t]),
     "pgx_optimize": (C.c_int, [C.c_void_p, C.POINTER(OptDesc), dptr, dptr, dptr, C.c_int32,
                                C.POINTER(OptResult)]),
+    "pgx_server_create": (C.c_int, [C.c_void_p, C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
+    "pgx_server_destroy": (C.c_int, [C.c_void_p]),
+    "pgx_submit": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(OptDesc), dptr,
+                             C.POINTER(C.c_uint64)]),
+    "pgx_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(JobStatus)]),
+    "pgx_fetch": (C.c_int, [C.c_void_p, C.c_uint64, dptr, C.POINTER(OptResult)]),
+    "pgx_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "pgx_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+    "pgx_server_stats": (C.c_int, [C.c_void_p, C.POINTER(ServeStats)]),
 }
 
 _LIB = None

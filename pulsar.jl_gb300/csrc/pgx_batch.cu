@@ -22,28 +22,11 @@
 #include "pgx.h"
 #include "pgx_runtime.h"
 
+using pgx::AscentState;
+using pgx::StepArgs;
+using pgx::kStepThreads;
+
 namespace {
-
-// Per-problem device state of the batched ascent loop.
-struct AscentState {
-  double step;     // current step size
-  double F_prev;   // objective of the previous iteration
-  int iter;        // iterations applied
-  int pad;
-};
-
-struct StepArgs {
-  double** u;            // [n] controls
-  double* const* G;      // [n] gradients
-  double* const* F;      // [n] objectives (F[i][0])
-  const int* len;        // [n] n_c * n_t
-  AscentState* st;       // [n]
-  double* trace;         // [cap][n] objective per iteration, or null
-  double* F_all;         // [n] gathered objectives
-  int n, trace_cap;
-  int adapt;
-  double lo, hi;         // step clamp
-};
 
 // One CTA per problem: the step rule of adapt_grape_step_size, then u += step G.
 __global__ void k_ascent_step(StepArgs a) {
@@ -70,7 +53,22 @@ __global__ void k_ascent_step(StepArgs a) {
   __syncthreads();
   double* u = a.u[i];
   const double* G = a.G[i];
-  for (int k = threadIdx.x; k < a.len[i]; k += blockDim.x) u[k] = fma(step, G[k], u[k]);
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < a.len[i]; k += blockDim.x) {
+    const double g = G[k];
+    acc = fma(g, g, acc);
+    u[k] = fma(step, g, u[k]);
+  }
+  if (a.gnorm) {  // fixed-order tree: the same bits on every run
+    __shared__ double red[kStepThreads];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kStepThreads / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) a.gnorm[i] = sqrt(red[0]);
+  }
 }
 
 __global__ void k_gather_F(double* const* F, double* out, int n) {
@@ -79,6 +77,11 @@ __global__ void k_gather_F(double* const* F, double* out, int n) {
 }
 
 }  // namespace
+
+cudaError_t pgx::launch_ascent_step(const StepArgs& a, cudaStream_t stream) {
+  k_ascent_step<<<a.n, kStepThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
 
 struct pgx_batch {
   pgx_ctx* ctx = nullptr;
@@ -134,7 +137,7 @@ static int capture(pgx_batch* b, bool with_step, cudaGraphExec_t* out) {
   }
   const int n = (int)b->probs.size();
   if (!st) {
-    if (with_step) k_ascent_step<<<n, 128, 0, s0>>>(b->step_args);
+    if (with_step) k_ascent_step<<<n, kStepThreads, 0, s0>>>(b->step_args);
     else k_gather_F<<<(n + 127) / 128, 128, 0, s0>>>(b->d_F, b->d_F_all, n);
     ++c->launches;
   }
@@ -325,7 +328,7 @@ extern "C" int pgx_batch_iterate(pgx_batch* b, int32_t n_iter, const pgx_opt_des
     b->iter_exec = nullptr;
   }
   if (!b->iter_exec) {
-    b->step_args = StepArgs{b->d_u, b->d_G, b->d_F, b->d_len, b->d_state, b->d_trace, b->d_F_all, n,
+    b->step_args = StepArgs{b->d_u, b->d_G, b->d_F, b->d_len, b->d_state, b->d_trace, b->d_F_all, nullptr, n,
                             b->trace_cap, o->adapt_step_size, o->min_step_size, o->max_step_size};
     if ((st = capture(b, true, &b->iter_exec))) return st;
     std::memcpy(b->opt_key, key, sizeof key);

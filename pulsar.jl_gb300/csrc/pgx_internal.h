@@ -61,6 +61,35 @@ struct LaunchInfo {
   int team[kNumTunable] = {0, 0};
 };
 
+// Device state of the grape_optimize ascent (GRAPE.jl:536-610) run on the
+// device by batches and the server.
+struct AscentState {
+  double step;     // current step size
+  double F_prev;   // objective of the previous iteration
+  int iter;        // steps applied
+  int pad;
+};
+
+constexpr int kStepThreads = 128;  // threads of the ascent-step CTA
+
+struct StepArgs {
+  double** u;            // [n] controls
+  double* const* G;      // [n] gradients
+  double* const* F;      // [n] objectives (F[i][0])
+  const int* len;        // [n] n_c * n_t
+  AscentState* st;       // [n]
+  double* trace;         // [cap][n] objective per step, or null
+  double* F_all;         // [n] gathered objectives
+  double* gnorm;         // [n] ||G|| of the gradient the step uses, or null
+  int n, trace_cap;
+  int adapt;
+  double lo, hi;         // step clamp
+};
+
+// adapt_grape_step_size (GRAPE.jl:309-334) then grape_step! (:261-268) for
+// the n problems of `a`, one CTA each.
+cudaError_t launch_ascent_step(const StepArgs& a, cudaStream_t stream);
+
 // Raises a kernel's dynamic shared-memory limit (once per kernel and device).
 void set_smem_once(const void* fn, size_t bytes);
 

@@ -45,10 +45,11 @@ int ctx_alloc(pgx_ctx* c, void** p, size_t bytes, std::vector<void*>& owned, uin
   if (c->budget && c->used + bytes > c->budget)
     return ctx_fail(c, PGX_ERR_BUDGET, "HBM budget exceeded: " + std::to_string(c->used + bytes) +
                                            " > " + std::to_string(c->budget) + " bytes");
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream) : cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return ctx_cuda(c, e, "cudaMalloc");
+    *p = nullptr;
+    return ctx_cuda(c, e, "device allocation");
   }
   owned.push_back(*p);
   c->used += bytes;
@@ -316,6 +317,9 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
          2 * sizeof(double) + consts;
 }
 
+int validate_desc(pgx_ctx* c, const pgx_problem_desc* d) { return validate(c, d); }
+uint64_t problem_footprint(const pgx_problem_desc* d, int num_sms) { return footprint(d, num_sms); }
+
 extern "C" int pgx_problem_footprint(const pgx_problem_desc* d, uint64_t* bytes) {
   if (!d || !bytes) return PGX_ERR_INVALID;
   if (d->struct_size < sizeof(pgx_problem_desc) || d->dim < 1 || d->dim > pgx::kMaxDim ||
@@ -358,8 +362,9 @@ static int upload(pgx_problem* p, T** dptr, const std::vector<T>& host) {
   int st = ctx_alloc(p->ctx, (void**)dptr, host.size() * sizeof(T), p->owned, p->bytes);
   if (st) return st;
   if (host.empty()) return PGX_OK;
-  return ctx_cuda(p->ctx, cudaMemcpy(*dptr, host.data(), host.size() * sizeof(T),
-                                     cudaMemcpyHostToDevice), "upload");
+  // pageable source: the call returns once `host` has been staged
+  return ctx_cuda(p->ctx, cudaMemcpyAsync(*dptr, host.data(), host.size() * sizeof(T),
+                                          cudaMemcpyHostToDevice, p->ctx->stream), "upload");
 }
 
 extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_problem** out) {
@@ -462,12 +467,23 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
     pgx_problem_destroy(p);
     return st;
   }
-  if (cudaMallocHost((void**)&p->h_stage, 2 * s.u + 2 * sizeof(double)) != cudaSuccess) {
-    cudaGetLastError();
+  if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "upload sync"))) {
     pgx_problem_destroy(p);
-    return ctx_fail(c, PGX_ERR_NOMEM, "pinned staging allocation failed");
+    return st;
   }
   *out = p;
+  return PGX_OK;
+}
+
+// Pinned staging buffer of the host-facing calls (u | G | F), made on first use.
+static int stage_buffer(pgx_problem* p) {
+  if (p->h_stage) return PGX_OK;
+  const size_t n = (size_t)p->desc.n_controls * p->desc.n_slices;
+  if (cudaMallocHost((void**)&p->h_stage, (2 * n + 2) * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    p->h_stage = nullptr;
+    return ctx_fail(p->ctx, PGX_ERR_NOMEM, "pinned staging allocation failed");
+  }
   return PGX_OK;
 }
 
@@ -475,7 +491,10 @@ extern "C" int pgx_problem_destroy(pgx_problem* p) {
   if (!p) return PGX_ERR_INVALID;
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
-  for (void* q : p->owned) cudaFree(q);
+  for (void* q : p->owned) {
+    if (p->ctx->pool) cudaFreeAsync(q, p->ctx->stream);
+    else cudaFree(q);
+  }
   if (p->h_stage) cudaFreeHost(p->h_stage);
   p->ctx->used -= p->bytes;
   delete p;
@@ -577,6 +596,7 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
     return PGX_OK;
   }
   cudaSetDevice(c->device);
+  if (const int sb = stage_buffer(p)) return sb;
   std::memcpy(p->h_stage, u, n * sizeof(double));
   int st = ctx_cuda(c, cudaMemcpyAsync(p->d_u, p->h_stage, n * sizeof(double), cudaMemcpyHostToDevice,
                                        c->stream), "H2D u");
@@ -677,6 +697,7 @@ int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_st
   if (!finite_all(u, n)) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
   cudaSetDevice(c->device);
   const int64_t l0 = c->launches;
+  if (const int sb = stage_buffer(p)) return sb;
   std::memcpy(p->h_stage, u, n * sizeof(double));
   int st;
   if ((st = ctx_cuda(c, cudaEventRecord(c->ev0, c->stream), "event"))) return st;
@@ -736,6 +757,7 @@ extern "C" int pgx_total_propagator(pgx_problem* p, const double* u, int32_t mem
   const size_t n = (size_t)p->desc.n_controls * p->desc.n_slices;
   if (!finite_all(u, n)) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
   cudaSetDevice(c->device);
+  if (const int sb = stage_buffer(p)) return sb;
   std::memcpy(p->h_stage, u, n * sizeof(double));
   int st = ctx_cuda(c, cudaMemcpyAsync(p->d_u, p->h_stage, n * sizeof(double), cudaMemcpyHostToDevice,
                                        c->stream), "H2D u");

@@ -18,6 +18,9 @@ struct pgx_ctx {
   uint64_t used = 0;                           // bytes held by live problems
   int64_t launches = 0;
   std::string err;
+  // Stream-ordered allocation: when set, problem buffers come from this pool
+  // on `stream` and are released with cudaFreeAsync (no device-wide sync).
+  cudaMemPool_t pool = nullptr;
   // per-stage timing (pgx_ctx_set_stage_timing)
   bool stage_timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -36,7 +39,7 @@ struct pgx_problem {
   double* d_u = nullptr;
   double* d_G = nullptr;
   double* d_F = nullptr;   // [2]: objective, scratch
-  double* h_stage = nullptr;  // pinned: u | G | F
+  double* h_stage = nullptr;  // pinned: u | G | F (allocated on first host evaluation)
   std::vector<double> h_weight;
   std::vector<void*> owned;
   uint64_t bytes = 0;
@@ -49,6 +52,9 @@ struct pgx_problem {
 };
 
 int ctx_fail(pgx_ctx* c, int status, const std::string& msg);
+// Descriptor validation (errors recorded on c) and device footprint in bytes.
+int validate_desc(pgx_ctx* c, const pgx_problem_desc* d);
+uint64_t problem_footprint(const pgx_problem_desc* d, int num_sms);
 int ctx_cuda(pgx_ctx* c, cudaError_t e, const char* where);
 // Enqueues one evaluation; stream = nullptr means the context stream.
 int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream = nullptr);

@@ -1,0 +1,689 @@
+// Continuous-batching optimisation server.
+//
+// A worker thread owns the GPU side and a private context.  Its loop:
+//   1. admission: queued jobs, oldest first, take a free slot (stream, event,
+//      pinned read-back block) while their HBM footprint fits the budget; the
+//      problem is created, the controls uploaded and the first evaluation
+//      enqueued -- everything stays device-resident from here on;
+//   2. progress: every job whose in-flight iteration has finished (its slot
+//      event) is checked against the stop rules of grape_optimize and either
+//      retired (best controls copied out, HBM and slot freed) or given its
+//      next iteration -- one CUDA graph: the ascent step, the evaluation at the
+//      new controls and a 24-byte read-back of (F, ||G||, step).
+// Jobs never wait for each other: a small job iterates at its own pace while a
+// large one runs, and a job that arrives while others are on the device is
+// admitted as soon as memory and a slot free up.  Each job runs exactly the
+// kernels of a solo run on its own stream, so its trajectory is bit-identical
+// alone and in any mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "pgx.h"
+#include "pgx_runtime.h"
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+// Device block of one job: the one-problem tables of its StepArgs.
+struct JobDev {
+  double* u;
+  double* G;
+  double* F;
+  int len;
+  int pad;
+  double gnorm;              // ||G|| the last step used
+  pgx::AscentState st;       // st.step follows gnorm: both read back together
+  double F_out;
+};
+
+// Host read-back block of a slot (pinned): F at the new controls, ||G|| and
+// step of the step that produced them.
+struct Readback {
+  double F;
+  double gnorm;
+  double step;
+};
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  Readback* hb = nullptr;
+};
+
+struct Job {
+  uint64_t id = 0;
+  int state = PGX_JOB_QUEUED;   // guarded by the server mutex
+  int status = PGX_OK;
+  std::string reason;
+  std::atomic<bool> cancel{false};
+  // owned copies of the descriptor's arrays
+  std::vector<double> dt, drifts, controls, offset, mscale, moffset, mweight, target, sinit, starg, sgrad;
+  std::vector<int32_t> mdrift;
+  pgx_problem_desc desc{};
+  pgx_opt_desc opt{};
+  std::vector<double> u;        // initial controls, then the result
+  uint64_t footprint = 0;
+  int64_t units = 0;            // member-slice units per evaluation
+  // device side (worker thread only)
+  int slot = -1;
+  pgx_problem* prob = nullptr;
+  JobDev* dev = nullptr;
+  double* d_best = nullptr;
+  cudaGraphExec_t iter_exec = nullptr;
+  int64_t iter_kernels = 0;
+  bool inflight = false;
+  // ascent bookkeeping (written by the worker under the server mutex)
+  int round = -1;               // completed evaluations - 1 = steps applied
+  std::vector<double> fh;       // grape_optimize fidelity history
+  double F = 0.0, bestF = -INFINITY, step = 0.0;
+  bool converged = false;
+  clk::time_point t_submit, t_start, t_end;
+};
+
+template <class T>
+std::vector<T> copy_of(const T* p, size_t n) {
+  return p ? std::vector<T>(p, p + n) : std::vector<T>();
+}
+
+}  // namespace
+
+struct pgx_server {
+  pgx_ctx* user = nullptr;   // submit errors are recorded here
+  pgx_ctx* ctx = nullptr;    // private: used by the worker thread only
+  cudaStream_t ctx_stream = nullptr;  // the private context's own stream
+  cudaMemPool_t pool = nullptr;       // stream-ordered job memory (kept for reuse)
+  pgx_server_desc cfg{};
+  std::vector<Slot> slots;
+  std::vector<int> free_slots;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv, done_cv;
+  bool stop = false;
+  uint64_t next_id = 1;
+  std::deque<std::shared_ptr<Job>> queue;
+  std::vector<std::shared_ptr<Job>> running;  // mutated by the worker under mu
+  std::map<uint64_t, std::shared_ptr<Job>> jobs;
+  uint64_t hbm_in_use = 0, hbm_peak = 0;
+  int64_t submitted = 0, completed = 0, failed = 0, cancelled = 0;
+  std::atomic<int64_t> units{0}, launches{0};  // written by the worker, read by stats
+  std::vector<double> latencies;
+  std::vector<int> iters_done;
+  clk::time_point t0;
+};
+
+namespace {
+
+// Points the private context at a slot stream for the duration of a scope, so
+// a job's allocations, uploads and frees are ordered on its own stream (and
+// never synchronise the device).
+struct OnStream {
+  pgx_server* s;
+  OnStream(pgx_server* srv, cudaStream_t st) : s(srv) { s->ctx->stream = st; }
+  ~OnStream() { s->ctx->stream = s->ctx_stream; }
+};
+
+// Copies the best controls out, frees the job's device side.  Worker thread,
+// mutex NOT held.
+void release_device(pgx_server* s, Job& j) {
+  if (j.slot < 0) return;
+  const cudaStream_t stm = s->slots[j.slot].stream;
+  OnStream on(s, stm);
+  cudaStreamSynchronize(stm);
+  if (j.prob) {
+    const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+    if (j.round >= 0 && j.d_best) {
+      j.u.resize(n);
+      cudaMemcpy(j.u.data(), j.d_best, n * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    pgx_problem_destroy(j.prob);
+    j.prob = nullptr;
+  }
+  if (j.iter_exec) cudaGraphExecDestroy(j.iter_exec);
+  j.iter_exec = nullptr;
+  if (j.dev) cudaFreeAsync(j.dev, stm);
+  j.dev = nullptr;
+  if (j.d_best) cudaFreeAsync(j.d_best, stm);
+  j.d_best = nullptr;
+  cudaGetLastError();
+}
+
+// Worker thread, mutex held: final bookkeeping of a job that left `running`;
+// frees its slot and budget share.
+void record_end(pgx_server* s, Job& j, int state, const std::string& why) {
+  j.state = state;
+  j.reason = why;
+  j.t_end = clk::now();
+  if (j.slot >= 0) {
+    s->free_slots.push_back(j.slot);
+    j.slot = -1;
+    s->hbm_in_use -= j.footprint;
+  }
+  if (state == PGX_JOB_DONE) {
+    ++s->completed;
+    s->latencies.push_back(secs(j.t_submit, j.t_end));
+    s->iters_done.push_back(std::max(j.round, 0));
+  } else if (state == PGX_JOB_FAILED) {
+    ++s->failed;
+  } else {
+    ++s->cancelled;
+  }
+}
+
+// Creates the job's problem and device block on its slot and enqueues the
+// evaluation at the initial controls.
+int admit(pgx_server* s, Job& j) {
+  pgx_ctx* c = s->ctx;
+  const Slot& sl = s->slots[j.slot];
+  OnStream on(s, sl.stream);
+  int st = pgx_problem_create(c, &j.desc, &j.prob);
+  if (st) return st;
+  const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+  if (cudaMallocFromPoolAsync((void**)&j.dev, sizeof(JobDev), s->pool, sl.stream) != cudaSuccess ||
+      cudaMallocFromPoolAsync((void**)&j.d_best, n * sizeof(double), s->pool, sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_NOMEM;
+  }
+  JobDev h{};
+  h.u = j.prob->d_u;
+  h.G = j.prob->d_G;
+  h.F = j.prob->d_F;
+  h.len = (int)n;
+  h.st = pgx::AscentState{j.opt.step_size, 0.0, 0, 0};
+  j.step = j.opt.step_size;
+  if (cudaMemcpyAsync(j.dev, &h, sizeof(JobDev), cudaMemcpyHostToDevice, sl.stream) != cudaSuccess ||
+      cudaMemcpyAsync(j.prob->d_u, j.u.data(), n * sizeof(double), cudaMemcpyHostToDevice, sl.stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  const int64_t l0 = c->launches;
+  if ((st = run_pipeline(j.prob, j.prob->d_u, j.prob->d_F, j.prob->d_G, sl.stream))) return st;
+  s->launches += c->launches - l0;
+  if (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) !=
+          cudaSuccess ||
+      cudaEventRecord(sl.done, sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  j.inflight = true;
+  return PGX_OK;
+}
+
+// One iteration of a job as a graph: step, evaluation, read-back.
+int capture_iteration(pgx_server* s, Job& j) {
+  pgx_ctx* c = s->ctx;
+  const Slot& sl = s->slots[j.slot];
+  JobDev* d = j.dev;
+  const pgx::StepArgs a{&d->u, &d->G, &d->F, &d->len, &d->st, nullptr, &d->F_out, &d->gnorm,
+                        1, 0, j.opt.adapt_step_size, j.opt.min_step_size, j.opt.max_step_size};
+  const int64_t l0 = c->launches;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  int st = pgx::launch_ascent_step(a, sl.stream) == cudaSuccess ? PGX_OK : PGX_ERR_CUDA;
+  if (!st) st = run_pipeline(j.prob, j.prob->d_u, j.prob->d_F, j.prob->d_G, sl.stream);
+  if (!st && (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) !=
+                  cudaSuccess ||
+              cudaMemcpyAsync(&sl.hb->gnorm, &d->gnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              sl.stream) != cudaSuccess))
+    st = PGX_ERR_CUDA;
+  const cudaError_t e = cudaStreamEndCapture(sl.stream, &g);
+  j.iter_kernels = 1 + (c->launches - l0);
+  c->launches = l0;  // recorded, not launched: each replay counts them
+  if (!st && e != cudaSuccess) st = PGX_ERR_CUDA;
+  if (!st && cudaGraphInstantiate(&j.iter_exec, g, 0) != cudaSuccess) st = PGX_ERR_CUDA;
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  return st;
+}
+
+// check_grape_convergence (GRAPE.jl:371-402) on the history as grape_optimize
+// holds it at iteration `round`: F(u0) twice, then F(u_1) .. F(u_{round-1}).
+bool ref_converged(const Job& j, double gnorm, const char** why) {
+  const size_t n = j.fh.size();
+  if (j.fh.back() >= 1.0 - 1e-12) { *why = "perfect fidelity (F >= 1 - 1e-12)"; return true; }
+  if (gnorm < j.opt.gradient_norm_tol) { *why = "gradient norm below tolerance"; return true; }
+  if (n >= 3 && std::fabs(j.fh[n - 1] - j.fh[n - 2]) < j.opt.convergence_tol) {
+    *why = "fidelity change below tolerance";
+    return true;
+  }
+  return false;
+}
+
+// A finished evaluation of job j: the ascent bookkeeping of grape_optimize
+// (GRAPE.jl:536-610) shifted by one -- the evaluation just read is F(u_round),
+// which the reference computes at the start of iteration round+1 (or as F_post
+// when iteration `round` converged).  Returns false when the job stops; *why
+// then names the rule.
+bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* err) {
+  const Slot& sl = s->slots[j.slot];
+  j.round += 1;
+  j.F = rb.F;
+  if (!std::isfinite(rb.F)) {
+    *err = PGX_ERR_NONFINITE;
+    *why = "non-finite objective";
+    return false;
+  }
+  bool consider = true;   // does grape_optimize ever compare F(u_round) with the best?
+  bool stop = false;
+  if (j.round == 0) {
+    j.fh.assign(2, rb.F);  // the initial F and iteration 1's F_curr
+  } else {
+    j.step = rb.step;
+    if (ref_converged(j, rb.gnorm, why)) {
+      j.converged = true;  // F(u_round) is the reference's F_post
+      stop = true;
+    } else if (rb.F >= s->cfg.target_fidelity) {
+      *why = "target fidelity reached";
+      j.converged = true;
+      stop = true;
+    } else if (j.round >= j.opt.max_iter) {
+      *why = "maximum iterations reached";
+      consider = false;  // the reference never evaluates the last step's controls
+      stop = true;
+    } else {
+      j.fh.push_back(rb.F);
+    }
+  }
+  if (consider && rb.F > j.bestF) {
+    j.bestF = rb.F;
+    const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+    if (cudaMemcpyAsync(j.d_best, j.prob->d_u, n * sizeof(double), cudaMemcpyDeviceToDevice, sl.stream) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      *err = PGX_ERR_CUDA;
+      *why = "best-controls copy failed";
+      return false;
+    }
+  }
+  return !stop;
+}
+
+int launch_iteration(pgx_server* s, Job& j) {
+  if (!j.iter_exec) {
+    const int st = capture_iteration(s, j);
+    if (st) return st;
+  }
+  const Slot& sl = s->slots[j.slot];
+  if (cudaGraphLaunch(j.iter_exec, sl.stream) != cudaSuccess || cudaEventRecord(sl.done, sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  s->launches += j.iter_kernels;
+  j.inflight = true;
+  return PGX_OK;
+}
+
+void worker_loop(pgx_server* s) {
+  cudaSetDevice(s->ctx->device);
+  while (true) {
+    // ---- admission ----
+    std::vector<std::shared_ptr<Job>> admitted;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      if (s->running.empty() && s->queue.empty()) {
+        s->done_cv.notify_all();
+        if (s->stop) break;
+        s->cv.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+        if (s->stop && s->queue.empty()) break;
+      }
+      if (s->stop)
+        for (auto& j : s->running) j->cancel.store(true);
+      while (!s->stop && !s->queue.empty() && !s->free_slots.empty()) {
+        auto j = s->queue.front();
+        if (s->cfg.hbm_budget_bytes && s->hbm_in_use + j->footprint > s->cfg.hbm_budget_bytes) break;
+        s->queue.pop_front();
+        j->slot = s->free_slots.back();
+        s->free_slots.pop_back();
+        s->hbm_in_use += j->footprint;
+        s->hbm_peak = std::max(s->hbm_peak, s->hbm_in_use);
+        j->state = PGX_JOB_RUNNING;
+        j->t_start = clk::now();
+        s->running.push_back(j);
+        admitted.push_back(j);
+      }
+    }
+    for (auto& j : admitted) {
+      const int st = admit(s, *j);
+      if (st) {
+        release_device(s, *j);
+        std::lock_guard<std::mutex> lk(s->mu);
+        j->status = st;
+        s->running.erase(std::find(s->running.begin(), s->running.end(), j));
+        record_end(s, *j, PGX_JOB_FAILED, std::string("admission failed: ") + pgx_status_string(st));
+        s->done_cv.notify_all();
+      }
+    }
+    // ---- progress ----
+    bool progress = !admitted.empty();
+    std::vector<std::shared_ptr<Job>> ended;
+    std::vector<std::pair<int, std::string>> end_how;
+    const size_t n_run = s->running.size();  // only this thread changes `running`
+    for (size_t i = 0; i < n_run; ++i) {
+      auto j = s->running[i];
+      if (!j->inflight) continue;
+      const Slot& sl = s->slots[j->slot];
+      const cudaError_t q = cudaEventQuery(sl.done);
+      if (q == cudaErrorNotReady) continue;
+      progress = true;
+      j->inflight = false;
+      int err = (q == cudaSuccess) ? PGX_OK : PGX_ERR_CUDA;
+      cudaGetLastError();
+      const char* why = "evaluation failed";
+      bool go = false;
+      if (!err) {
+        const Readback rb = *sl.hb;
+        s->units += j->units;
+        std::lock_guard<std::mutex> lk(s->mu);  // polls read what advance() updates
+        go = advance(s, *j, rb, &why, &err);
+      }
+      bool cancelled = false;
+      if (go && j->cancel.load()) {
+        go = false;
+        cancelled = true;
+      }
+      if (go) err = launch_iteration(s, *j);
+      if (go && !err) continue;
+      ended.push_back(j);
+      if (err) {
+        j->status = err;
+        end_how.emplace_back(PGX_JOB_FAILED, err == PGX_ERR_NONFINITE ? why : pgx_status_string(err));
+      } else if (cancelled) {
+        end_how.emplace_back(PGX_JOB_CANCELLED, "cancelled");
+      } else {
+        end_how.emplace_back(PGX_JOB_DONE, why);
+      }
+    }
+    for (auto& j : ended) release_device(s, *j);
+    if (!ended.empty()) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (size_t e = 0; e < ended.size(); ++e) {
+        s->running.erase(std::find(s->running.begin(), s->running.end(), ended[e]));
+        record_end(s, *ended[e], end_how[e].first, end_how[e].second);
+      }
+      s->done_cv.notify_all();
+    }
+    if (!progress) {
+      // new submissions wake the loop at once; device progress is polled
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv.wait_for(lk, std::chrono::microseconds(20),
+                     [&] { return s->stop || (!s->queue.empty() && !s->free_slots.empty()); });
+    }
+  }
+}
+
+double pct(std::vector<double> v, double q) {
+  if (v.empty()) return 0.0;
+  std::sort(v.begin(), v.end());
+  const double pos = q * (double)(v.size() - 1);
+  const size_t i = (size_t)pos;
+  const double f = pos - (double)i;
+  return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+}
+
+void fill_status(const Job& j, pgx_job_status* out) {
+  std::memset(out, 0, sizeof(*out));
+  out->state = j.state;
+  out->status = j.status;
+  out->iterations = std::max(j.round, 0);
+  out->fidelity = j.F;
+  out->best_fidelity = j.bestF;
+  const auto now = clk::now();
+  const bool ended = j.state == PGX_JOB_DONE || j.state == PGX_JOB_FAILED || j.state == PGX_JOB_CANCELLED;
+  const bool started = j.t_start.time_since_epoch().count() != 0;
+  out->latency_s = secs(j.t_submit, ended ? j.t_end : now);
+  out->queue_s = started ? secs(j.t_submit, j.t_start) : out->latency_s;
+  std::snprintf(out->reason, sizeof(out->reason), "%s", j.reason.c_str());
+}
+
+}  // namespace
+
+extern "C" int pgx_server_create(pgx_ctx* c, const pgx_server_desc* d, pgx_server** out) {
+  if (!c || !d || !out) return PGX_ERR_INVALID;
+  *out = nullptr;
+  if (d->struct_size < sizeof(pgx_server_desc) || d->max_inflight < 1 || d->max_inflight > 4096 ||
+      !(d->target_fidelity > 0.0))
+    return ctx_fail(c, PGX_ERR_INVALID, "invalid server settings");
+  auto* s = new pgx_server();
+  s->user = c;
+  s->cfg = *d;
+  s->t0 = clk::now();
+  int st = pgx_ctx_create(c->device, 0, &s->ctx);
+  cudaSetDevice(c->device);
+  if (!st) {
+    s->ctx_stream = s->ctx->stream;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = c->device;
+    uint64_t keep = UINT64_MAX;  // freed job memory stays in the pool for the next job
+    if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      cudaGetLastError();
+      st = PGX_ERR_CUDA;
+    } else {
+      s->ctx->pool = s->pool;
+    }
+  }
+  s->slots.resize(d->max_inflight);
+  for (int i = 0; i < d->max_inflight && !st; ++i) {
+    Slot& sl = s->slots[i];
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost((void**)&sl.hb, sizeof(Readback)) != cudaSuccess) {
+      cudaGetLastError();
+      st = PGX_ERR_CUDA;
+    }
+  }
+  for (int i = d->max_inflight - 1; i >= 0; --i) s->free_slots.push_back(i);
+  if (st) {
+    pgx_server_destroy(s);
+    return ctx_fail(c, st, "server resources could not be created");
+  }
+  s->worker = std::thread(worker_loop, s);
+  *out = s;
+  return PGX_OK;
+}
+
+extern "C" int pgx_server_destroy(pgx_server* s) {
+  if (!s) return PGX_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    for (auto& j : s->queue) {
+      j->state = PGX_JOB_CANCELLED;
+      j->reason = "server destroyed";
+      ++s->cancelled;
+    }
+    s->queue.clear();
+    for (auto& j : s->running) j->cancel.store(true);
+  }
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  if (s->ctx) cudaSetDevice(s->ctx->device);
+  for (auto& j : s->running) release_device(s, *j);  // only when the worker never started
+  for (auto& sl : s->slots) {
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.hb) cudaFreeHost(sl.hb);
+  }
+  if (s->ctx) pgx_ctx_destroy(s->ctx);
+  if (s->pool) {
+    cudaDeviceSynchronize();  // every cudaFreeAsync into the pool has run
+    cudaMemPoolDestroy(s->pool);
+  }
+  delete s;
+  return PGX_OK;
+}
+
+extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
+                          uint64_t* job_id) {
+  if (!s || !d || !o || !u0 || !job_id) return PGX_ERR_INVALID;
+  pgx_ctx* c = s->user;
+  int st = validate_desc(c, d);
+  if (st) return st;
+  if (o->struct_size < sizeof(pgx_opt_desc) || o->max_iter < 1 || o->step_size <= 0.0 ||
+      o->min_step_size <= 0.0 || o->max_step_size < o->step_size)
+    return ctx_fail(c, PGX_ERR_INVALID, "invalid optimiser settings (GRAPE.jl:108-119)");
+  if (o->method != PGX_OPT_GRAPE)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "the server runs grape_optimize (PGX_OPT_GRAPE) jobs");
+  const size_t D = d->dim, DD = D * D, nc = d->n_controls, nt = d->n_slices, nm = d->n_members;
+  const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
+  for (size_t i = 0; i < nc * nt; ++i)
+    if (!std::isfinite(u0[i])) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
+  auto j = std::make_shared<Job>();
+  j->footprint = problem_footprint(d, s->ctx->num_sms) + sizeof(JobDev) + nc * nt * sizeof(double);
+  if (s->cfg.hbm_budget_bytes && j->footprint > s->cfg.hbm_budget_bytes)
+    return ctx_fail(c, PGX_ERR_BUDGET, "job footprint exceeds the server's HBM budget");
+  j->units = (int64_t)nm * (int64_t)nt;
+  j->dt = copy_of(d->dt, nt);
+  j->drifts = copy_of(d->drifts, 2 * DD * d->n_drifts);
+  j->controls = copy_of(d->controls, 2 * DD * nc);
+  j->offset = copy_of(d->offset_op, 2 * DD);
+  j->mdrift = copy_of(d->member_drift, nm);
+  j->mscale = copy_of(d->member_scale, nm);
+  j->moffset = copy_of(d->member_offset, nm);
+  j->mweight = copy_of(d->member_weight, nm);
+  j->target = copy_of(d->target_op, 2 * DD);
+  j->sinit = copy_of(d->states_init, 2 * np * D);
+  j->starg = copy_of(d->states_target, 2 * np * D);
+  j->sgrad = copy_of(d->grad_states_init, 2 * np * D);
+  j->desc = *d;
+  auto P = [](std::vector<double>& v) -> const double* { return v.empty() ? nullptr : v.data(); };
+  j->desc.dt = P(j->dt);
+  j->desc.drifts = P(j->drifts);
+  j->desc.controls = P(j->controls);
+  j->desc.offset_op = P(j->offset);
+  j->desc.member_drift = j->mdrift.empty() ? nullptr : j->mdrift.data();
+  j->desc.member_scale = P(j->mscale);
+  j->desc.member_offset = P(j->moffset);
+  j->desc.member_weight = P(j->mweight);
+  j->desc.target_op = P(j->target);
+  j->desc.states_init = P(j->sinit);
+  j->desc.states_target = P(j->starg);
+  j->desc.grad_states_init = P(j->sgrad);
+  j->opt = *o;
+  j->u.assign(u0, u0 + nc * nt);
+  j->t_submit = clk::now();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return PGX_ERR_STATE;
+    j->id = s->next_id++;
+    s->jobs[j->id] = j;
+    s->queue.push_back(j);
+    ++s->submitted;
+    *job_id = j->id;
+  }
+  s->cv.notify_all();
+  return PGX_OK;
+}
+
+extern "C" int pgx_poll(pgx_server* s, uint64_t id, pgx_job_status* out) {
+  if (!s || !out) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return PGX_ERR_INVALID;
+  fill_status(*it->second, out);
+  return PGX_OK;
+}
+
+extern "C" int pgx_fetch(pgx_server* s, uint64_t id, double* u, pgx_opt_result* res) {
+  if (!s) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return PGX_ERR_INVALID;
+  const Job& j = *it->second;
+  if (j.state == PGX_JOB_QUEUED || j.state == PGX_JOB_RUNNING) return PGX_ERR_STATE;
+  if (res) {
+    std::memset(res, 0, sizeof(*res));
+    res->fidelity = j.bestF;
+    res->total_time_s = secs(j.t_submit, j.t_end);
+    res->step_size_final = j.step;
+    res->n_iterations = std::max(j.round, 0);
+    res->converged = j.converged;
+    res->n_fidelity_evals = j.round + 1;
+    res->n_gradient_evals = j.round + 1;
+    std::snprintf(res->reason, sizeof(res->reason), "%s", j.reason.c_str());
+  }
+  if (u && j.u.size() == (size_t)j.desc.n_controls * j.desc.n_slices) std::copy(j.u.begin(), j.u.end(), u);
+  const int rc = j.state == PGX_JOB_DONE ? PGX_OK : j.state == PGX_JOB_CANCELLED ? PGX_ERR_CANCELLED : j.status;
+  s->jobs.erase(it);
+  return rc;
+}
+
+extern "C" int pgx_cancel(pgx_server* s, uint64_t id) {
+  if (!s) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return PGX_ERR_INVALID;
+  auto& j = it->second;
+  if (j->state == PGX_JOB_QUEUED) {
+    s->queue.erase(std::remove(s->queue.begin(), s->queue.end(), j), s->queue.end());
+    j->state = PGX_JOB_CANCELLED;
+    j->reason = "cancelled";
+    j->t_end = clk::now();
+    ++s->cancelled;
+    s->done_cv.notify_all();
+    return PGX_OK;
+  }
+  if (j->state == PGX_JOB_RUNNING) {
+    j->cancel.store(true);  // stops after its in-flight iteration
+    return PGX_OK;
+  }
+  return PGX_ERR_STATE;
+}
+
+extern "C" int pgx_server_drain(pgx_server* s, double timeout_s) {
+  if (!s) return PGX_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  const auto idle = [&] { return s->queue.empty() && s->running.empty(); };
+  if (timeout_s <= 0) {
+    s->done_cv.wait(lk, idle);
+    return PGX_OK;
+  }
+  return s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), idle) ? PGX_OK : PGX_ERR_TIMEOUT;
+}
+
+extern "C" int pgx_server_stats(pgx_server* s, pgx_serve_stats* out) {
+  if (!s || !out) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->failed = s->failed;
+  out->cancelled = s->cancelled;
+  out->running = (int64_t)s->running.size();
+  out->queued = (int64_t)s->queue.size();
+  out->kernel_launches = s->launches.load();
+  out->units = s->units.load();
+  out->hbm_in_use = s->hbm_in_use;
+  out->hbm_peak = s->hbm_peak;
+  out->elapsed_s = secs(s->t0, clk::now());
+  out->jobs_per_s = out->elapsed_s > 0 ? (double)s->completed / out->elapsed_s : 0.0;
+  out->p50_latency_s = pct(s->latencies, 0.50);
+  out->p99_latency_s = pct(s->latencies, 0.99);
+  double it = 0;
+  for (int k : s->iters_done) it += k;
+  out->mean_iterations = s->iters_done.empty() ? 0.0 : it / (double)s->iters_done.size();
+  return PGX_OK;
+}

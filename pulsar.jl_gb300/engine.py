@@ -175,6 +175,97 @@ class Batch:
 
 
 @dataclass
+class JobResult:
+    job_id: int
+    state: str
+    controls: Optional[np.ndarray]
+    fidelity: float
+    n_iterations: int
+    converged: bool
+    termination_reason: str
+    latency_s: float
+    step_size_final: float
+
+
+class Server:
+    """Continuous-batching GRAPE server (pgx_server): jobs are admitted by HBM
+    footprint and iterate on the device, each at its own pace."""
+
+    def __init__(self, ctx: Optional[Context] = None, *, max_inflight: int = 64,
+                 hbm_budget_bytes: int = 0, target_fidelity: float = 0.999):
+        self.ctx = ctx or default_context()
+        d = A.ServerDesc()
+        d.struct_size = C.sizeof(A.ServerDesc)
+        d.max_inflight, d.hbm_budget_bytes = int(max_inflight), int(hbm_budget_bytes)
+        d.target_fidelity = float(target_fidelity)
+        self._h = C.c_void_p()
+        A.check(A.lib().pgx_server_create(self.ctx.handle, C.byref(d), C.byref(self._h)), self.ctx.handle)
+        self._shape = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            A.lib().pgx_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, drifts, controls, dt, u0, *, opt: Optional[dict] = None, **problem) -> int:
+        """Queue one grape_optimize job; ``problem`` takes Problem's keywords,
+        ``opt`` opt_desc's (GRAPEConfig defaults).  Returns the job id."""
+        d, keep, (D, n_c, n_t, _, _) = problem_desc(drifts, controls, dt, **problem)
+        u = np.asarray(u0, np.float64)
+        if u.shape != (n_c, n_t):
+            raise ValueError(f"controls have shape {u.shape}, expected {(n_c, n_t)}")
+        ub = np.ascontiguousarray(u.T.ravel())
+        o = opt_desc("grape", **(opt or {}))
+        jid = C.c_uint64()
+        A.check(A.lib().pgx_submit(self._h, C.byref(d), C.byref(o), A.as_dptr(ub), C.byref(jid)),
+                self.ctx.handle)
+        self._shape[int(jid.value)] = (n_c, n_t)
+        return int(jid.value)
+
+    def poll(self, job_id: int) -> dict:
+        st = A.JobStatus()
+        A.check(A.lib().pgx_poll(self._h, int(job_id), C.byref(st)))
+        return {"state": A.JOB_STATE[st.state], "status": int(st.status), "iterations": int(st.iterations),
+                "fidelity": st.fidelity, "best_fidelity": st.best_fidelity, "queue_s": st.queue_s,
+                "latency_s": st.latency_s, "reason": st.reason.decode(errors="replace")}
+
+    def fetch(self, job_id: int) -> JobResult:
+        """Result of a finished job (raises PgxError(9) while it runs)."""
+        n_c, n_t = self._shape[int(job_id)]
+        u = np.zeros(n_c * n_t)
+        r = A.OptResult()
+        rc = A.lib().pgx_fetch(self._h, int(job_id), A.as_dptr(u), C.byref(r))
+        if rc == 9:
+            A.check(rc)
+        self._shape.pop(int(job_id), None)
+        state = "done" if rc == 0 else ("cancelled" if rc == 8 else "failed")
+        return JobResult(int(job_id), state, u.reshape(n_t, n_c).T.copy(), r.fidelity, int(r.n_iterations),
+                         bool(r.converged), r.reason.decode(errors="replace"), r.total_time_s,
+                         r.step_size_final)
+
+    def cancel(self, job_id: int):
+        A.check(A.lib().pgx_cancel(self._h, int(job_id)))
+
+    def drain(self, timeout_s: float = 0.0) -> bool:
+        rc = A.lib().pgx_server_drain(self._h, float(timeout_s))
+        if rc == 7:
+            return False
+        A.check(rc)
+        return True
+
+    def stats(self) -> dict:
+        s = A.ServeStats()
+        A.check(A.lib().pgx_server_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in A.ServeStats._fields_}
+
+
+@dataclass
 class OptOutcome:
     controls: np.ndarray
     fidelity: float
@@ -189,6 +280,65 @@ class OptOutcome:
     step_size_final: float
 
 
+def problem_desc(drifts, controls, dt, *, generator: str = "hermitian", offset_op=None,
+                 member_drift=None, member_scale=None, member_offset=None, member_weight=None,
+                 target: str = "gate", fidelity: str = "square", grad_mode: str = "exact",
+                 precision: str = "fp64", target_op=None, states_init=None, states_target=None,
+                 grad_states_init=None, n_members: Optional[int] = None):
+    """pgx_problem_desc of an ensemble problem; returns (desc, keep, (D, n_c, n_t,
+    n_members, n_pairs)) where ``keep`` holds the buffers desc points into."""
+    drifts = np.asarray(drifts, np.complex128)
+    if drifts.ndim == 2:
+        drifts = drifts[None]
+    controls = np.asarray(controls, np.complex128)
+    dt = np.ascontiguousarray(np.asarray(dt, np.float64).ravel())
+    D = drifts.shape[-1]
+    n_c, n_t = controls.shape[0], dt.size
+    nm = n_members
+    for arr in (member_drift, member_scale, member_offset, member_weight):
+        if arr is not None:
+            nm = len(arr) if nm is None else nm
+    n_members = nm if nm is not None else 1
+    keep = {}
+
+    def buf(name, val):
+        keep[name] = val
+        return A.as_dptr(val) if val is not None else None
+
+    d = A.ProblemDesc()
+    d.struct_size = C.sizeof(A.ProblemDesc)
+    d.dim, d.n_controls, d.n_slices = D, n_c, n_t
+    d.generator, d.target = A.GEN[generator], A.TARGET[target]
+    d.fidelity, d.grad_mode, d.precision = A.FID[fidelity], A.GRAD[grad_mode], A.PREC[precision]
+    d.n_drifts, d.n_members = drifts.shape[0], n_members
+    d.dt = buf("dt", dt)
+    d.drifts = buf("drifts", A.cmat_buf(drifts))
+    d.controls = buf("controls", A.cmat_buf(controls))
+    d.offset_op = buf("off", None if offset_op is None else A.cmat_buf(offset_op))
+    if member_drift is not None:
+        md = np.ascontiguousarray(np.asarray(member_drift, np.int32))
+        keep["md"] = md
+        d.member_drift = md.ctypes.data_as(A.iptr)
+    for field, name, arr in (("member_scale", "ms", member_scale),
+                             ("member_offset", "mo", member_offset),
+                             ("member_weight", "mw", member_weight)):
+        if arr is not None:
+            setattr(d, field, buf(name, np.ascontiguousarray(np.asarray(arr, np.float64))))
+    if target == "gate":
+        d.n_pairs = 0
+        d.target_op = buf("tgt", A.cmat_buf(target_op))
+    else:
+        si = np.atleast_2d(np.asarray(states_init, np.complex128))
+        stt = np.atleast_2d(np.asarray(states_target, np.complex128))
+        d.n_pairs = si.shape[0]
+        d.states_init = buf("si", A.cvec_buf(si))
+        d.states_target = buf("st", A.cvec_buf(stt))
+        if grad_states_init is not None:
+            d.grad_states_init = buf("sg", A.cvec_buf(np.atleast_2d(
+                np.asarray(grad_states_init, np.complex128))))
+    return d, keep, (D, n_c, n_t, n_members, d.n_pairs)
+
+
 class Problem:
     """An ensemble GRAPE problem resident in device memory (pgx_problem)."""
 
@@ -199,55 +349,14 @@ class Problem:
                  precision: str = "fp64", target_op=None, states_init=None, states_target=None,
                  grad_states_init=None, n_members: Optional[int] = None):
         self.ctx = ctx or default_context()
-        drifts = np.asarray(drifts, np.complex128)
-        if drifts.ndim == 2:
-            drifts = drifts[None]
-        controls = np.asarray(controls, np.complex128)
-        dt = np.ascontiguousarray(np.asarray(dt, np.float64).ravel())
-        D = drifts.shape[-1]
-        self.D, self.n_c, self.n_t = D, controls.shape[0], dt.size
-        nm = n_members
-        for arr in (member_drift, member_scale, member_offset, member_weight):
-            if arr is not None:
-                nm = len(arr) if nm is None else nm
-        self.n_members = nm if nm is not None else 1
-        keep = {}
-
-        def buf(name, val):
-            keep[name] = val
-            return A.as_dptr(val) if val is not None else None
-
-        d = A.ProblemDesc()
-        d.struct_size = C.sizeof(A.ProblemDesc)
-        d.dim, d.n_controls, d.n_slices = D, self.n_c, self.n_t
-        d.generator, d.target = A.GEN[generator], A.TARGET[target]
-        d.fidelity, d.grad_mode, d.precision = A.FID[fidelity], A.GRAD[grad_mode], A.PREC[precision]
-        d.n_drifts, d.n_members = drifts.shape[0], self.n_members
-        d.dt = buf("dt", dt)
-        d.drifts = buf("drifts", A.cmat_buf(drifts))
-        d.controls = buf("controls", A.cmat_buf(controls))
-        d.offset_op = buf("off", None if offset_op is None else A.cmat_buf(offset_op))
-        if member_drift is not None:
-            md = np.ascontiguousarray(np.asarray(member_drift, np.int32))
-            keep["md"] = md
-            d.member_drift = md.ctypes.data_as(A.iptr)
-        for field, name, arr in (("member_scale", "ms", member_scale),
-                                 ("member_offset", "mo", member_offset),
-                                 ("member_weight", "mw", member_weight)):
-            if arr is not None:
-                setattr(d, field, buf(name, np.ascontiguousarray(np.asarray(arr, np.float64))))
-        if target == "gate":
-            d.n_pairs = 0
-            d.target_op = buf("tgt", A.cmat_buf(target_op))
-        else:
-            si = np.atleast_2d(np.asarray(states_init, np.complex128))
-            stt = np.atleast_2d(np.asarray(states_target, np.complex128))
-            d.n_pairs = si.shape[0]
-            d.states_init = buf("si", A.cvec_buf(si))
-            d.states_target = buf("st", A.cvec_buf(stt))
-            if grad_states_init is not None:
-                d.grad_states_init = buf("sg", A.cvec_buf(np.atleast_2d(
-                    np.asarray(grad_states_init, np.complex128))))
+        d, keep, dims = problem_desc(
+            drifts, controls, dt, generator=generator, offset_op=offset_op,
+            member_drift=member_drift, member_scale=member_scale, member_offset=member_offset,
+            member_weight=member_weight, target=target, fidelity=fidelity, grad_mode=grad_mode,
+            precision=precision, target_op=target_op, states_init=states_init,
+            states_target=states_target, grad_states_init=grad_states_init, n_members=n_members)
+        self.D, self.n_c, self.n_t, self.n_members, _ = dims
+        self._keep = keep
         self.n_pairs = d.n_pairs
         self._h = C.c_void_p()
         A.check(A.lib().pgx_problem_create(self.ctx.handle, C.byref(d), C.byref(self._h)),

@@ -40,7 +40,9 @@ def test_ctypes_layout_matches_c(tmp_path, pg):
     A = pg._abi
     src = tmp_path / "layout.c"
     fields = {"pgx_problem_desc": A.ProblemDesc, "pgx_eval_stats": A.EvalStats,
-              "pgx_opt_desc": A.OptDesc, "pgx_opt_result": A.OptResult}
+              "pgx_opt_desc": A.OptDesc, "pgx_opt_result": A.OptResult,
+              "pgx_server_desc": A.ServerDesc, "pgx_job_status": A.JobStatus,
+              "pgx_serve_stats": A.ServeStats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pgx.h"', "int main(void){"]
     for cname, py in fields.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
@@ -73,13 +75,14 @@ def test_no_device_means_loud_failure(pg):
 
 def test_c_oracle_matches_numpy_oracle():
     from oracle import cpu_port, members as mb
-    prob, u0 = mb.spin4_ensemble(n_t=12, n_off=2, n_b1=2)
+    import fx
+    prob, u0 = fx.spin4_ensemble(n_t=12, n_off=2, n_b1=2)
     for mode in ("ref_grape", "ref_mr", "exact"):
         F, G = cpu_port.CpuProblem(prob, mode).eval(u0, threads=2)
         Fo, Go = mb.eval_problem(prob, u0, mode)
         assert abs(F - Fo) < 1e-13
         assert np.max(np.abs(G - Go)) < 1e-11 * np.max(np.abs(Go))
-    prob, u0 = mb.single_qubit_transfer(explicit_init=True)
+    prob, u0 = fx.single_qubit_transfer(explicit_init=True)
     for mode in ("ref_grape", "exact"):
         F, G = cpu_port.CpuProblem(prob, mode).eval(u0, threads=1)
         Fo, Go = mb.eval_problem(prob, u0, mode)

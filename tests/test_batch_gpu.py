@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import members as mb
+import fx
 from test_parity_gpu import to_gpu
 
 pytestmark = pytest.mark.gpu
@@ -19,7 +20,7 @@ def _small_uneven(n=12, seed=21, precision="mixed"):
     out = []
     for i in range(n):
         d = [2, 3, 4, 8, 16, 32][i % 6]
-        prob, u0 = mb.uneven_problem(rng, d=d, n_t=int(rng.integers(5, 40)), n_members=int(rng.integers(1, 6)))
+        prob, u0 = fx.uneven_problem(rng, d=d, n_t=int(rng.integers(5, 40)), n_members=int(rng.integers(1, 6)))
         out.append((prob, u0))
     return out
 

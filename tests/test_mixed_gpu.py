@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import members as mb
+import fx
 from test_parity_gpu import random_gate_problem, to_gpu
 
 pytestmark = pytest.mark.gpu
@@ -35,7 +36,7 @@ def test_mixed_random_gate(pg, mode, d):
 
 
 def test_mixed_lindblad_superoperator(pg):
-    prob, u0 = mb.lindblad_3q(n_t=3, n_draws=2)
+    prob, u0 = fx.lindblad_3q(n_t=3, n_draws=2)
     p = to_gpu(pg, prob, "exact", precision="mixed")
     F, G = p.eval(u0)
     Fo, Go = mb.eval_problem(prob, u0, "exact")
@@ -57,7 +58,7 @@ def test_mixed_full_size_bench_workload(pg):
     """231 members x 1000 slices, d = 16: |dF| <= 1e-8 against the FP64 C
     oracle; the FP64 GPU path is the second reference for the gradient."""
     from oracle import cpu_port
-    prob, u0 = mb.spin4_ensemble()
+    prob, u0 = fx.spin4_ensemble()
     pm = to_gpu(pg, prob, "exact", precision="mixed")
     F, G = pm.eval(u0)
     Fo, Go = cpu_port.CpuProblem(prob, "exact").eval(u0)
@@ -80,7 +81,7 @@ def test_autotune_keeps_results_bit_identical(pg, d):
 
 
 def test_mixed_states_target_is_refused(pg):
-    prob, u0 = mb.single_qubit_transfer()
+    prob, u0 = fx.single_qubit_transfer()
     with pytest.raises(pg._abi.PgxError) as ei:
         to_gpu(pg, prob, "exact", precision="mixed")
     assert ei.value.status == 6

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import members as mb
+import fx
 from oracle import ref_semantics as rs
 
 pytestmark = pytest.mark.gpu
@@ -28,7 +29,7 @@ def _hist_close(a, b, tol):
 def test_grape_optimize_quickstart(pg, explicit):
     """Config-1 quickstart: 1 qubit, 100 slices over pi, GRAPEConfig(max_iter=500,
     step_size=0.05, adapt_step_size=true); legacy gradient semantics."""
-    prob, u0 = mb.single_qubit_transfer(explicit_init=explicit)
+    prob, u0 = fx.single_qubit_transfer(explicit_init=explicit)
     dt = prob.dt[0]
     psi_i = prob.states_init[0] if explicit else None
     sys_o = rs.QuantumSystem(prob.drifts[0], list(prob.controls))
@@ -119,7 +120,7 @@ def test_compute_fidelity_and_gradient_api(pg):
     H = (H + H.conj().T) / 2
     Hc = [np.kron(SX, np.eye(2)), np.kron(np.eye(2), SY)]
     u0 = rng.uniform(-1, 1, (2, 20))
-    T = mb.haar_unitary(rng, 4)
+    T = fx.haar_unitary(rng, 4)
     for tgt_o, tgt_g in ((rs.unitary_target(T), pg.unitary_target(T)),
                          (rs.state_target(T[:, 0], psi_init=T[:, 1]), pg.state_target(T[:, 0], psi_init=T[:, 1]))):
         so, sg = rs.QuantumSystem(H, Hc), pg.quantum_system(H, Hc)

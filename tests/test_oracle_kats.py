@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import members as mb
+import fx
 from oracle import ref_semantics as rs
 
 SX = np.array([[0, 1], [1, 0]], complex)
@@ -67,7 +68,7 @@ def test_fidelity_bounds():                    # :88-140
     assert abs(rs.gate_fidelity(I2, I2) - 1.0) < 1e-12
     rng = np.random.default_rng(7)
     for _ in range(20):
-        Ua, Ub = mb.haar_unitary(rng, 2), mb.haar_unitary(rng, 2)
+        Ua, Ub = fx.haar_unitary(rng, 2), fx.haar_unitary(rng, 2)
         assert -1e-12 <= rs.gate_fidelity(Ua, Ub) <= 1 + 1e-12
     assert abs(rs.state_fidelity([1, 0], [0, 1], "square")) < 1e-14
     p = np.array([1, 1]) / np.sqrt(2)
@@ -199,7 +200,7 @@ def test_lindblad_kernel_matches_member_model():
 # --- GRAPETests.jl ------------------------------------------------------------
 
 def test_grape_optimize_reproducible_and_monotone_best():   # :141-161, :106-111
-    prob, u0 = mb.single_qubit_transfer()
+    prob, u0 = fx.single_qubit_transfer()
     sysq = rs.QuantumSystem(prob.drifts[0], list(prob.controls))
     tgt = rs.state_target([0, 1])
     cfg = rs.GRAPEConfig(max_iter=60, step_size=0.05, adapt_step_size=True)
@@ -214,7 +215,7 @@ def test_exact_gradient_of_modulus_and_real_metrics_vs_fd():
     H = herm(rng, 3) * 0.3
     C = [herm(rng, 3) * 0.2, herm(rng, 3) * 0.2]
     psi = np.array([1, 0, 0], complex)
-    tgt = mb.haar_unitary(rng, 3)[:, 0]
+    tgt = fx.haar_unitary(rng, 3)[:, 0]
     for fid in ("real", "modulus", "square"):
         prob = mb.Problem(drifts=H[None], controls=np.stack(C), dt=np.full(6, 0.4), target="states",
                           fidelity=fid, states_init=psi[None], states_target=tgt[None])

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import members as mb
+import fx
 
 pytestmark = pytest.mark.gpu
 
@@ -47,7 +48,7 @@ def random_gate_problem(rng, d, n_t, n_c=2, n_members=1, dt=0.05, scale=1.0):
     ctrls = np.stack([rand_herm(rng, d, scale) for _ in range(n_c)])
     prob = mb.Problem(drifts=drifts, controls=ctrls, dt=np.full(n_t, dt), member_drift=np.arange(n_members),
                       member_scale=rng.uniform(0.9, 1.1, n_members), n_members=n_members, target="gate",
-                      target_op=mb.haar_unitary(rng, d))
+                      target_op=fx.haar_unitary(rng, d))
     return prob, rng.uniform(-1, 1, (n_c, n_t))
 
 
@@ -57,7 +58,7 @@ MODES = ("ref_grape", "ref_mr", "exact")
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("explicit", [False, True])
 def test_single_qubit_transfer(pg, mode, explicit):
-    prob, u0 = mb.single_qubit_transfer(explicit_init=explicit)
+    prob, u0 = fx.single_qubit_transfer(explicit_init=explicit)
     p = to_gpu(pg, prob, mode)
     F, G = p.eval(u0)
     Fo, Go = mb.eval_problem(prob, u0, mode)
@@ -90,7 +91,7 @@ def test_large_norm_needs_squaring(pg, mode):
 
 @pytest.mark.parametrize("mode", MODES)
 def test_spin4_broadband_ensemble_small(pg, mode):
-    prob, u0 = mb.spin4_ensemble(n_t=10, n_off=3, n_b1=2)
+    prob, u0 = fx.spin4_ensemble(n_t=10, n_off=3, n_b1=2)
     p = to_gpu(pg, prob, mode)
     F, G = p.eval(u0)
     Fo, Go = mb.eval_problem(prob, u0, mode)
@@ -105,8 +106,8 @@ def test_state_pairs_mr(pg, fid, mode, d):
     rng = np.random.default_rng(7 * d)
     drifts = np.stack([rand_herm(rng, d, 0.5) for _ in range(3)])
     ctrls = np.stack([rand_herm(rng, d, 0.5) for _ in range(2)])
-    si = np.stack([mb.haar_unitary(rng, d)[:, 0] for _ in range(2)])
-    st = np.stack([mb.haar_unitary(rng, d)[:, 0] for _ in range(2)])
+    si = np.stack([fx.haar_unitary(rng, d)[:, 0] for _ in range(2)])
+    st = np.stack([fx.haar_unitary(rng, d)[:, 0] for _ in range(2)])
     prob = mb.Problem(drifts=drifts, controls=ctrls, dt=rng.uniform(0.05, 0.2, 9),
                       member_drift=np.repeat(np.arange(3), 2), member_scale=np.tile([0.8, 1.3], 3),
                       n_members=6, target="states", fidelity=fid, states_init=si, states_target=st)
@@ -120,7 +121,7 @@ def test_state_pairs_mr(pg, fid, mode, d):
 
 @pytest.mark.parametrize("mode", MODES)
 def test_lindblad_gate_superoperator(pg, mode):
-    prob, u0 = mb.lindblad_3q(n_t=3, n_draws=2)
+    prob, u0 = fx.lindblad_3q(n_t=3, n_draws=2)
     p = to_gpu(pg, prob, mode)
     F, G = p.eval(u0)
     Fo, Go = mb.eval_problem(prob, u0, mode)
@@ -153,7 +154,7 @@ def test_lindblad_states_mr(pg, mode):
 
 
 def test_forward_only_matches(pg):
-    prob, u0 = mb.spin4_ensemble(n_t=7, n_off=2, n_b1=2)
+    prob, u0 = fx.spin4_ensemble(n_t=7, n_off=2, n_b1=2)
     p = to_gpu(pg, prob, "exact")
     F1, _ = p.eval(u0, want_grad=False)
     F2, _ = p.eval(u0)
@@ -183,7 +184,7 @@ def test_propagator_kats(pg):
 
 def test_total_propagator(pg):
     from oracle import ref_semantics as rs
-    prob, u0 = mb.spin4_ensemble(n_t=9, n_off=2, n_b1=1)
+    prob, u0 = fx.spin4_ensemble(n_t=9, n_off=2, n_b1=1)
     p = to_gpu(pg, prob, "exact")
     for m in range(2):
         Gs = np.stack([prob.generator_of(m, u0[:, k]) for k in range(9)])
@@ -193,7 +194,7 @@ def test_total_propagator(pg):
 
 
 def test_deterministic_and_member_independent(pg):
-    prob, u0 = mb.spin4_ensemble(n_t=20, n_off=3, n_b1=3)
+    prob, u0 = fx.spin4_ensemble(n_t=20, n_off=3, n_b1=3)
     p = to_gpu(pg, prob, "exact")
     F1, G1 = p.eval(u0)
     Fm1 = p.member_fidelities()
@@ -240,7 +241,7 @@ def test_spin4_full_size_vs_c_oracle(pg):
     """The bench workload at full size (231 members x 1000 slices, d = 16,
     exact gradient) against the oracle's C restatement."""
     from oracle import cpu_port
-    prob, u0 = mb.spin4_ensemble()
+    prob, u0 = fx.spin4_ensemble()
     p = to_gpu(pg, prob, "exact")
     F, G = p.eval(u0)
     Fo, Go = cpu_port.CpuProblem(prob, "exact").eval(u0)

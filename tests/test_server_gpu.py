@@ -1,0 +1,174 @@
+"""Continuous-batching server (pgx_server).
+
+A served job runs the kernels of a solo run on its own stream, so its result
+must be bit-identical whether it runs alone or among other jobs of other
+sizes; its stop rules and best-controls bookkeeping must be those of
+grape_optimize (GRAPE.jl:536-610, check_grape_convergence :371-402), which the
+device-resident optimiser (itself checked against the oracle's restated loop)
+implements on the host.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import fx
+
+pytestmark = pytest.mark.gpu
+
+W = fx.W
+OPT = dict(max_iter=15, step_size=0.5, convergence_tol=1e-12, gradient_norm_tol=1e-12)
+
+
+def _jobs(seed=13):
+    rng = np.random.default_rng(seed)
+    out = []
+    for d, n_t, nm in [(4, 30, 3), (16, 20, 2), (2, 60, 5), (8, 25, 4), (32, 10, 2), (3, 17, 1)]:
+        out.append(W.uneven_problem(rng, d=d, n_t=n_t, n_members=nm))
+    out.append(W.lindblad_gate(seed=3, n_qubits=2, n_t=12, n_draws=2))
+    return out
+
+
+def _run(server, jobs, precision, opt=OPT, stagger_s=0.0):
+    ids = []
+    for i, (spec, u0) in enumerate(jobs):
+        ids.append(server.submit(u0=u0, opt=opt, **spec.problem_kwargs("exact", precision)))
+        if stagger_s and i == len(jobs) // 2:
+            time.sleep(stagger_s)
+    assert server.drain(timeout_s=300)
+    return [server.fetch(j) for j in ids]
+
+
+def _same(a, b):
+    assert a.state == b.state == "done"
+    assert a.n_iterations == b.n_iterations, (a.n_iterations, b.n_iterations)
+    assert a.termination_reason == b.termination_reason
+    assert a.fidelity == b.fidelity, (a.fidelity, b.fidelity)
+    assert a.step_size_final == b.step_size_final
+    assert np.array_equal(a.controls, b.controls)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_job_identical_alone_and_in_the_mix(pg, ctx, precision):
+    jobs = _jobs()
+    solo = []
+    s = pg.Server(ctx, max_inflight=1, target_fidelity=2.0)
+    for job in jobs:
+        solo.extend(_run(s, [job], precision))
+    s.close()
+    mix = pg.Server(ctx, max_inflight=8, target_fidelity=2.0)
+    mixed = _run(mix, jobs, precision, stagger_s=0.002)
+    st = mix.stats()
+    mix.close()
+    for a, b in zip(solo, mixed):
+        _same(a, b)
+    assert st["completed"] == len(jobs) and st["failed"] == 0
+    assert st["kernel_launches"] > 0
+    assert st["units"] == sum(sp.n_members * sp.n_t * (r.n_iterations + 1) for (sp, _), r in zip(jobs, mixed))
+    assert 0 < st["p50_latency_s"] <= st["p99_latency_s"]
+
+
+def test_served_job_follows_grape_optimize(pg, ctx):
+    """Stop rules, iteration count and best controls as grape_optimize."""
+    rng = np.random.default_rng(5)
+    cases = [W.uneven_problem(rng, d=4, n_t=40, n_members=2), W.single_qubit_transfer(explicit_init=True)]
+    settings = [dict(max_iter=30, step_size=0.5, convergence_tol=1e-9),   # stops at max_iter
+                dict(max_iter=500, step_size=0.05, convergence_tol=1e-8)]  # stops on a reference rule
+    srv = pg.Server(ctx, max_inflight=4, target_fidelity=2.0)
+    for (spec, u0), opt in zip(cases, settings):
+        p = pg.Problem(ctx=ctx, **spec.problem_kwargs("exact", "fp64"))
+        ref = p.optimize(u0, "grape", **opt)
+        p.close()
+        jid = srv.submit(u0=u0, opt=opt, **spec.problem_kwargs("exact", "fp64"))
+        assert srv.drain(timeout_s=300)
+        r = srv.fetch(jid)
+        assert r.state == "done"
+        assert r.n_iterations == ref.n_iterations
+        assert r.converged == ref.converged
+        assert r.termination_reason == ref.termination_reason
+        assert abs(r.fidelity - ref.fidelity) <= 1e-12, (r.fidelity, ref.fidelity)
+        scale = max(np.max(np.abs(ref.controls)), 1.0)
+        assert np.max(np.abs(r.controls - ref.controls)) <= 1e-10 * scale
+        assert abs(r.step_size_final - ref.step_size_final) <= 1e-12 * ref.step_size_final
+    srv.close()
+
+
+def test_target_fidelity_stops_a_job(pg, ctx):
+    spec, u0 = W.single_qubit_transfer(explicit_init=True)
+    srv = pg.Server(ctx, max_inflight=2, target_fidelity=0.99)
+    jid = srv.submit(u0=u0, opt=dict(max_iter=500, step_size=0.05), **spec.problem_kwargs("exact", "fp64"))
+    assert srv.drain(timeout_s=120)
+    r = srv.fetch(jid)
+    srv.close()
+    assert r.state == "done" and r.converged
+    assert r.termination_reason == "target fidelity reached"
+    assert r.fidelity >= 0.99
+
+
+def test_admission_by_hbm_budget(pg, ctx):
+    jobs = _jobs()[:4]
+    opt = dict(OPT, max_iter=6)
+    footprints = []
+    for sp, _ in jobs:
+        d, _, _ = pg.problem_desc(**sp.problem_kwargs("exact", "fp64"))
+        b = pg._abi.C.c_uint64()
+        pg._abi.check(pg._abi.lib().pgx_problem_footprint(pg._abi.C.byref(d), pg._abi.C.byref(b)))
+        footprints.append(int(b.value))
+    budget = int(1.5 * max(footprints)) + (1 << 20)
+    # a job larger than the whole budget is refused at submission
+    small = pg.Server(ctx, max_inflight=4, hbm_budget_bytes=min(footprints) // 2)
+    with pytest.raises(pg._abi.PgxError) as e:
+        small.submit(u0=jobs[0][1], opt=opt, **jobs[0][0].problem_kwargs("exact", "fp64"))
+    assert e.value.status == 4
+    small.close()
+    # jobs that fit only a few at a time still all complete, with the same results
+    srv = pg.Server(ctx, max_inflight=4, hbm_budget_bytes=budget)
+    got = _run(srv, jobs, "fp64", opt=opt)
+    st = srv.stats()
+    srv.close()
+    assert st["hbm_peak"] <= budget
+    ref = pg.Server(ctx, max_inflight=4)
+    want = _run(ref, jobs, "fp64", opt=opt)
+    ref.close()
+    for a, b in zip(got, want):
+        _same(a, b)
+
+
+def test_cancel_queued_and_running(pg, ctx):
+    spec, u0 = W.uneven_problem(np.random.default_rng(9), d=16, n_t=200, n_members=8)
+    kw = spec.problem_kwargs("exact", "fp64")
+    srv = pg.Server(ctx, max_inflight=1, target_fidelity=2.0)
+    long_opt = dict(max_iter=100000, step_size=1e-3, convergence_tol=1e-300, gradient_norm_tol=0.0)
+    a = srv.submit(u0=u0, opt=long_opt, **kw)
+    b = srv.submit(u0=u0, opt=long_opt, **kw)
+    assert srv.poll(b)["state"] == "queued"
+    srv.cancel(b)
+    assert srv.poll(b)["state"] == "cancelled"
+    t0 = time.time()
+    while srv.poll(a)["iterations"] < 2 and time.time() - t0 < 60:
+        time.sleep(0.01)
+    assert srv.poll(a)["state"] == "running"
+    srv.cancel(a)
+    assert srv.drain(timeout_s=60)
+    ra, rb = srv.fetch(a), srv.fetch(b)
+    assert ra.state == "cancelled" and rb.state == "cancelled"
+    assert ra.n_iterations >= 2
+    assert ra.controls.shape == u0.shape and np.all(np.isfinite(ra.controls))
+    st = srv.stats()
+    assert st["cancelled"] == 2 and st["completed"] == 0
+    srv.close()
+
+
+def test_submit_validation(pg, ctx):
+    spec, u0 = W.uneven_problem(np.random.default_rng(2), d=4, n_t=10, n_members=1)
+    srv = pg.Server(ctx, max_inflight=2)
+    with pytest.raises(pg._abi.PgxError) as e:
+        srv.submit(u0=u0, opt=dict(max_iter=0), **spec.problem_kwargs("exact", "fp64"))
+    assert e.value.status == 1
+    bad = u0.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(pg._abi.PgxError) as e:
+        srv.submit(u0=bad, **spec.problem_kwargs("exact", "fp64"))
+    assert e.value.status == 10
+    assert srv.stats()["submitted"] == 0
+    srv.close()

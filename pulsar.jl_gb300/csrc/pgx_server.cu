@@ -288,6 +288,14 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
   bool stop = false;
   if (j.round == 0) {
     j.fh.assign(2, rb.F);  // the initial F and iteration 1's F_curr
+    // the step rule's previous objective starts at F(u0), as in the history
+    if (cudaMemcpyAsync(&j.dev->st.F_prev, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToDevice, sl.stream) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      *err = PGX_ERR_CUDA;
+      *why = "step state initialisation failed";
+      return false;
+    }
   } else {
     j.step = rb.step;
     if (ref_converged(j, rb.gnorm, why)) {

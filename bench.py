@@ -53,7 +53,13 @@ K_EXP = 8  # conventional matrix-product count of one expm in the FLOP model
 
 # DRAM bytes per launch of the dominant kernel from ncu captures, scaled from
 # the captured 200-slice case to 1000 slices (one M_k read per unit: linear).
-TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6)}
+TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
+           ("spin4", "mixed", "expm"): 5 * (239.104000e6 + 127.746304e6),
+           ("spin4", "mixed", "grad"): 5 * (94.714112e6 + 2.698240e6)}
+# FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
+# accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
+# busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).
+DF_OPS_PER_CMAC = 46
 
 
 def flops_per_unit(stage: str, D: int, n_c: int, grad_mode: str) -> float:
@@ -137,11 +143,17 @@ def gpu_problem(pg, ctx, spec, grad_mode: str, precision: str):
 class Single:
     """One ensemble problem; step = one (F, G) evaluation."""
 
-    def __init__(self, name, prob, u0, pg, ctx, grad_mode, precision, torch, dev):
+    def __init__(self, name, prob, u0, pg, ctx, grad_mode, precision, torch, dev, teams=None):
         self.name, self.prob, self.u0, self.grad_mode, self.precision = name, prob, u0, grad_mode, precision
         self.p = gpu_problem(pg, ctx, prob, grad_mode, precision)
         self.units_per_step = prob.n_members * prob.n_t
-        self.tune = self.p.autotune(u0, reps=2) if precision == "mixed" else "FP64 path: no tunable kernels"
+        if precision != "mixed":
+            self.tune = "FP64 path: no tunable kernels"
+        elif teams:
+            self.p.set_teams(*teams)
+            self.tune = f"fixed teams (expm, grad) = {self.p.teams}"
+        else:
+            self.tune = self.p.autotune(u0, reps=2) + f" -> (expm, grad) = {self.p.teams}"
         self.d_u = torch.tensor(np.ascontiguousarray(u0.T).ravel(), dtype=torch.float64, device=dev)
         self.d_F = torch.zeros(2, dtype=torch.float64, device=dev)
         self.d_G = torch.zeros(u0.size, dtype=torch.float64, device=dev)
@@ -381,11 +393,11 @@ def make_workload(args, pg, ctx, torch, dev):
     if args.workload == "spin4":
         prob, u0 = W.spin4_ensemble(n_t=args.slices)
         return Single(f"spin4_d16_231members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
-                      args.precision, torch, dev)
+                      args.precision, torch, dev, teams=args.teams)
     if args.workload == "lindblad3q":
         prob, u0 = W.lindblad_3q()
         return Single("lindblad3q_D64_32members_500slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
-                      torch, dev)
+                      torch, dev, teams=args.teams)
     if args.workload == "uneven512":
         return Uneven("uneven512", W.uneven_batch(512), pg, ctx, args.grad_mode, args.precision)
     raise ValueError(args.workload)
@@ -458,6 +470,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip timing the plain FP64 GPU form beside the mixed one")
+    ap.add_argument("--teams", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
+                    help="fixed mixed-kernel team sizes EXPM,GRAD instead of autotuning (e.g. for profiling)")
     ap.add_argument("--slices", type=int, default=1000,
                     help="spin4 slices per member (1000 = the benchmark workload; smaller for profiling)")
     sv = ap.add_argument_group("serve workload (Poisson job stream through pgx_server)")
@@ -570,6 +584,13 @@ def main():
                      "flop_model": "conventional per-unit W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 "
                                    "(K_exp = 8) split by stage; the exact gradient executes one Frechet "
                                    "derivative per slice where the model counts 2 n_c"})
+        if args.precision == "mixed" and single and dom in ("expm", "chain_fwd"):
+            # df32 stages: each model FLOP costs DF_OPS_PER_CMAC / 8 FP32 operations
+            eff = peak / (DF_OPS_PER_CMAC / 8.0)
+            roof.update({"df32_effective_peak": eff / 1e12, "frac_of_df32_effective": achieved / eff,
+                         "df32_note": f"df32 arithmetic: one complex MAC = {DF_OPS_PER_CMAC} FP32 operations "
+                                      "vs 8 model FLOPs; frac_of_df32_effective is the model-FLOP rate over "
+                                      "what a fully busy FP32 pipe reaches on df32 work"})
         extra = {}
         if args.precision == "mixed" and single and not args.no_fp64_compare:
             # the plain FP64 GPU form of the same workload, timed in the same run

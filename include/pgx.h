@@ -180,6 +180,13 @@ int pgx_propagator(pgx_ctx* ctx, int32_t dim, int32_t generator, const double* g
  * to threads; every dot product is summed in the same order, so results are
  * bit-identical whatever is chosen.  The FP64 path has no variants.         */
 int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report, size_t report_len);
+/* Sets the team sizes directly (a plan kept from an earlier pgx_autotune);
+ * 0 = the built-in default.  Values the dimension does not admit are refused
+ * with PGX_ERR_INVALID.  Kernel indices: 0 = mixed expm, 1 = mixed gradient. */
+#define PGX_TUNE_EXPM 0
+#define PGX_TUNE_GRAD 1
+int pgx_problem_set_team(pgx_problem* prob, int32_t kernel, int32_t team);
+int pgx_problem_get_team(const pgx_problem* prob, int32_t kernel, int32_t* team);
 
 /* ---- allocation-free total propagator ----------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -118,6 +118,8 @@ SIGNATURES = {
     "pgx_total_propagator": (C.c_int, [C.c_void_p, dptr, C.c_int32, dptr]),
     "pgx_propagator": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.c_double, dptr]),
     "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
+    "pgx_problem_set_team": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "pgx_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "pgx_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -641,6 +641,24 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
   return run_pipeline(p, p->d_u, p->d_F, p->d_G);
 }
 
+extern "C" int pgx_problem_set_team(pgx_problem* p, int32_t kernel, int32_t team) {
+  if (!p || kernel < 0 || kernel >= pgx::kNumTunable) return PGX_ERR_INVALID;
+  if (team != 0) {
+    int vs[4];
+    const int nv = pgx::mixed_variants(p->Dp, vs);
+    if (std::find(vs, vs + nv, team) == vs + nv)
+      return ctx_fail(p->ctx, PGX_ERR_INVALID, "team size not admitted at this dimension");
+  }
+  p->team[kernel] = team;
+  return PGX_OK;
+}
+
+extern "C" int pgx_problem_get_team(const pgx_problem* p, int32_t kernel, int32_t* team) {
+  if (!p || !team || kernel < 0 || kernel >= pgx::kNumTunable) return PGX_ERR_INVALID;
+  *team = p->team[kernel] ? p->team[kernel] : pgx::mixed_default_team(p->Dp, kernel);
+  return PGX_OK;
+}
+
 extern "C" int pgx_ctx_set_stage_timing(pgx_ctx* c, int enabled) {
   if (!c) return PGX_ERR_INVALID;
   c->stage_timing = enabled != 0;

@@ -409,6 +409,21 @@ class Problem:
         A.check(A.lib().pgx_autotune(self._h, A.as_dptr(ub), int(reps), buf, 1024), self.ctx.handle)
         return buf.value.decode()
 
+    @property
+    def teams(self) -> tuple:
+        """(expm, gradient) team sizes of the mixed kernels in use."""
+        out = []
+        for k in (0, 1):
+            t = C.c_int32()
+            A.check(A.lib().pgx_problem_get_team(self._h, k, C.byref(t)), self.ctx.handle)
+            out.append(int(t.value))
+        return tuple(out)
+
+    def set_teams(self, expm: int = 0, grad: int = 0):
+        """Fix the team sizes (0 = default), e.g. a plan from an earlier autotune."""
+        for k, t in ((0, expm), (1, grad)):
+            A.check(A.lib().pgx_problem_set_team(self._h, k, int(t)), self.ctx.handle)
+
     def member_fidelities(self) -> np.ndarray:
         out = np.zeros(self.n_members)
         A.check(A.lib().pgx_member_fidelities(self._h, A.as_dptr(out)), self.ctx.handle)

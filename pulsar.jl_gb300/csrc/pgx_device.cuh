@@ -68,11 +68,13 @@ struct EpiNone {
 // block, but the same row of different columns lands in different banks, so
 // the row-wise operand loads of a product are conflict-free.
 template <int D, int SW> struct Lay {
-  __device__ __forceinline__ static int idx(int r, int c) { return (SW ? (r ^ (c & (D - 1))) : r) + D * c; }
-  __device__ __forceinline__ static int row(int e) {
-    const int c = e / D;
-    return SW ? ((e % D) ^ (c & (D - 1))) : e % D;
-  }
+  // SW = 0: column-major, leading dimension D.  SW = 1: rows XOR-swizzled by
+  // the column.  SW = 2: column-major with leading dimension D + 1, so the
+  // columns one warp reads at the same k fall in different shared-memory
+  // banks; the inner-loop index stays one multiply-add.
+  static constexpr int LD = (SW == 2) ? D + 1 : D;
+  static constexpr int SIZE = LD * D;  // storage elements of one matrix
+  __device__ __forceinline__ static int idx(int r, int c) { return (SW == 1 ? (r ^ (c & (D - 1))) : r) + LD * c; }
 };
 
 // Register blocking of a D x D product over T lanes: each lane owns an RB x CB
@@ -252,12 +254,11 @@ __device__ __forceinline__ C block_der(int i, C d1, C d2, C d3, const R* invf) {
 }
 
 // Workspace layout (10 matrices) used by the Taylor routines.
-template <class C, int D> struct Work {
+template <class C, int D, int S = D * D> struct Work {
   C* B; C* B2; C* B3; C* B4; C* Y;
   C* dB; C* dB2; C* dB3; C* dB4; C* dY;
   __device__ __forceinline__ static Work at(C* base) {
     Work w;
-    constexpr int S = D * D;
     w.B = base; w.B2 = base + S; w.B3 = base + 2 * S; w.B4 = base + 3 * S; w.Y = base + 4 * S;
     w.dB = base + 5 * S; w.dB2 = base + 6 * S; w.dB3 = base + 7 * S; w.dB4 = base + 8 * S;
     w.dY = base + 9 * S;
@@ -268,14 +269,14 @@ template <class C, int D> struct Work {
 // Y = T_m(B)^(2^s).  B holds A / 2^s on entry (destroyed: B..B4 are scratch).
 // Paterson-Stockmeyer with q = 4: powers B2, B3, B4, then Horner in B4 over
 // blocks of four coefficients.  m = 4L costs 3 + (L - 1) products.
-template <int D, int T, int SW = 0, class C, class R>
-__device__ void taylor_exp(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
+template <int D, int T, int SW = 0, class C, int S, class R>
+__device__ void taylor_exp(const Team<T>& tm, const Work<C, D, S>& w, int m, int s, const R* invf) {
   mm1<D, T, SW>(tm, w.B2, w.B, w.B);
   mm1<D, T, SW>(tm, w.B3, w.B2, w.B);
   mm1<D, T, SW>(tm, w.B4, w.B2, w.B2);
   const int L = m / 4;
-  for (int e = tm.lane; e < D * D; e += T) {
-    const int r = Lay<D, SW>::row(e), c = e / D;
+  for (int q = tm.lane; q < D * D; q += T) {
+    const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
     C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
     w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
   }
@@ -293,8 +294,8 @@ __device__ void taylor_exp(const Team<T>& tm, const Work<C, D>& w, int m, int s,
 // (Y, dY) = (f(A), L_f(A, M)) for f(A) = T_m(A/2^s)^(2^s).  On entry B = A/2^s
 // and dB = M/2^s.  The derivative is exact for the polynomial f actually
 // evaluated, so Tr(L_f(A, M) E) equals Tr(M L_f(A, E)) to rounding.
-template <int D, int T, int SW = 0, class C, class R>
-__device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D>& w, int m, int s, const R* invf) {
+template <int D, int T, int SW = 0, class C, int S, class R>
+__device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D, S>& w, int m, int s, const R* invf) {
   mm1<D, T, SW>(tm, w.B2, w.B, w.B);
   mm<D, T, true, SW>(tm, w.dB2, w.dB, w.B, w.B, w.dB, EpiNone{});
   mm1<D, T, SW>(tm, w.B3, w.B2, w.B);
@@ -302,8 +303,8 @@ __device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D>& w, int m
   mm1<D, T, SW>(tm, w.B4, w.B2, w.B2);
   mm<D, T, true, SW>(tm, w.dB4, w.dB2, w.B2, w.B2, w.dB2, EpiNone{});
   const int L = m / 4;
-  for (int e = tm.lane; e < D * D; e += T) {
-    const int r = Lay<D, SW>::row(e), c = e / D;
+  for (int q = tm.lane; q < D * D; q += T) {
+    const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
     C v = block_val(L - 1, r, c, w.B[e], w.B2[e], w.B3[e], invf);
     w.Y[e] = cadd(v, cscale(w.B4[e], invf[4 * L]));
     C dv = block_der(L - 1, w.dB[e], w.dB2[e], w.dB3[e], invf);

@@ -186,8 +186,8 @@ __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* 
   mm1_df<D, T, SW>(tm, B3, B2, B);
   mm1_df<D, T, SW>(tm, B4, B2, B2);
   const int L = m / 4;
-  for (int e = tm.lane; e < D * D; e += T) {
-    const int r = Lay<D, SW>::row(e), c = e / D;
+  for (int q = tm.lane; q < D * D; q += T) {
+    const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
     dfc v = df_block(L - 1, r, c, B[e], B2[e], B3[e], coef);
     Y[e] = dfc_store(dfc_add(v, dfc_scale(dfc_load(B4[e]), coef[4 * L])));
   }

@@ -30,6 +30,14 @@ struct ProbDev {
   const double2* target_op;  // gate: [Dp*Dp]
   const double2* psi_init;   // states: [n_pairs][Dp]
   const double2* psi_targ;   // states: [n_pairs][Dp]
+  // mixed precision only: the same constants as df pairs
+  // {re.hi, im.hi, re.lo, im.lo} (the first two floats are the FP32 rounding)
+  const float4* drifts_df;   // [n_drifts][Dp*Dp]
+  const float4* ctrls_df;    // [n_c][Dp*Dp]
+  const float4* offset_df;   // [Dp*Dp]
+  const float2* dt_df;       // [n_t] df pairs {hi, lo}
+  const float2* m_scale_df;  // [n_members]
+  const float2* m_offset_df; // [n_members]
 };
 
 // Device work buffers of one evaluation.
@@ -48,6 +56,7 @@ struct WorkDev {
   const double* u;  // [n_t][n_c]  (column-major [n_c x n_t])
   double* G;        // [n_t][n_c]
   double* F;        // [1]
+  float2* u_df;     // mixed: [n_t][n_c] df pairs of u, written once per evaluation
 };
 
 // Tunable kernels: their team size (threads per matrix problem) is chosen per
@@ -113,6 +122,8 @@ cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
 cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store);
 cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+// u -> w.u_df (df pairs), the first stage of a mixed evaluation.
+cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 // Global slab size (in double2 elements) the Dp = 64 path needs.
 size_t slab_elems(int Dp, int num_sms);
 int slab_team_count(int Dp, int num_sms);

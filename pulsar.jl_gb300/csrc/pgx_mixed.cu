@@ -26,6 +26,11 @@ static __constant__ df c_dfcoef[PGX_N_INVFACT] = PGX_INVFACT_DF_INIT;
 // the XOR swizzle removes bank conflicts but its index arithmetic costs more
 // than the conflicts do, so the plain column-major layout is used.
 constexpr int kSwz = 0;
+// The FP32 gradient is bound by shared-memory bandwidth, not FMAs: with
+// leading dimension D the columns a warp reads at one k share a bank.  It
+// keeps its Taylor workspace padded to leading dimension D + 1.
+constexpr int kSwzGrad = 2;
+constexpr int kSwzExpm = 2;
 
 // Teams of the slice-parallel mixed kernels.  A team of T threads owns one
 // matrix problem; a CTA holds 256 / T teams (T = 32: independent warps on
@@ -43,6 +48,12 @@ template <int D, int T> struct CfgM {
   static constexpr size_t WS = (size_t)80 * D * D;                 // workspace bytes per team
   static constexpr size_t RED = (size_t)2 * T * sizeof(float2);    // reduction scratch per team
   static constexpr size_t SMEM = (SLAB ? 0 : TPC * WS) + TPC * RED;
+  // expm kernel: five df matrices in the padded layout
+  static constexpr size_t WSE = (size_t)5 * Lay<D, 2>::SIZE * sizeof(float4);
+  static constexpr size_t SMEM_E = (SLAB ? 0 : TPC * WSE) + TPC * RED;
+  // gradient kernel: ten complex-float matrices in the padded layout
+  static constexpr size_t WSG = (size_t)10 * Lay<D, 2>::SIZE * sizeof(float2);
+  static constexpr size_t SMEM_G = (SLAB ? 0 : TPC * WSG) + TPC * RED;
 };
 
 template <int D, int T>
@@ -52,42 +63,124 @@ __device__ __forceinline__ Team<T> team_of() {
   return tm;
 }
 
+// ---- per-slice prologue without the FP64 pipe -----------------------------------
+// GB300 runs FP64 at 1/64 of its FP32 rate, so an FP64 assembly of A_k and an
+// FP64 1-norm cost as much pipe time as the products they feed.  The mixed
+// kernels assemble A_k from df copies of the constants (expm: df arithmetic,
+// gradient: FP32) and take the 1-norm in FP32.
+
+__global__ void k_prep_mx(const double* u, float2* u_df, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double x = u[i];
+    const float hi = (float)x;
+    u_df[i] = make_float2(hi, (float)(x - (double)hi));
+  }
+}
+
+__device__ __forceinline__ df df_ld(const float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+
+// A = c dt_k (drift + off O + scale sum_j u_jk C_j) in df.
+template <int D, int T, int SW>
+__device__ __forceinline__ void build_A_df(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m,
+                                           int k, float4* A) {
+  const df dt = df_ld(p.dt_df[k]), sc = df_ld(p.m_scale_df[m]), off = df_ld(p.m_offset_df[m]);
+  const bool has_off = off.hi != 0.f;
+  const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
+  const float2* uk = w.u_df + (size_t)k * p.n_c;
+  for (int q = tm.lane; q < D * D; q += T) {
+    dfc v = dfc_load(Gd[q]);
+    if (has_off) v = dfc_add(v, dfc_scale(dfc_load(p.offset_df[q]), off));
+    for (int j = 0; j < p.n_c; ++j) {
+      const df a = df_mul(sc, df_ld(uk[j]));
+      v = dfc_add(v, dfc_scale(dfc_load(p.ctrls_df[(size_t)j * D * D + q]), a));
+    }
+    v = dfc_scale(v, dt);
+    if (p.gen == GEN_HERM) v = {v.im, df_neg(v.re)};  // times -i
+    A[Lay<D, SW>::idx(q % D, q / D)] = dfc_store(v);
+  }
+}
+
+// The same in FP32 from the leading halves of the df constants.
+template <int D, int T, int SW>
+__device__ __forceinline__ void build_A32(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m,
+                                          int k, float2* A) {
+  const float dt = p.dt_df[k].x, sc = p.m_scale_df[m].x, off = p.m_offset_df[m].x;
+  const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
+  const float2* uk = w.u_df + (size_t)k * p.n_c;
+  for (int q = tm.lane; q < D * D; q += T) {
+    const float4 g = Gd[q];
+    const float4 o = p.offset_df[q];
+    float vx = fmaf(off, o.x, g.x), vy = fmaf(off, o.y, g.y);
+    for (int j = 0; j < p.n_c; ++j) {
+      const float a = sc * uk[j].x;
+      const float4 c = p.ctrls_df[(size_t)j * D * D + q];
+      vx = fmaf(a, c.x, vx);
+      vy = fmaf(a, c.y, vy);
+    }
+    vx *= dt;
+    vy *= dt;
+    A[Lay<D, SW>::idx(q % D, q / D)] = (p.gen == GEN_HERM) ? make_float2(vy, -vx) : make_float2(vx, vy);
+  }
+}
+
+// 1-norm from the FP32 (leading) parts, enlarged by 1e-5 to cover their
+// rounding: it only selects the Taylor degree and the squarings, whose
+// thresholds are tail bounds.
+template <int D, int T, int SW, class C>
+__device__ __forceinline__ double norm1f(const Team<T>& tm, const C* A, double* scratch) {
+  float best = 0.f;
+  for (int c = tm.lane; c < D; c += T) {
+    float s = 0.f;
+    for (int r = 0; r < D; ++r) {
+      const C a = A[Lay<D, SW>::idx(r, c)];
+      s += sqrtf(fmaf(a.x, a.x, a.y * a.y));
+    }
+    best = fmaxf(best, s);
+  }
+  return team_max<T>(tm, (double)(best * 1.00001f), scratch);
+}
+
 // ---- expm in df --------------------------------------------------------------
 template <int D, int T>
 __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
   using G = CfgM<D, T>;
+  using L = Lay<D, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int team = threadIdx.x / T;
   const Team<T> tm = team_of<D, T>();
   float4* base;
   if constexpr (G::SLAB)
-    base = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * 10 * D * D;
+    base = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * 5 * L::SIZE;
   else
-    base = reinterpret_cast<float4*>(smem_raw + (size_t)team * G::WS);
-  float4* red = reinterpret_cast<float4*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WS) + (size_t)team * G::RED);
+    base = reinterpret_cast<float4*>(smem_raw + (size_t)team * G::WSE);
+  float4* red = reinterpret_cast<float4*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WSE) + (size_t)team * G::RED);
   float4* B = base;
-  float4* B2 = base + D * D;
-  float4* B3 = base + 2 * D * D;
-  float4* B4 = base + 3 * D * D;
-  float4* Y = base + 4 * D * D;
+  float4* B2 = base + L::SIZE;
+  float4* B3 = base + 2 * L::SIZE;
+  float4* B4 = base + 3 * L::SIZE;
+  float4* Y = base + 4 * L::SIZE;
   const long items = (long)p.n_members * p.n_t;
   for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
-    double2* Ad = reinterpret_cast<double2*>(B);  // FP64 assembly in the same bytes
-    build_A<D, T, kSwz>(tm, p, w.u, m, k, Ad);
+    build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
     tm.sync();
-    const double nrm = norm1<D, T, kSwz>(tm, Ad, reinterpret_cast<double*>(red));
+    const double nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<double*>(red));
     int deg, s;
     choose_degree(nrm, c_theta64, deg, s);
-    const double sc = ldexp(1.0, -s);
-    for (int e = tm.lane; e < D * D; e += T) {  // in place: same bytes, same lane (after the barriers above)
-      const double2 a = Ad[e];
-      B[e] = dfc_store(dfc_from(make_double2(a.x * sc, a.y * sc)));
+    if (s > 0) {  // B <- B / 2^s, exact in df
+      const float sc = ldexpf(1.f, -s);
+      for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df
+        const int e = L::idx(q % D, q / D);
+        const float4 a = B[e];
+        B[e] = make_float4(a.x * sc, a.y * sc, a.z * sc, a.w * sc);
+      }
+      tm.sync();
     }
-    tm.sync();
-    taylor_exp_df<D, T, kSwz>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
+    taylor_exp_df<D, T, kSwzExpm>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
-    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[Lay<D, kSwz>::idx(e % D, e / D)];
+    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
     tm.sync();
   }
 }
@@ -215,12 +308,12 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
   const double cds = p.dt[k] * p.m_scale[m];
   if (tm.lane < 32) {
     for (int j = 0; j < p.n_c; ++j) {
-      const double2* Cj = p.ctrls + (size_t)j * D * D;
+      const float4* Cj = p.ctrls_df + (size_t)j * D * D;
       float2 acc = make_float2(0.f, 0.f);
-      for (int e = tm.lane; e < D * D; e += 32) {
-        const int r = Lay<D, SW>::row(e), c = e / D;
-        const double2 cv = Cj[c + D * r];
-        acc = cmac(acc, X[e], make_float2((float)cv.x, (float)cv.y));
+      for (int q = tm.lane; q < D * D; q += 32) {
+        const int r = q % D, c = q / D;
+        const float4 cv = Cj[c + D * r];
+        acc = cmac(acc, X[Lay<D, SW>::idx(r, c)], make_float2(cv.x, cv.y));
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -236,16 +329,17 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
 template <int D, int T>
 __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p, WorkDev w) {
   using G = CfgM<D, T>;
+  using L = Lay<D, kSwzGrad>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int team = threadIdx.x / T;
   const Team<T> tm = team_of<D, T>();
   float2* base;
   if constexpr (G::SLAB)
-    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * 10 * D * D;
+    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * 10 * L::SIZE;
   else
-    base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WS);
-  float2* red = reinterpret_cast<float2*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WS) + (size_t)team * G::RED);
-  const Work<float2, D> W = Work<float2, D>::at(base);
+    base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WSG);
+  float2* red = reinterpret_cast<float2*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WSG) + (size_t)team * G::RED);
+  const Work<float2, D, L::SIZE> W = Work<float2, D, L::SIZE>::at(base);
   const bool exact = (p.grad_mode == GRAD_EXACT);
   const long items = (long)p.n_members * p.n_t;
   for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
@@ -256,20 +350,21 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
       trace_controls32<D, T, 0>(tm, p, Mk, m, k, Gout, red);
       continue;
     }
-    for (int e = tm.lane; e < D * D; e += T) W.dB[Lay<D, kSwz>::idx(e % D, e / D)] = Mk[e];
-    build_A<D, T, kSwz>(tm, p, w.u, m, k, W.B);
+    for (int e = tm.lane; e < D * D; e += T) W.dB[L::idx(e % D, e / D)] = Mk[e];
+    build_A32<D, T, kSwzGrad>(tm, p, w, m, k, W.B);
     tm.sync();
-    const double nrm = norm1<D, T, kSwz>(tm, W.B, reinterpret_cast<double*>(red));
+    const double nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<double*>(red));
     int deg, s;
     choose_degree(nrm, c_theta32, deg, s);
     const float sc = ldexpf(1.f, -s);
-    for (int e = tm.lane; e < D * D; e += T) {
+    for (int q = tm.lane; q < D * D; q += T) {
+      const int e = L::idx(q % D, q / D);
       W.B[e] = cscale(W.B[e], sc);
       W.dB[e] = cscale(W.dB[e], sc);
     }
     tm.sync();
-    taylor_exp_frechet<D, T, kSwz>(tm, W, deg, s, c_invf32);
-    trace_controls32<D, T, kSwz>(tm, p, W.dY, m, k, Gout, red);
+    taylor_exp_frechet<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
+    trace_controls32<D, T, kSwzGrad>(tm, p, W.dY, m, k, Gout, red);
     tm.sync();
   }
 }
@@ -343,7 +438,7 @@ int mixed_default_team(int Dp, int kernel) {
 template <int D, int T>
 static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = CfgM<D, T>;
-  const size_t smem = G::SMEM;
+  const size_t smem = G::SMEM_E;
   ensure_smem_mx(k_expm_mx<D, T>, smem);
   const int grid = grid_for(k_expm_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
                             li.num_sms, G::SLAB ? w.slab_teams : 0);
@@ -388,7 +483,7 @@ cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Launch
 template <int D, int T>
 static cudaError_t do_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = CfgM<D, T>;
-  const size_t smem = G::SMEM;
+  const size_t smem = G::SMEM_G;
   ensure_smem_mx(k_grad_gate_mx<D, T>, smem);
   const int grid = grid_for(k_grad_gate_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
                             li.num_sms, G::SLAB ? w.slab_teams : 0);
@@ -396,6 +491,13 @@ static cudaError_t do_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchIn
   ++*li.launches;
   return cudaGetLastError();
 }
+cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  const int n = p.n_t * p.n_c;
+  k_prep_mx<<<(n + 255) / 256, 256, 0, li.stream>>>(w.u, w.u_df, n);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   const int t = li.team[kTuneGradMx] ? li.team[kTuneGradMx] : mixed_default_team(p.Dp, kTuneGradMx);
   PGX_DISPATCH_MX_T(p.Dp, t, return (do_grad_mx<D_, T_>(p, w, li)));

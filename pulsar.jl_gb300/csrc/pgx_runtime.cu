@@ -313,8 +313,13 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
                         2 * (size_t)std::max(d->n_pairs, 0) * Dp * sizeof(double2) * 2 +
                         (size_t)d->n_members * (sizeof(int) + 3 * sizeof(double)) +
                         (size_t)d->n_slices * sizeof(double);
+  // mixed: df copies of the generator constants and scalars, df controls
+  const size_t mixed = d->precision == PGX_PREC_MIXED
+                           ? DD * (d->n_drifts + d->n_controls + 1) +
+                                 sizeof(float2) * ((size_t)d->n_slices + 2 * (size_t)d->n_members) + s.u
+                           : 0;
   return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
-         2 * sizeof(double) + consts;
+         2 * sizeof(double) + consts + mixed;
 }
 
 int validate_desc(pgx_ctx* c, const pgx_problem_desc* d) { return validate(c, d); }
@@ -343,6 +348,29 @@ static std::vector<double> pad_mats(const double* src, int n, int D, int Dp) {
         out[di] = src[si];
         out[di + 1] = src[si + 1];
       }
+  return out;
+}
+
+// Interleaved complex doubles -> df pairs {re.hi, im.hi, re.lo, im.lo}.
+static std::vector<float> to_df_pairs(const std::vector<double>& z) {
+  std::vector<float> out(2 * z.size());
+  for (size_t i = 0; i + 1 < z.size(); i += 2) {
+    const float rh = (float)z[i], ih = (float)z[i + 1];
+    out[2 * i] = rh;
+    out[2 * i + 1] = ih;
+    out[2 * i + 2] = (float)(z[i] - (double)rh);
+    out[2 * i + 3] = (float)(z[i + 1] - (double)ih);
+  }
+  return out;
+}
+
+// Doubles -> df pairs {hi, lo}.
+static std::vector<float> to_df_scalars(const std::vector<double>& x) {
+  std::vector<float> out(2 * x.size());
+  for (size_t i = 0; i < x.size(); ++i) {
+    out[2 * i] = (float)x[i];
+    out[2 * i + 1] = (float)(x[i] - (double)out[2 * i]);
+  }
   return out;
 }
 
@@ -416,6 +444,27 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
     return st;
   }
   ProbDev& pd = p->pd;
+  if (d->precision == PGX_PREC_MIXED) {
+    // df copies of the generator constants for the mixed kernels
+    float *f_dr, *f_ct, *f_of;
+    if ((st = upload(p, &f_dr, to_df_pairs(drifts))) || (st = upload(p, &f_ct, to_df_pairs(ctrls))) ||
+        (st = upload(p, &f_of, to_df_pairs(offs)))) {
+      pgx_problem_destroy(p);
+      return st;
+    }
+    pd.drifts_df = (const float4*)f_dr;
+    pd.ctrls_df = (const float4*)f_ct;
+    pd.offset_df = (const float4*)f_of;
+    float *f_dt, *f_ms, *f_mo;
+    if ((st = upload(p, &f_dt, to_df_scalars(dt))) || (st = upload(p, &f_ms, to_df_scalars(mscale))) ||
+        (st = upload(p, &f_mo, to_df_scalars(moff)))) {
+      pgx_problem_destroy(p);
+      return st;
+    }
+    pd.dt_df = (const float2*)f_dt;
+    pd.m_scale_df = (const float2*)f_ms;
+    pd.m_offset_df = (const float2*)f_mo;
+  }
   pd.D = D;
   pd.Dp = Dp;
   pd.n_c = nc;
@@ -463,6 +512,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   p->d_u = (double*)A(s.u);
   p->d_G = (double*)A(s.G);
   p->d_F = (double*)A(2 * sizeof(double));
+  if (d->precision == PGX_PREC_MIXED) w.u_df = (float2*)A(s.u);
   if (st) {
     pgx_problem_destroy(p);
     return st;
@@ -539,6 +589,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
   int st;
   if (p->desc.precision == PGX_PREC_MIXED) {  // gate targets (validated at create)
     mk.mark(PGX_STAGE_EXPM);
+    if ((st = ctx_cuda(c, pgx::launch_prep_mx(p->pd, w, li), "prep_mx"))) return st;
     if ((st = ctx_cuda(c, pgx::launch_expm_mx(p->pd, w, li), "expm_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_FWD);
     if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, want_grad), "chain_fwd_mx"))) return st;

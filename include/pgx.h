@@ -172,6 +172,32 @@ int pgx_total_propagator(pgx_problem* prob, const double* u, int32_t member, dou
 int pgx_propagator(pgx_ctx* ctx, int32_t dim, int32_t generator, const double* gen, double dt,
                    double* U);
 
+/* ---- propagator stacks and chains (standalone building blocks) ---------- */
+/* The pieces of Propagators.jl / Objectives.jl the evaluation fuses, as
+ * device calls on host buffers (all FP64, column-major complex):
+ *   H[k] = H_drift + sum_j u[j + n_controls k] H_controls[j]
+ *        (build_total_hamiltonian, Propagators.jl:485-544; H [n][dim^2]) */
+int pgx_total_hamiltonian(pgx_ctx* ctx, int32_t dim, int32_t n_controls, int32_t n, const double* H_drift,
+                          const double* H_controls, const double* u, double* H);
+/*   U[k] = exp(c dt_k H[k]), c = -i (Hermitian) or 1 (Liouvillian), dt_count
+ *   = 1 (uniform) or n (compute_propagators, Propagators.jl:127-184). */
+int pgx_propagator_stack(pgx_ctx* ctx, int32_t dim, int32_t generator, int32_t n, const double* H,
+                         const double* dt, int32_t dt_count, double* U);
+/*   P[0] = I, P[k+1] = U[k] P[k]          (compute_forward_propagators, :291-325)
+ *   Q[n] = seed (NULL: I), Q[k] = U[k]' Q[k+1]
+ *                                         (compute_backward_propagators(!), :390-440)
+ *   U_total = U[n-1] ... U[0]             (compute_total_propagator, :212-238)
+ * P and Q hold n + 1 matrices; any of P, Q, U_total may be NULL. */
+int pgx_propagator_chains(pgx_ctx* ctx, int32_t dim, int32_t n, const double* U, const double* seed, double* P,
+                          double* Q, double* U_total);
+/*   z = sum_i conj(A_i) B_i over n complex entries: Tr(A'B) for matrices,
+ *   <a|b> for vectors (the overlaps of Objectives.jl:221,239-246). */
+int pgx_overlap(pgx_ctx* ctx, int64_t n, const double* A, const double* B, double* z);
+/*   out[j + m k] = Tr(X[k] E[j] Y[k]) for k < n, j < m (complex): the per-slice
+ *   traces of a first-order GRAPE gradient (CUDABackend.jl:352-356). */
+int pgx_trace_products(pgx_ctx* ctx, int32_t dim, int32_t n, int32_t m, const double* X, const double* E,
+                       const double* Y, double* out);
+
 /* ---- autotuning --------------------------------------------------------- */
 /* Times every team-size variant (threads per matrix problem, with the
  * matching register blocking) of the problem's slice-parallel mixed-precision

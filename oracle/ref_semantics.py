@@ -330,6 +330,35 @@ def compute_grape_gradient_with(system, target, P, Q, U_total, dt) -> np.ndarray
                           target.target_state, dt)
 
 
+def gradient_cuda_formula(H_drift, H_ctrl, controls, target, dt) -> np.ndarray:
+    """The reference's CUDA-backend gradient as written (its CPU form,
+    src/Backend/Hardware/CUDABackend.jl:283-305): P[0] = I, P[k+1] = U_k P[k];
+    Q[n] = T', Q[k] = Q[k+1] U_k; Phi = Tr(T' P[n]) / d;
+    G[j, k] = (2 / d^2) Re(conj(Phi) Tr(Q[k+1]' (-i dt H_j) P[k])).
+    Q[k+1]' (not Q[k+1]) and the extra 1/d are kept as the reference has them."""
+    H_drift = np.asarray(H_drift, C128)
+    d = H_drift.shape[0]
+    u = np.asarray(controls, float)
+    n_c, n = u.shape
+    T = np.asarray(target, C128)
+    Hk = [H_drift + sum(u[j, k] * np.asarray(H_ctrl[j], C128) for j in range(n_c)) for k in range(n)]
+    Uk = [expm_neg_i(H, dt) for H in Hk]
+    P = [np.eye(d, dtype=C128)]
+    for k in range(n):
+        P.append(Uk[k] @ P[k])
+    Q = [None] * (n + 1)
+    Q[n] = T.conj().T
+    for k in range(n - 1, -1, -1):
+        Q[k] = Q[k + 1] @ Uk[k]
+    Phi = np.trace(T.conj().T @ P[n]) / d
+    G = np.zeros((n_c, n))
+    for k in range(n):
+        for j in range(n_c):
+            M = Q[k + 1].conj().T @ (-1j * dt * np.asarray(H_ctrl[j], C128)) @ P[k]
+            G[j, k] = (2.0 / d ** 2) * np.real(np.conj(Phi) * np.trace(M))
+    return G
+
+
 def finite_difference_gradient(system, controls, target, eps=1e-6) -> np.ndarray:
     """Central differences (Gradients.jl:442-479)."""
     u = np.array(controls.controls, float)

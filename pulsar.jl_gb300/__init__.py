@@ -15,6 +15,11 @@ from .api import (
     compute_grape_gradient, compute_propagator, fidelity_forward, grape_lindblad_kernel,
     grape_optimize, grape_optimize_ensemble, grape_state_kernel, mat_rho, optimcon, propagate,
     pure_state_to_vec_rho, quantum_system, random_controls, state_target, unitary_target, vec_rho,
+    CUDABackend, batch_propagators_cuda, build_ensemble_from_mrcontrol, build_total_hamiltonian,
+    compute_backward_propagators, compute_forward_propagators, compute_propagators,
+    compute_total_propagator, cuda_backend, ensemble_value, ensemble_value_and_grad,
+    fidelity_cuda, fidelity_grad_prefactor, finite_difference_gradient, gate_fidelity, gradient_cuda,
+    grape_gradient_check, lindblad_grad_prefactor, matrix_exponential_cuda, state_fidelity,
 )
 
 LIB_PATH = _abi.LIB_PATH

@@ -117,6 +117,12 @@ SIGNATURES = {
     "pgx_member_fidelities": (C.c_int, [C.c_void_p, dptr]),
     "pgx_total_propagator": (C.c_int, [C.c_void_p, dptr, C.c_int32, dptr]),
     "pgx_propagator": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, C.c_double, dptr]),
+    "pgx_total_hamiltonian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr]),
+    "pgx_propagator_stack": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dptr, dptr, C.c_int32,
+                                       dptr]),
+    "pgx_propagator_chains": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr, dptr]),
+    "pgx_overlap": (C.c_int, [C.c_void_p, C.c_int64, dptr, dptr, dptr]),
+    "pgx_trace_products": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr]),
     "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
     "pgx_problem_set_team": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),

@@ -39,6 +39,7 @@ from typing import Callable, Optional, Sequence
 
 import numpy as np
 
+from . import _abi as _A
 from .engine import Context, Problem, default_context
 
 C128 = np.complex128
@@ -320,6 +321,282 @@ def compute_grape_gradient(system: QuantumSystem, controls: ControlSequence, tar
 
 
 # ---------------------------------------------------------------------------
+# Propagator stacks, chains and metrics (Propagators.jl, Objectives.jl,
+# Gradients.jl building blocks) -- each a device call
+# ---------------------------------------------------------------------------
+
+def _ctx_handle(ctx: Optional[Context]):
+    return (ctx or default_context()).handle
+
+
+def _cbuf(stack: np.ndarray) -> np.ndarray:
+    """[n, d, d] complex -> n column-major interleaved matrices (doubles)."""
+    return _A.cmat_buf(np.asarray(stack, C128))
+
+
+def _cstack(buf: np.ndarray, n: int, d: int) -> np.ndarray:
+    m = buf.reshape(n, d, d, 2)
+    return (m[..., 0] + 1j * m[..., 1]).transpose(0, 2, 1).copy()
+
+
+def build_total_hamiltonian(system: QuantumSystem, controls: ControlSequence,
+                            ctx: Optional[Context] = None) -> np.ndarray:
+    """H_total[k] = H_drift + sum_j amplitudes[k, j] H_j, [n_steps, d, d]
+    (Propagators.jl:485-544)."""
+    n_t, n_c = controls.amplitudes.shape
+    if n_c != system.n_controls:
+        raise ValueError(f"controls has {n_c} control channels but system has {system.n_controls} "
+                         "control fields")
+    d = system.dim
+    Hd = _cbuf(system.H_drift[None])
+    Hc = _cbuf(np.stack(system.H_controls)) if n_c else np.zeros(2)
+    u = np.ascontiguousarray(np.asarray(controls.controls, float).T).ravel()
+    out = np.zeros(2 * d * d * max(n_t, 1))
+    _A.check(_A.lib().pgx_total_hamiltonian(_ctx_handle(ctx), d, n_c, n_t, _A.as_dptr(Hd), _A.as_dptr(Hc),
+                                            _A.as_dptr(u if u.size else np.zeros(1)), _A.as_dptr(out)),
+             _ctx_handle(ctx))
+    return _cstack(out, n_t, d) if n_t else np.zeros((0, d, d), C128)
+
+
+def compute_propagators(H_total, dt, ctx: Optional[Context] = None, generator: str = "hermitian") -> np.ndarray:
+    """U[k] = exp(-i H[k] dt) for H_total [n_steps, d, d] (Propagators.jl:127-184);
+    dt a scalar or one value per slice."""
+    H = np.asarray(H_total, C128)
+    if H.ndim != 3:
+        raise ValueError(f"H_total must be a 3-D array [n_timesteps x dim x dim], got {H.ndim}-D")
+    n, d1, d2 = H.shape
+    if d1 != d2:
+        raise ValueError(f"H_total last two dimensions must be equal (square matrices), got {d1} x {d2}")
+    dts = np.atleast_1d(np.asarray(dt, float))
+    if np.any(dts <= 0):
+        raise ValueError(f"dt must be positive, got {dt}")
+    if n == 0:
+        return np.zeros((0, d1, d1), C128)
+    out = np.zeros(2 * d1 * d1 * n)
+    _A.check(_A.lib().pgx_propagator_stack(_ctx_handle(ctx), d1, _A.GEN[generator], n, _A.as_dptr(_cbuf(H)),
+                                           _A.as_dptr(np.ascontiguousarray(dts)), dts.size, _A.as_dptr(out)),
+             _ctx_handle(ctx))
+    return _cstack(out, n, d1)
+
+
+def _chains(props, seed=None, want=("P",), ctx: Optional[Context] = None):
+    U = np.asarray(props, C128)
+    if U.ndim != 3 or U.shape[1] != U.shape[2]:
+        raise ValueError(f"propagators must be a 3-D array [n x dim x dim], got shape {U.shape}")
+    n, d, _ = U.shape
+    if seed is not None:
+        seed = np.asarray(seed, C128)
+        if seed.shape != (d, d):
+            raise ValueError(f"seed must be {d} x {d}, got {seed.shape}")
+    P = np.zeros(2 * d * d * (n + 1)) if "P" in want else None
+    Q = np.zeros(2 * d * d * (n + 1)) if "Q" in want else None
+    T = np.zeros(2 * d * d) if "T" in want else None
+    ub = _cbuf(U) if n else np.zeros(2)
+    _A.check(_A.lib().pgx_propagator_chains(
+        _ctx_handle(ctx), d, n, _A.as_dptr(ub), _A.as_dptr(_cbuf(seed[None])) if seed is not None else None,
+        _A.as_dptr(P) if P is not None else None, _A.as_dptr(Q) if Q is not None else None,
+        _A.as_dptr(T) if T is not None else None), _ctx_handle(ctx))
+    return (_cstack(P, n + 1, d) if P is not None else None, _cstack(Q, n + 1, d) if Q is not None else None,
+            _cstack(T, 1, d)[0] if T is not None else None)
+
+
+def compute_total_propagator(propagators, ctx: Optional[Context] = None) -> np.ndarray:
+    """U_total = U[n-1] ... U[0]; identity for n = 0 (Propagators.jl:212-238)."""
+    return _chains(propagators, want=("T",), ctx=ctx)[2]
+
+
+def compute_forward_propagators(propagators, ctx: Optional[Context] = None) -> np.ndarray:
+    """P[0] = I, P[k+1] = U[k] P[k]; [n+1, d, d] (Propagators.jl:291-325)."""
+    return _chains(propagators, want=("P",), ctx=ctx)[0]
+
+
+def compute_backward_propagators(propagators, seed=None, ctx: Optional[Context] = None) -> np.ndarray:
+    """Q[n] = I (or seed), Q[k] = U[k]' Q[k+1]; [n+1, d, d].  As the reference's
+    code (Propagators.jl:399-404) Q[k] includes the slice's own propagator."""
+    return _chains(propagators, seed=seed, want=("Q",), ctx=ctx)[1]
+
+
+def _overlap(a, b, ctx: Optional[Context] = None) -> complex:
+    """sum conj(a) b over all entries, on the device (matrices: Tr(a'b))."""
+    a = np.asarray(a, C128)
+    b = np.asarray(b, C128)
+    if a.shape != b.shape:
+        raise ValueError(f"shape mismatch {a.shape} vs {b.shape}")
+    fa = np.ascontiguousarray(np.stack([a.real, a.imag], -1).ravel())
+    fb = np.ascontiguousarray(np.stack([b.real, b.imag], -1).ravel())
+    z = np.zeros(2)
+    _A.check(_A.lib().pgx_overlap(_ctx_handle(ctx), a.size, _A.as_dptr(fa), _A.as_dptr(fb), _A.as_dptr(z)),
+             _ctx_handle(ctx))
+    return complex(z[0], z[1])
+
+
+def gate_fidelity(U, U_target, type: str = "normalized", ctx: Optional[Context] = None) -> float:
+    """:normalized |Tr(U_t'U)|^2/d^2, :real Re Tr(U_t'U)/d, :average
+    (d F_norm + 1)/(d + 1) (Objectives.jl:239-265)."""
+    U = np.asarray(U, C128)
+    d = U.shape[0]
+    z = _overlap(U_target, U, ctx) / d
+    if type == "normalized":
+        return abs(z) ** 2
+    if type == "real":
+        return z.real
+    if type == "average":
+        return (d * abs(z) ** 2 + 1.0) / (d + 1.0)
+    raise ValueError(f"unknown gate fidelity type :{type}")
+
+
+def state_fidelity(psi_targ, psi_final, type: str = "real", ctx: Optional[Context] = None) -> float:
+    """:real Re<t|f>, :square |<t|f>|^2, :modulus |<t|f>|, :dm_linear Re Tr(rho'sigma)
+    (Objectives.jl:455-470).  :dm_uhlmann (matrix square roots of density
+    matrices) is outside the GRAPE path and not served."""
+    if type == "dm_uhlmann":
+        raise ValueError("state_fidelity(:dm_uhlmann) is not served by the GPU library")
+    z = _overlap(psi_targ, psi_final, ctx)
+    if type in ("real", "dm_linear"):
+        return z.real
+    if type == "square":
+        return abs(z) ** 2
+    if type == "modulus":
+        return abs(z)
+    raise ValueError(f"unknown state fidelity type :{type}")
+
+
+def fidelity_grad_prefactor(z: complex, inner: complex, dt_pwr: float, type: str) -> float:
+    """GRAPE chain-rule prefactor (Objectives.jl:352-361); :modulus keeps the
+    reference's dt_pwr Im(inner/|z|)."""
+    if type == "real":
+        return dt_pwr * inner.imag
+    if type == "square":
+        return 2.0 * dt_pwr * (np.conj(z) * inner).imag
+    if type == "modulus":
+        az = abs(z)
+        return 0.0 if az < 1e-14 else dt_pwr * (inner / az).imag
+    raise ValueError(f"unknown fidelity metric :{type}")
+
+
+def lindblad_grad_prefactor(z: complex, inner: complex, dt_pwr: float, type: str) -> float:
+    """Liouville-space prefactor with Re in place of Im (Lindblad.jl:220-232)."""
+    if type == "square":
+        return 2.0 * dt_pwr * (np.conj(z) * inner).real
+    if type == "real":
+        return dt_pwr * inner.real
+    raise ValueError(f"lindblad_grad_prefactor: ':{type}' not supported. Use :square or :real.")
+
+
+def finite_difference_gradient(system: QuantumSystem, controls: ControlSequence, target: QuantumTarget,
+                               eps: float = 1e-6) -> np.ndarray:
+    """Central differences (F(u + eps e_jk) - F(u - eps e_jk)) / 2 eps with F =
+    compute_fidelity (Gradients.jl:442-479); every F is a device evaluation."""
+    if eps <= 0:
+        raise ValueError(f"eps must be positive, got {eps}")
+    prob = _system_problem(system, target, controls.n_steps, controls.dt, grad_mode="ref_grape")
+    try:
+        u = np.array(controls.controls, float)
+        G = np.zeros_like(u)
+        for j in range(u.shape[0]):
+            for k in range(u.shape[1]):
+                up, um = u.copy(), u.copy()
+                up[j, k] += eps
+                um[j, k] -= eps
+                G[j, k] = (prob.eval(up, want_grad=False)[0] - prob.eval(um, want_grad=False)[0]) / (2 * eps)
+        return G
+    finally:
+        prob.close()
+
+
+def grape_gradient_check(system: QuantumSystem, target: QuantumTarget, controls: ControlSequence,
+                         eps: float = 1e-5) -> dict:
+    """Analytical vs central-difference gradient (GRAPE.jl:911-951): the
+    gradient grape_optimize uses against finite differences of its objective."""
+    G_ana = compute_grape_gradient(system, controls, target)
+    prob = _system_problem(system, target, controls.n_steps, controls.dt, grad_mode="ref_grape")
+    try:
+        u = np.array(controls.controls, float)
+        G_num = np.zeros_like(u)
+        for j in range(u.shape[0]):
+            for k in range(u.shape[1]):
+                up, um = u.copy(), u.copy()
+                up[j, k] += eps
+                um[j, k] -= eps
+                G_num[j, k] = (prob.eval(up, want_grad=False)[0] - prob.eval(um, want_grad=False)[0]) / (2 * eps)
+    finally:
+        prob.close()
+    diff = np.abs(G_ana - G_num)
+    max_err = float(np.max(diff)) if diff.size else 0.0
+    scale = max(1.0, float(np.max(np.abs(G_num))) if G_num.size else 0.0)
+    return {"analytical_gradient": G_ana, "numerical_gradient": G_num, "max_error": max_err,
+            "max_relative_error": max_err / scale, "passed": max_err < 1e-4}
+
+
+# ---- the reference's CUDA backend entry points (CUDABackend.jl) -------------
+
+@dataclass(frozen=True)
+class CUDABackend:
+    """CUDABackend.jl:55-75 (fields kept; the library always runs on the GPU)."""
+    device_id: int = 0
+    memory_limit_gb: float = math.inf
+    use_tensor_cores: bool = False
+    use_async: bool = False
+
+
+def cuda_backend(device_id: int = 0, memory_limit_gb: float = math.inf, use_tensor_cores: bool = False,
+                 use_async: bool = False) -> CUDABackend:
+    return CUDABackend(device_id, memory_limit_gb, use_tensor_cores, use_async)
+
+
+def _backend_ctx(backend: CUDABackend) -> Context:
+    return default_context() if backend.device_id == 0 else Context(backend.device_id)
+
+
+def matrix_exponential_cuda(H, dt: float, backend: CUDABackend) -> np.ndarray:
+    """exp(-i H dt) (CUDABackend.jl:126-150); no CPU fallback."""
+    return compute_propagator(H, dt, ctx=_backend_ctx(backend))
+
+
+def batch_propagators_cuda(H_array, dt: float, backend: CUDABackend) -> np.ndarray:
+    """H_array [dim, dim, n_steps] -> exp(-i H_k dt) in the same layout
+    (CUDABackend.jl:166-207)."""
+    H = np.asarray(H_array, C128)
+    U = compute_propagators(np.moveaxis(H, 2, 0), dt, ctx=_backend_ctx(backend))
+    return np.moveaxis(U, 0, 2)
+
+
+def fidelity_cuda(U_total, U_target, backend: CUDABackend) -> float:
+    """|Tr(U_target' U_total)|^2 / dim^2 (CUDABackend.jl:222-245)."""
+    d = np.asarray(U_total).shape[0]
+    return abs(_overlap(U_target, U_total, _backend_ctx(backend))) ** 2 / d ** 2
+
+
+def gradient_cuda(H_drift, H_ctrl, controls, target, dt: float, backend: CUDABackend) -> np.ndarray:
+    """The reference's GPU gradient, restated as it computes
+    (CUDABackend.jl:271-373): P[0] = I, P[k+1] = U_k P[k]; Q[n] = T',
+    Q[k] = Q[k+1] U_k; G[j, k] = (2/d^2) Re(conj(Phi) Tr(Q[k+1]' (-i dt H_j) P[k]))
+    with Phi = Tr(T'P[n])/d.  The Q[k+1]' there (the adjoint chain would use
+    Q[k+1]) and the extra 1/d make this differ from compute_grape_gradient;
+    it is kept as written.  Every product and trace runs on the device."""
+    ctx = _backend_ctx(backend)
+    Hd = np.asarray(H_drift, C128)
+    Hc = [np.asarray(h, C128) for h in H_ctrl]
+    u = np.asarray(controls, float)
+    T = np.asarray(target, C128)
+    d, n_c, n = Hd.shape[0], len(Hc), u.shape[1]
+    sysq = QuantumSystem(Hd, Hc)
+    H = build_total_hamiltonian(sysq, ControlSequence.from_controls(u, dt), ctx=ctx)
+    U = compute_propagators(H, dt, ctx=ctx)
+    # the reference's Q[k] = T' U_{n-1} ... U_k is the adjoint of the
+    # backward chain seeded with T: Q_ref[k+1]' = Q[k+1]
+    P, Q, Utot = _chains(U, seed=T, want=("P", "Q", "T"), ctx=ctx)
+    Phi = _overlap(T, Utot, ctx) / d
+    X = np.ascontiguousarray(Q[1:])                     # Q_ref[k+1]'
+    Y = np.ascontiguousarray(P[:n])                     # P[k]
+    out = np.zeros(2 * n_c * n)
+    _A.check(_A.lib().pgx_trace_products(ctx.handle, d, n, n_c, _A.as_dptr(_cbuf(X)), _A.as_dptr(_cbuf(np.stack(Hc))),
+                                         _A.as_dptr(_cbuf(Y)), _A.as_dptr(out)), ctx.handle)
+    tr = (out[0::2] + 1j * out[1::2]).reshape(n, n_c).T      # tr[j, k] = Tr(Q[k+1] H_j P[k])
+    return (2.0 / d ** 2) * np.real(np.conj(Phi) * (-1j * dt) * tr)
+
+
+# ---------------------------------------------------------------------------
 # Optimisation
 # ---------------------------------------------------------------------------
 
@@ -594,6 +871,29 @@ class LindbladMRControl:
                                  states_target=np.stack(self._sigma_targ), grad_mode=self.grad_mode,
                                  precision=self.precision)
         return self._prob
+
+
+def ensemble_value(obj: EnsembleObjective, theta) -> float:
+    """Aggregated ensemble fidelity at the flat parameter vector theta
+    (EnsembleObjective.jl:224-244, batched :mean path)."""
+    return obj.value(theta)
+
+
+def ensemble_value_and_grad(obj: EnsembleObjective, theta):
+    """(F, grad F) at theta (EnsembleObjective.jl:265-307, batched :mean path)."""
+    return obj.value_and_grad(theta)
+
+
+def build_ensemble_from_mrcontrol(ctrl, aggregator: str = "mean", cvar_alpha: float = 0.2) -> EnsembleObjective:
+    """EnsembleBuilder.jl:72-182, :mean: one batched device evaluation over
+    drifts x pwr_levels x state pairs, n_samples = their product."""
+    if aggregator != "mean":
+        raise ValueError("only the :mean aggregator runs batched on the device")
+    n_pairs = len(ctrl.rho_init)
+    n_drifts = len(ctrl.drifts)
+    prob = ctrl.problem()
+    return EnsembleObjective(prob, n_drifts * len(ctrl.pwr_levels) * n_pairs, len(ctrl.operators),
+                             len(ctrl.pulse_dt))
 
 
 def grape_state_kernel(waveform, ctrl: MRControl):

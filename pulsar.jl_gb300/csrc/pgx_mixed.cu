@@ -129,7 +129,7 @@ __device__ __forceinline__ void build_A32(const Team<T>& tm, const ProbDev& p, c
 // rounding: it only selects the Taylor degree and the squarings, whose
 // thresholds are tail bounds.
 template <int D, int T, int SW, class C>
-__device__ __forceinline__ double norm1f(const Team<T>& tm, const C* A, double* scratch) {
+__device__ __forceinline__ float norm1f(const Team<T>& tm, const C* A, float* scratch) {
   float best = 0.f;
   for (int c = tm.lane; c < D; c += T) {
     float s = 0.f;
@@ -139,7 +139,20 @@ __device__ __forceinline__ double norm1f(const Team<T>& tm, const C* A, double* 
     }
     best = fmaxf(best, s);
   }
-  return team_max<T>(tm, (double)(best * 1.00001f), scratch);
+  if constexpr (T <= 32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+  } else {
+    scratch[tm.lane] = best;
+    tm.sync();
+    for (int w = T / 2; w > 0; w >>= 1) {
+      if (tm.lane < w) scratch[tm.lane] = fmaxf(scratch[tm.lane], scratch[tm.lane + w]);
+      tm.sync();
+    }
+    best = scratch[0];
+    tm.sync();
+  }
+  return best * 1.00001f;
 }
 
 // ---- expm in df --------------------------------------------------------------
@@ -166,9 +179,9 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
     build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
     tm.sync();
-    const double nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<double*>(red));
+    const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
     int deg, s;
-    choose_degree(nrm, c_theta64, deg, s);
+    choose_degree_f(nrm, c_theta64f, deg, s);
     if (s > 0) {  // B <- B / 2^s, exact in df
       const float sc = ldexpf(1.f, -s);
       for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df
@@ -305,7 +318,6 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd_mx(ProbDev p
 template <int D, int T, int SW>
 __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDev& p, const float2* X,
                                                  int m, int k, double* Gout, float2*) {
-  const double cds = p.dt[k] * p.m_scale[m];
   if (tm.lane < 32) {
     for (int j = 0; j < p.n_c; ++j) {
       const float4* Cj = p.ctrls_df + (size_t)j * D * D;
@@ -320,7 +332,7 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
         acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
         acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
       }
-      if (tm.lane == 0) Gout[j] = cds * (double)(p.gen == GEN_HERM ? acc.y : acc.x);
+      if (tm.lane == 0) Gout[j] = p.dt[k] * p.m_scale[m] * (double)(p.gen == GEN_HERM ? acc.y : acc.x);
     }
   }
   tm.sync();
@@ -353,9 +365,9 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
     for (int e = tm.lane; e < D * D; e += T) W.dB[L::idx(e % D, e / D)] = Mk[e];
     build_A32<D, T, kSwzGrad>(tm, p, w, m, k, W.B);
     tm.sync();
-    const double nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<double*>(red));
+    const float nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<float*>(red));
     int deg, s;
-    choose_degree(nrm, c_theta32, deg, s);
+    choose_degree_f(nrm, c_theta32f, deg, s);
     const float sc = ldexpf(1.f, -s);
     for (int q = tm.lane; q < D * D; q += T) {
       const int e = L::idx(q % D, q / D);

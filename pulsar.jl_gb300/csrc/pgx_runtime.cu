@@ -167,19 +167,19 @@ extern "C" int pgx_ctx_launch_count(const pgx_ctx* c, int64_t* count) {
 // ---------------------------------------------------------------------------
 // problem validation / sizing
 // ---------------------------------------------------------------------------
-static int pad_dim(int d) {
+int pad_dim(int d) {
   int p = 2;
   while (p < d) p *= 2;
   return p;
 }
 
-static bool finite_all(const double* x, size_t n) {
+bool finite_all(const double* x, size_t n) {
   for (size_t i = 0; i < n; ++i)
     if (!std::isfinite(x[i])) return false;
   return true;
 }
 
-static double herm_dev(const double* m, int D) {
+double herm_dev(const double* m, int D) {
   double dev = 0.0;
   for (int r = 0; r < D; ++r)
     for (int c = 0; c < D; ++c) {
@@ -337,7 +337,7 @@ extern "C" int pgx_problem_footprint(const pgx_problem_desc* d, uint64_t* bytes)
 // ---------------------------------------------------------------------------
 // problem create / destroy
 // ---------------------------------------------------------------------------
-static std::vector<double> pad_mats(const double* src, int n, int D, int Dp) {
+std::vector<double> pad_mats(const double* src, int n, int D, int Dp) {
   std::vector<double> out((size_t)n * Dp * Dp * 2, 0.0);
   if (!src) return out;
   for (int i = 0; i < n; ++i)

@@ -52,6 +52,13 @@ struct pgx_problem {
 };
 
 int ctx_fail(pgx_ctx* c, int status, const std::string& msg);
+// Host helpers: padded size (power of two >= max(d, 2)), finiteness, the
+// Hermiticity defect max |A - A'|, and n column-major D x D complex matrices
+// copied into zero-padded Dp x Dp ones.
+int pad_dim(int d);
+bool finite_all(const double* x, size_t n);
+double herm_dev(const double* m, int D);
+std::vector<double> pad_mats(const double* src, int n, int D, int Dp);
 // Descriptor validation (errors recorded on c) and device footprint in bytes.
 int validate_desc(pgx_ctx* c, const pgx_problem_desc* d);
 uint64_t problem_footprint(const pgx_problem_desc* d, int num_sms);

@@ -1,0 +1,145 @@
+"""Standalone building blocks of the path, each a device call, against the
+oracle's restatements: build_total_hamiltonian, compute_propagators, the
+forward / backward / total chains (Propagators.jl:127-544), gate and state
+fidelities (Objectives.jl), finite differences and grape_gradient_check
+(Gradients.jl:442-479, GRAPE.jl:911-951), the CUDA-backend entry points
+(CUDABackend.jl:126-373) and the batched ensemble objective.
+"""
+import numpy as np
+import pytest
+
+from oracle import ref_semantics as rs
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _herm(rng, d, s=1.0):
+    A = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+    return s * (A + A.conj().T) / 2
+
+
+def _unitary(rng, d):
+    Z = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+    Q, R = np.linalg.qr(Z)
+    return Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]
+
+
+@pytest.mark.parametrize("d", [2, 3, 16, 40])
+def test_total_hamiltonian_and_propagator_stack(pg, d):
+    rng = np.random.default_rng(d)
+    n_t, n_c = 6, 3
+    sys_g = pg.quantum_system(_herm(rng, d), [_herm(rng, d) for _ in range(n_c)])
+    cs = pg.ControlSequence(rng.uniform(-1, 1, (n_t, n_c)), 0.03)
+    H = pg.build_total_hamiltonian(sys_g, cs)
+    Ho = rs.build_total_hamiltonian(rs.QuantumSystem(sys_g.H_drift, sys_g.H_controls),
+                                    rs.ControlSequence(cs.amplitudes, cs.dt))
+    assert np.max(np.abs(H - Ho)) <= TOL * max(1.0, np.max(np.abs(Ho)))
+    U = pg.compute_propagators(H, cs.dt)
+    Uo = rs.compute_propagators(Ho, cs.dt)
+    assert np.max(np.abs(U - Uo)) <= 1e-12
+    dts = rng.uniform(0.01, 0.05, n_t)                   # one dt per slice (MR pulse_dt)
+    assert np.max(np.abs(pg.compute_propagators(H, dts) - rs.compute_propagators(Ho, dts))) <= 1e-12
+
+
+def test_liouvillian_stack(pg):
+    rng = np.random.default_rng(5)
+    L = np.stack([rs.build_drift_liouvillian(_herm(rng, 2), [np.array([[0, 1], [0, 0]], complex)], [0.3])
+                  for _ in range(4)])
+    U = pg.compute_propagators(L, 0.2, generator="liouvillian")
+    Uo = np.stack([rs.expm_general(0.2 * L[k]) for k in range(4)])
+    assert np.max(np.abs(U - Uo)) <= 1e-12
+
+
+@pytest.mark.parametrize("d", [3, 16, 64])
+def test_chains(pg, d):
+    rng = np.random.default_rng(10 + d)
+    n = 7
+    U = np.stack([_unitary(rng, d) for _ in range(n)])
+    seed = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+    P = pg.compute_forward_propagators(U)
+    assert np.max(np.abs(P - rs.forward_propagators(U))) <= 1e-12
+    assert np.max(np.abs(pg.compute_backward_propagators(U) - rs.backward_propagators(U))) <= 1e-12
+    Qs = pg.compute_backward_propagators(U, seed)
+    assert np.max(np.abs(Qs - rs.backward_propagators(U, seed))) <= 1e-12 * np.max(np.abs(seed))
+    assert np.max(np.abs(pg.compute_total_propagator(U) - rs.compute_total_propagator(U))) <= 1e-12
+    assert np.array_equal(pg.compute_total_propagator(U[:0]), np.eye(d))     # empty product
+
+
+def test_fidelities_and_prefactors(pg):
+    rng = np.random.default_rng(3)
+    d = 5
+    U, T = _unitary(rng, d), _unitary(rng, d)
+    z = np.trace(T.conj().T @ U) / d
+    assert abs(pg.gate_fidelity(U, T) - rs.gate_fidelity(U, T)) <= TOL
+    assert abs(pg.gate_fidelity(U, T, type="real") - z.real) <= TOL
+    assert abs(pg.gate_fidelity(U, T, type="average") - (d * abs(z) ** 2 + 1) / (d + 1)) <= TOL
+    a = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+    b = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+    for t in ("real", "square", "modulus"):
+        assert abs(pg.state_fidelity(a, b, type=t) - rs.state_fidelity(a, b, t)) <= TOL
+    with pytest.raises(ValueError):
+        pg.state_fidelity(a, b, type="dm_uhlmann")
+    zc, inner = 0.3 + 0.4j, -0.2 + 0.7j
+    for t in ("real", "square", "modulus"):
+        assert pg.fidelity_grad_prefactor(zc, inner, 0.1, t) == rs.fidelity_grad_prefactor(zc, inner, 0.1, t)
+    for t in ("real", "square"):
+        assert pg.lindblad_grad_prefactor(zc, inner, 0.1, t) == rs.lindblad_grad_prefactor(zc, inner, 0.1, t)
+
+
+def test_finite_differences_and_gradient_check(pg):
+    rng = np.random.default_rng(8)
+    d, n_c, n_t = 3, 2, 5
+    Hd, Hc = _herm(rng, d), [_herm(rng, d) for _ in range(n_c)]
+    u = rng.uniform(-1, 1, (n_c, n_t))
+    T = _unitary(rng, d)
+    sys_g = pg.quantum_system(Hd, Hc)
+    cs = pg.ControlSequence.from_controls(u, 0.1)
+    G = pg.finite_difference_gradient(sys_g, cs, pg.unitary_target(T))
+    Go = rs.finite_difference_gradient(rs.QuantumSystem(Hd, Hc), rs.ControlSequence.from_controls(u, 0.1),
+                                       rs.unitary_target(T))
+    assert np.max(np.abs(G - Go)) <= 1e-8
+    chk = pg.grape_gradient_check(sys_g, pg.unitary_target(T), cs)
+    assert set(chk) >= {"analytical_gradient", "numerical_gradient", "max_error", "max_relative_error", "passed"}
+    assert np.max(np.abs(chk["numerical_gradient"] - Go)) <= 1e-6
+
+
+def test_cuda_backend_entry_points(pg):
+    rng = np.random.default_rng(21)
+    d, n_c, n_t, dt = 4, 2, 6, 0.07
+    be = pg.cuda_backend()
+    Hd, Hc = _herm(rng, d), [_herm(rng, d) for _ in range(n_c)]
+    u = rng.uniform(-1, 1, (n_c, n_t))
+    T = _unitary(rng, d)
+    assert np.max(np.abs(pg.matrix_exponential_cuda(Hd, dt, be) - rs.expm_neg_i(Hd, dt))) <= 1e-12
+    Harr = np.stack([_herm(rng, d) for _ in range(3)], axis=2)           # (dim, dim, n_steps)
+    Ub = pg.batch_propagators_cuda(Harr, dt, be)
+    for k in range(3):
+        assert np.max(np.abs(Ub[:, :, k] - rs.expm_neg_i(Harr[:, :, k], dt))) <= 1e-12
+    U = _unitary(rng, d)
+    assert abs(pg.fidelity_cuda(U, T, be) - abs(np.trace(T.conj().T @ U)) ** 2 / d ** 2) <= TOL
+    G = pg.gradient_cuda(Hd, Hc, u, T, dt, be)
+    Go = rs.gradient_cuda_formula(Hd, Hc, u, T, dt)
+    assert np.max(np.abs(G - Go)) <= 1e-12 * max(1.0, np.max(np.abs(Go)))
+
+
+def test_ensemble_value_functions_and_mr_builder(pg):
+    rng = np.random.default_rng(4)
+    d, n_t = 2, 8
+    SX = np.array([[0, 1], [1, 0]], complex)
+    SY = np.array([[0, -1j], [1j, 0]], complex)
+    SZ = np.diag([1.0, -1.0]).astype(complex)
+    ctrl = pg.MRControl(drifts=[0.5 * o * SZ for o in (-0.2, 0.0, 0.3)], operators=[0.5 * SX, 0.5 * SY],
+                        rho_init=[np.array([1, 0], complex)], rho_targ=[np.array([0, 1], complex)],
+                        pwr_levels=[0.9, 1.0, 1.1], pulse_dt=np.full(n_t, 0.2))
+    obj = pg.build_ensemble_from_mrcontrol(ctrl)
+    assert obj.n_samples == 9
+    w = rng.uniform(-1, 1, (2, n_t))
+    theta = w.reshape(-1, order="F")
+    F, G = pg.grape_state_kernel(w, ctrl)
+    assert pg.ensemble_value(obj, theta) == F
+    Fv, g = pg.ensemble_value_and_grad(obj, theta)
+    assert Fv == F and np.array_equal(g, G.reshape(-1, order="F"))
+    with pytest.raises(ValueError):
+        pg.build_ensemble_from_mrcontrol(ctrl, aggregator="cvar")

@@ -54,8 +54,9 @@ K_EXP = 8  # conventional matrix-product count of one expm in the FLOP model
 # DRAM bytes per launch of the dominant kernel from ncu captures, scaled from
 # the captured 200-slice case to 1000 slices (one M_k read per unit: linear).
 TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
-           ("spin4", "mixed", "expm"): 5 * (239.104000e6 + 127.746304e6),
-           ("spin4", "mixed", "grad"): 5 * (94.714112e6 + 2.698240e6)}
+           ("spin4", "mixed", "expm"): 5 * (73.728000e6 + 127.458816e6),
+           ("spin4", "mixed", "grad"): 5 * (94.700032e6 + 2.850560e6),
+           ("spin4", "mixed", "chain_fwd"): 5 * (189.268736e6 + 67.549952e6)}
 # FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
 # accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
 # busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).

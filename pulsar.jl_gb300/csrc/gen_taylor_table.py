@@ -39,12 +39,14 @@ def theta_for(m: int, u: float) -> float:
 
 
 def main(out=sys.stdout):
-    u64, u32 = 2.0 ** -53, 2.0 ** -24
+    # df32 (hi + lo float pairs) carries ~48 significant bits; its table keeps
+    # the truncation below 2^-47, under the df rounding of one product.
+    u64, u32, udf = 2.0 ** -53, 2.0 ** -24, 2.0 ** -47
     print("// Generated by gen_taylor_table.py -- do not edit.", file=out)
     print("#pragma once", file=out)
     assert DEGREES == tuple(4 * (i + 1) for i in range(len(DEGREES)))
     print(f"#define PGX_N_DEGREES {len(DEGREES)}  /* degrees 4, 8, ..., 4*N */", file=out)
-    for name, u in (("PGX_THETA64_INIT", u64), ("PGX_THETA32_INIT", u32)):
+    for name, u in (("PGX_THETA64_INIT", u64), ("PGX_THETA32_INIT", u32), ("PGX_THETADF_INIT", udf)):
         vals = ", ".join(f"{theta_for(m, u):.17g}" for m in DEGREES)
         print(f"#define {name} {{{vals}}}", file=out)
     inv = ", ".join(f"{1.0 / math.factorial(k):.17g}" for k in range(max(DEGREES) + 1))

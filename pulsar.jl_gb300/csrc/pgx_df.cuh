@@ -161,6 +161,61 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
   tm.sync();
 }
 
+// out = A*B from the FP32 (leading) parts of df operands, plain FP32
+// accumulation, then epi(e, r, c, value as df) -- for products whose
+// contribution is small enough that FP32 rounding stays below df precision.
+template <int D, int T, int SW = 0, class Epi>
+__device__ __forceinline__ void mm_df_lo(const Team<T>& tm, float4* out, const float4* A, const float4* B,
+                                         Epi epi) {
+  using BK = Blocking<D, T>;
+  using L = Lay<D, SW>;
+  constexpr int RB = BK::RB, CB = BK::CB;
+  const bool active = tm.lane < BK::ACTIVE;
+  const int rb = tm.lane % BK::NR, cb = tm.lane / BK::NR;
+  float2 acc[RB][CB];
+#pragma unroll
+  for (int i = 0; i < RB; ++i)
+#pragma unroll
+    for (int j = 0; j < CB; ++j) acc[i][j] = make_float2(0.f, 0.f);
+  float4 res[RB][CB];
+  if (active) {
+#pragma unroll 4
+    for (int k = 0; k < D; ++k) {
+      float2 a[RB], b[CB];
+#pragma unroll
+      for (int i = 0; i < RB; ++i) {
+        const float4 v = A[L::idx(rb + BK::NR * i, k)];
+        a[i] = make_float2(v.x, v.y);
+      }
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const float4 v = B[L::idx(k, cb + BK::NCB * j)];
+        b[j] = make_float2(v.x, v.y);
+      }
+#pragma unroll
+      for (int i = 0; i < RB; ++i)
+#pragma unroll
+        for (int j = 0; j < CB; ++j) acc[i][j] = cmac(acc[i][j], a[i], b[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int r = rb + BK::NR * i, c = cb + BK::NCB * j;
+        const dfc v = {{acc[i][j].x, 0.f}, {acc[i][j].y, 0.f}};
+        res[i][j] = dfc_store(epi(L::idx(r, c), r, c, v));
+      }
+  }
+  tm.sync();
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) out[L::idx(rb + BK::NR * i, cb + BK::NCB * j)] = res[i][j];
+  }
+  tm.sync();
+}
+
 template <int D, int T, int SW = 0>
 __device__ __forceinline__ void mm1_df(const Team<T>& tm, float4* out, const float4* A, const float4* B) {
   mm_df<D, T, false, SW>(tm, out, A, B, (const float4*)nullptr, (const float4*)nullptr, DfEpiNone{});
@@ -179,9 +234,12 @@ __device__ __forceinline__ dfc df_block(int i, int r, int c, const float4& b1, c
 
 // Y = T_m(B)^(2^s) in df (B = A / 2^s on entry).  Same Paterson-Stockmeyer
 // schedule as taylor_exp: m = 4L costs 3 + (L - 1) products, then s squarings.
+// Horner steps i >= lo_from multiply B4 by a tail of size <= 1/(4(i+1))!; the
+// caller sets lo_from where D u32 ||B4||^(i+1) / (4(i+1))! is below df
+// precision, and those steps run in plain FP32.
 template <int D, int T, int SW = 0>
 __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* B3, float4* B4, float4* Y,
-                              int m, int s, const df* coef) {
+                              int m, int s, const df* coef, int lo_from = 1 << 30) {
   mm1_df<D, T, SW>(tm, B2, B, B);
   mm1_df<D, T, SW>(tm, B3, B2, B);
   mm1_df<D, T, SW>(tm, B4, B2, B2);
@@ -193,10 +251,13 @@ __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* 
   }
   tm.sync();
   for (int i = L - 2; i >= 0; --i) {
-    mm_df<D, T, false, SW>(tm, Y, B4, Y, (const float4*)nullptr, (const float4*)nullptr,
-                           [=](int e, int r, int c, dfc v) {
-                             return dfc_add(v, df_block(i, r, c, B[e], B2[e], B3[e], coef));
-                           });
+    const auto add_block = [=](int e, int r, int c, dfc v) {
+      return dfc_add(v, df_block(i, r, c, B[e], B2[e], B3[e], coef));
+    };
+    if (i >= lo_from)
+      mm_df_lo<D, T, SW>(tm, Y, B4, Y, add_block);
+    else
+      mm_df<D, T, false, SW>(tm, Y, B4, Y, (const float4*)nullptr, (const float4*)nullptr, add_block);
   }
   for (int k = 0; k < s; ++k) mm1_df<D, T, SW>(tm, Y, Y, Y);
 }

@@ -155,6 +155,22 @@ __device__ __forceinline__ float norm1f(const Team<T>& tm, const C* A, float* sc
   return best * 1.00001f;
 }
 
+// First Horner step of the df Taylor polynomial that may run in FP32.  Step i
+// computes B4 * Y with ||B4|| <= a^4 and ||Y|| <= e^a / (4(i+1))!, and its
+// error reaches the result through i more factors B4: bound
+// D u32 a^(4(i+1)) e^a / (4(i+1))!, required below 2^-47.
+__device__ __forceinline__ int lo_horner_from(float a, int L, int D) {
+  const float a4 = (a * a) * (a * a);
+  float pw = a4, fact = 24.f;  // a^(4(i+1)), (4(i+1))! for i = 0
+  const float lim = 7.1e-15f / (float)D / 5.96e-8f / __expf(a);
+  for (int i = 0; i < L - 1; ++i) {
+    if (i >= 1 && pw / fact <= lim) return i;
+    pw *= a4;
+    fact *= (float)((4 * i + 5) * (4 * i + 6) * (4 * i + 7) * (4 * i + 8));
+  }
+  return 1 << 30;
+}
+
 // ---- expm in df --------------------------------------------------------------
 template <int D, int T>
 __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
@@ -181,7 +197,8 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
     tm.sync();
     const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
     int deg, s;
-    choose_degree_f(nrm, c_theta64f, deg, s);
+    choose_degree_f(nrm, c_thetadf, deg, s);
+    const int lo_from = lo_horner_from(ldexpf(nrm, -s), deg / 4, D);
     if (s > 0) {  // B <- B / 2^s, exact in df
       const float sc = ldexpf(1.f, -s);
       for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df
@@ -191,7 +208,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
       }
       tm.sync();
     }
-    taylor_exp_df<D, T, kSwzExpm>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef);
+    taylor_exp_df<D, T, kSwzExpm>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef, lo_from);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
     for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
     tm.sync();

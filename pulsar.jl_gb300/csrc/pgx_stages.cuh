@@ -103,6 +103,7 @@ static __constant__ double c_theta32[PGX_N_DEGREES] = PGX_THETA32_INIT;
 // safety margin, far above the float rounding of a threshold).
 static __constant__ float c_theta64f[PGX_N_DEGREES] = PGX_THETA64_INIT;
 static __constant__ float c_theta32f[PGX_N_DEGREES] = PGX_THETA32_INIT;
+static __constant__ float c_thetadf[PGX_N_DEGREES] = PGX_THETADF_INIT;
 
 // choose_degree in float (same cost model, same tie-breaking).
 __device__ __forceinline__ void choose_degree_f(float nrm, const float* theta, int& m, int& s) {

@@ -250,6 +250,8 @@ def run_serve(args, pg, ctx, rank: int, world: int):
                           max_slices=args.serve_max_slices, max_members=args.serve_max_members,
                           lindblad_slices=args.serve_lindblad_slices, lindblad_draws=args.serve_lindblad_draws)
     opt = dict(max_iter=args.serve_max_iter, step_size=args.serve_step)
+    if args.serve_method == "ensemble_lbfgs":
+        opt["lbfgs_memory"] = 10
     budget = int(args.serve_budget_gb * 1e9)
     kw = [j.spec.problem_kwargs("exact", args.precision) for j in jobs]
     srv = pg.Server(ctx, max_inflight=args.serve_slots, hbm_budget_bytes=budget, target_fidelity=0.999)
@@ -265,7 +267,7 @@ def run_serve(args, pg, ctx, rank: int, world: int):
             dt = t0 + j.arrival_s - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            ids.append(srv.submit(u0=j.u0, opt=opt, **k))
+            ids.append(srv.submit(u0=j.u0, opt=opt, method=args.serve_method, **k))
         srv.drain()
         el = time.perf_counter() - t0
     st = srv.stats()
@@ -307,7 +309,8 @@ def run_serve(args, pg, ctx, rank: int, world: int):
                        "max_slices": args.serve_max_slices, "max_members": args.serve_max_members,
                        "lindblad": f"2-3 qubits, {args.serve_lindblad_slices} slices, "
                                    f"{args.serve_lindblad_draws} draws",
-                       "stop": f"F >= 0.999 or {args.serve_max_iter} iterations or grape_optimize's rules",
+                       "method": args.serve_method,
+                       "stop": f"F >= 0.999 or {args.serve_max_iter} iterations or the method's own rules",
                        "slots": args.serve_slots, "hbm_budget_gb": args.serve_budget_gb,
                        "precision": args.precision, "grad_mode": "exact",
                        "l2": "many concurrent jobs; working set of the stream >> 129 MB L2",
@@ -485,6 +488,8 @@ def main():
     sv.add_argument("--serve-lindblad-draws", type=int, default=4)
     sv.add_argument("--serve-max-iter", type=int, default=100)
     sv.add_argument("--serve-step", type=float, default=0.01)
+    sv.add_argument("--serve-method", default="ensemble_lbfgs", choices=["ensemble_lbfgs", "grape"],
+                    help="L-BFGS (history device-resident) or the GRAPE ascent")
     sv.add_argument("--serve-slots", type=int, default=128)
     sv.add_argument("--serve-budget-gb", type=float, default=80.0)
     sv.add_argument("--serve-check", type=int, default=48, help="jobs re-evaluated in FP64 for |dF|")

@@ -99,6 +99,37 @@ struct StepArgs {
 // the n problems of `a`, one CTA each.
 cudaError_t launch_ascent_step(const StepArgs& a, cudaStream_t stream);
 
+// Device state of one L-BFGS job (grape_optimize_ensemble, GRAPE.jl:1012-1230)
+// run by the server.  dmax, gnorm and zero come first: the host reads them back
+// as one 24-byte block.
+constexpr int kLbMaxMemory = 64;
+struct LbState {
+  double dmax;    // max |d| of the last direction (before normalisation)
+  double gnorm;   // ||g|| at the current controls
+  double zero;    // 1.0 when dmax < 1e-14
+  double a;       // current trial step
+  int head;       // next history slot
+  int count;      // stored pairs (<= m)
+  int m, n;       // memory, control count
+};
+struct LbArgs {
+  LbState* st;
+  double* S;          // [m][n]
+  double* Y;          // [m][n]
+  double* rho;        // [m]
+  const double* u;    // current controls
+  const double* g;    // gradient at u
+  double* d;          // direction
+  double* ut;         // trial controls
+  const double* gn;   // gradient at the accepted trial point
+  double a0;          // first trial step
+  double lim;         // amplitude limit (clip when clip != 0)
+  int clip;
+};
+cudaError_t launch_lb_direction(const LbArgs& a, cudaStream_t stream);
+cudaError_t launch_lb_trial(const LbArgs& a, bool halve, cudaStream_t stream);
+cudaError_t launch_lb_accept(const LbArgs& a, cudaStream_t stream);
+
 // Raises a kernel's dynamic shared-memory limit (once per kernel and device).
 void set_smem_once(const void* fn, size_t bytes);
 

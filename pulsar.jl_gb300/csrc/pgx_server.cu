@@ -15,6 +15,10 @@
 // admitted as soon as memory and a slot free up.  Each job runs exactly the
 // kernels of a solo run on its own stream, so its trajectory is bit-identical
 // alone and in any mix.
+// L-BFGS jobs (grape_optimize_ensemble, GRAPE.jl:1012-1230) advance one
+// evaluation at a time instead: the direction, the trial points of the
+// backtracking line search and the history update are device kernels on the
+// job's stream (pgx_lbfgs.cu); each step reads back (F, max|d|, ||g||).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -59,7 +63,12 @@ struct Readback {
   double F;
   double gnorm;
   double step;
+  double lb[3];  // L-BFGS jobs: dmax, gnorm, zero of the last direction
 };
+
+// Phases of an L-BFGS job: the evaluation in flight is F and G at the initial
+// controls, F at a trial point, or F and G at the accepted point.
+enum { LB_INIT = 0, LB_TRIAL = 1, LB_ACCEPT = 2 };
 
 struct Slot {
   cudaStream_t stream = nullptr;
@@ -95,6 +104,14 @@ struct Job {
   double F = 0.0, bestF = -INFINITY, step = 0.0;
   bool converged = false;
   clk::time_point t_submit, t_start, t_end;
+  // L-BFGS jobs (PGX_OPT_ENSEMBLE_LBFGS)
+  bool lbfgs = false;
+  int lb_phase = LB_INIT, lb_bt = 0, lb_it = 0;
+  bool lb_grad_eval = true;      // the evaluation in flight computes G
+  double lb_gnorm = 0.0;         // ||g|| at the start of the current iteration
+  pgx::LbState* lb = nullptr;
+  double *S = nullptr, *Yh = nullptr, *rho = nullptr, *own_u = nullptr, *own_g = nullptr, *dvec = nullptr;
+  double *ucur = nullptr, *utry = nullptr, *gcur = nullptr, *gtry = nullptr;
 };
 
 template <class T>
@@ -161,6 +178,11 @@ void release_device(pgx_server* s, Job& j) {
   j.dev = nullptr;
   if (j.d_best) cudaFreeAsync(j.d_best, stm);
   j.d_best = nullptr;
+  for (void* q : {(void*)j.lb, (void*)j.S, (void*)j.Yh, (void*)j.rho, (void*)j.own_u, (void*)j.own_g,
+                  (void*)j.dvec})
+    if (q) cudaFreeAsync(q, stm);
+  j.lb = nullptr;
+  j.S = j.Yh = j.rho = j.own_u = j.own_g = j.dvec = nullptr;
   cudaGetLastError();
 }
 
@@ -199,6 +221,29 @@ int admit(pgx_server* s, Job& j) {
       cudaMallocFromPoolAsync((void**)&j.d_best, n * sizeof(double), s->pool, sl.stream) != cudaSuccess) {
     cudaGetLastError();
     return PGX_ERR_NOMEM;
+  }
+  if (j.lbfgs) {
+    const int mm = j.opt.lbfgs_memory;
+    auto alloc = [&](double** q, size_t count) {
+      return cudaMallocFromPoolAsync((void**)q, sizeof(double) * count, s->pool, sl.stream) == cudaSuccess;
+    };
+    if (cudaMallocFromPoolAsync((void**)&j.lb, sizeof(pgx::LbState), s->pool, sl.stream) != cudaSuccess ||
+        !alloc(&j.S, (size_t)mm * n) || !alloc(&j.Yh, (size_t)mm * n) || !alloc(&j.rho, (size_t)mm) ||
+        !alloc(&j.own_u, n) || !alloc(&j.own_g, n) || !alloc(&j.dvec, n)) {
+      cudaGetLastError();
+      return PGX_ERR_NOMEM;
+    }
+    pgx::LbState ls{};
+    ls.m = mm;
+    ls.n = (int)n;
+    if (cudaMemcpyAsync(j.lb, &ls, sizeof ls, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess) {
+      cudaGetLastError();
+      return PGX_ERR_CUDA;
+    }
+    j.ucur = j.prob->d_u;
+    j.gcur = j.prob->d_G;
+    j.utry = j.own_u;
+    j.gtry = j.own_g;
   }
   JobDev h{};
   h.u = j.prob->d_u;
@@ -327,6 +372,151 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
   return !stop;
 }
 
+// ---- L-BFGS jobs (opt_ensemble_lbfgs semantics, GRAPE.jl:1012-1230) --------
+
+pgx::LbArgs lb_args(const Job& j) {
+  const double lim = j.opt.amplitude_limit;
+  const bool clip = std::isfinite(lim);
+  return pgx::LbArgs{j.lb, j.S, j.Yh, j.rho, j.ucur, j.gcur, j.dvec, j.utry, j.gtry,
+                     clip ? j.opt.step_size * lim : j.opt.step_size, clip ? lim : 0.0, clip ? 1 : 0};
+}
+
+// Enqueues the evaluation at the trial point (with G when `grad`) and the
+// read-back of (F, dmax, gnorm, zero).
+int lb_eval(pgx_server* s, Job& j, bool grad) {
+  const Slot& sl = s->slots[j.slot];
+  const int64_t l0 = s->ctx->launches;
+  const int st = run_pipeline(j.prob, j.utry, j.prob->d_F, grad ? j.gtry : nullptr, sl.stream);
+  s->launches += s->ctx->launches - l0;
+  if (st) return st;
+  j.lb_grad_eval = grad;
+  if (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hb->lb, j.lb, 3 * sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
+      cudaEventRecord(sl.done, sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  j.inflight = true;
+  return PGX_OK;
+}
+
+// Direction, first trial point, and F there.
+int lb_start_iteration(pgx_server* s, Job& j) {
+  if (!j.lb || !j.S || !j.Yh || !j.rho || !j.ucur || !j.gcur || !j.utry || !j.gtry || !j.dvec)
+    return PGX_ERR_STATE;  // never launch on a job whose L-BFGS state is not allocated
+  const cudaStream_t stm = s->slots[j.slot].stream;
+  const pgx::LbArgs a = lb_args(j);
+  if (pgx::launch_lb_direction(a, stm) != cudaSuccess || pgx::launch_lb_trial(a, false, stm) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  s->launches += 2;
+  j.lb_phase = LB_TRIAL;
+  j.lb_bt = 0;
+  return lb_eval(s, j, false);
+}
+
+int lb_copy_best(pgx_server* s, Job& j) {
+  const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+  if (cudaMemcpyAsync(j.d_best, j.ucur, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                      s->slots[j.slot].stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  return PGX_OK;
+}
+
+// A finished evaluation of an L-BFGS job.  The evaluation at the start of
+// each reference iteration, F and G at u, repeats the one at the end of the
+// previous iteration (same controls, deterministic evaluation) and is not run
+// again.  Returns false when the job stops; *why names the rule.  Further
+// device work is enqueued here.
+bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, int* err) {
+  auto fail = [&](int e, const char* w) {
+    *err = e;
+    *why = w;
+    return false;
+  };
+  if (!std::isfinite(rb.F)) return fail(PGX_ERR_NONFINITE, "non-finite objective");
+  int st = PGX_OK;
+  switch (j.lb_phase) {
+    case LB_INIT:  // F and G at the initial controls
+      j.F = rb.F;
+      j.fh.assign(1, rb.F);
+      j.bestF = rb.F;
+      j.round = 0;
+      j.lb_it = 1;
+      if ((st = lb_copy_best(s, j)) || (st = lb_start_iteration(s, j))) return fail(st, "launch failed");
+      return true;
+    case LB_TRIAL:
+      if (j.lb_bt == 0) {
+        j.lb_gnorm = rb.lb[1];
+        if (rb.lb[2] != 0.0) {
+          j.converged = true;
+          *why = "zero gradient direction";
+          return false;
+        }
+      }
+      if (rb.F >= j.F) {  // accepted: F and G there
+        j.lb_phase = LB_ACCEPT;
+        if ((st = lb_eval(s, j, true))) return fail(st, "launch failed");
+        return true;
+      }
+      j.lb_bt += 1;  // backtrack: halve (20 halvings, then take the last one)
+      if (pgx::launch_lb_trial(lb_args(j), true, s->slots[j.slot].stream) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PGX_ERR_CUDA, "launch failed");
+      }
+      s->launches += 1;
+      if (j.lb_bt >= 20) j.lb_phase = LB_ACCEPT;
+      if ((st = lb_eval(s, j, j.lb_bt >= 20))) return fail(st, "launch failed");
+      return true;
+    default: {  // LB_ACCEPT: F and G at the accepted point
+      if (pgx::launch_lb_accept(lb_args(j), s->slots[j.slot].stream) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PGX_ERR_CUDA, "launch failed");
+      }
+      s->launches += 1;
+      std::swap(j.ucur, j.utry);
+      std::swap(j.gcur, j.gtry);
+      const double Fprev = j.F;
+      j.F = rb.F;
+      j.fh.push_back(rb.F);
+      j.round = (int)j.fh.size() - 1;
+      if (j.F > j.bestF) {
+        j.bestF = j.F;
+        if ((st = lb_copy_best(s, j))) return fail(st, "launch failed");
+      }
+      if (j.lb_gnorm < j.opt.gradient_norm_tol) {
+        j.converged = true;
+        *why = "gradient norm below tolerance";
+        return false;
+      }
+      if (j.F >= 1.0 - 1e-8) {
+        j.converged = true;
+        *why = "near-perfect fidelity";
+        return false;
+      }
+      if (std::fabs(j.F - Fprev) < j.opt.convergence_tol) {
+        j.converged = true;
+        *why = "fidelity change below tolerance";
+        return false;
+      }
+      if (j.F >= s->cfg.target_fidelity) {
+        j.converged = true;
+        *why = "target fidelity reached";
+        return false;
+      }
+      if (++j.lb_it > j.opt.max_iter) {
+        *why = "maximum iterations reached";
+        return false;
+      }
+      if ((st = lb_start_iteration(s, j))) return fail(st, "launch failed");
+      return true;
+    }
+  }
+}
+
 int launch_iteration(pgx_server* s, Job& j) {
   if (!j.iter_exec) {
     const int st = capture_iteration(s, j);
@@ -401,16 +591,16 @@ void worker_loop(pgx_server* s) {
       bool go = false;
       if (!err) {
         const Readback rb = *sl.hb;
-        s->units += j->units;
+        if (!j->lbfgs || j->lb_grad_eval) s->units += j->units;
         std::lock_guard<std::mutex> lk(s->mu);  // polls read what advance() updates
-        go = advance(s, *j, rb, &why, &err);
+        go = j->lbfgs ? advance_lbfgs(s, *j, rb, &why, &err) : advance(s, *j, rb, &why, &err);
       }
       bool cancelled = false;
       if (go && j->cancel.load()) {
         go = false;
         cancelled = true;
       }
-      if (go) err = launch_iteration(s, *j);
+      if (go && !j->lbfgs) err = launch_iteration(s, *j);
       if (go && !err) continue;
       ended.push_back(j);
       if (err) {
@@ -553,14 +743,22 @@ extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_op
   if (o->struct_size < sizeof(pgx_opt_desc) || o->max_iter < 1 || o->step_size <= 0.0 ||
       o->min_step_size <= 0.0 || o->max_step_size < o->step_size)
     return ctx_fail(c, PGX_ERR_INVALID, "invalid optimiser settings (GRAPE.jl:108-119)");
-  if (o->method != PGX_OPT_GRAPE)
-    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "the server runs grape_optimize (PGX_OPT_GRAPE) jobs");
+  if (o->method != PGX_OPT_GRAPE && o->method != PGX_OPT_ENSEMBLE_LBFGS)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED,
+                    "the server runs grape_optimize and grape_optimize_ensemble (L-BFGS) jobs");
+  if (o->method == PGX_OPT_ENSEMBLE_LBFGS &&
+      (o->lbfgs_memory < 1 || o->lbfgs_memory > pgx::kLbMaxMemory || !(o->amplitude_limit > 0.0)))
+    return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory must be in [1, 64] and amplitude_limit positive");
   const size_t D = d->dim, DD = D * D, nc = d->n_controls, nt = d->n_slices, nm = d->n_members;
   const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
   for (size_t i = 0; i < nc * nt; ++i)
     if (!std::isfinite(u0[i])) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
   auto j = std::make_shared<Job>();
+  j->lbfgs = o->method == PGX_OPT_ENSEMBLE_LBFGS;
   j->footprint = problem_footprint(d, s->ctx->num_sms) + sizeof(JobDev) + nc * nt * sizeof(double);
+  if (j->lbfgs)  // (s, y) history, rho, trial controls and gradient, direction
+    j->footprint += sizeof(pgx::LbState) + sizeof(double) * ((2 * (size_t)o->lbfgs_memory + 3) * nc * nt +
+                                                             (size_t)o->lbfgs_memory);
   if (s->cfg.hbm_budget_bytes && j->footprint > s->cfg.hbm_budget_bytes)
     return ctx_fail(c, PGX_ERR_BUDGET, "job footprint exceeds the server's HBM budget");
   j->units = (int64_t)nm * (int64_t)nt;
@@ -626,8 +824,8 @@ extern "C" int pgx_fetch(pgx_server* s, uint64_t id, double* u, pgx_opt_result* 
     std::memset(res, 0, sizeof(*res));
     res->fidelity = j.bestF;
     res->total_time_s = secs(j.t_submit, j.t_end);
-    res->step_size_final = j.step;
-    res->n_iterations = std::max(j.round, 0);
+    res->step_size_final = j.lbfgs ? j.opt.step_size : j.step;
+    res->n_iterations = j.lbfgs ? (int)j.fh.size() : std::max(j.round, 0);
     res->converged = j.converged;
     res->n_fidelity_evals = j.round + 1;
     res->n_gradient_evals = j.round + 1;

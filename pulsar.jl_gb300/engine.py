@@ -213,15 +213,18 @@ class Server:
         except Exception:
             pass
 
-    def submit(self, drifts, controls, dt, u0, *, opt: Optional[dict] = None, **problem) -> int:
-        """Queue one grape_optimize job; ``problem`` takes Problem's keywords,
-        ``opt`` opt_desc's (GRAPEConfig defaults).  Returns the job id."""
+    def submit(self, drifts, controls, dt, u0, *, opt: Optional[dict] = None, method: str = "grape",
+               **problem) -> int:
+        """Queue one job: grape_optimize (method "grape") or the ensemble
+        L-BFGS of grape_optimize_ensemble ("ensemble_lbfgs").  ``problem``
+        takes Problem's keywords, ``opt`` opt_desc's (GRAPEConfig defaults).
+        Returns the job id."""
         d, keep, (D, n_c, n_t, _, _) = problem_desc(drifts, controls, dt, **problem)
         u = np.asarray(u0, np.float64)
         if u.shape != (n_c, n_t):
             raise ValueError(f"controls have shape {u.shape}, expected {(n_c, n_t)}")
         ub = np.ascontiguousarray(u.T.ravel())
-        o = opt_desc("grape", **(opt or {}))
+        o = opt_desc(method, **(opt or {}))
         jid = C.c_uint64()
         A.check(A.lib().pgx_submit(self._h, C.byref(d), C.byref(o), A.as_dptr(ub), C.byref(jid)),
                 self.ctx.handle)

@@ -172,3 +172,65 @@ def test_submit_validation(pg, ctx):
     assert e.value.status == 10
     assert srv.stats()["submitted"] == 0
     srv.close()
+
+
+LB_OPT = dict(max_iter=12, step_size=0.3, lbfgs_memory=5, convergence_tol=1e-12, gradient_norm_tol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lbfgs_job_identical_alone_and_in_the_mix(pg, ctx, precision):
+    jobs = _jobs()[:5]
+    solo = []
+    s = pg.Server(ctx, max_inflight=1, target_fidelity=2.0)
+    for spec, u0 in jobs:
+        jid = s.submit(u0=u0, opt=LB_OPT, method="ensemble_lbfgs", **spec.problem_kwargs("exact", precision))
+        assert s.drain(timeout_s=300)
+        solo.append(s.fetch(jid))
+    s.close()
+    mix = pg.Server(ctx, max_inflight=8, target_fidelity=2.0)
+    ids = []
+    for i, (spec, u0) in enumerate(jobs):  # L-BFGS and GRAPE jobs side by side
+        ids.append(mix.submit(u0=u0, opt=LB_OPT, method="ensemble_lbfgs", **spec.problem_kwargs("exact", precision)))
+        mix.submit(u0=u0, opt=OPT, **spec.problem_kwargs("exact", precision))
+    assert mix.drain(timeout_s=300)
+    mixed = [mix.fetch(j) for j in ids]
+    mix.close()
+    for a, b in zip(solo, mixed):
+        _same(a, b)
+
+
+def test_lbfgs_job_follows_grape_optimize_ensemble(pg, ctx):
+    """Iteration count, stop rule and result of the device-resident L-BFGS
+    against the host loop of grape_optimize_ensemble (GRAPE.jl:1012-1230); the
+    two differ only in the summation order of the dot products."""
+    rng = np.random.default_rng(17)
+    cases = [W.uneven_problem(rng, d=4, n_t=30, n_members=3), W.uneven_problem(rng, d=8, n_t=20, n_members=2)]
+    opts = [dict(max_iter=15, step_size=0.5, lbfgs_memory=4, convergence_tol=1e-12),
+            dict(max_iter=40, step_size=0.2, lbfgs_memory=6, convergence_tol=1e-6, amplitude_limit=1.5)]
+    srv = pg.Server(ctx, max_inflight=4, target_fidelity=2.0)
+    for (spec, u0), opt in zip(cases, opts):
+        p = pg.Problem(ctx=ctx, **spec.problem_kwargs("exact", "fp64"))
+        ref = p.optimize(u0, "ensemble_lbfgs", **opt)
+        p.close()
+        jid = srv.submit(u0=u0, opt=opt, method="ensemble_lbfgs", **spec.problem_kwargs("exact", "fp64"))
+        assert srv.drain(timeout_s=300)
+        r = srv.fetch(jid)
+        assert r.state == "done"
+        assert r.n_iterations == ref.n_iterations, (r.n_iterations, ref.n_iterations)
+        assert r.termination_reason == ref.termination_reason
+        assert r.converged == ref.converged
+        assert abs(r.fidelity - ref.fidelity) <= 1e-9, (r.fidelity, ref.fidelity)
+        assert np.max(np.abs(r.controls - ref.controls)) <= 1e-6 * max(1.0, np.max(np.abs(ref.controls)))
+    srv.close()
+
+
+def test_lbfgs_submit_validation(pg, ctx):
+    spec, u0 = W.uneven_problem(np.random.default_rng(2), d=4, n_t=10, n_members=1)
+    srv = pg.Server(ctx, max_inflight=2)
+    with pytest.raises(pg._abi.PgxError) as e:
+        srv.submit(u0=u0, opt=dict(lbfgs_memory=0), method="ensemble_lbfgs", **spec.problem_kwargs("exact", "fp64"))
+    assert e.value.status == 1
+    with pytest.raises(pg._abi.PgxError) as e:
+        srv.submit(u0=u0, method="mr_lbfgs", **spec.problem_kwargs("exact", "fp64"))
+    assert e.value.status == 6
+    srv.close()

@@ -117,8 +117,8 @@ struct LbArgs {
   double* S;          // [m][n]
   double* Y;          // [m][n]
   double* rho;        // [m]
-  const double* u;    // current controls
-  const double* g;    // gradient at u
+  double* u;          // current controls (accept: <- ut)
+  double* g;          // gradient at u (accept: <- gn)
   double* d;          // direction
   double* ut;         // trial controls
   const double* gn;   // gradient at the accepted trial point

@@ -111,14 +111,13 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_trial(LbArgs A, int halve) {
 }
 
 // s = a d, y = gn - g; kept when y.s > 1e-14 ||s||^2 (the oldest pair drops
-// out beyond m).
+// out beyond m).  Then u <- ut and g <- gn, so a job's buffers never move and
+// its steps can be replayed as CUDA graphs.
 __global__ void __launch_bounds__(kLbThreads) k_lb_accept(LbArgs A) {
   __shared__ double red[kLbThreads];
   LbState* st = A.st;
   const int n = st->n, m = st->m, head = st->head;
   const double a = st->a;
-  double* s = A.S + (size_t)head * n;  // written only if kept: stage in place, slot head is free or oldest
-  double* y = A.Y + (size_t)head * n;
   double ss = 0.0, ys = 0.0;
   for (int i = threadIdx.x; i < n; i += kLbThreads) {
     const double si = a * A.d[i], yi = A.gn[i] - A.g[i];
@@ -128,17 +127,24 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_accept(LbArgs A) {
   ss = block_sum(ss, red);
   ys = block_sum(ys, red);
   const double sn = sqrt(ss);
-  if (ys > 1e-14 * sn * sn) {
-    for (int i = threadIdx.x; i < n; i += kLbThreads) {
+  const bool keep = ys > 1e-14 * sn * sn;
+  double* s = A.S + (size_t)head * n;
+  double* y = A.Y + (size_t)head * n;
+  double* u = A.u;
+  double* g = A.g;
+  for (int i = threadIdx.x; i < n; i += kLbThreads) {
+    const double gi = A.gn[i];
+    if (keep) {
       s[i] = a * A.d[i];
-      y[i] = A.gn[i] - A.g[i];
+      y[i] = gi - g[i];
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      A.rho[head] = 1.0 / fmax(ys, 1e-14);
-      st->head = (head + 1) % m;
-      st->count = st->count < m ? st->count + 1 : m;
-    }
+    g[i] = gi;
+    u[i] = A.ut[i];
+  }
+  if (keep && threadIdx.x == 0) {
+    A.rho[head] = 1.0 / fmax(ys, 1e-14);
+    st->head = (head + 1) % m;
+    st->count = st->count < m ? st->count + 1 : m;
   }
 }
 

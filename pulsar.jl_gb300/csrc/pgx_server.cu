@@ -112,6 +112,8 @@ struct Job {
   pgx::LbState* lb = nullptr;
   double *S = nullptr, *Yh = nullptr, *rho = nullptr, *own_u = nullptr, *own_g = nullptr, *dvec = nullptr;
   double *ucur = nullptr, *utry = nullptr, *gcur = nullptr, *gtry = nullptr;
+  cudaGraphExec_t lb_exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int64_t lb_kernels[5] = {0, 0, 0, 0, 0};
 };
 
 template <class T>
@@ -174,6 +176,10 @@ void release_device(pgx_server* s, Job& j) {
   }
   if (j.iter_exec) cudaGraphExecDestroy(j.iter_exec);
   j.iter_exec = nullptr;
+  for (auto& g : j.lb_exec) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   if (j.dev) cudaFreeAsync(j.dev, stm);
   j.dev = nullptr;
   if (j.d_best) cudaFreeAsync(j.d_best, stm);
@@ -373,6 +379,13 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
 }
 
 // ---- L-BFGS jobs (opt_ensemble_lbfgs semantics, GRAPE.jl:1012-1230) --------
+// A job's buffers never move (the accept kernel copies ut -> u and gn -> g),
+// so each kind of step is captured once per job as a CUDA graph:
+//   start       direction, first trial point, F there, read-back
+//   halve       halved trial point, F there, read-back
+//   fg          F and G at the trial point, read-back
+//   halve_fg    halved trial point, F and G there, read-back (after 20 halvings)
+//   acc_start   accept (history, u, g), then as start
 
 pgx::LbArgs lb_args(const Job& j) {
   const double lim = j.opt.amplitude_limit;
@@ -381,39 +394,72 @@ pgx::LbArgs lb_args(const Job& j) {
                      clip ? j.opt.step_size * lim : j.opt.step_size, clip ? lim : 0.0, clip ? 1 : 0};
 }
 
-// Enqueues the evaluation at the trial point (with G when `grad`) and the
-// read-back of (F, dmax, gnorm, zero).
-int lb_eval(pgx_server* s, Job& j, bool grad) {
+// Evaluation at the trial point (with G when `grad`) and the read-back of
+// (F, dmax, gnorm, zero); *k counts the kernels enqueued outside the pipeline.
+int lb_enqueue_eval(pgx_server* s, Job& j, bool grad) {
   const Slot& sl = s->slots[j.slot];
-  const int64_t l0 = s->ctx->launches;
   const int st = run_pipeline(j.prob, j.utry, j.prob->d_F, grad ? j.gtry : nullptr, sl.stream);
-  s->launches += s->ctx->launches - l0;
   if (st) return st;
-  j.lb_grad_eval = grad;
   if (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
-      cudaMemcpyAsync(sl.hb->lb, j.lb, 3 * sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
-      cudaEventRecord(sl.done, sl.stream) != cudaSuccess) {
+      cudaMemcpyAsync(sl.hb->lb, j.lb, 3 * sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
-  j.inflight = true;
   return PGX_OK;
 }
 
-// Direction, first trial point, and F there.
-int lb_start_iteration(pgx_server* s, Job& j) {
-  if (!j.lb || !j.S || !j.Yh || !j.rho || !j.ucur || !j.gcur || !j.utry || !j.gtry || !j.dvec)
-    return PGX_ERR_STATE;  // never launch on a job whose L-BFGS state is not allocated
+enum { G_START = 0, G_HALVE = 1, G_FG = 2, G_HALVE_FG = 3, G_ACC_START = 4, G_COUNT = 5 };
+
+int lb_enqueue_step(pgx_server* s, Job& j, int kind, int* extra) {
   const cudaStream_t stm = s->slots[j.slot].stream;
   const pgx::LbArgs a = lb_args(j);
-  if (pgx::launch_lb_direction(a, stm) != cudaSuccess || pgx::launch_lb_trial(a, false, stm) != cudaSuccess) {
+  auto ok = [&](cudaError_t e) {
+    ++*extra;
+    return e == cudaSuccess;
+  };
+  bool good = true;
+  if (kind == G_ACC_START) good = ok(pgx::launch_lb_accept(a, stm));
+  if (good && (kind == G_START || kind == G_ACC_START))
+    good = ok(pgx::launch_lb_direction(a, stm)) && ok(pgx::launch_lb_trial(a, false, stm));
+  if (good && (kind == G_HALVE || kind == G_HALVE_FG)) good = ok(pgx::launch_lb_trial(a, true, stm));
+  if (!good) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
-  s->launches += 2;
-  j.lb_phase = LB_TRIAL;
-  j.lb_bt = 0;
-  return lb_eval(s, j, false);
+  return lb_enqueue_eval(s, j, kind == G_FG || kind == G_HALVE_FG);
+}
+
+// Launches step `kind` of job j (capturing its graph on first use).
+int lb_launch(pgx_server* s, Job& j, int kind) {
+  if (!j.lb || !j.S || !j.Yh || !j.rho || !j.ucur || !j.gcur || !j.utry || !j.gtry || !j.dvec)
+    return PGX_ERR_STATE;  // never launch on a job whose L-BFGS state is not allocated
+  pgx_ctx* c = s->ctx;
+  const Slot& sl = s->slots[j.slot];
+  if (!j.lb_exec[kind]) {
+    const int64_t l0 = c->launches;
+    int extra = 0;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return PGX_ERR_CUDA;
+    }
+    int st = lb_enqueue_step(s, j, kind, &extra);
+    const cudaError_t e = cudaStreamEndCapture(sl.stream, &g);
+    j.lb_kernels[kind] = extra + (c->launches - l0);
+    c->launches = l0;  // recorded, not launched: each replay counts them
+    if (!st && e != cudaSuccess) st = PGX_ERR_CUDA;
+    if (!st && cudaGraphInstantiate(&j.lb_exec[kind], g, 0) != cudaSuccess) st = PGX_ERR_CUDA;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (st) return st;
+  }
+  if (cudaGraphLaunch(j.lb_exec[kind], sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  s->launches += j.lb_kernels[kind];
+  j.lb_grad_eval = (kind == G_FG || kind == G_HALVE_FG);
+  return PGX_OK;
 }
 
 int lb_copy_best(pgx_server* s, Job& j) {
@@ -426,11 +472,20 @@ int lb_copy_best(pgx_server* s, Job& j) {
   return PGX_OK;
 }
 
+int lb_arm(pgx_server* s, Job& j) {
+  if (cudaEventRecord(s->slots[j.slot].done, s->slots[j.slot].stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  j.inflight = true;
+  return PGX_OK;
+}
+
 // A finished evaluation of an L-BFGS job.  The evaluation at the start of
 // each reference iteration, F and G at u, repeats the one at the end of the
 // previous iteration (same controls, deterministic evaluation) and is not run
-// again.  Returns false when the job stops; *why names the rule.  Further
-// device work is enqueued here.
+// again.  Returns false when the job stops; *why names the rule.  The next
+// step is enqueued here.
 bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, int* err) {
   auto fail = [&](int e, const char* w) {
     *err = e;
@@ -446,7 +501,10 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       j.bestF = rb.F;
       j.round = 0;
       j.lb_it = 1;
-      if ((st = lb_copy_best(s, j)) || (st = lb_start_iteration(s, j))) return fail(st, "launch failed");
+      j.lb_phase = LB_TRIAL;
+      j.lb_bt = 0;
+      if ((st = lb_copy_best(s, j)) || (st = lb_launch(s, j, G_START)) || (st = lb_arm(s, j)))
+        return fail(st, "launch failed");
       return true;
     case LB_TRIAL:
       if (j.lb_bt == 0) {
@@ -459,59 +517,54 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       }
       if (rb.F >= j.F) {  // accepted: F and G there
         j.lb_phase = LB_ACCEPT;
-        if ((st = lb_eval(s, j, true))) return fail(st, "launch failed");
-        return true;
+        st = lb_launch(s, j, G_FG);
+      } else {  // backtrack: halve (20 halvings, then take the last one)
+        j.lb_bt += 1;
+        if (j.lb_bt >= 20) j.lb_phase = LB_ACCEPT;
+        st = lb_launch(s, j, j.lb_bt >= 20 ? G_HALVE_FG : G_HALVE);
       }
-      j.lb_bt += 1;  // backtrack: halve (20 halvings, then take the last one)
-      if (pgx::launch_lb_trial(lb_args(j), true, s->slots[j.slot].stream) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(PGX_ERR_CUDA, "launch failed");
-      }
-      s->launches += 1;
-      if (j.lb_bt >= 20) j.lb_phase = LB_ACCEPT;
-      if ((st = lb_eval(s, j, j.lb_bt >= 20))) return fail(st, "launch failed");
+      if (st || (st = lb_arm(s, j))) return fail(st, "launch failed");
       return true;
     default: {  // LB_ACCEPT: F and G at the accepted point
-      if (pgx::launch_lb_accept(lb_args(j), s->slots[j.slot].stream) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(PGX_ERR_CUDA, "launch failed");
-      }
-      s->launches += 1;
-      std::swap(j.ucur, j.utry);
-      std::swap(j.gcur, j.gtry);
       const double Fprev = j.F;
       j.F = rb.F;
       j.fh.push_back(rb.F);
       j.round = (int)j.fh.size() - 1;
-      if (j.F > j.bestF) {
-        j.bestF = j.F;
-        if ((st = lb_copy_best(s, j))) return fail(st, "launch failed");
-      }
+      const bool improved = j.F > j.bestF;
+      if (improved) j.bestF = j.F;
+      bool stop = true;
       if (j.lb_gnorm < j.opt.gradient_norm_tol) {
         j.converged = true;
         *why = "gradient norm below tolerance";
-        return false;
-      }
-      if (j.F >= 1.0 - 1e-8) {
+      } else if (j.F >= 1.0 - 1e-8) {
         j.converged = true;
         *why = "near-perfect fidelity";
-        return false;
-      }
-      if (std::fabs(j.F - Fprev) < j.opt.convergence_tol) {
+      } else if (std::fabs(j.F - Fprev) < j.opt.convergence_tol) {
         j.converged = true;
         *why = "fidelity change below tolerance";
-        return false;
-      }
-      if (j.F >= s->cfg.target_fidelity) {
+      } else if (j.F >= s->cfg.target_fidelity) {
         j.converged = true;
         *why = "target fidelity reached";
-        return false;
-      }
-      if (++j.lb_it > j.opt.max_iter) {
+      } else if (++j.lb_it > j.opt.max_iter) {
         *why = "maximum iterations reached";
+      } else {
+        stop = false;
+      }
+      if (stop) {  // accept only: u <- ut for the best copy
+        if (pgx::launch_lb_accept(lb_args(j), s->slots[j.slot].stream) != cudaSuccess) {
+          cudaGetLastError();
+          return fail(PGX_ERR_CUDA, "launch failed");
+        }
+        s->launches += 1;
+        if (improved && (st = lb_copy_best(s, j))) return fail(st, "launch failed");
         return false;
       }
-      if ((st = lb_start_iteration(s, j))) return fail(st, "launch failed");
+      j.lb_phase = LB_TRIAL;
+      j.lb_bt = 0;
+      // the graph's accept updates u before its trial point reads it; the
+      // best copy follows the graph (nothing in it writes u after the accept)
+      if ((st = lb_launch(s, j, G_ACC_START)) || (improved && (st = lb_copy_best(s, j))) || (st = lb_arm(s, j)))
+        return fail(st, "launch failed");
       return true;
     }
   }

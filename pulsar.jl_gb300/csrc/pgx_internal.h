@@ -57,6 +57,10 @@ struct WorkDev {
   double* G;        // [n_t][n_c]
   double* F;        // [1]
   float2* u_df;     // mixed: [n_t][n_c] df pairs of u, written once per evaluation
+  // mixed gate chains, parallel in time over pit_blocks blocks of pit_len slices
+  int pit_blocks, pit_len;
+  float4* pit_tot;  // [n_members][pit_blocks][Dp*Dp] df block products
+  float2* pit_pre;  // [n_members][pit_blocks][Dp*Dp] prefix at each block start
 };
 
 // Tunable kernels: their team size (threads per matrix problem) is chosen per

@@ -216,6 +216,133 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
 }
 
 // ---- forward chain in df -------------------------------------------------------
+// U_total = P_n in FP64 from the df chain, the overlap z = Tr(T'U)/D in FP64,
+// f(z) and the weighted chain-rule coefficient of member m.
+template <int D, int T>
+__device__ __forceinline__ void chain_epilogue_mx(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m,
+                                                  const float4* Pc, double2* red) {
+  double2* Ut = w.Utot + (size_t)m * D * D;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int e = tm.lane; e < D * D; e += T) {
+    const double2 v = dfc_to(dfc_load(Pc[e]));
+    Ut[e] = v;
+    acc = cmac_cj(acc, p.target_op[e], v);
+  }
+  double2 z = team_sum<T>(tm, acc, red);
+  if (tm.lane == 0) {
+    z.x /= p.D;
+    z.y /= p.D;
+    double f;
+    double2 kap;
+    fid_kappa(z, p.fid, p.grad_mode, f, kap);
+    const double sc = p.m_weight[m] / p.D;
+    w.z[m] = z;
+    w.kap[m] = make_double2(kap.x * sc, kap.y * sc);
+    w.Fm[m] = f;
+  }
+}
+
+// Parallel in time (members with few teams each would leave SMs idle): the
+// slices of member m fall into pit_blocks blocks of pit_len.
+//   local   per (m, b): local prefixes Q_i = U_{k0+i-1} ... U_{k0} in df,
+//           stored as FP32 in the P slots k0 + i, the block product in df;
+//   combine per m: T_0 = I, T_{b+1} = Q_b T_b in df (T_b saved as FP32),
+//           P_n = T_B gives U_total and z exactly as the sequential chain;
+//   fix     per (m, k), k >= pit_len: P_k <- Q_i T_b in FP32 (the gradient
+//           consumes P in FP32).
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_local_mx(ProbDev p, WorkDev w, int store) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  constexpr int NE = (D * D + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* smem = reinterpret_cast<float4*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  float4* Pc = smem + (size_t)team * (2 * D * D);
+  float4* Ub = Pc + D * D;
+  const long items = (long)p.n_members * w.pit_blocks;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / w.pit_blocks), b = (int)(it % w.pit_blocks);
+    const int k0 = b * w.pit_len, k1 = min(p.n_t, k0 + w.pit_len);
+    const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+    float2* Pst = reinterpret_cast<float2*>(w.P) + (size_t)m * p.n_t * D * D;
+    for (int e = tm.lane; e < D * D; e += T) {
+      Pc[e] = make_float4((e % D) == (e / D) ? 1.f : 0.f, 0.f, 0.f, 0.f);
+      if (store && k0 < k1) Pst[(size_t)k0 * D * D + e] = make_float2(Pc[e].x, Pc[e].y);
+    }
+    float4 pre[NE];
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      const int e = tm.lane + i * T;
+      if (e < D * D && k0 < k1) pre[i] = Um[(size_t)k0 * D * D + e];
+    }
+    tm.sync();
+    for (int k = k0; k < k1; ++k) {
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        const int e = tm.lane + i * T;
+        if (e < D * D) Ub[e] = pre[i];
+      }
+      if (k + 1 < k1) {
+        const float4* nx = Um + (size_t)(k + 1) * D * D;
+#pragma unroll
+        for (int i = 0; i < NE; ++i) {
+          const int e = tm.lane + i * T;
+          if (e < D * D) pre[i] = nx[e];
+        }
+      }
+      tm.sync();
+      mm1_df<D, T>(tm, Pc, Ub, Pc);
+      if (store && k + 1 < k1)
+        for (int e = tm.lane; e < D * D; e += T) Pst[(size_t)(k + 1) * D * D + e] = make_float2(Pc[e].x, Pc[e].y);
+    }
+    float4* tot = w.pit_tot + ((size_t)m * w.pit_blocks + b) * D * D;
+    for (int e = tm.lane; e < D * D; e += T) tot[e] = Pc[e];
+    tm.sync();
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_combine_mx(ProbDev p, WorkDev w, int store) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* smem = reinterpret_cast<float4*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  float4* Pc = smem + (size_t)team * (D * D + T);
+  double2* red = reinterpret_cast<double2*>(Pc + D * D);
+  for (int e = tm.lane; e < D * D; e += T) Pc[e] = make_float4((e % D) == (e / D) ? 1.f : 0.f, 0.f, 0.f, 0.f);
+  tm.sync();
+  for (int b = 0; b < w.pit_blocks; ++b) {
+    if (store) {
+      float2* pre = w.pit_pre + ((size_t)m * w.pit_blocks + b) * D * D;
+      for (int e = tm.lane; e < D * D; e += T) pre[e] = make_float2(Pc[e].x, Pc[e].y);
+    }
+    mm1_df<D, T>(tm, Pc, w.pit_tot + ((size_t)m * w.pit_blocks + b) * D * D, Pc);
+  }
+  chain_epilogue_mx<D, T>(tm, p, w, m, Pc, red);
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_fix_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int L = w.pit_len, nk = p.n_t - L;
+  const long items = (long)p.n_members * (nk > 0 ? nk : 0);
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / nk), k = L + (int)(it % nk), b = k / L;
+    float2* Pk = reinterpret_cast<float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
+    const float2* Tb = w.pit_pre + ((size_t)m * w.pit_blocks + b) * D * D;
+    mm1<D, T>(tm, Pk, Pk, Tb);
+  }
+}
+
 template <int D>
 __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_fwd_mx(ProbDev p, WorkDev w, int store) {
   using G = Cfg<D>;
@@ -260,25 +387,7 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_fwd_mx(ProbDev p
     tm.sync();
     mm1_df<D, T>(tm, Pc, Ub, Pc);
   }
-  double2* Ut = w.Utot + (size_t)m * D * D;
-  double2 acc = make_double2(0.0, 0.0);
-  for (int e = tm.lane; e < D * D; e += T) {
-    const double2 v = dfc_to(dfc_load(Pc[e]));
-    Ut[e] = v;
-    acc = cmac_cj(acc, p.target_op[e], v);
-  }
-  double2 z = team_sum<T>(tm, acc, red);
-  if (tm.lane == 0) {
-    z.x /= p.D;
-    z.y /= p.D;
-    double f;
-    double2 kap;
-    fid_kappa(z, p.fid, p.grad_mode, f, kap);
-    const double sc = p.m_weight[m] / p.D;
-    w.z[m] = z;
-    w.kap[m] = make_double2(kap.x * sc, kap.y * sc);
-    w.Fm[m] = f;
-  }
+  chain_epilogue_mx<D, T>(tm, p, w, m, Pc, red);
 }
 
 // ---- backward chain in FP32 -------------------------------------------------------
@@ -484,10 +593,28 @@ cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
 template <int D>
 static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
   using G = Cfg<D>;
-  const size_t smem = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
-  ensure_smem_mx(k_chain_gate_fwd_mx<D>, smem);
-  k_chain_gate_fwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w, store);
-  ++*li.launches;
+  if (w.pit_blocks <= 1) {
+    const size_t smem = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
+    ensure_smem_mx(k_chain_gate_fwd_mx<D>, smem);
+    k_chain_gate_fwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w, store);
+    ++*li.launches;
+    return cudaGetLastError();
+  }
+  const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float4);
+  ensure_smem_mx(k_chainf_local_mx<D>, smem_l);
+  const int grid_l = grid_for(k_chainf_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,
+                              li.num_sms, 0);
+  k_chainf_local_mx<D><<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
+  const size_t smem_c = (size_t)G::TPC * (D * D + G::T) * sizeof(float4);
+  ensure_smem_mx(k_chainf_combine_mx<D>, smem_c);
+  k_chainf_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
+  *li.launches += 2;
+  if (store && p.n_t > w.pit_len) {
+    const int grid_f = grid_for(k_chainf_fix_mx<D>, G::THREADS, 0, (long)p.n_members * (p.n_t - w.pit_len), G::TPC,
+                                li.num_sms, 0);
+    k_chainf_fix_mx<D><<<grid_f, G::THREADS, 0, li.stream>>>(p, w);
+    ++*li.launches;
+  }
   return cudaGetLastError();
 }
 cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {

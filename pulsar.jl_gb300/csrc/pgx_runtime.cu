@@ -305,6 +305,22 @@ static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
   return s;
 }
 
+// Blocks of the parallel-in-time mixed gate chain: enough (member, block)
+// teams to fill the GPU (about 4 teams of 256 threads per SM, 16 warp-teams at
+// Dp <= 8), blocks of at least 8 slices; 1 = the sequential chain.
+static void pit_shape(const pgx_problem_desc* d, int Dp, int num_sms, int* blocks, int* len) {
+  *blocks = 1;
+  *len = d->n_slices;
+  if (d->precision != PGX_PREC_MIXED || d->target != PGX_TARGET_GATE) return;
+  const long target = (long)(Dp <= 8 ? 16 : 4) * num_sms;
+  long b = (target + d->n_members - 1) / d->n_members;
+  b = std::min<long>(b, std::max(1, d->n_slices / 8));
+  if (b <= 1) return;
+  const int L = (int)((d->n_slices + b - 1) / b);
+  *len = L;
+  *blocks = (d->n_slices + L - 1) / L;
+}
+
 static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
   const int Dp = pad_dim(d->dim);
   const Sizes s = sizes_of(d, Dp, num_sms);
@@ -313,11 +329,14 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
                         2 * (size_t)std::max(d->n_pairs, 0) * Dp * sizeof(double2) * 2 +
                         (size_t)d->n_members * (sizeof(int) + 3 * sizeof(double)) +
                         (size_t)d->n_slices * sizeof(double);
+  int pit_b, pit_l;
+  pit_shape(d, Dp, num_sms, &pit_b, &pit_l);
+  const size_t pit = pit_b > 1 ? (size_t)d->n_members * pit_b * Dp * Dp * (sizeof(float4) + sizeof(float2)) : 0;
   // mixed: df copies of the generator constants and scalars, df controls
-  const size_t mixed = d->precision == PGX_PREC_MIXED
+  const size_t mixed = pit + (d->precision == PGX_PREC_MIXED
                            ? DD * (d->n_drifts + d->n_controls + 1) +
                                  sizeof(float2) * ((size_t)d->n_slices + 2 * (size_t)d->n_members) + s.u
-                           : 0;
+                           : 0);
   return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
          2 * sizeof(double) + consts + mixed;
 }
@@ -513,6 +532,12 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   p->d_G = (double*)A(s.G);
   p->d_F = (double*)A(2 * sizeof(double));
   if (d->precision == PGX_PREC_MIXED) w.u_df = (float2*)A(s.u);
+  pit_shape(d, Dp, c->num_sms, &w.pit_blocks, &w.pit_len);
+  if (w.pit_blocks > 1) {
+    const size_t blk = (size_t)d->n_members * w.pit_blocks * Dp * Dp;
+    w.pit_tot = (float4*)A(blk * sizeof(float4));
+    w.pit_pre = (float2*)A(blk * sizeof(float2));
+  }
   if (st) {
     pgx_problem_destroy(p);
     return st;

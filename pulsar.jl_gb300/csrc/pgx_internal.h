@@ -61,6 +61,8 @@ struct WorkDev {
   int pit_blocks, pit_len;
   float4* pit_tot;  // [n_members][pit_blocks][Dp*Dp] df block products
   float2* pit_pre;  // [n_members][pit_blocks][Dp*Dp] prefix at each block start
+  float2* pit_r;    // [n_members][n_t][Dp*Dp] backward: in-block suffixes U_{k1-1}...U_k
+  float2* pit_lam;  // [n_members][pit_blocks][Dp*Dp] costate at each block end
 };
 
 // Tunable kernels: their team size (threads per matrix problem) is chosen per

@@ -437,6 +437,102 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_gate_bwd_mx(ProbDev p
   }
 }
 
+// Backward chain in parallel in time (FP32), blocks as the forward chain's:
+//   local   per (m, b): in-block suffixes R_k = U_{k1-1} ... U_k;
+//   combine per m: Lambda_n = kappa T', Lambda_{k0} = Lambda_{k1} R_{k0} block
+//           by block from the end (Lambda_{k1} of each block saved);
+//   fix     per (m, k): Lambda_{k+1} = Lambda_{k1} R_{k+1} (or Lambda_{k1} at
+//           the block end), M_k = P_k Lambda_{k+1}; the first-order GRAPE
+//           formula takes Lambda_k = Lambda_{k1} R_k instead.
+template <int D, int T>
+__device__ __forceinline__ void load_hi(const Team<T>& tm, float2* dst, const float4* src) {
+  for (int e = tm.lane; e < D * D; e += T) {
+    const float4 u = src[e];
+    dst[e] = make_float2(u.x, u.y);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_local_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* smem = reinterpret_cast<float2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  float2* R = smem + (size_t)team * 2 * D * D;
+  float2* Ub = R + D * D;
+  const long items = (long)p.n_members * w.pit_blocks;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / w.pit_blocks), b = (int)(it % w.pit_blocks);
+    const int k0 = b * w.pit_len, k1 = min(p.n_t, k0 + w.pit_len);
+    const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+    float2* Rm = w.pit_r + (size_t)m * p.n_t * D * D;
+    for (int e = tm.lane; e < D * D; e += T) R[e] = make_float2((e % D) == (e / D) ? 1.f : 0.f, 0.f);
+    for (int k = k1 - 1; k >= k0; --k) {
+      load_hi<D, T>(tm, Ub, Um + (size_t)k * D * D);
+      tm.sync();
+      mm1<D, T>(tm, R, R, Ub);
+      for (int e = tm.lane; e < D * D; e += T) Rm[(size_t)k * D * D + e] = R[e];
+    }
+    tm.sync();
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_combine_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* smem = reinterpret_cast<float2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  float2* Lam = smem + (size_t)team * D * D;
+  const double2 kap = w.kap[m];
+  for (int e = tm.lane; e < D * D; e += T) {
+    const int r = e % D, c = e / D;
+    const double2 t = p.target_op[c + D * r];
+    const double2 v = cmul(kap, make_double2(t.x, -t.y));
+    Lam[e] = make_float2((float)v.x, (float)v.y);
+  }
+  tm.sync();
+  const float2* Rm = w.pit_r + (size_t)m * p.n_t * D * D;
+  for (int b = w.pit_blocks - 1; b >= 0; --b) {
+    float2* lam_b = w.pit_lam + ((size_t)m * w.pit_blocks + b) * D * D;
+    for (int e = tm.lane; e < D * D; e += T) lam_b[e] = Lam[e];
+    mm1<D, T>(tm, Lam, Lam, Rm + (size_t)(b * w.pit_len) * D * D);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_fix_mx(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* smem = reinterpret_cast<float2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  float2* Lam = smem + (size_t)team * D * D;
+  const bool grape = (p.grad_mode == GRAD_REF_GRAPE);
+  const long items = (long)p.n_members * p.n_t;
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t), b = k / w.pit_len;
+    const int k1 = min(p.n_t, (b + 1) * w.pit_len);
+    const int kk = grape ? k : k + 1;  // costate index the formula uses
+    const float2* lam_b = w.pit_lam + ((size_t)m * w.pit_blocks + b) * D * D;
+    if (kk == k1) {
+      for (int e = tm.lane; e < D * D; e += T) Lam[e] = lam_b[e];
+      tm.sync();
+    } else {
+      mm1<D, T>(tm, Lam, lam_b, w.pit_r + ((size_t)m * p.n_t + kk) * D * D);
+    }
+    float2* Pk = reinterpret_cast<float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
+    mm1<D, T>(tm, Pk, Pk, Lam);
+  }
+}
+
 // ---- gradient in FP32 -----------------------------------------------------------
 // g_j = Re(c dt scale Tr(X C_j)).  The team's first warp sums in a fixed order
 // (stride-32 partial sums, then a fixed shuffle tree) so that the result does
@@ -625,10 +721,26 @@ cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Launch
 template <int D>
 static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = Cfg<D>;
-  const size_t smem = (size_t)G::TPC * 2 * D * D * sizeof(float2);
-  ensure_smem_mx(k_chain_gate_bwd_mx<D>, smem);
-  k_chain_gate_bwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w);
-  ++*li.launches;
+  if (w.pit_blocks <= 1) {
+    const size_t smem = (size_t)G::TPC * 2 * D * D * sizeof(float2);
+    ensure_smem_mx(k_chain_gate_bwd_mx<D>, smem);
+    k_chain_gate_bwd_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem, li.stream>>>(p, w);
+    ++*li.launches;
+    return cudaGetLastError();
+  }
+  const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float2);
+  ensure_smem_mx(k_chainb_local_mx<D>, smem_l);
+  const int grid_l = grid_for(k_chainb_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,
+                              li.num_sms, 0);
+  k_chainb_local_mx<D><<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w);
+  const size_t smem_c = (size_t)G::TPC * D * D * sizeof(float2);
+  ensure_smem_mx(k_chainb_combine_mx<D>, smem_c);
+  k_chainb_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w);
+  ensure_smem_mx(k_chainb_fix_mx<D>, smem_c);
+  const int grid_f = grid_for(k_chainb_fix_mx<D>, G::THREADS, smem_c, (long)p.n_members * p.n_t, G::TPC,
+                              li.num_sms, 0);
+  k_chainb_fix_mx<D><<<grid_f, G::THREADS, smem_c, li.stream>>>(p, w);
+  *li.launches += 3;
   return cudaGetLastError();
 }
 cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {

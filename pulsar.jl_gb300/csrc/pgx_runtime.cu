@@ -331,7 +331,9 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
                         (size_t)d->n_slices * sizeof(double);
   int pit_b, pit_l;
   pit_shape(d, Dp, num_sms, &pit_b, &pit_l);
-  const size_t pit = pit_b > 1 ? (size_t)d->n_members * pit_b * Dp * Dp * (sizeof(float4) + sizeof(float2)) : 0;
+  const size_t pit = pit_b > 1 ? (size_t)d->n_members * Dp * Dp *
+                                     (pit_b * (sizeof(float4) + 2 * sizeof(float2)) + (size_t)d->n_slices * sizeof(float2))
+                               : 0;
   // mixed: df copies of the generator constants and scalars, df controls
   const size_t mixed = pit + (d->precision == PGX_PREC_MIXED
                            ? DD * (d->n_drifts + d->n_controls + 1) +
@@ -537,6 +539,8 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
     const size_t blk = (size_t)d->n_members * w.pit_blocks * Dp * Dp;
     w.pit_tot = (float4*)A(blk * sizeof(float4));
     w.pit_pre = (float2*)A(blk * sizeof(float2));
+    w.pit_lam = (float2*)A(blk * sizeof(float2));
+    w.pit_r = (float2*)A((size_t)d->n_members * d->n_slices * Dp * Dp * sizeof(float2));
   }
   if (st) {
     pgx_problem_destroy(p);

@@ -395,12 +395,12 @@ def cpu_baseline_multi(cases, budget_s: float):
 def make_workload(args, pg, ctx, torch, dev):
     from pulsar_gb300 import workloads as W
     if args.workload == "spin4":
-        prob, u0 = W.spin4_ensemble(n_t=args.slices)
+        prob, u0 = W.spin4_ensemble(n_t=args.slices or 1000)
         return Single(f"spin4_d16_231members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
                       args.precision, torch, dev, teams=args.teams)
     if args.workload == "lindblad3q":
-        prob, u0 = W.lindblad_3q()
-        return Single("lindblad3q_D64_32members_500slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
+        prob, u0 = W.lindblad_3q(n_t=args.slices or 500)
+        return Single(f"lindblad3q_D64_32members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
                       torch, dev, teams=args.teams)
     if args.workload == "uneven512":
         return Uneven("uneven512", W.uneven_batch(512), pg, ctx, args.grad_mode, args.precision)
@@ -419,7 +419,7 @@ def run_reference(args, rank: int):
     from pulsar_gb300 import workloads as W
     from oracle import members as mb
     if args.workload == "spin4":
-        prob, u0 = W.spin4_ensemble(n_t=args.slices)
+        prob, u0 = W.spin4_ensemble(n_t=args.slices or 1000)
         cases = [(prob, u0)]
         name = f"spin4_d16_231members_{prob.n_t}slices"
     elif args.workload == "uneven512":
@@ -476,8 +476,9 @@ def main():
                     help="skip timing the plain FP64 GPU form beside the mixed one")
     ap.add_argument("--teams", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
                     help="fixed mixed-kernel team sizes EXPM,GRAD instead of autotuning (e.g. for profiling)")
-    ap.add_argument("--slices", type=int, default=1000,
-                    help="spin4 slices per member (1000 = the benchmark workload; smaller for profiling)")
+    ap.add_argument("--slices", type=int, default=None,
+                    help="slices per member (spin4: 1000, lindblad3q: 500 = the benchmark workloads; "
+                         "smaller for profiling)")
     sv = ap.add_argument_group("serve workload (Poisson job stream through pgx_server)")
     sv.add_argument("--serve-rate", type=float, default=200.0, help="offered jobs/s")
     sv.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window")

@@ -331,4 +331,52 @@ __device__ void taylor_exp_frechet(const Team<T>& tm, const Work<C, D, S>& w, in
   }
 }
 
+// Six-matrix workspace of the q = 2 Frechet evaluation (fits shared memory at
+// D = 64, where the ten matrices of the q = 4 form do not).
+template <class C, int D, int S = D * D> struct Work2 {
+  C* B; C* X; C* Y; C* dB; C* dX; C* dY;
+  __device__ __forceinline__ static Work2 at(C* base) {
+    Work2 w;
+    w.B = base; w.X = base + S; w.Y = base + 2 * S;
+    w.dB = base + 3 * S; w.dX = base + 4 * S; w.dY = base + 5 * S;
+    return w;
+  }
+};
+
+// As taylor_exp_frechet with Paterson-Stockmeyer q = 2: X = B^2, then Horner
+// in X over pairs of coefficients,
+//   Y_{L-1} = c_{2L} X + c_{2L-1} B + c_{2L-2} I,  Y_i = X Y_{i+1} + c_{2i+1} B + c_{2i} I,
+//   dY_{L-1} = c_{2L} dX + c_{2L-1} dB,          dY_i = dX Y_{i+1} + X dY_{i+1} + c_{2i+1} dB,
+// m = 2L; then the s squarings.  1.5 m product units against 3 (m/4 + 2) for
+// q = 4, in six matrices instead of ten.
+template <int D, int T, int SW = 0, class C, int S, class R>
+__device__ void taylor_exp_frechet2(const Team<T>& tm, const Work2<C, D, S>& w, int m, int s, const R* invf) {
+  mm1<D, T, SW>(tm, w.X, w.B, w.B);
+  mm<D, T, true, SW>(tm, w.dX, w.B, w.dB, w.dB, w.B, EpiNone{});
+  const int L = m / 2;
+  for (int q = tm.lane; q < D * D; q += T) {
+    const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
+    C y = cadd(cscale(w.X[e], invf[2 * L]), cscale(w.B[e], invf[2 * L - 1]));
+    if (r == c) y.x += invf[2 * L - 2];
+    w.Y[e] = y;
+    w.dY[e] = cadd(cscale(w.dX[e], invf[2 * L]), cscale(w.dB[e], invf[2 * L - 1]));
+  }
+  tm.sync();
+  for (int i = L - 2; i >= 0; --i) {
+    const C* B = w.B;
+    const C* dB = w.dB;
+    mm<D, T, true, SW>(tm, w.dY, w.dX, w.Y, w.X, w.dY,
+                       [=](int e, int, int, C v) { return cadd(v, cscale(dB[e], invf[2 * i + 1])); });
+    mm<D, T, false, SW>(tm, w.Y, w.X, w.Y, (const C*)nullptr, (const C*)nullptr, [=](int e, int r, int c, C v) {
+      C t = cadd(v, cscale(B[e], invf[2 * i + 1]));
+      if (r == c) t.x += invf[2 * i];
+      return t;
+    });
+  }
+  for (int k = 0; k < s; ++k) {
+    mm<D, T, true, SW>(tm, w.dY, w.Y, w.dY, w.dY, w.Y, EpiNone{});
+    mm1<D, T, SW>(tm, w.Y, w.Y, w.Y);
+  }
+}
+
 }  // namespace pgx

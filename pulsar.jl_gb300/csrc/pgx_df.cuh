@@ -116,8 +116,11 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
   const int rb = tm.lane % BK::NR, cb = tm.lane / BK::NR;
   DfAcc acc[RB][CB];
   float4 res[RB][CB];
+  // at D = 64 a lane owns 16 accumulators: an unrolled k-loop overflows the
+  // instruction cache (ncu: "no instruction" stalls)
+  constexpr int UNR = (D >= 64) ? 1 : 2;
   if (active) {
-#pragma unroll 2
+#pragma unroll UNR
     for (int k = 0; k < D; ++k) {
       float4 a[RB], b[CB];
 #pragma unroll
@@ -130,7 +133,7 @@ __device__ __forceinline__ void mm_df(const Team<T>& tm, float4* out, const floa
         for (int j = 0; j < CB; ++j) acc[i][j].mac(a[i], b[j]);
     }
     if constexpr (TWO) {
-#pragma unroll 2
+#pragma unroll UNR
       for (int k = 0; k < D; ++k) {
         float4 a[RB], b[CB];
 #pragma unroll

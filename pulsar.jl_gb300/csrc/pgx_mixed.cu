@@ -15,6 +15,8 @@
 //              table) and traces; results accumulated as FP64.
 // F therefore carries df (~1e-13 per product) rounding; G carries FP32
 // (~1e-6 relative) rounding.
+#include <type_traits>
+
 #include "pgx_df.cuh"
 #include "pgx_stages.cuh"
 
@@ -51,9 +53,11 @@ template <int D, int T> struct CfgM {
   // expm kernel: five df matrices in the padded layout
   static constexpr size_t WSE = (size_t)5 * Lay<D, 2>::SIZE * sizeof(float4);
   static constexpr size_t SMEM_E = (SLAB ? 0 : TPC * WSE) + TPC * RED;
-  // gradient kernel: ten complex-float matrices in the padded layout
-  static constexpr size_t WSG = (size_t)10 * Lay<D, 2>::SIZE * sizeof(float2);
-  static constexpr size_t SMEM_G = (SLAB ? 0 : TPC * WSG) + TPC * RED;
+  // gradient kernel: ten complex-float matrices in the padded layout; at
+  // D = 64 the six of the q = 2 form, which fit shared memory
+  static constexpr bool GRAD_Q2 = (D >= 64);
+  static constexpr size_t WSG = (size_t)(GRAD_Q2 ? 6 : 10) * Lay<D, 2>::SIZE * sizeof(float2);
+  static constexpr size_t SMEM_G = TPC * WSG + TPC * RED;
 };
 
 template <int D, int T>
@@ -567,13 +571,10 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int team = threadIdx.x / T;
   const Team<T> tm = team_of<D, T>();
-  float2* base;
-  if constexpr (G::SLAB)
-    base = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * 10 * L::SIZE;
-  else
-    base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WSG);
-  float2* red = reinterpret_cast<float2*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WSG) + (size_t)team * G::RED);
-  const Work<float2, D, L::SIZE> W = Work<float2, D, L::SIZE>::at(base);
+  float2* base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WSG);
+  float2* red = reinterpret_cast<float2*>(smem_raw + G::TPC * G::WSG + (size_t)team * G::RED);
+  using Wk = std::conditional_t<G::GRAD_Q2, Work2<float2, D, L::SIZE>, Work<float2, D, L::SIZE>>;
+  const Wk W = Wk::at(base);
   const bool exact = (p.grad_mode == GRAD_EXACT);
   const long items = (long)p.n_members * p.n_t;
   for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
@@ -597,7 +598,10 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
       W.dB[e] = cscale(W.dB[e], sc);
     }
     tm.sync();
-    taylor_exp_frechet<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
+    if constexpr (G::GRAD_Q2)
+      taylor_exp_frechet2<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
+    else
+      taylor_exp_frechet<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
     trace_controls32<D, T, kSwzGrad>(tm, p, W.dY, m, k, Gout, red);
     tm.sync();
   }
@@ -754,7 +758,7 @@ static cudaError_t do_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchIn
   const size_t smem = G::SMEM_G;
   ensure_smem_mx(k_grad_gate_mx<D, T>, smem);
   const int grid = grid_for(k_grad_gate_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
-                            li.num_sms, G::SLAB ? w.slab_teams : 0);
+                            li.num_sms, 0);
   k_grad_gate_mx<D, T><<<grid, G::THREADS, smem, li.stream>>>(p, w);
   ++*li.launches;
   return cudaGetLastError();

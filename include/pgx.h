@@ -198,6 +198,28 @@ int pgx_overlap(pgx_ctx* ctx, int64_t n, const double* A, const double* B, doubl
 int pgx_trace_products(pgx_ctx* ctx, int32_t dim, int32_t n, int32_t m, const double* X, const double* E,
                        const double* Y, double* out);
 
+/* ---- penalties ---------------------------------------------------------- */
+/* Waveform penalties of Penalties.jl:197-330 (the PENALTY_TYPES of :205):
+ *   NS     sum w^2                       SNS   sum max(0, w-u_b)^2 + max(0, l_b-w)^2
+ *   SNSA   sum_k max(0, ||w[:,k]|| - u_b)^2                 DNS   sum (w[:,k+1] - w[:,k])^2
+ *   ENERGY sum w^2 dt_k                                     (w = the control amplitudes u). */
+enum { PGX_PEN_NS = 0, PGX_PEN_SNS = 1, PGX_PEN_SNSA = 2, PGX_PEN_DNS = 3, PGX_PEN_ENERGY = 4 };
+#define PGX_MAX_PENALTIES 8
+typedef struct pgx_penalty {
+  int32_t type;                /* PGX_PEN_*                                        */
+  int32_t reserved;
+  double weight;
+  double l_bound, u_bound;     /* SNS / SNSA bounds (reference defaults -1, 1)     */
+} pgx_penalty;
+/* Every later evaluation of the problem returns F - sum weight P and
+ * G - sum weight dP/du, as _apply_penalties! (GRAPEState.jl:571-584); n = 0
+ * removes them.  n <= PGX_MAX_PENALTIES. */
+int pgx_problem_set_penalties(pgx_problem* prob, int32_t n, const pgx_penalty* penalties);
+/* Standalone penalty_value_and_gradient (Penalties.jl:260-271): P = weight
+ * P(u), G = weight dP/du ([n_c x n_t], nullable); dt nullable (uniform 1). */
+int pgx_penalty_eval(pgx_ctx* ctx, int32_t n_controls, int32_t n_slices, const double* u, const double* dt,
+                     const pgx_penalty* penalty, double* P, double* G);
+
 /* ---- autotuning --------------------------------------------------------- */
 /* Times every team-size variant (threads per matrix problem, with the
  * matching register blocking) of the problem's slice-parallel mixed-precision

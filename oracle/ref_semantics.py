@@ -330,6 +330,42 @@ def compute_grape_gradient_with(system, target, P, Q, U_total, dt) -> np.ndarray
                           target.target_state, dt)
 
 
+def penalty_value_and_gradient(w, type, weight=1.0, l_bound=-1.0, u_bound=1.0, dt=None):
+    """(weight P, weight dP/dw) of Penalties.jl:273-330 for w [n_ctrl, n_t]."""
+    w = np.asarray(w, float)
+    n_c, n_t = w.shape
+    G = np.zeros_like(w)
+    F = 0.0
+    if type == "NS":
+        F = float(np.sum(w ** 2))
+        G = 2 * w
+    elif type == "SNS":
+        e = np.where(w > u_bound, w - u_bound, np.where(w < l_bound, w - l_bound, 0.0))
+        F = float(np.sum(e ** 2))
+        G = 2 * e
+    elif type == "SNSA":
+        for n in range(n_t):
+            A = np.sqrt(np.sum(w[:, n] ** 2))
+            sp = max(0.0, A - u_bound)
+            F += sp ** 2
+            if sp > 0.0 and A > 1e-14:
+                G[:, n] += 2.0 * sp / A * w[:, n]
+    elif type == "DNS":
+        for k in range(n_c):
+            for n in range(n_t - 1):
+                d = w[k, n + 1] - w[k, n]
+                F += d ** 2
+                G[k, n] -= 2 * d
+                G[k, n + 1] += 2 * d
+    elif type == "energy":
+        t = np.ones(n_t) if dt is None else np.broadcast_to(np.asarray(dt, float), (n_t,))
+        F = float(np.sum(w ** 2 * t[None, :]))
+        G = 2 * w * t[None, :]
+    else:
+        raise ValueError(type)
+    return weight * F, weight * G
+
+
 def gradient_cuda_formula(H_drift, H_ctrl, controls, target, dt) -> np.ndarray:
     """The reference's CUDA-backend gradient as written (its CPU form,
     src/Backend/Hardware/CUDABackend.jl:283-305): P[0] = I, P[k+1] = U_k P[k];

@@ -20,6 +20,7 @@ from .api import (
     compute_total_propagator, cuda_backend, ensemble_value, ensemble_value_and_grad,
     fidelity_cuda, fidelity_grad_prefactor, finite_difference_gradient, gate_fidelity, gradient_cuda,
     grape_gradient_check, lindblad_grad_prefactor, matrix_exponential_cuda, state_fidelity,
+    penalty_gradient, penalty_value, penalty_value_and_gradient,
 )
 
 LIB_PATH = _abi.LIB_PATH

@@ -528,6 +528,41 @@ def grape_gradient_check(system: QuantumSystem, target: QuantumTarget, controls:
             "max_relative_error": max_err / scale, "passed": max_err < 1e-4}
 
 
+def penalty_value_and_gradient(w, type: str, weight: float = 1.0, l_bound: float = -1.0, u_bound: float = 1.0,
+                               dt=None, ctx: Optional[Context] = None):
+    """(weight P(w), weight dP/dw) for the waveform w [n_ctrl, n_t]
+    (Penalties.jl:260-271), on the device."""
+    w = np.asarray(w, np.float64)
+    if w.ndim != 2:
+        raise ValueError("w must be [n_ctrl x n_t]")
+    if type not in _A.PENALTY:
+        raise ValueError(f"Unknown penalty ':{type}'. Valid: {', '.join(_A.PENALTY)}")
+    if weight == 0.0:
+        return 0.0, np.zeros_like(w)
+    n_c, n_t = w.shape
+    pen = _A.Penalty(_A.PENALTY[type], 0, float(weight), float(l_bound), float(u_bound))
+    ub = np.ascontiguousarray(w.T).ravel()
+    G = np.zeros(n_c * n_t)
+    P = np.zeros(1)
+    dtb = None if dt is None else np.ascontiguousarray(np.broadcast_to(np.asarray(dt, float), (n_t,)))
+    _A.check(_A.lib().pgx_penalty_eval(_ctx_handle(ctx), n_c, n_t, _A.as_dptr(ub),
+                                       _A.as_dptr(dtb) if dtb is not None else None, _A.C.byref(pen),
+                                       _A.as_dptr(P), _A.as_dptr(G)), _ctx_handle(ctx))
+    return float(P[0]), G.reshape(n_t, n_c).T.copy()
+
+
+def penalty_value(w, type: str, weight: float = 1.0, l_bound: float = -1.0, u_bound: float = 1.0,
+                  dt=None) -> float:
+    """weight P(w) (Penalties.jl:226-241)."""
+    return penalty_value_and_gradient(w, type, weight, l_bound, u_bound, dt)[0]
+
+
+def penalty_gradient(w, type: str, weight: float = 1.0, l_bound: float = -1.0, u_bound: float = 1.0,
+                     dt=None) -> np.ndarray:
+    """weight dP/dw (Penalties.jl:243-258)."""
+    return penalty_value_and_gradient(w, type, weight, l_bound, u_bound, dt)[1]
+
+
 # ---- the reference's CUDA backend entry points (CUDABackend.jl) -------------
 
 @dataclass(frozen=True)
@@ -786,6 +821,8 @@ class MRControl:
     backend: str = "cuda"
     grad_mode: str = "ref_mr"
     precision: str = "fp64"
+    penalties: list = field(default_factory=list)   # symbols, OptControl.jl (:none skipped)
+    p_weights: list = field(default_factory=list)
 
     def __post_init__(self):
         self.rho_init = _wrap_states(self.rho_init)
@@ -805,7 +842,17 @@ class MRControl:
                                  fidelity=self.fidelity, states_init=np.stack(self.rho_init),
                                  states_target=np.stack(self.rho_targ), grad_mode=self.grad_mode,
                                  precision=self.precision)
+            _set_ctrl_penalties(self, self._prob)
         return self._prob
+
+
+def _set_ctrl_penalties(ctrl, prob: Problem):
+    """_apply_penalties! (GRAPEState.jl:571-584): every (pen, weight) with pen
+    != :none and weight != 0, bounds l_bound / u_bound of the control."""
+    pens = [(str(p), float(wt), ctrl.l_bound, ctrl.u_bound) for p, wt in zip(ctrl.penalties, ctrl.p_weights)
+            if str(p) != "none" and float(wt) != 0.0]
+    if pens:
+        prob.set_penalties(pens)
 
 
 @dataclass
@@ -829,6 +876,8 @@ class LindbladMRControl:
     backend: str = "cuda"
     precision: str = "fp64"
     grad_mode: str = "ref_mr"
+    penalties: list = field(default_factory=list)
+    p_weights: list = field(default_factory=list)
 
     def __post_init__(self):
         if len(self.jump_ops) != len(self.decay_rates):
@@ -870,6 +919,7 @@ class LindbladMRControl:
                                  states_init=np.stack(self._sigma_init),
                                  states_target=np.stack(self._sigma_targ), grad_mode=self.grad_mode,
                                  precision=self.precision)
+            _set_ctrl_penalties(self, self._prob)
         return self._prob
 
 

@@ -534,6 +534,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   p->d_G = (double*)A(s.G);
   p->d_F = (double*)A(2 * sizeof(double));
   if (d->precision == PGX_PREC_MIXED) w.u_df = (float2*)A(s.u);
+  p->d_pen = (pgx_penalty*)A(sizeof(pgx_penalty) * PGX_MAX_PENALTIES);
   pit_shape(d, Dp, c->num_sms, &w.pit_blocks, &w.pit_len);
   if (w.pit_blocks > 1) {
     const size_t blk = (size_t)d->n_members * w.pit_blocks * Dp * Dp;
@@ -605,6 +606,14 @@ struct Marks {
   }
 };
 
+// F -= sum weight P(u), G -= sum weight dP/du after the member reduction.
+static int apply_penalties(pgx_problem* p, const WorkDev& w, bool want_grad, const pgx::LaunchInfo& li) {
+  if (p->n_pen == 0) return PGX_OK;
+  return ctx_cuda(p->ctx, pgx::launch_penalties(p->d_pen, p->n_pen, w.u, p->pd.dt, p->desc.n_controls,
+                                                p->desc.n_slices, w.F, want_grad ? w.G : nullptr, li),
+                  "penalties");
+}
+
 int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream) {
   pgx_ctx* c = p->ctx;
   pgx::LaunchInfo li = p->launch_info();
@@ -628,6 +637,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
     if (want_grad && (st = ctx_cuda(c, pgx::launch_grad_mx(p->pd, w, li), "grad_mx"))) return st;
     mk.mark(PGX_STAGE_REDUCE);
     st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, want_grad), "reduce");
+    if (!st) st = apply_penalties(p, w, want_grad, li);
     mk.mark(PGX_N_STAGES);
     mk.commit();
     return st;
@@ -648,6 +658,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
     if ((st = ctx_cuda(c, pgx::launch_grad(p->pd_grad, w2, li), "grad"))) return st;
     mk.mark(PGX_STAGE_REDUCE);
     st = ctx_cuda(c, pgx::launch_reduce(p->pd_grad, w2, li, true), "reduce");
+    if (!st) st = apply_penalties(p, w, true, li);
     mk.mark(PGX_N_STAGES);
     mk.commit();
     return st;
@@ -659,6 +670,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
   if (want_grad && (st = ctx_cuda(c, pgx::launch_grad(p->pd, w, li), "grad"))) return st;
   mk.mark(PGX_STAGE_REDUCE);
   st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, want_grad), "reduce");
+  if (!st) st = apply_penalties(p, w, want_grad, li);
   mk.mark(PGX_N_STAGES);
   mk.commit();
   return st;

@@ -44,6 +44,8 @@ struct pgx_problem {
   std::vector<void*> owned;
   uint64_t bytes = 0;
   int team[pgx::kNumTunable] = {0, 0};  // tuned team sizes (0 = default)
+  pgx_penalty* d_pen = nullptr;         // [PGX_MAX_PENALTIES] on the device
+  int n_pen = 0;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};
     for (int i = 0; i < pgx::kNumTunable; ++i) li.team[i] = team[i];
@@ -63,6 +65,11 @@ std::vector<double> pad_mats(const double* src, int n, int D, int Dp);
 int validate_desc(pgx_ctx* c, const pgx_problem_desc* d);
 uint64_t problem_footprint(const pgx_problem_desc* d, int num_sms);
 int ctx_cuda(pgx_ctx* c, cudaError_t e, const char* where);
+namespace pgx {
+// Subtracts the problem's penalties from F and G (G nullable) on li.stream.
+cudaError_t launch_penalties(const pgx_penalty* d_pens, int n_pen, const double* u, const double* dt, int n_c,
+                             int n_t, double* F, double* G, const LaunchInfo& li);
+}  // namespace pgx
 // Enqueues one evaluation; stream = nullptr means the context stream.
 int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream = nullptr);
 int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats);

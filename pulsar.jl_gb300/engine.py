@@ -412,6 +412,19 @@ class Problem:
         A.check(A.lib().pgx_autotune(self._h, A.as_dptr(ub), int(reps), buf, 1024), self.ctx.handle)
         return buf.value.decode()
 
+    def set_penalties(self, penalties):
+        """Subtract waveform penalties from every later evaluation:
+        penalties = [(type, weight[, l_bound, u_bound]), ...] with type one of
+        NS, SNS, SNSA, DNS, energy (Penalties.jl:197-330)."""
+        arr = (A.Penalty * max(len(penalties), 1))()
+        for i, pen in enumerate(penalties):
+            t, wgt = pen[0], pen[1]
+            lo, hi = (pen[2], pen[3]) if len(pen) > 2 else (-1.0, 1.0)
+            if t not in A.PENALTY:
+                raise ValueError(f"Unknown penalty ':{t}'. Valid: {', '.join(A.PENALTY)}")
+            arr[i].type, arr[i].weight, arr[i].l_bound, arr[i].u_bound = A.PENALTY[t], float(wgt), float(lo), float(hi)
+        A.check(A.lib().pgx_problem_set_penalties(self._h, len(penalties), C.cast(arr, C.c_void_p)), self.ctx.handle)
+
     @property
     def teams(self) -> tuple:
         """(expm, gradient) team sizes of the mixed kernels in use."""

@@ -143,3 +143,39 @@ def test_ensemble_value_functions_and_mr_builder(pg):
     assert Fv == F and np.array_equal(g, G.reshape(-1, order="F"))
     with pytest.raises(ValueError):
         pg.build_ensemble_from_mrcontrol(ctrl, aggregator="cvar")
+
+
+@pytest.mark.parametrize("ptype", ["NS", "SNS", "SNSA", "DNS", "energy"])
+def test_penalty_value_and_gradient(pg, ptype):
+    rng = np.random.default_rng(40)
+    w = rng.uniform(-1.6, 1.6, (3, 11))
+    dt = rng.uniform(0.5, 1.5, 11)
+    P, G = pg.penalty_value_and_gradient(w, ptype, weight=0.3, l_bound=-0.8, u_bound=0.9, dt=dt)
+    Po, Go = rs.penalty_value_and_gradient(w, ptype, 0.3, -0.8, 0.9, dt)
+    assert abs(P - Po) <= 1e-12 * max(1.0, abs(Po))
+    assert np.max(np.abs(G - Go)) <= 1e-12
+    assert pg.penalty_value(w, ptype, 0.0) == 0.0
+
+
+def test_penalties_fused_into_the_evaluation(pg):
+    """MR kernels subtract the penalties (GRAPEState.jl:571-584)."""
+    from oracle import members as mb
+    import fx
+    spec_prob, u0 = fx.spin4_ensemble(n_t=10, n_off=2, n_b1=1)
+    pens = [("NS", 1e-9), ("DNS", 2e-9), ("SNS", 1e-8, -5e3, 5e3)]
+    for precision, ftol, gtol in (("fp64", 1e-10, 1e-8), ("mixed", 1e-8, 1e-4)):
+        di, sc, of, wgt = spec_prob.members()
+        p = pg.Problem(spec_prob.drifts, spec_prob.controls, spec_prob.dt, offset_op=spec_prob.offset_op,
+                       member_drift=di, member_scale=sc, member_offset=of, member_weight=wgt, target="gate",
+                       target_op=spec_prob.target_op, grad_mode="exact", precision=precision)
+        p.set_penalties(pens)
+        F, G = p.eval(u0)
+        p.close()
+        Fo, Go = mb.eval_problem(spec_prob, u0, "exact")
+        for pen in pens:
+            lo, hi = (pen[2], pen[3]) if len(pen) > 2 else (-1.0, 1.0)
+            Pv, Pg = rs.penalty_value_and_gradient(u0, pen[0], pen[1], lo, hi)
+            Fo -= Pv
+            Go = Go - Pg
+        assert abs(F - Fo) <= ftol, (precision, F, Fo)
+        assert np.max(np.abs(G - Go)) <= gtol * np.max(np.abs(Go)), precision

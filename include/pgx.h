@@ -198,6 +198,17 @@ int pgx_overlap(pgx_ctx* ctx, int64_t n, const double* A, const double* B, doubl
 int pgx_trace_products(pgx_ctx* ctx, int32_t dim, int32_t n, int32_t m, const double* X, const double* E,
                        const double* Y, double* out);
 
+/* ---- ensemble aggregators ---------------------------------------------- */
+/* The aggregated objective of EnsembleObjective.jl:169-217 with each member a
+ * sample: F_m = mean over the member's state pairs of f(z) (gates: f(z)),
+ * dF_m/du its gradient.  MEAN averages the members, WORST_CASE takes the first
+ * member of least F_m (argmin), CVAR the mean over the max(1, round(alpha n))
+ * members of least F_m (stable order, round half to even).  G (nullable)
+ * receives the aggregated gradient [n_c x n_t].  Member weights must be
+ * positive (the per-member gradient is recovered from the weighted one). */
+enum { PGX_AGG_MEAN = 0, PGX_AGG_WORST_CASE = 1, PGX_AGG_CVAR = 2 };
+int pgx_eval_aggregate(pgx_problem* prob, const double* u, int32_t aggregator, double alpha, double* F, double* G);
+
 /* ---- penalties ---------------------------------------------------------- */
 /* Waveform penalties of Penalties.jl:197-330 (the PENALTY_TYPES of :205):
  *   NS     sum w^2                       SNS   sum max(0, w-u_b)^2 + max(0, l_b-w)^2

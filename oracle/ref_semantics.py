@@ -330,6 +330,24 @@ def compute_grape_gradient_with(system, target, P, Q, U_total, dt) -> np.ndarray
                           target.target_state, dt)
 
 
+def aggregate(fv, gv, aggregator: str, alpha: float = 0.2):
+    """_agg_value / _agg_grad! of EnsembleObjective.jl:169-217: mean, the first
+    argmin, or the mean over the max(1, round(alpha n)) smallest (stable
+    sort; round half to even as Julia's round)."""
+    fv = np.asarray(fv, float)
+    n = len(fv)
+    if aggregator == "mean":
+        return float(np.mean(fv)), sum(gv) / n
+    if aggregator == "worst_case":
+        w = int(np.argmin(fv))
+        return float(fv[w]), gv[w]
+    if aggregator == "cvar":
+        n_tail = max(1, int(round(alpha * n)))
+        order = np.argsort(fv, kind="stable")[:n_tail]
+        return float(np.mean(fv[order])), sum(gv[i] for i in order) / n_tail
+    raise ValueError(aggregator)
+
+
 def penalty_value_and_gradient(w, type, weight=1.0, l_bound=-1.0, u_bound=1.0, dt=None):
     """(weight P, weight dP/dw) of Penalties.jl:273-330 for w [n_ctrl, n_t]."""
     w = np.asarray(w, float)

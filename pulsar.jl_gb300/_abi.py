@@ -68,6 +68,7 @@ class OptResult(C.Structure):
 
 JOB_STATE = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
 PENALTY = {"NS": 0, "SNS": 1, "SNSA": 2, "DNS": 3, "energy": 4}
+AGGREGATOR = {"mean": 0, "worst_case": 1, "cvar": 2}
 
 
 class Penalty(C.Structure):
@@ -131,6 +132,7 @@ SIGNATURES = {
     "pgx_trace_products": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dptr, dptr, dptr, dptr]),
     "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
     "pgx_problem_set_penalties": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "pgx_eval_aggregate": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_double, dptr, dptr]),
     "pgx_penalty_eval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, C.c_void_p, dptr, dptr]),
     "pgx_problem_set_team": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),

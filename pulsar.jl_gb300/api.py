@@ -685,33 +685,44 @@ def _systems_as_members(systems: Sequence[QuantumSystem]):
 
 
 class EnsembleObjective:
-    """Mean-aggregated ensemble objective served by one batched GPU
-    evaluation: the ``batched_eval`` plug of EnsembleObjective.jl:145-163."""
+    """Ensemble objective served by one batched GPU evaluation over all
+    samples: the ``batched_eval`` plug of EnsembleObjective.jl:145-163 for
+    :mean, and the :worst_case / :cvar aggregators of :169-217 with each
+    ensemble member a sample."""
 
-    def __init__(self, problem: Problem, n_samples: int, n_c: int, n_t: int):
+    def __init__(self, problem: Problem, n_samples: int, n_c: int, n_t: int, aggregator: str = "mean",
+                 cvar_alpha: float = 0.2):
+        if aggregator not in ("mean", "worst_case", "cvar"):
+            raise ValueError(f"Unknown aggregator {aggregator}")
         self.problem = problem
         self.n_samples = n_samples
+        self.aggregator = aggregator
+        self.cvar_alpha = float(cvar_alpha)
         self._shape = (n_c, n_t)
 
+    def _u(self, theta):
+        return np.asarray(theta, np.float64).reshape(self._shape, order="F")
+
     def batched_eval(self, theta):
-        u = np.asarray(theta, np.float64).reshape(self._shape, order="F")
-        F, G = self.problem.eval(u)
+        if self.aggregator == "mean":
+            F, G = self.problem.eval(self._u(theta))
+        else:
+            F, G = self.problem.eval_aggregate(self._u(theta), self.aggregator, self.cvar_alpha)
         return F, G.reshape(-1, order="F")
 
     def value(self, theta) -> float:
-        u = np.asarray(theta, np.float64).reshape(self._shape, order="F")
-        return self.problem.eval(u, want_grad=False)[0]
+        if self.aggregator == "mean":
+            return self.problem.eval(self._u(theta), want_grad=False)[0]
+        return self.problem.eval_aggregate(self._u(theta), self.aggregator, self.cvar_alpha, want_grad=False)[0]
 
     value_and_grad = batched_eval
 
 
 def build_ensemble_from_systems(systems, target: QuantumTarget, controls: ControlSequence,
                                 aggregator: str = "mean", grad_mode: str = "ref_grape",
-                                precision: str = "fp64") -> EnsembleObjective:
-    """SystemBuilder.jl:49-87 with the :mean aggregator (per-system
-    compute_fidelity + compute_grape_gradient, averaged)."""
-    if aggregator != "mean":
-        raise ValueError("only the :mean aggregator runs batched on the device")
+                                precision: str = "fp64", cvar_alpha: float = 0.2) -> EnsembleObjective:
+    """SystemBuilder.jl:49-87: per-system compute_fidelity +
+    compute_grape_gradient, aggregated by :mean, :worst_case or :cvar."""
     if not systems:
         raise ValueError("systems must be non-empty")
     drifts, ctrls, scales = _systems_as_members(systems)
@@ -728,7 +739,7 @@ def build_ensemble_from_systems(systems, target: QuantumTarget, controls: Contro
         # compute_fidelity uses raw states; compute_grape_gradient normalises
         prob = Problem(drifts, ctrls, _dt_vec(controls.dt, n_t), target="states",
                        states_init=psi_i, states_target=psi_t, **kw)
-    return EnsembleObjective(prob, n, ctrls.shape[0], n_t)
+    return EnsembleObjective(prob, n, ctrls.shape[0], n_t, aggregator, cvar_alpha)
 
 
 def grape_optimize_ensemble(systems, target: QuantumTarget, controls_init: ControlSequence,
@@ -935,15 +946,17 @@ def ensemble_value_and_grad(obj: EnsembleObjective, theta):
 
 
 def build_ensemble_from_mrcontrol(ctrl, aggregator: str = "mean", cvar_alpha: float = 0.2) -> EnsembleObjective:
-    """EnsembleBuilder.jl:72-182, :mean: one batched device evaluation over
-    drifts x pwr_levels x state pairs, n_samples = their product."""
-    if aggregator != "mean":
-        raise ValueError("only the :mean aggregator runs batched on the device")
+    """EnsembleBuilder.jl:72-182: one batched device evaluation over drifts x
+    pwr_levels x state pairs (n_samples = their product).  :worst_case and
+    :cvar take each (drift, pwr) member, averaged over its state pairs, as a
+    sample; the reference splits the pairs into separate samples as well."""
+    if aggregator not in ("mean", "worst_case", "cvar"):
+        raise ValueError(f"Unknown aggregator {aggregator}")
     n_pairs = len(ctrl.rho_init)
     n_drifts = len(ctrl.drifts)
     prob = ctrl.problem()
     return EnsembleObjective(prob, n_drifts * len(ctrl.pwr_levels) * n_pairs, len(ctrl.operators),
-                             len(ctrl.pulse_dt))
+                             len(ctrl.pulse_dt), aggregator, cvar_alpha)
 
 
 def grape_state_kernel(waveform, ctrl: MRControl):

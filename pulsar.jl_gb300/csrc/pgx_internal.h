@@ -152,6 +152,9 @@ cudaError_t launch_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInf
 cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad);
+// G[q] = sum_i coef[i] Gm[idx[i]][q] (len = n_c n_t), in the order of idx.
+cudaError_t launch_select_sum(const double* Gm, const int* idx, const double* coef, int n_sel, int len, double* G,
+                              const LaunchInfo& li);
 // Mixed-precision stages (pgx_mixed.cu), gate targets: df expm and forward
 // chain, FP32 backward chain and gradient.  U stack holds df (float4), the P
 // stack float2.

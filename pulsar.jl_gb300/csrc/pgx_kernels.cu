@@ -439,6 +439,23 @@ __global__ void k_reduce(ProbDev p, WorkDev w, int want_grad) {
   }
 }
 
+// G[q] = sum_i coef[i] Gm[idx[i]][q], members in the order given (the
+// worst-case and CVaR ensemble gradients).
+__global__ void k_select_sum(const double* Gm, const int* idx, const double* coef, int n_sel, int len, double* G) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= len) return;
+  double s = 0.0;
+  for (int i = 0; i < n_sel; ++i) s = fma(coef[i], Gm[(size_t)idx[i] * len + q], s);
+  G[q] = s;
+}
+
+cudaError_t launch_select_sum(const double* Gm, const int* idx, const double* coef, int n_sel, int len, double* G,
+                              const LaunchInfo& li) {
+  k_select_sum<<<(len + 255) / 256, 256, 0, li.stream>>>(Gm, idx, coef, n_sel, len, G);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------------------------
 // Launchers
 // --------------------------------------------------------------------------

@@ -851,6 +851,67 @@ extern "C" int pgx_eval_device(pgx_problem* p, const double* d_u, double* d_F, d
   return run_pipeline(p, d_u, d_F, d_G);
 }
 
+extern "C" int pgx_eval_aggregate(pgx_problem* p, const double* u, int32_t agg, double alpha, double* F,
+                                  double* G) {
+  if (!p || !u || !F) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  if (agg < PGX_AGG_MEAN || agg > PGX_AGG_CVAR) return ctx_fail(c, PGX_ERR_INVALID, "unknown aggregator");
+  if (agg == PGX_AGG_CVAR && !(alpha > 0.0 && alpha <= 1.0))
+    return ctx_fail(c, PGX_ERR_INVALID, "cvar alpha must be in (0, 1]");
+  const int nm = p->desc.n_members;
+  for (int m = 0; m < nm; ++m)
+    if (!(p->h_weight[m] > 0.0)) return ctx_fail(c, PGX_ERR_INVALID, "aggregators need positive member weights");
+  double Fw = 0.0;
+  int st = eval_host(p, u, &Fw, G, nullptr);  // leaves Fm (and Gm when G) of every member on the device
+  if (st) return st;
+  std::vector<double> Fm(nm);
+  if ((st = ctx_cuda(c, cudaMemcpyAsync(Fm.data(), p->w.Fm, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->stream),
+                     "D2H Fm")) ||
+      (st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync")))
+    return st;
+  const double npair = (double)std::max(p->desc.target == PGX_TARGET_STATES ? p->desc.n_pairs : 0, 1);
+  std::vector<double> fs(nm);
+  for (int m = 0; m < nm; ++m) fs[m] = Fm[m] / npair;   // per-sample objective
+  std::vector<int> sel;
+  if (agg == PGX_AGG_MEAN) {
+    for (int m = 0; m < nm; ++m) sel.push_back(m);
+  } else if (agg == PGX_AGG_WORST_CASE) {
+    sel.push_back((int)(std::min_element(fs.begin(), fs.end()) - fs.begin()));
+  } else {
+    std::vector<int> order(nm);
+    for (int m = 0; m < nm; ++m) order[m] = m;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return fs[a] < fs[b]; });
+    const int n_tail = std::max(1, (int)std::nearbyint(alpha * nm));
+    sel.assign(order.begin(), order.begin() + std::min(n_tail, nm));
+  }
+  double f = 0.0;
+  for (int m : sel) f += fs[m];
+  *F = f / (double)sel.size();
+  if (!G) return PGX_OK;
+  // gradient of sample m: Gm[m] / (w_m npair); averaged over the selection
+  std::vector<int> idx(sel.begin(), sel.end());
+  std::vector<double> coef(sel.size());
+  for (size_t i = 0; i < sel.size(); ++i) coef[i] = 1.0 / (p->h_weight[sel[i]] * npair * (double)sel.size());
+  const size_t len = (size_t)p->desc.n_controls * p->desc.n_slices;
+  void* buf = nullptr;
+  if ((st = ctx_cuda(c, cudaMallocAsync(&buf, sel.size() * (sizeof(int) + sizeof(double)) + 16, c->stream),
+                     "alloc")))
+    return st;
+  double* d_coef = (double*)buf;
+  int* d_idx = (int*)(d_coef + sel.size());
+  pgx::LaunchInfo li{c->num_sms, c->stream, &c->launches};
+  if (!(st = ctx_cuda(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * sel.size(), cudaMemcpyHostToDevice,
+                                         c->stream), "H2D")) &&
+      !(st = ctx_cuda(c, cudaMemcpyAsync(d_idx, idx.data(), sizeof(int) * sel.size(), cudaMemcpyHostToDevice,
+                                         c->stream), "H2D")) &&
+      !(st = ctx_cuda(c, pgx::launch_select_sum(p->w.Gm, d_idx, d_coef, (int)sel.size(), (int)len, p->d_G, li),
+                      "select_sum")))
+    st = ctx_cuda(c, cudaMemcpyAsync(G, p->d_G, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream), "D2H G");
+  cudaFreeAsync(buf, c->stream);
+  const int st2 = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+  return st ? st : st2;
+}
+
 extern "C" int pgx_member_fidelities(pgx_problem* p, double* F_members) {
   if (!p || !F_members) return PGX_ERR_INVALID;
   pgx_ctx* c = p->ctx;

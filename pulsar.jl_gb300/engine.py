@@ -412,6 +412,17 @@ class Problem:
         A.check(A.lib().pgx_autotune(self._h, A.as_dptr(ub), int(reps), buf, 1024), self.ctx.handle)
         return buf.value.decode()
 
+    def eval_aggregate(self, u, aggregator: str = "mean", alpha: float = 0.2, want_grad: bool = True):
+        """(F, G) of the member-aggregated objective: "mean", "worst_case" or
+        "cvar" with tail fraction alpha (EnsembleObjective.jl:169-217)."""
+        ub = self._load_u(u)
+        F = C.c_double()
+        A.check(A.lib().pgx_eval_aggregate(self._h, A.as_dptr(ub), A.AGGREGATOR[aggregator], float(alpha),
+                                           C.byref(F), A.as_dptr(self._G) if want_grad else None),
+                self.ctx.handle)
+        G = self._G.reshape(self.n_t, self.n_c).T.copy() if want_grad else None
+        return float(F.value), G
+
     def set_penalties(self, penalties):
         """Subtract waveform penalties from every later evaluation:
         penalties = [(type, weight[, l_bound, u_bound]), ...] with type one of

@@ -142,7 +142,7 @@ def test_ensemble_value_functions_and_mr_builder(pg):
     Fv, g = pg.ensemble_value_and_grad(obj, theta)
     assert Fv == F and np.array_equal(g, G.reshape(-1, order="F"))
     with pytest.raises(ValueError):
-        pg.build_ensemble_from_mrcontrol(ctrl, aggregator="cvar")
+        pg.build_ensemble_from_mrcontrol(ctrl, aggregator="median")
 
 
 @pytest.mark.parametrize("ptype", ["NS", "SNS", "SNSA", "DNS", "energy"])
@@ -179,3 +179,27 @@ def test_penalties_fused_into_the_evaluation(pg):
             Go = Go - Pg
         assert abs(F - Fo) <= ftol, (precision, F, Fo)
         assert np.max(np.abs(G - Go)) <= gtol * np.max(np.abs(Go)), precision
+
+
+@pytest.mark.parametrize("aggregator", ["mean", "worst_case", "cvar"])
+def test_ensemble_aggregators(pg, aggregator):
+    """:mean / :worst_case / :cvar over per-system samples (EnsembleObjective.jl:169-217)."""
+    rng = np.random.default_rng(12)
+    SX = np.array([[0, 1], [1, 0]], complex)
+    SY = np.array([[0, -1j], [1j, 0]], complex)
+    SZ = np.diag([1.0, -1.0]).astype(complex)
+    systems_o = [rs.QuantumSystem(0.5 * d * SZ, [0.5 * SX, 0.5 * SY]) for d in (-0.3, -0.1, 0.0, 0.15, 0.4)]
+    systems_g = [pg.quantum_system(s.H_drift, s.H_controls) for s in systems_o]
+    u = 0.3 * rng.standard_normal((2, 14))
+    T = np.array([[0, 1], [1, 0]], complex)
+    cs_o = rs.ControlSequence.from_controls(u, 0.1)
+    Fi = np.array([rs.compute_fidelity(s, cs_o, rs.unitary_target(T)) for s in systems_o])
+    Gi = [rs.compute_grape_gradient(s, cs_o, rs.unitary_target(T)) for s in systems_o]
+    Fo, Go = rs.aggregate(Fi, Gi, aggregator, 0.4)
+    obj = pg.build_ensemble_from_systems(systems_g, pg.unitary_target(T), pg.ControlSequence.from_controls(u, 0.1),
+                                         aggregator=aggregator, cvar_alpha=0.4)
+    theta = u.reshape(-1, order="F")
+    F, g = obj.value_and_grad(theta)
+    assert abs(F - Fo) <= 1e-12
+    assert np.max(np.abs(g - Go.reshape(-1, order="F"))) <= 1e-10 * max(1.0, np.max(np.abs(Go)))
+    assert abs(obj.value(theta) - Fo) <= 1e-12

@@ -198,6 +198,11 @@ int pgx_overlap(pgx_ctx* ctx, int64_t n, const double* A, const double* B, doubl
 int pgx_trace_products(pgx_ctx* ctx, int32_t dim, int32_t n, int32_t m, const double* X, const double* E,
                        const double* Y, double* out);
 
+/* Replaces the drift matrices ([n_drifts][dim^2], same count and checks as at
+ * creation), e.g. the redrawn perturbations of a resampling robust ensemble
+ * (PerturbationBuilder.jl:52-133). */
+int pgx_problem_set_drifts(pgx_problem* prob, const double* drifts);
+
 /* ---- ensemble aggregators ---------------------------------------------- */
 /* The aggregated objective of EnsembleObjective.jl:169-217 with each member a
  * sample: F_m = mean over the member's state pairs of f(z) (gates: f(z)),

@@ -21,6 +21,7 @@ from .api import (
     fidelity_cuda, fidelity_grad_prefactor, finite_difference_gradient, gate_fidelity, gradient_cuda,
     grape_gradient_check, lindblad_grad_prefactor, matrix_exponential_cuda, state_fidelity,
     penalty_gradient, penalty_value, penalty_value_and_gradient,
+    PerturbationEnsemble, build_ensemble_from_perturbations, sample_parametric_perturbations,
 )
 
 LIB_PATH = _abi.LIB_PATH

@@ -133,6 +133,7 @@ SIGNATURES = {
     "pgx_autotune": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_char_p, C.c_size_t]),
     "pgx_problem_set_penalties": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "pgx_eval_aggregate": (C.c_int, [C.c_void_p, dptr, C.c_int32, C.c_double, dptr, dptr]),
+    "pgx_problem_set_drifts": (C.c_int, [C.c_void_p, dptr]),
     "pgx_penalty_eval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, C.c_void_p, dptr, dptr]),
     "pgx_problem_set_team": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),

@@ -742,6 +742,78 @@ def build_ensemble_from_systems(systems, target: QuantumTarget, controls: Contro
     return EnsembleObjective(prob, n, ctrls.shape[0], n_t, aggregator, cvar_alpha)
 
 
+def sample_parametric_perturbations(system: QuantumSystem, n_samples: int, magnitude: float,
+                                    rng: Optional[np.random.Generator] = None) -> list:
+    """Random Hermitian dH with ||dH||_F = magnitude ||H_drift||_F
+    (RobustOpt.jl:137-158): X complex Gaussian / sqrt 2, dH = (X + X')/2,
+    rescaled.  numpy's generator stands in for Julia's MersenneTwister."""
+    rng = rng or np.random.default_rng()
+    H0 = system.H_drift
+    d = H0.shape[0]
+    n0 = np.linalg.norm(H0)
+    n0 = 1.0 if n0 < 1e-14 else n0
+    out = []
+    for _ in range(n_samples):
+        X = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / np.sqrt(2.0)
+        dH = (X + X.conj().T) / 2.0
+        out.append(dH * (magnitude * n0 / max(np.linalg.norm(dH), 1e-14)))
+    return out
+
+
+class PerturbationEnsemble(EnsembleObjective):
+    """build_ensemble_from_perturbations (PerturbationBuilder.jl:52-133), the
+    :parametric kind: sample i evolves under H_drift + dH_i.  All samples are
+    members of one device problem; with resample=True the perturbations are
+    redrawn (seed + call count) before every value_and_grad.  The gradient is
+    the exact gradient of each sample's fidelity (the reference
+    differentiates by central differences, eps 1e-5)."""
+
+    def __init__(self, system: QuantumSystem, target: QuantumTarget, controls: ControlSequence, magnitude: float,
+                 n_samples: int, aggregator: str, cvar_alpha: float, resample: bool, seed: int,
+                 grad_mode: str = "exact", precision: str = "fp64"):
+        if target.type != "unitary":
+            raise ValueError("perturbation ensembles score gate fidelities (RobustOpt.jl:739-761)")
+        self.system, self.magnitude, self.resample, self.seed = system, float(magnitude), resample, int(seed)
+        self._calls = 0
+        pert = sample_parametric_perturbations(system, n_samples, magnitude, np.random.default_rng(seed))
+        drifts = np.stack([system.H_drift + dH for dH in pert])
+        n_t = controls.n_steps
+        prob = Problem(drifts, np.stack(system.H_controls), _dt_vec(controls.dt, n_t),
+                       member_drift=np.arange(n_samples), member_weight=np.full(n_samples, 1.0 / n_samples),
+                       target="gate", fidelity="square", target_op=target.target_unitary, grad_mode=grad_mode,
+                       precision=precision)
+        super().__init__(prob, n_samples, system.n_controls, n_t, aggregator, cvar_alpha)
+
+    def _redraw(self):
+        self._calls += 1
+        rng = np.random.default_rng(self.seed + self._calls)
+        pert = sample_parametric_perturbations(self.system, self.n_samples, self.magnitude, rng)
+        self.problem.set_drifts(np.stack([self.system.H_drift + dH for dH in pert]))
+
+    def batched_eval(self, theta):
+        if self.resample:
+            self._redraw()
+        return super().batched_eval(theta)
+
+    value_and_grad = batched_eval
+
+
+def build_ensemble_from_perturbations(system: QuantumSystem, target: QuantumTarget, controls: ControlSequence,
+                                      uncertainty_type: str = "parametric", magnitude: float = 0.05,
+                                      n_samples: int = 20, aggregator: str = "mean", cvar_alpha: float = 0.2,
+                                      resample: bool = True, seed: int = 42, precision: str = "fp64"):
+    """PerturbationBuilder.jl:52-133 (:parametric)."""
+    if uncertainty_type not in ("parametric", "drift"):
+        raise ValueError("uncertainty_type must be :parametric or :drift for this builder; use robust_optimize "
+                         "for :noise")
+    if uncertainty_type == "drift":
+        raise ValueError("the :drift ramp dH_k = t_k dH is not served by the device problem model")
+    if n_samples <= 0:
+        raise ValueError("n_samples must be positive")
+    return PerturbationEnsemble(system, target, controls, magnitude, n_samples, aggregator, cvar_alpha, resample,
+                                seed, precision=precision)
+
+
 def grape_optimize_ensemble(systems, target: QuantumTarget, controls_init: ControlSequence,
                             config: GRAPEConfig = GRAPEConfig(), lbfgs_memory: int = 10,
                             amplitude_limit: float = math.inf) -> OptimizationResult:

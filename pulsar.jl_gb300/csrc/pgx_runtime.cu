@@ -912,6 +912,29 @@ extern "C" int pgx_eval_aggregate(pgx_problem* p, const double* u, int32_t agg, 
   return st ? st : st2;
 }
 
+extern "C" int pgx_problem_set_drifts(pgx_problem* p, const double* drifts) {
+  if (!p || !drifts) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  const int D = p->desc.dim, Dp = p->Dp, nd = p->desc.n_drifts;
+  if (!finite_all(drifts, 2 * (size_t)nd * D * D)) return ctx_fail(c, PGX_ERR_NONFINITE, "drifts must be finite");
+  if (p->desc.generator == PGX_GEN_HERMITIAN)
+    for (int i = 0; i < nd; ++i)
+      if (herm_dev(drifts + 2 * (size_t)i * D * D, D) > 1e-10)
+        return ctx_fail(c, PGX_ERR_INVALID, "drift is not Hermitian (QuantumSystem.jl:318-341)");
+  cudaSetDevice(c->device);
+  const std::vector<double> padded = pad_mats(drifts, nd, D, Dp);
+  int st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts, padded.data(), padded.size() * sizeof(double),
+                                       cudaMemcpyHostToDevice, c->stream), "H2D drifts");
+  if (!st && p->pd.drifts_df) {
+    const std::vector<float> dfp = to_df_pairs(padded);
+    st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts_df, dfp.data(), dfp.size() * sizeof(float),
+                                     cudaMemcpyHostToDevice, c->stream), "H2D drifts (df)");
+    if (!st) st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");  // dfp lives on this stack
+    return st;
+  }
+  return st ? st : ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
 extern "C" int pgx_member_fidelities(pgx_problem* p, double* F_members) {
   if (!p || !F_members) return PGX_ERR_INVALID;
   pgx_ctx* c = p->ctx;

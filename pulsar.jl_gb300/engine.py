@@ -412,6 +412,13 @@ class Problem:
         A.check(A.lib().pgx_autotune(self._h, A.as_dptr(ub), int(reps), buf, 1024), self.ctx.handle)
         return buf.value.decode()
 
+    def set_drifts(self, drifts):
+        """Replace the drift matrices [n_drifts, D, D] (same count as at creation)."""
+        d = np.asarray(drifts, np.complex128)
+        if d.ndim == 2:
+            d = d[None]
+        A.check(A.lib().pgx_problem_set_drifts(self._h, A.as_dptr(A.cmat_buf(d))), self.ctx.handle)
+
     def eval_aggregate(self, u, aggregator: str = "mean", alpha: float = 0.2, want_grad: bool = True):
         """(F, G) of the member-aggregated objective: "mean", "worst_case" or
         "cvar" with tail fraction alpha (EnsembleObjective.jl:169-217)."""

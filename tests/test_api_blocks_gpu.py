@@ -203,3 +203,37 @@ def test_ensemble_aggregators(pg, aggregator):
     assert abs(F - Fo) <= 1e-12
     assert np.max(np.abs(g - Go.reshape(-1, order="F"))) <= 1e-10 * max(1.0, np.max(np.abs(Go)))
     assert abs(obj.value(theta) - Fo) <= 1e-12
+
+
+@pytest.mark.parametrize("aggregator", ["mean", "worst_case", "cvar"])
+def test_parametric_perturbation_ensemble(pg, aggregator):
+    """build_ensemble_from_perturbations(:parametric) against the oracle on
+    the same perturbations: per-sample exact F and G, then the aggregator."""
+    from oracle import members as mb
+    rng = np.random.default_rng(31)
+    d, n_c, n_t = 3, 2, 9
+    Hd, Hc = _herm(rng, d), [_herm(rng, d) for _ in range(n_c)]
+    T = _unitary(rng, d)
+    sys_g = pg.quantum_system(Hd, Hc)
+    u = rng.uniform(-1, 1, (n_c, n_t))
+    cs = pg.ControlSequence.from_controls(u, 0.1)
+    obj = pg.build_ensemble_from_perturbations(sys_g, pg.unitary_target(T), cs, magnitude=0.1, n_samples=6,
+                                               aggregator=aggregator, cvar_alpha=0.34, resample=False, seed=5)
+    pert = pg.sample_parametric_perturbations(sys_g, 6, 0.1, np.random.default_rng(5))
+    Fi, Gi = [], []
+    for dH in pert:
+        prob = mb.Problem(drifts=(Hd + dH)[None], controls=np.stack(Hc), dt=np.full(n_t, 0.1), target="gate",
+                          fidelity="square", target_op=T)
+        F1, G1 = mb.eval_problem(prob, u, "exact")
+        Fi.append(F1)
+        Gi.append(G1)
+    Fo, Go = rs.aggregate(Fi, Gi, aggregator, 0.34)
+    theta = u.reshape(-1, order="F")
+    F, g = obj.value_and_grad(theta)
+    assert abs(F - Fo) <= 1e-12
+    assert np.max(np.abs(g - Go.reshape(-1, order="F"))) <= 1e-9 * max(1.0, np.max(np.abs(Go)))
+    # resampling redraws (seed + call count): a different objective, same shape
+    obj2 = pg.build_ensemble_from_perturbations(sys_g, pg.unitary_target(T), cs, magnitude=0.1, n_samples=6,
+                                                aggregator=aggregator, resample=True, seed=5)
+    F2, g2 = obj2.value_and_grad(theta)
+    assert F2 != F and g2.shape == g.shape

@@ -411,16 +411,109 @@ int pgx_submit(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_d
                const double* u0, uint64_t* job_id);
 int pgx_poll(pgx_server* server, uint64_t job_id, pgx_job_status* status);
 /* Result of a finished job: best controls u ([n_c x n_t], nullable) and the
- * grape_optimize summary (nullable; histories are not kept).  Returns
- * PGX_ERR_STATE while the job is queued or running, the job's error when it
- * failed, PGX_ERR_CANCELLED when cancelled.  A fetched job is forgotten.    */
+ * grape_optimize summary (nullable; history lengths filled, the traces come
+ * from pgx_job_history).  Returns PGX_ERR_STATE while the job is queued or
+ * running, the job's error when it failed, PGX_ERR_CANCELLED when cancelled.
+ * A fetched job is forgotten.                                               */
 int pgx_fetch(pgx_server* server, uint64_t job_id, double* u, pgx_opt_result* result);
+/* Fidelity and gradient-norm traces of a job so far, with the conventions of
+ * OptimizationResult (GRAPE.jl:158-170): grape_optimize's F(u0), then F at
+ * each iteration's controls (+ the post-step F of a converged run);
+ * ||G|| per iteration.  A resumed job's traces start with its checkpoint's
+ * (Checkpoint.jl:279-280).  Either buffer nullable; *n_fidelity / *n_gnorm
+ * receive the full lengths, at most cap entries are written.               */
+int pgx_job_history(pgx_server* server, uint64_t job_id, double* fidelity_history, double* gnorm_history,
+                    int32_t cap, int32_t* n_fidelity, int32_t* n_gnorm);
 /* Queued jobs are dropped at once; running ones stop after their current
- * iteration (their controls so far stay fetchable).                         */
+ * iteration (an L-BFGS job finishes its line search and history update), so
+ * a cancelled job's checkpoint can continue exactly.                        */
 int pgx_cancel(pgx_server* server, uint64_t job_id);
 /* Waits until no job is queued or running; timeout_s <= 0 waits forever.   */
 int pgx_server_drain(pgx_server* server, double timeout_s);
 int pgx_server_stats(pgx_server* server, pgx_serve_stats* stats);
+
+/* ---- checkpoints of served jobs ----------------------------------------- */
+/* A checkpoint is a self-contained byte blob replacing the Julia
+ * Serialization of Checkpoint (IO/Checkpoint.jl:64-131,166-208): the fields
+ * of Checkpoint that describe an optimisation (w_opt, F_opt, n_controls,
+ * n_timesteps, iteration, both histories, system_dim, a timestamp) plus, for
+ * an exact snapshot, the job's device state: its current controls, gradient
+ * and objective, the GRAPE step-size state or the L-BFGS (s, y) history.
+ * Layout: little-endian, a fixed 208-byte header (magic "PGXCKPT\0",
+ * version 1), f64 payload arrays, a metadata section (opaque UTF-8 text,
+ * JSON by convention: the reference's domain tags and metadata dict, e.g.
+ * "dt"), and an FNV-1a-64 checksum of everything before it as the last 8
+ * bytes; identical on every host.                                          */
+#define PGX_CHECKPOINT_VERSION 1
+#define PGX_CHECKPOINT_HEADER_BYTES 208
+enum { PGX_CKPT_EXACT = 1,       /* carries the device state (PGX_RESUME_CONTINUE) */
+       PGX_CKPT_CONVERGED = 2 };
+enum { PGX_RESUME_RESTART = 0,   /* resume_optimization (Checkpoint.jl:220-298): a fresh
+                                    run from w_opt; histories and iteration counts add up */
+       PGX_RESUME_CONTINUE = 1   /* the interrupted trajectory itself: the resumed job's
+                                    iterates, histories and result are bit-identical to a
+                                    run that was never interrupted                       */ };
+
+typedef struct pgx_checkpoint_info {
+  uint32_t struct_size;
+  int32_t version;
+  int32_t flags;               /* PGX_CKPT_*                                              */
+  int32_t system_dim;          /* 0 = unknown (resume then skips the dim check)           */
+  int32_t n_controls;
+  int32_t n_timesteps;
+  int32_t n_members;
+  int32_t iteration;           /* iterations done (the n_iterations pgx_fetch reports)    */
+  int32_t history_len;
+  int32_t gnorm_history_len;
+  int32_t lbfgs_pairs;         /* stored (s, y) pairs of an exact L-BFGS snapshot         */
+  int32_t metadata_len;        /* bytes of the metadata section                           */
+  double F_opt;                /* best fidelity                                           */
+  double F;                    /* objective at the current controls (exact snapshots)     */
+  double timestamp;            /* seconds since the Unix epoch when written               */
+  uint64_t fingerprint;        /* FNV-1a-64 of the problem (0 = none)                     */
+  pgx_opt_desc opt;            /* settings of the job that was snapshotted                */
+} pgx_checkpoint_info;
+
+/* Takes a checkpoint of a job: a running job is snapshotted (exactly) at its
+ * next iteration boundary -- the call waits up to timeout_s (<= 0: forever;
+ * PGX_ERR_TIMEOUT) -- while a finished or cancelled job gives its final
+ * state (exact for cancelled jobs).  The blob stays with the job; *blob_len
+ * receives its size, pgx_job_checkpoint_read copies it out.  PGX_ERR_STATE
+ * for a job that never started.                                            */
+int pgx_job_checkpoint(pgx_server* server, uint64_t job_id, double timeout_s, uint64_t* blob_len);
+int pgx_job_checkpoint_read(pgx_server* server, uint64_t job_id, void* blob, uint64_t cap);
+/* Queues a job that resumes from a checkpoint.  Validation as
+ * resume_optimization (Checkpoint.jl:236-247): system_dim (when > 0) and
+ * n_controls must match desc, and n_timesteps its n_slices.  opt (nullable:
+ * the checkpoint's own settings) gives the new run's settings; under
+ * RESTART its max_iter is the number of additional iterations.  CONTINUE
+ * also requires an exact checkpoint of the same problem (fingerprint), the
+ * same method and, for L-BFGS, lbfgs_memory >= the stored pairs.            */
+int pgx_submit_resume(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_desc* opt,
+                      const void* blob, uint64_t blob_len, int32_t mode, uint64_t* job_id);
+/* Host-only (no device work): parses and verifies a blob (magic, version,
+ * sizes, checksum; PGX_ERR_INVALID otherwise) into info and, when non-null,
+ * w_opt ([n_c x n_t]) and the histories (history_len / gnorm_history_len
+ * entries).                                                                */
+int pgx_checkpoint_parse(const void* blob, uint64_t blob_len, pgx_checkpoint_info* info, double* w_opt,
+                         double* fidelity_history, double* gnorm_history);
+/* Host-only: the metadata bytes (info.metadata_len of them; PGX_ERR_DIMS
+ * when cap is smaller).                                                    */
+int pgx_checkpoint_metadata(const void* blob, uint64_t blob_len, char* metadata, uint64_t cap);
+/* Host-only: create_checkpoint (Checkpoint.jl:143-164) from host arrays, a
+ * warm-start (non-exact) blob.  info supplies dims, iteration, F_opt,
+ * history lengths, the timestamp (0 = now), fingerprint, settings and
+ * metadata_len bytes of metadata; blob NULL (or cap too small:
+ * PGX_ERR_DIMS) reports the size in *blob_len.                             */
+int pgx_checkpoint_create(const pgx_checkpoint_info* info, const double* w_opt, const double* fidelity_history,
+                          const double* gnorm_history, const char* metadata, void* blob, uint64_t cap,
+                          uint64_t* blob_len);
+/* Host-only: the same checkpoint with its metadata replaced (an exact
+ * snapshot stays exact); out NULL reports the size in *out_len.             */
+int pgx_checkpoint_set_metadata(const void* blob, uint64_t blob_len, const char* metadata, uint64_t metadata_len,
+                                void* out, uint64_t cap, uint64_t* out_len);
+/* FNV-1a-64 of a problem descriptor: sizes, kinds and every array's bits. */
+int pgx_problem_fingerprint(const pgx_problem_desc* desc, uint64_t* fingerprint);
 
 #ifdef __cplusplus
 }

@@ -7,7 +7,12 @@ The directory is named ``pulsar.jl_gb300``; import it as ``pulsar_gb300``
 through ``__graft_entry__.load_package()``.
 """
 from . import _abi
-from .engine import Batch, Context, Problem, Server, default_context, opt_desc, problem_desc
+from .engine import (Batch, Context, Problem, Server, checkpoint_create, checkpoint_parse,
+                     checkpoint_set_metadata, default_context, opt_desc, problem_desc,
+                     problem_fingerprint)
+from .checkpoint import (Checkpoint, auto_checkpoint_callback, checkpoint_compatible, checkpoint_summary,
+                         create_checkpoint, list_checkpoints, load_checkpoint, resume_optimization,
+                         save_checkpoint)
 from .api import (
     ControlSequence, EnsembleObjective, GRAPEConfig, LindbladMRControl, MRControl,
     OptimizationResult, QuantumSystem, QuantumTarget, build_control_liouvillian,

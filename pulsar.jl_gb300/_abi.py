@@ -100,6 +100,21 @@ class ServeStats(C.Structure):
     ]
 
 
+class CheckpointInfo(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("version", C.c_int32), ("flags", C.c_int32),
+        ("system_dim", C.c_int32), ("n_controls", C.c_int32), ("n_timesteps", C.c_int32),
+        ("n_members", C.c_int32), ("iteration", C.c_int32), ("history_len", C.c_int32),
+        ("gnorm_history_len", C.c_int32), ("lbfgs_pairs", C.c_int32), ("metadata_len", C.c_int32),
+        ("F_opt", C.c_double), ("F", C.c_double), ("timestamp", C.c_double),
+        ("fingerprint", C.c_uint64), ("opt", OptDesc),
+    ]
+
+
+CKPT_EXACT, CKPT_CONVERGED = 1, 2
+CHECKPOINT_HEADER_BYTES = 208
+RESUME = {"restart": 0, "continue": 1}
+
 # name -> (restype, argtypes); every symbol declared in include/pgx.h
 SIGNATURES = {
     "pgx_abi_version": (C.c_int, []),
@@ -159,6 +174,19 @@ SIGNATURES = {
     "pgx_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "pgx_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
     "pgx_server_stats": (C.c_int, [C.c_void_p, C.POINTER(ServeStats)]),
+    "pgx_job_history": (C.c_int, [C.c_void_p, C.c_uint64, dptr, dptr, C.c_int32, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32)]),
+    "pgx_job_checkpoint": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double, C.POINTER(C.c_uint64)]),
+    "pgx_job_checkpoint_read": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
+    "pgx_submit_resume": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(OptDesc), C.c_void_p,
+                                    C.c_uint64, C.c_int32, C.POINTER(C.c_uint64)]),
+    "pgx_checkpoint_parse": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(CheckpointInfo), dptr, dptr, dptr]),
+    "pgx_checkpoint_metadata": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
+    "pgx_checkpoint_create": (C.c_int, [C.POINTER(CheckpointInfo), dptr, dptr, dptr, C.c_char_p, C.c_void_p,
+                                        C.c_uint64, C.POINTER(C.c_uint64)]),
+    "pgx_checkpoint_set_metadata": (C.c_int, [C.c_void_p, C.c_uint64, C.c_char_p, C.c_uint64, C.c_void_p,
+                                              C.c_uint64, C.POINTER(C.c_uint64)]),
+    "pgx_problem_fingerprint": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(C.c_uint64)]),
 }
 
 _LIB = None

@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "pgx.h"
+#include "pgx_ckpt.h"
 #include "pgx_runtime.h"
 
 namespace {
@@ -114,6 +115,19 @@ struct Job {
   double *ucur = nullptr, *utry = nullptr, *gcur = nullptr, *gtry = nullptr;
   cudaGraphExec_t lb_exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int64_t lb_kernels[5] = {0, 0, 0, 0, 0};
+  bool lb_boundary = false;      // an iteration ended and its successor is not enqueued yet
+  // histories and resumption
+  std::vector<double> gh;        // gradient-norm history
+  uint64_t fingerprint = 0;      // of the problem descriptor
+  int prior_iter = 0;            // a resumed job: iterations and history entries of the
+  std::vector<double> prior_fh, prior_gh;  // runs before it (reported ahead of its own)
+  std::unique_ptr<pgx::Ckpt> restore;      // exact state to upload at admission
+  // checkpoints (guarded by the server mutex)
+  bool snap_req = false;         // a caller waits for a snapshot at the next boundary
+  uint64_t snap_seq = 0;         // snapshots taken
+  std::unique_ptr<pgx::Ckpt> snap;
+  bool snap_final = false;       // snap holds the state the job ended in
+  std::vector<uint8_t> blob;     // the last checkpoint taken by pgx_job_checkpoint
 };
 
 template <class T>
@@ -192,6 +206,108 @@ void release_device(pgx_server* s, Job& j) {
   cudaGetLastError();
 }
 
+// Iterations a job reports: grape_optimize counts steps, grape_optimize_ensemble
+// the entries of its fidelity history (GRAPE.jl:1218).
+int own_iterations(const Job& j) { return j.lbfgs ? (int)j.fh.size() : std::max(j.round, 0); }
+
+template <class T>
+std::vector<T> joined(const std::vector<T>& a, const std::vector<T>& b) {
+  std::vector<T> out(a);
+  out.insert(out.end(), b.begin(), b.end());
+  return out;
+}
+
+// Mutex held: the fields of Checkpoint (Checkpoint.jl:64-80) a job's host
+// side knows.  A resumed job's histories are its checkpoint's followed by
+// its own, its iteration count their sum (resume_optimization, :279-287).
+void fill_checkpoint(const Job& j, pgx::Ckpt* c) {
+  pgx_checkpoint_info& I = c->info;
+  I.struct_size = sizeof(pgx_checkpoint_info);
+  I.version = PGX_CHECKPOINT_VERSION;
+  I.system_dim = j.desc.dim;
+  I.n_controls = j.desc.n_controls;
+  I.n_timesteps = j.desc.n_slices;
+  I.n_members = j.desc.n_members;
+  I.iteration = j.prior_iter + own_iterations(j);
+  I.F_opt = j.bestF;
+  I.F = j.F;
+  I.timestamp = pgx::unix_now();
+  I.fingerprint = j.fingerprint;
+  I.opt = j.opt;
+  if (j.converged) I.flags |= PGX_CKPT_CONVERGED;
+  c->prior_iteration = j.prior_iter;
+  c->prior_history_len = (int32_t)j.prior_fh.size();
+  c->prior_gnorm_len = (int32_t)j.prior_gh.size();
+  c->fh = joined(j.prior_fh, j.fh);
+  c->gh = joined(j.prior_gh, j.gh);
+  c->round = j.lbfgs ? j.lb_it : j.round;
+}
+
+// Worker thread, mutex NOT held, job at an iteration boundary (nothing of it
+// in flight): copies its device state into an exact snapshot -- best and
+// current controls, the gradient there, the step-size state (GRAPE) or the
+// (s, y) pairs oldest first (L-BFGS) -- and wakes callers waiting for it.
+int take_snapshot(pgx_server* s, Job& j, bool final_state) {
+  const cudaStream_t stm = s->slots[j.slot].stream;
+  const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+  auto c = std::make_unique<pgx::Ckpt>();
+  c->w.resize(n);
+  c->u.resize(n);
+  c->g.resize(n);
+  auto d2h = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stm) == cudaSuccess;
+  };
+  bool ok = d2h(c->w.data(), j.d_best, n * sizeof(double));
+  int32_t pairs = 0;
+  JobDev h{};
+  pgx::LbState ls{};
+  std::vector<double> S, Y, rho;
+  if (j.lbfgs) {
+    const size_t m = (size_t)j.opt.lbfgs_memory;
+    S.resize(m * n);
+    Y.resize(m * n);
+    rho.resize(m);
+    ok = ok && d2h(c->u.data(), j.ucur, n * sizeof(double)) && d2h(c->g.data(), j.gcur, n * sizeof(double)) &&
+         d2h(&ls, j.lb, sizeof ls) && d2h(S.data(), j.S, m * n * sizeof(double)) &&
+         d2h(Y.data(), j.Yh, m * n * sizeof(double)) && d2h(rho.data(), j.rho, m * sizeof(double));
+  } else {
+    ok = ok && d2h(c->u.data(), j.prob->d_u, n * sizeof(double)) &&
+         d2h(c->g.data(), j.prob->d_G, n * sizeof(double)) && d2h(&h, j.dev, sizeof h);
+  }
+  if (!ok || cudaStreamSynchronize(stm) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  if (j.lbfgs) {
+    const int m = j.opt.lbfgs_memory;
+    if (ls.count < 0 || ls.count > m || ls.head < 0 || ls.head >= m) return PGX_ERR_STATE;
+    pairs = ls.count;
+    c->rho.resize(pairs);
+    c->S.resize((size_t)pairs * n);
+    c->Y.resize((size_t)pairs * n);
+    for (int t = 0; t < pairs; ++t) {  // slot of the t-th oldest pair
+      const int idx = (ls.head - pairs + t + 2 * m) % m;
+      c->rho[t] = rho[idx];
+      std::copy(S.begin() + (size_t)idx * n, S.begin() + (size_t)(idx + 1) * n, c->S.begin() + (size_t)t * n);
+      std::copy(Y.begin() + (size_t)idx * n, Y.begin() + (size_t)(idx + 1) * n, c->Y.begin() + (size_t)t * n);
+    }
+  } else {
+    c->step = h.st.step;
+    c->F_prev = h.st.F_prev;
+    c->step_iter = h.st.iter;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  fill_checkpoint(j, c.get());
+  c->info.flags |= PGX_CKPT_EXACT;
+  c->info.lbfgs_pairs = pairs;
+  j.snap = std::move(c);
+  j.snap_final = final_state;
+  j.snap_req = false;
+  ++j.snap_seq;
+  s->done_cv.notify_all();
+  return PGX_OK;
+}
+
 // Worker thread, mutex held: final bookkeeping of a job that left `running`;
 // frees its slot and budget share.
 void record_end(pgx_server* s, Job& j, int state, const std::string& why) {
@@ -214,8 +330,11 @@ void record_end(pgx_server* s, Job& j, int state, const std::string& why) {
   }
 }
 
+int admit_restored(pgx_server* s, Job& j);
+
 // Creates the job's problem and device block on its slot and enqueues the
-// evaluation at the initial controls.
+// evaluation at the initial controls (a job resumed with its exact state
+// enqueues its next iteration instead).
 int admit(pgx_server* s, Job& j) {
   pgx_ctx* c = s->ctx;
   const Slot& sl = s->slots[j.slot];
@@ -242,6 +361,10 @@ int admit(pgx_server* s, Job& j) {
     pgx::LbState ls{};
     ls.m = mm;
     ls.n = (int)n;
+    if (j.restore) {  // the pairs go to slots 0 .. count-1, oldest first
+      ls.count = (int)j.restore->rho.size();
+      ls.head = ls.count % mm;
+    }
     if (cudaMemcpyAsync(j.lb, &ls, sizeof ls, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess) {
       cudaGetLastError();
       return PGX_ERR_CUDA;
@@ -257,7 +380,8 @@ int admit(pgx_server* s, Job& j) {
   h.F = j.prob->d_F;
   h.len = (int)n;
   h.st = pgx::AscentState{j.opt.step_size, 0.0, 0, 0};
-  j.step = j.opt.step_size;
+  if (j.restore && !j.lbfgs) h.st = pgx::AscentState{j.restore->step, j.restore->F_prev, j.restore->step_iter, 0};
+  j.step = h.st.step;
   if (cudaMemcpyAsync(j.dev, &h, sizeof(JobDev), cudaMemcpyHostToDevice, sl.stream) != cudaSuccess ||
       cudaMemcpyAsync(j.prob->d_u, j.u.data(), n * sizeof(double), cudaMemcpyHostToDevice, sl.stream) !=
           cudaSuccess ||
@@ -265,6 +389,7 @@ int admit(pgx_server* s, Job& j) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
+  if (j.restore) return admit_restored(s, j);
   const int64_t l0 = c->launches;
   if ((st = run_pipeline(j.prob, j.prob->d_u, j.prob->d_F, j.prob->d_G, sl.stream))) return st;
   s->launches += c->launches - l0;
@@ -349,12 +474,15 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
     }
   } else {
     j.step = rb.step;
+    j.gh.push_back(rb.gnorm);  // ||G(u_{round-1})||: the step's gradient
     if (ref_converged(j, rb.gnorm, why)) {
-      j.converged = true;  // F(u_round) is the reference's F_post
+      j.converged = true;  // F(u_round) is the reference's F_post, recorded too
+      j.fh.push_back(rb.F);
       stop = true;
     } else if (rb.F >= s->cfg.target_fidelity) {
       *why = "target fidelity reached";
       j.converged = true;
+      j.fh.push_back(rb.F);
       stop = true;
     } else if (j.round >= j.opt.max_iter) {
       *why = "maximum iterations reached";
@@ -503,11 +631,16 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       j.lb_it = 1;
       j.lb_phase = LB_TRIAL;
       j.lb_bt = 0;
-      if ((st = lb_copy_best(s, j)) || (st = lb_launch(s, j, G_START)) || (st = lb_arm(s, j)))
-        return fail(st, "launch failed");
+      if ((st = lb_copy_best(s, j))) return fail(st, "launch failed");
+      if (j.cancel.load() || j.snap_req) {  // a boundary: the worker snapshots or stops
+        j.lb_boundary = true;
+        return true;
+      }
+      if ((st = lb_launch(s, j, G_START)) || (st = lb_arm(s, j))) return fail(st, "launch failed");
       return true;
     case LB_TRIAL:
       if (j.lb_bt == 0) {
+        j.gh.push_back(rb.lb[1]);  // ||g|| of the iteration (GRAPE.jl:1062)
         j.lb_gnorm = rb.lb[1];
         if (rb.lb[2] != 0.0) {
           j.converged = true;
@@ -561,6 +694,16 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       }
       j.lb_phase = LB_TRIAL;
       j.lb_bt = 0;
+      if (j.cancel.load() || j.snap_req) {  // a boundary: accept only, the worker goes on
+        if (pgx::launch_lb_accept(lb_args(j), s->slots[j.slot].stream) != cudaSuccess) {
+          cudaGetLastError();
+          return fail(PGX_ERR_CUDA, "launch failed");
+        }
+        s->launches += 1;
+        if (improved && (st = lb_copy_best(s, j))) return fail(st, "launch failed");
+        j.lb_boundary = true;
+        return true;
+      }
       // the graph's accept updates u before its trial point reads it; the
       // best copy follows the graph (nothing in it writes u after the accept)
       if ((st = lb_launch(s, j, G_ACC_START)) || (improved && (st = lb_copy_best(s, j))) || (st = lb_arm(s, j)))
@@ -583,6 +726,52 @@ int launch_iteration(pgx_server* s, Job& j) {
   s->launches += j.iter_kernels;
   j.inflight = true;
   return PGX_OK;
+}
+
+// The first step of the next L-BFGS iteration after a boundary.
+int lb_start(pgx_server* s, Job& j) {
+  j.lb_boundary = false;
+  int st = lb_launch(s, j, G_START);
+  if (!st) st = lb_arm(s, j);
+  return st;
+}
+
+// Admission of a job resumed with its exact state: the gradient, objective,
+// best controls and L-BFGS pairs join the controls admit() uploaded, the
+// host bookkeeping takes the snapshot's, and the job's next iteration is
+// enqueued as if it had never stopped.
+int admit_restored(pgx_server* s, Job& j) {
+  const pgx::Ckpt& r = *j.restore;
+  const Slot& sl = s->slots[j.slot];
+  const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+  const size_t pairs = r.rho.size();
+  auto h2d = [&](void* dst, const void* src, size_t bytes) {
+    return bytes == 0 || cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, sl.stream) == cudaSuccess;
+  };
+  bool ok = h2d(j.prob->d_G, r.g.data(), n * sizeof(double)) && h2d(j.prob->d_F, &r.info.F, sizeof(double)) &&
+            h2d(j.d_best, r.w.data(), n * sizeof(double));
+  if (j.lbfgs)
+    ok = ok && h2d(j.S, r.S.data(), pairs * n * sizeof(double)) &&
+         h2d(j.Yh, r.Y.data(), pairs * n * sizeof(double)) && h2d(j.rho, r.rho.data(), pairs * sizeof(double));
+  if (!ok || cudaStreamSynchronize(sl.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return PGX_ERR_CUDA;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    j.F = r.info.F;
+    j.bestF = r.info.F_opt;
+    if (j.lbfgs) {
+      j.round = (int)j.fh.size() - 1;
+      j.lb_it = r.round;
+      j.lb_phase = LB_TRIAL;
+      j.lb_bt = 0;
+    } else {
+      j.round = r.round;
+    }
+  }
+  j.restore.reset();
+  return j.lbfgs ? lb_start(s, j) : launch_iteration(s, j);
 }
 
 void worker_loop(pgx_server* s) {
@@ -641,19 +830,28 @@ void worker_loop(pgx_server* s) {
       int err = (q == cudaSuccess) ? PGX_OK : PGX_ERR_CUDA;
       cudaGetLastError();
       const char* why = "evaluation failed";
-      bool go = false;
+      bool go = false, want_snap = false;
       if (!err) {
         const Readback rb = *sl.hb;
         if (!j->lbfgs || j->lb_grad_eval) s->units += j->units;
         std::lock_guard<std::mutex> lk(s->mu);  // polls read what advance() updates
         go = j->lbfgs ? advance_lbfgs(s, *j, rb, &why, &err) : advance(s, *j, rb, &why, &err);
+        want_snap = j->snap_req;
       }
+      // An iteration boundary: the job continues and nothing of it is in
+      // flight.  Cancellation and snapshots happen only here, so a cancelled
+      // job's state is one an exact resumption can continue from.
+      const bool boundary = go && (!j->lbfgs || j->lb_boundary);
       bool cancelled = false;
-      if (go && j->cancel.load()) {
+      if (boundary && j->cancel.load()) {
         go = false;
         cancelled = true;
       }
-      if (go && !j->lbfgs) err = launch_iteration(s, *j);
+      if (boundary && (cancelled || want_snap)) {
+        const int st = take_snapshot(s, *j, cancelled);
+        if (st && !cancelled) err = st;  // a cancelled job keeps its host-side checkpoint
+      }
+      if (go && !err) err = !j->lbfgs ? launch_iteration(s, *j) : j->lb_boundary ? lb_start(s, *j) : PGX_OK;
       if (go && !err) continue;
       ended.push_back(j);
       if (err) {
@@ -696,7 +894,7 @@ void fill_status(const Job& j, pgx_job_status* out) {
   std::memset(out, 0, sizeof(*out));
   out->state = j.state;
   out->status = j.status;
-  out->iterations = std::max(j.round, 0);
+  out->iterations = j.prior_iter + own_iterations(j);
   out->fidelity = j.F;
   out->best_fidelity = j.bestF;
   const auto now = clk::now();
@@ -787,9 +985,11 @@ extern "C" int pgx_server_destroy(pgx_server* s) {
   return PGX_OK;
 }
 
-extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
-                          uint64_t* job_id) {
-  if (!s || !d || !o || !u0 || !job_id) return PGX_ERR_INVALID;
+namespace {
+
+// Validates a submission and builds its job (owned copies of every array).
+int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
+             std::shared_ptr<Job>* out) {
   pgx_ctx* c = s->user;
   int st = validate_desc(c, d);
   if (st) return st;
@@ -815,6 +1015,7 @@ extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_op
   if (s->cfg.hbm_budget_bytes && j->footprint > s->cfg.hbm_budget_bytes)
     return ctx_fail(c, PGX_ERR_BUDGET, "job footprint exceeds the server's HBM budget");
   j->units = (int64_t)nm * (int64_t)nt;
+  j->fingerprint = pgx::problem_fingerprint(d);
   j->dt = copy_of(d->dt, nt);
   j->drifts = copy_of(d->drifts, 2 * DD * d->n_drifts);
   j->controls = copy_of(d->controls, 2 * DD * nc);
@@ -843,6 +1044,11 @@ extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_op
   j->desc.grad_states_init = P(j->sgrad);
   j->opt = *o;
   j->u.assign(u0, u0 + nc * nt);
+  *out = std::move(j);
+  return PGX_OK;
+}
+
+int enqueue(pgx_server* s, std::shared_ptr<Job> j, uint64_t* job_id) {
   j->t_submit = clk::now();
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -854,6 +1060,131 @@ extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_op
     *job_id = j->id;
   }
   s->cv.notify_all();
+  return PGX_OK;
+}
+
+std::shared_ptr<Job> find_job(pgx_server* s, uint64_t id) {
+  auto it = s->jobs.find(id);
+  return it == s->jobs.end() ? nullptr : it->second;
+}
+
+}  // namespace
+
+extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
+                          uint64_t* job_id) {
+  if (!s || !d || !o || !u0 || !job_id) return PGX_ERR_INVALID;
+  std::shared_ptr<Job> j;
+  const int st = make_job(s, d, o, u0, &j);
+  return st ? st : enqueue(s, std::move(j), job_id);
+}
+
+extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const void* blob,
+                                 uint64_t blob_len, int32_t mode, uint64_t* job_id) {
+  if (!s || !d || !blob || !job_id) return PGX_ERR_INVALID;
+  pgx_ctx* c = s->user;
+  if (mode != PGX_RESUME_RESTART && mode != PGX_RESUME_CONTINUE)
+    return ctx_fail(c, PGX_ERR_INVALID, "mode must be PGX_RESUME_RESTART or PGX_RESUME_CONTINUE");
+  auto ck = std::make_unique<pgx::Ckpt>();
+  std::string why;
+  if (pgx::ckpt_decode(blob, blob_len, ck.get(), &why)) return ctx_fail(c, PGX_ERR_INVALID, why.c_str());
+  const pgx_checkpoint_info& I = ck->info;
+  char msg[160];
+  if (I.system_dim > 0 && I.system_dim != d->dim) {  // Checkpoint.jl:236-240
+    std::snprintf(msg, sizeof msg, "System dimension mismatch: checkpoint has dim=%d, provided system has dim=%d",
+                  I.system_dim, d->dim);
+    return ctx_fail(c, PGX_ERR_INVALID, msg);
+  }
+  if (I.n_controls != d->n_controls) {  // Checkpoint.jl:242-246
+    std::snprintf(msg, sizeof msg, "n_controls mismatch: checkpoint=%d, system=%d", I.n_controls, d->n_controls);
+    return ctx_fail(c, PGX_ERR_INVALID, msg);
+  }
+  if (I.n_timesteps != d->n_slices) {
+    std::snprintf(msg, sizeof msg, "n_timesteps mismatch: checkpoint=%d, problem=%d", I.n_timesteps, d->n_slices);
+    return ctx_fail(c, PGX_ERR_DIMS, msg);
+  }
+  const pgx_opt_desc opt = o ? *o : I.opt;
+  const bool cont = mode == PGX_RESUME_CONTINUE;
+  if (cont) {
+    if (!(I.flags & PGX_CKPT_EXACT))
+      return ctx_fail(c, PGX_ERR_INVALID, "exact continuation needs a snapshot of a running or cancelled job");
+    if (validate_desc(c, d)) return PGX_ERR_INVALID;
+    if (pgx::problem_fingerprint(d) != I.fingerprint)
+      return ctx_fail(c, PGX_ERR_INVALID, "the checkpoint was taken on a different problem");
+    if (opt.method != I.opt.method)
+      return ctx_fail(c, PGX_ERR_INVALID, "exact continuation keeps the checkpoint's method");
+    if (opt.method == PGX_OPT_ENSEMBLE_LBFGS && opt.lbfgs_memory < I.lbfgs_pairs)
+      return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory is below the checkpoint's stored pairs");
+  }
+  std::shared_ptr<Job> j;
+  const int st = make_job(s, d, &opt, cont ? ck->u.data() : ck->w.data(), &j);
+  if (st) return st;
+  if (cont) {  // the run goes on: its own histories continue, earlier runs' stay ahead
+    j->prior_iter = ck->prior_iteration;
+    j->prior_fh.assign(ck->fh.begin(), ck->fh.begin() + ck->prior_history_len);
+    j->prior_gh.assign(ck->gh.begin(), ck->gh.begin() + ck->prior_gnorm_len);
+    j->fh.assign(ck->fh.begin() + ck->prior_history_len, ck->fh.end());
+    j->gh.assign(ck->gh.begin() + ck->prior_gnorm_len, ck->gh.end());
+    j->restore = std::move(ck);
+  } else {  // resume_optimization: a fresh run after the checkpoint's
+    j->prior_iter = I.iteration;
+    j->prior_fh = std::move(ck->fh);
+    j->prior_gh = std::move(ck->gh);
+  }
+  return enqueue(s, std::move(j), job_id);
+}
+
+extern "C" int pgx_job_checkpoint(pgx_server* s, uint64_t id, double timeout_s, uint64_t* blob_len) {
+  if (!s || !blob_len) return PGX_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  const std::shared_ptr<Job> jp = find_job(s, id);
+  if (!jp) return PGX_ERR_INVALID;
+  Job& j = *jp;
+  if (j.state == PGX_JOB_QUEUED) return PGX_ERR_STATE;
+  if (j.state == PGX_JOB_RUNNING) {
+    const uint64_t seq0 = j.snap_seq;
+    j.snap_req = true;
+    const auto ready = [&] { return j.snap_seq != seq0 || j.state != PGX_JOB_RUNNING; };
+    if (timeout_s <= 0) {
+      s->done_cv.wait(lk, ready);
+    } else if (!s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
+      return PGX_ERR_TIMEOUT;
+    }
+  }
+  if (j.state == PGX_JOB_RUNNING || (j.snap && j.snap_final)) {
+    j.blob = pgx::ckpt_encode(*j.snap);
+  } else {  // finished: the final best controls and histories
+    if (j.round < 0 || j.u.size() != (size_t)j.desc.n_controls * j.desc.n_slices) return PGX_ERR_STATE;
+    pgx::Ckpt c;
+    fill_checkpoint(j, &c);
+    c.w = j.u;
+    j.blob = pgx::ckpt_encode(c);
+  }
+  *blob_len = j.blob.size();
+  return PGX_OK;
+}
+
+extern "C" int pgx_job_checkpoint_read(pgx_server* s, uint64_t id, void* blob, uint64_t cap) {
+  if (!s || !blob) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  const std::shared_ptr<Job> j = find_job(s, id);
+  if (!j) return PGX_ERR_INVALID;
+  if (j->blob.empty()) return PGX_ERR_STATE;
+  if (cap < j->blob.size()) return PGX_ERR_DIMS;
+  std::memcpy(blob, j->blob.data(), j->blob.size());
+  return PGX_OK;
+}
+
+extern "C" int pgx_job_history(pgx_server* s, uint64_t id, double* fh, double* gh, int32_t cap, int32_t* n_f,
+                               int32_t* n_g) {
+  if (!s || cap < 0) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  const std::shared_ptr<Job> j = find_job(s, id);
+  if (!j) return PGX_ERR_INVALID;
+  const std::vector<double> f = joined(j->prior_fh, j->fh), g = joined(j->prior_gh, j->gh);
+  if (n_f) *n_f = (int32_t)f.size();
+  if (n_g) *n_g = (int32_t)g.size();
+  if (fh) std::copy(f.begin(), f.begin() + std::min<size_t>(f.size(), (size_t)cap), fh);
+  if (gh) std::copy(g.begin(), g.begin() + std::min<size_t>(g.size(), (size_t)cap), gh);
   return PGX_OK;
 }
 
@@ -878,7 +1209,9 @@ extern "C" int pgx_fetch(pgx_server* s, uint64_t id, double* u, pgx_opt_result* 
     res->fidelity = j.bestF;
     res->total_time_s = secs(j.t_submit, j.t_end);
     res->step_size_final = j.lbfgs ? j.opt.step_size : j.step;
-    res->n_iterations = j.lbfgs ? (int)j.fh.size() : std::max(j.round, 0);
+    res->n_iterations = j.prior_iter + own_iterations(j);
+    res->history_len = (int32_t)(j.prior_fh.size() + j.fh.size());
+    res->gnorm_history_len = (int32_t)(j.prior_gh.size() + j.gh.size());
     res->converged = j.converged;
     res->n_fidelity_evals = j.round + 1;
     res->n_gradient_evals = j.round + 1;

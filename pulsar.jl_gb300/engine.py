@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 from typing import Optional
 
 import numpy as np
@@ -185,6 +185,104 @@ class JobResult:
     termination_reason: str
     latency_s: float
     step_size_final: float
+    fidelity_history: list = field(default_factory=list)
+    gradient_norm_history: list = field(default_factory=list)
+    n_fidelity_evaluations: int = 0
+    n_gradient_evaluations: int = 0
+
+
+OPT_NAMES = {v: k for k, v in A.OPT.items()}
+
+
+def opt_settings(o: "A.OptDesc") -> dict:
+    """pgx_opt_desc -> (method name, opt_desc keywords)."""
+    kw = {k: getattr(o, k) for k in ("max_iter", "convergence_tol", "step_size", "min_step_size",
+                                     "max_step_size", "gradient_norm_tol", "lbfgs_memory",
+                                     "amplitude_limit", "l_bound", "u_bound")}
+    kw["adapt_step_size"] = bool(o.adapt_step_size)
+    return {"method": OPT_NAMES.get(int(o.method), str(o.method)), **kw}
+
+
+def checkpoint_parse(blob: bytes) -> dict:
+    """Verify and decode a checkpoint blob on the host (pgx_checkpoint_parse):
+    its Checkpoint fields (Checkpoint.jl:64-80) with w_opt as [n_c, n_t]."""
+    b = bytes(blob)
+    info = A.CheckpointInfo()
+    buf = C.create_string_buffer(b, len(b))
+    A.check(A.lib().pgx_checkpoint_parse(buf, len(b), C.byref(info), None, None, None))
+    n_c, n_t = info.n_controls, info.n_timesteps
+    w = np.zeros(n_c * n_t)
+    fh = np.zeros(max(info.history_len, 1))
+    gh = np.zeros(max(info.gnorm_history_len, 1))
+    A.check(A.lib().pgx_checkpoint_parse(buf, len(b), C.byref(info), A.as_dptr(w), A.as_dptr(fh),
+                                         A.as_dptr(gh)))
+    return {"w_opt": w.reshape(n_t, n_c).T.copy(), "F_opt": info.F_opt, "F": info.F,
+            "n_controls": n_c, "n_timesteps": n_t, "iteration": info.iteration,
+            "fidelity_history": fh[:info.history_len].tolist(),
+            "gradient_norm_history": gh[:info.gnorm_history_len].tolist(),
+            "system_dim": info.system_dim, "n_members": info.n_members, "timestamp": info.timestamp,
+            "fingerprint": int(info.fingerprint), "exact": bool(info.flags & A.CKPT_EXACT),
+            "converged": bool(info.flags & A.CKPT_CONVERGED), "lbfgs_pairs": info.lbfgs_pairs,
+            "optimizer": opt_settings(info.opt), "metadata": _checkpoint_metadata(buf, len(b), info.metadata_len)}
+
+
+def _checkpoint_metadata(buf, n: int, m: int) -> bytes:
+    out = C.create_string_buffer(max(m, 1))
+    A.check(A.lib().pgx_checkpoint_metadata(buf, n, out, m))
+    return out.raw[:m]
+
+
+def checkpoint_set_metadata(blob: bytes, metadata: bytes) -> bytes:
+    """The same checkpoint with its metadata section replaced (pgx_checkpoint_set_metadata)."""
+    b, m = bytes(blob), bytes(metadata)
+    need = C.c_uint64()
+    A.check(A.lib().pgx_checkpoint_set_metadata(b, len(b), m, len(m), None, 0, C.byref(need)))
+    out = C.create_string_buffer(need.value)
+    A.check(A.lib().pgx_checkpoint_set_metadata(b, len(b), m, len(m), out, need.value, C.byref(need)))
+    return out.raw[:need.value]
+
+
+def checkpoint_create(w_opt, F_opt: float, *, iteration: int = 0, fidelity_history=(),
+                      gradient_norm_history=(), system_dim: int = 0, n_members: int = 0,
+                      converged: bool = False, timestamp: float = 0.0, fingerprint: int = 0,
+                      method: str = "grape", opt: Optional[dict] = None, metadata: bytes = b"") -> bytes:
+    """create_checkpoint (Checkpoint.jl:143-164) as a warm-start blob
+    (pgx_checkpoint_create); w_opt is [n_c, n_t]."""
+    w = np.asarray(w_opt, np.float64)
+    if w.ndim != 2:
+        raise ValueError("w_opt must be a [n_controls, n_timesteps] matrix")
+    n_c, n_t = w.shape
+    wb = np.ascontiguousarray(w.T.ravel())
+    fh = np.ascontiguousarray(np.asarray(list(fidelity_history), np.float64))
+    gh = np.ascontiguousarray(np.asarray(list(gradient_norm_history), np.float64))
+    info = A.CheckpointInfo()
+    info.struct_size = C.sizeof(A.CheckpointInfo)
+    info.version = 1
+    info.flags = A.CKPT_CONVERGED if converged else 0
+    info.system_dim, info.n_controls, info.n_timesteps = int(system_dim), n_c, n_t
+    info.n_members, info.iteration = int(n_members), int(iteration)
+    info.history_len, info.gnorm_history_len = fh.size, gh.size
+    info.F_opt, info.F, info.timestamp = float(F_opt), float(F_opt), float(timestamp)
+    info.fingerprint = int(fingerprint)
+    info.opt = opt_desc(method, **(opt or {}))
+    meta = bytes(metadata)
+    info.metadata_len = len(meta)
+    need = C.c_uint64()
+    fp = A.as_dptr(fh) if fh.size else None
+    gp = A.as_dptr(gh) if gh.size else None
+    A.check(A.lib().pgx_checkpoint_create(C.byref(info), A.as_dptr(wb), fp, gp, meta, None, 0, C.byref(need)))
+    out = C.create_string_buffer(need.value)
+    A.check(A.lib().pgx_checkpoint_create(C.byref(info), A.as_dptr(wb), fp, gp, meta, out, need.value,
+                                          C.byref(need)))
+    return out.raw[:need.value]
+
+
+def problem_fingerprint(drifts, controls, dt, **problem) -> int:
+    """FNV-1a-64 of the problem descriptor (what an exact resumption checks)."""
+    d, keep, _ = problem_desc(drifts, controls, dt, **problem)
+    fp = C.c_uint64()
+    A.check(A.lib().pgx_problem_fingerprint(C.byref(d), C.byref(fp)))
+    return int(fp.value)
 
 
 class Server:
@@ -231,6 +329,51 @@ class Server:
         self._shape[int(jid.value)] = (n_c, n_t)
         return int(jid.value)
 
+    def submit_resume(self, drifts, controls, dt, checkpoint: bytes, *, mode: str = "restart",
+                      opt: Optional[dict] = None, method: Optional[str] = None, **problem) -> int:
+        """Queue a job resumed from a checkpoint blob.  ``mode`` "restart" is
+        resume_optimization (Checkpoint.jl:220-298): a fresh run from w_opt
+        whose histories and iteration count follow the checkpoint's (opt's
+        max_iter = the additional iterations); "continue" resumes an exact
+        snapshot bit-identically.  With neither opt nor method the
+        checkpoint's own settings are used."""
+        d, keep, (D, n_c, n_t, _, _) = problem_desc(drifts, controls, dt, **problem)
+        b = bytes(checkpoint)
+        buf = C.create_string_buffer(b, len(b))
+        o = None
+        if opt is not None or method is not None:
+            base = checkpoint_parse(b)["optimizer"]
+            kw = {k: v for k, v in base.items() if k != "method"}
+            kw.update(opt or {})
+            o = opt_desc(method or base["method"], **kw)
+        jid = C.c_uint64()
+        A.check(A.lib().pgx_submit_resume(self._h, C.byref(d), C.byref(o) if o is not None else None, buf,
+                                          len(b), A.RESUME[mode], C.byref(jid)), self.ctx.handle)
+        self._shape[int(jid.value)] = (n_c, n_t)
+        return int(jid.value)
+
+    def checkpoint(self, job_id: int, timeout_s: float = 0.0) -> bytes:
+        """Checkpoint blob of a job: a running job is snapshotted at its next
+        iteration boundary; a finished one gives its final state."""
+        n = C.c_uint64()
+        rc = A.lib().pgx_job_checkpoint(self._h, int(job_id), float(timeout_s), C.byref(n))
+        if rc == 7:
+            raise TimeoutError("no iteration boundary within the timeout")
+        A.check(rc)
+        out = C.create_string_buffer(n.value)
+        A.check(A.lib().pgx_job_checkpoint_read(self._h, int(job_id), out, n.value))
+        return out.raw[:n.value]
+
+    def history(self, job_id: int):
+        """(fidelity history, gradient-norm history) of a job so far."""
+        nf, ng = C.c_int32(), C.c_int32()
+        A.check(A.lib().pgx_job_history(self._h, int(job_id), None, None, 0, C.byref(nf), C.byref(ng)))
+        cap = max(nf.value, ng.value, 1)
+        fh, gh = np.zeros(cap), np.zeros(cap)
+        A.check(A.lib().pgx_job_history(self._h, int(job_id), A.as_dptr(fh), A.as_dptr(gh), cap, C.byref(nf),
+                                        C.byref(ng)))
+        return fh[:nf.value].tolist(), gh[:ng.value].tolist()
+
     def poll(self, job_id: int) -> dict:
         st = A.JobStatus()
         A.check(A.lib().pgx_poll(self._h, int(job_id), C.byref(st)))
@@ -241,6 +384,10 @@ class Server:
     def fetch(self, job_id: int) -> JobResult:
         """Result of a finished job (raises PgxError(9) while it runs)."""
         n_c, n_t = self._shape[int(job_id)]
+        st = self.poll(job_id)["state"]
+        if st in ("queued", "running"):
+            A.check(9)
+        fh, gh = self.history(job_id)
         u = np.zeros(n_c * n_t)
         r = A.OptResult()
         rc = A.lib().pgx_fetch(self._h, int(job_id), A.as_dptr(u), C.byref(r))
@@ -250,7 +397,7 @@ class Server:
         state = "done" if rc == 0 else ("cancelled" if rc == 8 else "failed")
         return JobResult(int(job_id), state, u.reshape(n_t, n_c).T.copy(), r.fidelity, int(r.n_iterations),
                          bool(r.converged), r.reason.decode(errors="replace"), r.total_time_s,
-                         r.step_size_final)
+                         r.step_size_final, fh, gh, int(r.n_fidelity_evals), int(r.n_gradient_evals))
 
     def cancel(self, job_id: int):
         A.check(A.lib().pgx_cancel(self._h, int(job_id)))

@@ -19,6 +19,11 @@
 // evaluation at a time instead: the direction, the trial points of the
 // backtracking line search and the history update are device kernels on the
 // job's stream (pgx_lbfgs.cu); each step reads back (F, max|d|, ||g||).
+// Checkpoints: at an iteration boundary (nothing of the job in flight) the
+// worker can copy a job's device state out -- on request, or when the job is
+// cancelled -- and a job submitted with that snapshot uploads it back and
+// continues with the iteration that would have come next (pgx_ckpt.h holds
+// the state, pgx_checkpoint.cpp its byte encoding).
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -97,12 +97,26 @@ typedef struct pgx_problem_desc {
                                      the target here (Gradients.jl:153-157).      */
 } pgx_problem_desc;
 
+/* Oracle-free error estimate of an evaluation, the largest over members:
+ *   UNITARITY  gate, Hermitian:      max_ij |(U'U - I)_ij| of U_total
+ *   TRACE      gate, Liouvillian:    max_c |sum_i Phi[i + N i, c] - [c = j + N j]|,
+ *              the trace-preservation defect of Phi = U_total
+ *   NORM       states, Hermitian:    max_s | ||psi_s(T)||^2 - ||psi_s(0)||^2 |
+ *   STATE_TRACE states, Liouvillian: max_s |Tr rho_s(T) - Tr rho_s(0)|
+ * (state targets: evaluations that compute G; NONE otherwise).  The mixed
+ * path has no refinement step, so this is its only a-posteriori check.     */
+enum { PGX_RESID_NONE = 0, PGX_RESID_UNITARITY = 1, PGX_RESID_TRACE = 2, PGX_RESID_NORM = 3,
+       PGX_RESID_STATE_TRACE = 4 };
+
 typedef struct pgx_eval_stats {
   double ms_device;            /* device time of the call (CUDA events)           */
   double ms_host;              /* wall time of the call                           */
   int64_t units;               /* member-slice units processed                    */
-  int32_t n_launches;          /* kernels launched by the call                    */
+  int32_t n_launches;          /* kernels launched by the call (residual excluded) */
   int32_t max_taylor_degree;   /* largest degree chosen (0 = not recorded)        */
+  double residual;             /* PGX_RESID_* estimate (after the timed region)   */
+  int32_t residual_kind;       /* PGX_RESID_*                                      */
+  int32_t reserved;
 } pgx_eval_stats;
 
 typedef struct pgx_ctx pgx_ctx;
@@ -251,6 +265,14 @@ int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report,
 #define PGX_TUNE_GRAD 1
 int pgx_problem_set_team(pgx_problem* prob, int32_t kernel, int32_t team);
 int pgx_problem_get_team(const pgx_problem* prob, int32_t kernel, int32_t* team);
+/* Plans: pgx_autotune records its choice process-wide under (device, padded
+ * dimension, n_controls, generator, target, precision, grad_mode), and
+ * problems created later with the same key -- on any context, a server's
+ * private one included -- start from it.  pgx_plan_lookup reports the plan
+ * for a descriptor (PGX_ERR_STATE and zeros when none); pgx_plan_clear
+ * forgets every plan.  Plans never change results, only time.              */
+int pgx_plan_lookup(int device, const pgx_problem_desc* desc, int32_t* team_expm, int32_t* team_grad);
+int pgx_plan_clear(void);
 
 /* ---- allocation-free total propagator ----------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

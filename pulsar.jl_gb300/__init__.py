@@ -8,8 +8,8 @@ through ``__graft_entry__.load_package()``.
 """
 from . import _abi
 from .engine import (Batch, Context, Problem, Server, checkpoint_create, checkpoint_parse,
-                     checkpoint_set_metadata, default_context, opt_desc, problem_desc,
-                     problem_fingerprint)
+                     checkpoint_set_metadata, default_context, opt_desc, plan_clear, plan_lookup,
+                     problem_desc, problem_fingerprint)
 from .checkpoint import (Checkpoint, auto_checkpoint_callback, checkpoint_compatible, checkpoint_summary,
                          create_checkpoint, list_checkpoints, load_checkpoint, resume_optimization,
                          save_checkpoint)

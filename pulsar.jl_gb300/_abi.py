@@ -44,7 +44,11 @@ class ProblemDesc(C.Structure):
 
 class EvalStats(C.Structure):
     _fields_ = [("ms_device", C.c_double), ("ms_host", C.c_double), ("units", C.c_int64),
-                ("n_launches", C.c_int32), ("max_taylor_degree", C.c_int32)]
+                ("n_launches", C.c_int32), ("max_taylor_degree", C.c_int32), ("residual", C.c_double),
+                ("residual_kind", C.c_int32), ("reserved", C.c_int32)]
+
+
+RESIDUAL_KIND = {0: "none", 1: "unitarity", 2: "trace", 3: "norm", 4: "state_trace"}
 
 
 class OptDesc(C.Structure):
@@ -152,6 +156,8 @@ SIGNATURES = {
     "pgx_penalty_eval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, dptr, dptr, C.c_void_p, dptr, dptr]),
     "pgx_problem_set_team": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "pgx_plan_lookup": (C.c_int, [C.c_int, C.POINTER(ProblemDesc), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "pgx_plan_clear": (C.c_int, []),
     "pgx_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "pgx_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -152,6 +152,10 @@ cudaError_t launch_chain_fwd(const ProbDev& p, const WorkDev& w, const LaunchInf
 cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad);
+// Largest PGX_RESID_* residual over members into *out (bits of a
+// non-negative double; *out must hold 0 before the launch).
+cudaError_t launch_residual(const ProbDev& p, const WorkDev& w, int kind, int N, unsigned long long* out,
+                            const LaunchInfo& li);
 // G[q] = sum_i coef[i] Gm[idx[i]][q] (len = n_c n_t), in the order of idx.
 cudaError_t launch_select_sum(const double* Gm, const int* idx, const double* coef, int n_sel, int len, double* G,
                               const LaunchInfo& li);

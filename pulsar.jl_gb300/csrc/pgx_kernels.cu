@@ -23,6 +23,7 @@
 #include <set>
 #include <utility>
 
+#include "pgx.h"
 #include "pgx_stages.cuh"
 
 namespace pgx {
@@ -439,6 +440,71 @@ __global__ void k_reduce(ProbDev p, WorkDev w, int want_grad) {
   }
 }
 
+// Oracle-free residual of one evaluation (the PGX_RESID_* kinds of pgx.h),
+// one block per member.  Non-negative doubles order like their bit patterns,
+// so atomicMax on the bits gives the exact maximum in any order; a NaN (sign
+// cleared) sorts above +inf and survives.
+constexpr int kResidThreads = 256;
+
+__global__ void __launch_bounds__(kResidThreads) k_residual(ProbDev p, WorkDev w, int kind, int N,
+                                                            unsigned long long* out) {
+  __shared__ double red[kResidThreads];
+  const int m = blockIdx.x;
+  const int Dp = p.Dp, D = p.D;
+  double r = 0.0;
+  auto keep = [&r](double v) {
+    v = fabs(v);
+    if (!(v <= r)) r = v;
+  };
+  if (kind == PGX_RESID_UNITARITY) {
+    const double2* U = w.Utot + (size_t)m * Dp * Dp;
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      const int i = e % D, j = e / D;
+      double2 acc = make_double2(i == j ? -1.0 : 0.0, 0.0);
+      for (int k = 0; k < D; ++k) acc = cmac_cj(acc, U[k + (size_t)Dp * i], U[k + (size_t)Dp * j]);
+      keep(hypot(acc.x, acc.y));
+    }
+  } else if (kind == PGX_RESID_TRACE) {
+    const double2* U = w.Utot + (size_t)m * Dp * Dp;
+    for (int c = threadIdx.x; c < D; c += blockDim.x) {
+      double sx = c % (N + 1) == 0 ? -1.0 : 0.0, sy = 0.0;
+      for (int i = 0; i < N; ++i) {
+        const double2 v = U[(i + N * i) + (size_t)Dp * c];
+        sx += v.x;
+        sy += v.y;
+      }
+      keep(hypot(sx, sy));
+    }
+  } else {
+    const size_t pan = (size_t)p.n_pairs * Dp;
+    const double2* p0 = w.psi + (size_t)m * (p.n_t + 1) * pan;
+    const double2* pT = p0 + (size_t)p.n_t * pan;
+    for (int s = threadIdx.x; s < p.n_pairs; s += blockDim.x) {
+      double ax = 0.0, ay = 0.0;
+      if (kind == PGX_RESID_NORM) {
+        for (int i = 0; i < D; ++i) {
+          const double2 a = pT[(size_t)s * Dp + i], b = p0[(size_t)s * Dp + i];
+          ax += (a.x * a.x + a.y * a.y) - (b.x * b.x + b.y * b.y);
+        }
+      } else {
+        for (int i = 0; i < N; ++i) {
+          const double2 a = pT[(size_t)s * Dp + i + N * i], b = p0[(size_t)s * Dp + i + N * i];
+          ax += a.x - b.x;
+          ay += a.y - b.y;
+        }
+      }
+      keep(hypot(ax, ay));
+    }
+  }
+  red[threadIdx.x] = r;
+  __syncthreads();
+  for (int h = kResidThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h && !(red[threadIdx.x + h] <= red[threadIdx.x])) red[threadIdx.x] = red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(red[0]));
+}
+
 // G[q] = sum_i coef[i] Gm[idx[i]][q], members in the order given (the
 // worst-case and CVaR ensemble gradients).
 __global__ void k_select_sum(const double* Gm, const int* idx, const double* coef, int n_sel, int len, double* G) {
@@ -583,6 +649,13 @@ cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& 
   const int n = p.n_t * p.n_c;
   const int grid = want_grad ? (n + 255) / 256 : 1;
   k_reduce<<<grid, 256, 0, li.stream>>>(p, w, want_grad ? 1 : 0);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_residual(const ProbDev& p, const WorkDev& w, int kind, int N, unsigned long long* out,
+                            const LaunchInfo& li) {
+  k_residual<<<p.n_members, kResidThreads, 0, li.stream>>>(p, w, kind, N, out);
   ++*li.launches;
   return cudaGetLastError();
 }

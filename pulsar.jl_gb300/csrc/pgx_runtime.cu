@@ -13,8 +13,11 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "pgx.h"
@@ -340,7 +343,7 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
                                  sizeof(float2) * ((size_t)d->n_slices + 2 * (size_t)d->n_members) + s.u
                            : 0);
   return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
-         2 * sizeof(double) + consts + mixed;
+         3 * sizeof(double) + consts + mixed;
 }
 
 int validate_desc(pgx_ctx* c, const pgx_problem_desc* d) { return validate(c, d); }
@@ -414,6 +417,41 @@ static int upload(pgx_problem* p, T** dptr, const std::vector<T>& host) {
   // pageable source: the call returns once `host` has been staged
   return ctx_cuda(p->ctx, cudaMemcpyAsync(*dptr, host.data(), host.size() * sizeof(T),
                                           cudaMemcpyHostToDevice, p->ctx->stream), "upload");
+}
+
+// Tuned plans (team sizes of the tunable kernels), process-wide: pgx_autotune
+// records its choice under (device, padded dimension, n_controls, generator,
+// target, precision, grad_mode) and every problem created later with the same
+// key -- on any context, the server's private one included -- starts with it.
+// Team sizes never change results (the variants are bit-identical), so a plan
+// only moves time.
+namespace {
+using PlanKey = std::tuple<int, int, int, int, int, int, int>;
+std::mutex g_plan_mu;
+std::map<PlanKey, std::pair<int, int>> g_plans;
+
+PlanKey plan_key(int device, const pgx_problem_desc* d) {
+  return PlanKey{device, pad_dim(d->dim), d->n_controls, d->generator, d->target, d->precision, d->grad_mode};
+}
+}  // namespace
+
+extern "C" int pgx_plan_lookup(int device, const pgx_problem_desc* d, int32_t* team_expm, int32_t* team_grad) {
+  if (!d || !team_expm || !team_grad || d->dim < 1 || d->dim > pgx::kMaxDim) return PGX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  const auto it = g_plans.find(plan_key(device, d));
+  if (it == g_plans.end()) {
+    *team_expm = *team_grad = 0;
+    return PGX_ERR_STATE;
+  }
+  *team_expm = it->second.first;
+  *team_grad = it->second.second;
+  return PGX_OK;
+}
+
+extern "C" int pgx_plan_clear(void) {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  g_plans.clear();
+  return PGX_OK;
 }
 
 extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_problem** out) {
@@ -532,7 +570,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   w.slab_teams = pgx::slab_team_count(Dp, c->num_sms);
   p->d_u = (double*)A(s.u);
   p->d_G = (double*)A(s.G);
-  p->d_F = (double*)A(2 * sizeof(double));
+  p->d_F = (double*)A(3 * sizeof(double));  // objective, gradient-pass scratch, residual bits
   if (d->precision == PGX_PREC_MIXED) w.u_df = (float2*)A(s.u);
   p->d_pen = (pgx_penalty*)A(sizeof(pgx_penalty) * PGX_MAX_PENALTIES);
   pit_shape(d, Dp, c->num_sms, &w.pit_blocks, &w.pit_len);
@@ -550,6 +588,14 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "upload sync"))) {
     pgx_problem_destroy(p);
     return st;
+  }
+  if (d->precision == PGX_PREC_MIXED) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    const auto it = g_plans.find(plan_key(c->device, d));
+    if (it != g_plans.end()) {
+      p->team[pgx::kTuneExpmMx] = it->second.first;
+      p->team[pgx::kTuneGradMx] = it->second.second;
+    }
   }
   *out = p;
   return PGX_OK;
@@ -729,6 +775,10 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
     p->team[kern] = best;
     rep += " -> T=" + std::to_string(best);
   }
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    g_plans[plan_key(c->device, &p->desc)] = {p->team[pgx::kTuneExpmMx], p->team[pgx::kTuneGradMx]};
+  }
   if (report && len) std::snprintf(report, len, "%s", rep.c_str());
   return run_pipeline(p, p->d_u, p->d_F, p->d_G);
 }
@@ -800,6 +850,39 @@ extern "C" int pgx_ctx_measure_peak(pgx_ctx* c, int32_t pipe, double* gflops) {
   return st;
 }
 
+// The oracle-free residual of the evaluation just run (pgx_eval_stats):
+// from U_total for gate targets, from the stored states for state targets
+// when the evaluation computed G (F-only state evaluations store none).
+static int eval_residual(pgx_problem* p, bool had_grad, double* out, int32_t* kind_out) {
+  pgx_ctx* c = p->ctx;
+  const pgx_problem_desc& d = p->desc;
+  const bool liou = d.generator == PGX_GEN_LIOUVILLIAN;
+  int kind = PGX_RESID_NONE, N = 0;
+  if (liou) {
+    N = (int)std::lround(std::sqrt((double)d.dim));
+    if (N * N != d.dim) N = 0;  // not a vectorised density matrix: no trace to check
+  }
+  if (d.target == PGX_TARGET_GATE)
+    kind = liou ? (N ? PGX_RESID_TRACE : PGX_RESID_NONE) : PGX_RESID_UNITARITY;
+  else if (had_grad)
+    kind = liou ? (N ? PGX_RESID_STATE_TRACE : PGX_RESID_NONE) : PGX_RESID_NORM;
+  *kind_out = kind;
+  *out = 0.0;
+  if (kind == PGX_RESID_NONE) return PGX_OK;
+  unsigned long long* bits = reinterpret_cast<unsigned long long*>(p->d_F + 2);
+  pgx::LaunchInfo li = p->launch_info();
+  double* h = p->h_stage + 2 * (size_t)d.n_controls * d.n_slices + 1;
+  int st;
+  if ((st = ctx_cuda(c, cudaMemsetAsync(bits, 0, sizeof(double), c->stream), "memset")) ||
+      (st = ctx_cuda(c, pgx::launch_residual(p->split_grad_states && had_grad ? p->pd_grad : p->pd, p->w, kind, N,
+                                             bits, li), "residual")) ||
+      (st = ctx_cuda(c, cudaMemcpyAsync(h, bits, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H")) ||
+      (st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync")))
+    return st;
+  *out = *h;
+  return PGX_OK;
+}
+
 int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats) {
   pgx_ctx* c = p->ctx;
   const auto t0 = std::chrono::steady_clock::now();
@@ -835,6 +918,7 @@ int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_st
     stats->units = (int64_t)p->desc.n_members * p->desc.n_slices;
     stats->n_launches = (int32_t)(c->launches - l0);
     stats->max_taylor_degree = 0;
+    if ((st = eval_residual(p, G != nullptr, &stats->residual, &stats->residual_kind))) return st;
   }
   if (!std::isfinite(*hF)) return ctx_fail(c, PGX_ERR_NONFINITE, "objective is not finite");
   return PGX_OK;

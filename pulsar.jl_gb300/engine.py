@@ -277,6 +277,22 @@ def checkpoint_create(w_opt, F_opt: float, *, iteration: int = 0, fidelity_histo
     return out.raw[:need.value]
 
 
+def plan_lookup(drifts, controls, dt, *, device: int = 0, **problem):
+    """(expm, gradient) team sizes pgx_autotune recorded for problems of this
+    key, or None (pgx_plan_lookup)."""
+    d, keep, _ = problem_desc(drifts, controls, dt, **problem)
+    te, tg = C.c_int32(), C.c_int32()
+    rc = A.lib().pgx_plan_lookup(int(device), C.byref(d), C.byref(te), C.byref(tg))
+    if rc == 9:
+        return None
+    A.check(rc)
+    return int(te.value), int(tg.value)
+
+
+def plan_clear():
+    A.check(A.lib().pgx_plan_clear())
+
+
 def problem_fingerprint(drifts, controls, dt, **problem) -> int:
     """FNV-1a-64 of the problem descriptor (what an exact resumption checks)."""
     d, keep, _ = problem_desc(drifts, controls, dt, **problem)
@@ -539,12 +555,14 @@ class Problem:
         F = C.c_double()
         st = A.EvalStats()
         A.check(A.lib().pgx_eval(self._h, A.as_dptr(ub), C.byref(F),
-                                 A.as_dptr(self._G) if want_grad else None, C.byref(st)),
+                                 A.as_dptr(self._G) if want_grad else None, C.byref(st) if stats else None),
                 self.ctx.handle)
         G = self._G.reshape(self.n_t, self.n_c).T.copy() if want_grad else None
         if stats:
             return float(F.value), G, {"ms_device": st.ms_device, "ms_host": st.ms_host,
-                                       "units": int(st.units), "n_launches": int(st.n_launches)}
+                                       "units": int(st.units), "n_launches": int(st.n_launches),
+                                       "residual": st.residual,
+                                       "residual_kind": A.RESIDUAL_KIND.get(int(st.residual_kind), "?")}
         return float(F.value), G
 
     def eval_device(self, d_u: int, d_F: int, d_G: Optional[int]):

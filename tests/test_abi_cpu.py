@@ -88,3 +88,15 @@ def test_c_oracle_matches_numpy_oracle():
         F, G = cpu_port.CpuProblem(prob, mode).eval(u0, threads=1)
         Fo, Go = mb.eval_problem(prob, u0, mode)
         assert abs(F - Fo) < 1e-13 and np.max(np.abs(G - Go)) < 1e-11 * np.max(np.abs(Go))
+
+
+def test_plan_cache_is_host_side(pg):
+    """pgx_plan_lookup / pgx_plan_clear touch no device: an unknown key reports
+    PGX_ERR_STATE, and invalid descriptors are refused."""
+    from pulsar_gb300 import workloads as W
+    spec, _ = W.spin4_ensemble(n_t=4, n_off=1, n_b1=1)
+    pg.plan_clear()
+    assert pg.plan_lookup(**spec.problem_kwargs("exact", "mixed")) is None
+    A = pg._abi
+    t1, t2 = C.c_int32(), C.c_int32()
+    assert A.lib().pgx_plan_lookup(0, None, C.byref(t1), C.byref(t2)) == 1

@@ -299,6 +299,27 @@ int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slice
                                  const double* d_gens, const double* d_dt, double* d_U_total,
                                  void* stream, char* err, size_t err_len);
 
+/* ---- trajectory tracking and phase-only controls ------------------------ */
+/* Tracking (MR/GRAPETracking.jl:166-277): on a Hermitian state-target
+ * problem, n > 0 checkpoints replace the terminal objective by
+ *   F = sum_m w_m sum_s sum_c weights[c] Re Tr(rho_c rho_ms(steps[c])),
+ * rho(k) the state after k slices from rho(0) = psi_s psi_s' (states_init;
+ * states_target and the fidelity metric are not used).  steps are 1..n_slices
+ * (PGX_ERR_INVALID outside, GRAPETracking.jl:190-191), targets [n][D*D]
+ * complex Hermitian density matrices.  PGX_GRAD_REF_MR gives the reference's
+ * co-state formula (twice the first-order derivative: its co-state carries
+ * 2 w_c), PGX_GRAD_EXACT the exact gradient.  n = 0 restores the terminal
+ * objective.  pgx_optimize's MR methods on a tracking problem are
+ * _optimcon_lbfgs_tracking / _optimcon_grape_tracking (OptControl.jl:1040-1236). */
+int pgx_problem_set_tracking(pgx_problem* prob, int32_t n, const int32_t* steps, const double* weights,
+                             const double* targets);
+/* Phase-only evaluation (grape_phase_kernel, MR/GRAPEPhase.jl:52-93): the
+ * n_controls / 2 channels of phases phi [n_ch x n_t] (column-major) and
+ * amplitudes (same shape, >= 0, NULL = 1) become w[2ch] = a cos(phi),
+ * w[2ch+1] = a sin(phi); F as pgx_eval, G_phase = -G_x sin(phi) + G_y cos(phi)
+ * (nullable).                                                               */
+int pgx_eval_phase(pgx_problem* prob, const double* phi, const double* amplitudes, double* F, double* G_phase);
+
 /* ---- optimisation ------------------------------------------------------ */
 enum { PGX_OPT_GRAPE = 0,          /* grape_optimize ascent loop (GRAPE.jl:469-643)       */
        PGX_OPT_ENSEMBLE_LBFGS = 1, /* grape_optimize_ensemble (GRAPE.jl:1012-1230)        */

@@ -776,6 +776,80 @@ def grape_state_kernel(waveform: np.ndarray, ctrl: MRControl):
     return fid / N_ens, grad / N_ens
 
 
+@dataclass
+class TrackingPoint:
+    """GRAPETracking.jl:82-91: the density matrix after propagating through
+    ``step`` (1-based, 1..n_t) is compared with ``target_dm``, weight w."""
+    step: int
+    target_dm: np.ndarray
+    weight: float
+
+
+def grape_tracking_kernel(waveform: np.ndarray, ctrl: MRControl, tracking):
+    """_grape_tracking_cpu_threaded (GRAPETracking.jl:166-277), density-matrix
+    form as the reference computes it: rho[1] = psi0 psi0', rho[n+1] = U_n
+    rho[n] U_n'; Phi += w Re Tr(rho_tar rho[step+1]); co-state Lambda = 0,
+    at a checkpoint step Lambda += 2 w (rho_tar - rho[n+1]), grad[k,n] +=
+    -dt_n Re(i Tr(Lambda' [pwr Op_k, rho[n+1]])), Lambda <- U_n' Lambda U_n;
+    ensemble and pairs averaged.  Penalties are not applied here."""
+    n_ctrl, n_t = waveform.shape
+    pairs = [(H, p) for H in ctrl.drifts for p in ctrl.pwr_levels]
+    N_ens = len(pairs) * len(ctrl.rho_init)
+    ckpt = {}
+    for tp in tracking:
+        if tp.step < 1 or tp.step > n_t:
+            raise ValueError(f"TrackingPoint.step={tp.step} out of range [1, {n_t}]")
+        ckpt.setdefault(tp.step, []).append((float(tp.weight), np.asarray(tp.target_dm, C128)))
+    steps = sorted(ckpt)
+    ops = [np.asarray(o, C128) for o in ctrl.operators]
+    fid = 0.0
+    grad = np.zeros((n_ctrl, n_t))
+    for H_d, pwr in pairs:
+        Ps = []
+        for n in range(n_t):
+            H = np.asarray(H_d, C128) + sum(pwr * waveform[k, n] * ops[k] for k in range(n_ctrl))
+            Ps.append(expm_neg_i(H, float(ctrl.pulse_dt[n])))
+        for psi0 in ctrl.rho_init:
+            psi0 = np.asarray(psi0, C128)
+            rho = [np.outer(psi0, psi0.conj())]          # rho[0] here = rho_traj[1]
+            for n in range(n_t):
+                rho.append(Ps[n] @ rho[-1] @ Ps[n].conj().T)
+            for n_ck in steps:
+                for w_k, rt in ckpt[n_ck]:
+                    fid += w_k * float(np.real(np.trace(rt @ rho[n_ck])))
+            Lam = np.zeros_like(rho[0])
+            for n in range(n_t, 0, -1):                 # 1-based step n, slice n-1
+                for w_k, rt in ckpt.get(n, ()):
+                    Lam = Lam + 2.0 * w_k * (rt - rho[n])
+                r1 = rho[n]
+                dt_n = float(ctrl.pulse_dt[n - 1])
+                for k in range(n_ctrl):
+                    Hk = pwr * ops[k]
+                    comm = Hk @ r1 - r1 @ Hk
+                    grad[k, n - 1] += -dt_n * float(np.real(1j * np.trace(Lam.conj().T @ comm)))
+                Lam = Ps[n - 1].conj().T @ Lam @ Ps[n - 1]
+    return fid / N_ens, grad / N_ens
+
+
+def grape_phase_kernel(phi: np.ndarray, ctrl: MRControl, amplitudes=None):
+    """grape_phase_kernel (GRAPEPhase.jl:52-93): w[2ch-1] = a cos(phi),
+    w[2ch] = a sin(phi); dF/dphi = -G_x sin(phi) + G_y cos(phi)."""
+    phi = np.asarray(phi, float)
+    n_ch, n_t = phi.shape
+    a = np.ones_like(phi) if amplitudes is None else np.asarray(amplitudes, float)
+    if len(ctrl.operators) != 2 * n_ch:
+        raise ValueError("length(operators) must be 2 x n_channels")
+    if a.shape != phi.shape:
+        raise ValueError("amplitudes must match phi_profile")
+    if np.any(a < 0):
+        raise ValueError("all amplitudes must be >= 0")
+    w = np.zeros((2 * n_ch, n_t))
+    w[0::2] = a * np.cos(phi)
+    w[1::2] = a * np.sin(phi)
+    F, G = grape_state_kernel(w, ctrl)
+    return F, -G[0::2] * np.sin(phi) + G[1::2] * np.cos(phi)
+
+
 def expm_general(A: np.ndarray) -> np.ndarray:
     """Julia LinearAlgebra.exp (Higham 2005 scaling-and-squaring Pade-13) is
     restated by scipy.linalg.expm (Al-Mohy-Higham 2009, same family)."""
@@ -898,3 +972,36 @@ def optimcon_lbfgs(kernel, guess: np.ndarray, l_bound=-1.0, u_bound=1.0, max_ite
             break
     return OptimizationResult(best_w, best_F, fh, gh, len(fh) - 1, converged, reason,
                               time.time() - t0, nf, ng, {"algorithm": "L-BFGS"})
+
+
+def optimcon_grape(kernel, guess: np.ndarray, l_bound=-1.0, u_bound=1.0, max_iter=500,
+                   grad_tol=1e-7) -> OptimizationResult:
+    """_optimcon_grape (OptControl.jl:486-561): step 0.05 (u-l) / max|G| along
+    G, clamp, stop at F >= 1 - 1e-8 or ||G|| below grad_tol."""
+    t0 = time.time()
+    w = np.clip(np.array(guess, float), l_bound, u_bound)
+    F, G = kernel(w)
+    best_w, best_F = w.copy(), F
+    nf = ng = 1
+    fh, gh = [F], [float(np.linalg.norm(G))]
+    converged, reason = False, "max iterations reached"
+    for it in range(1, max_iter + 1):
+        g_max = float(np.max(np.abs(G)))
+        if g_max > 1e-14:
+            w = np.clip(w + (0.05 * (u_bound - l_bound) / g_max) * G, l_bound, u_bound)
+        F, G = kernel(w)
+        nf += 1
+        ng += 1
+        fh.append(F)
+        gn = float(np.linalg.norm(G))
+        gh.append(gn)
+        if F > best_F:
+            best_F, best_w = F, w.copy()
+        if F >= 1.0 - 1e-8:
+            converged, reason = True, "near-perfect fidelity"
+            break
+        if gn < grad_tol:
+            converged, reason = True, "gradient norm below tolerance"
+            break
+    return OptimizationResult(best_w, best_F, fh, gh, len(fh) - 1, converged, reason,
+                              time.time() - t0, nf, ng, {"algorithm": "GRAPE"})

@@ -158,6 +158,8 @@ SIGNATURES = {
     "pgx_problem_get_team": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "pgx_plan_lookup": (C.c_int, [C.c_int, C.POINTER(ProblemDesc), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "pgx_plan_clear": (C.c_int, []),
+    "pgx_problem_set_tracking": (C.c_int, [C.c_void_p, C.c_int32, iptr, dptr, dptr]),
+    "pgx_eval_phase": (C.c_int, [C.c_void_p, dptr, dptr, dptr, dptr]),
     "pgx_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "pgx_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -886,6 +886,20 @@ def _wrap_states(x):
 
 
 @dataclass
+class TrackingPoint:
+    """GRAPETracking.jl:82-91: the density matrix after propagating through
+    ``step`` (1-based) should match ``target_dm`` with weight ``weight``."""
+    step: int
+    target_dm: np.ndarray
+    weight: float
+
+    def __post_init__(self):
+        self.step = int(self.step)
+        self.target_dm = np.array(self.target_dm, C128)
+        self.weight = float(self.weight)
+
+
+@dataclass
 class MRControl:
     """OptControl.jl:137-259 (fields the GRAPE path uses; defaults kept)."""
     drifts: list
@@ -906,6 +920,7 @@ class MRControl:
     precision: str = "fp64"
     penalties: list = field(default_factory=list)   # symbols, OptControl.jl (:none skipped)
     p_weights: list = field(default_factory=list)
+    tracking: list = field(default_factory=list)    # TrackingPoint checkpoints (OptControl.jl:156,222)
 
     def __post_init__(self):
         self.rho_init = _wrap_states(self.rho_init)
@@ -913,20 +928,38 @@ class MRControl:
         if len(self.rho_init) != len(self.rho_targ):
             raise ValueError("rho_init and rho_targ must have the same length")
         self.pulse_dt = np.asarray(self.pulse_dt, np.float64)
+        self.tracking = [tp if isinstance(tp, TrackingPoint) else TrackingPoint(tp.step, tp.target_dm, tp.weight)
+                         for tp in self.tracking]
         self._prob = None
+        self._track_prob = None
 
-    def problem(self) -> Problem:
-        if self._prob is None:
-            n_d, n_p = len(self.drifts), len(self.pwr_levels)
-            md = np.repeat(np.arange(n_d), n_p)
-            ms = np.tile(np.asarray(self.pwr_levels, np.float64), n_d)
-            self._prob = Problem(np.stack(self.drifts), np.stack(self.operators), self.pulse_dt,
-                                 member_drift=md, member_scale=ms, target="states",
-                                 fidelity=self.fidelity, states_init=np.stack(self.rho_init),
-                                 states_target=np.stack(self.rho_targ), grad_mode=self.grad_mode,
-                                 precision=self.precision)
-            _set_ctrl_penalties(self, self._prob)
-        return self._prob
+    def _make_problem(self) -> Problem:
+        n_d, n_p = len(self.drifts), len(self.pwr_levels)
+        md = np.repeat(np.arange(n_d), n_p)
+        ms = np.tile(np.asarray(self.pwr_levels, np.float64), n_d)
+        prob = Problem(np.stack(self.drifts), np.stack(self.operators), self.pulse_dt,
+                       member_drift=md, member_scale=ms, target="states",
+                       fidelity=self.fidelity, states_init=np.stack(self.rho_init),
+                       states_target=np.stack(self.rho_targ), grad_mode=self.grad_mode,
+                       precision=self.precision)
+        _set_ctrl_penalties(self, prob)
+        return prob
+
+    def problem(self, tracking: bool = False) -> Problem:
+        """The device problem of grape_state_kernel, or (tracking=True) of
+        grape_tracking_kernel: the same ensemble with the checkpoints set."""
+        if not tracking:
+            if self._prob is None:
+                self._prob = self._make_problem()
+            return self._prob
+        if not self.tracking:
+            raise RuntimeError("grape_tracking_kernel: ctrl.tracking is empty. "
+                               "Add TrackingPoint entries or call grape_state_kernel instead.")
+        if self._track_prob is None:
+            self._track_prob = self._make_problem()
+            self._track_prob.set_tracking([tp.step for tp in self.tracking], [tp.weight for tp in self.tracking],
+                                          np.stack([tp.target_dm for tp in self.tracking]))
+        return self._track_prob
 
 
 def _set_ctrl_penalties(ctrl, prob: Problem):
@@ -1040,6 +1073,30 @@ def grape_lindblad_kernel(waveform, ctrl: LindbladMRControl):
     return ctrl.problem().eval(np.asarray(waveform, np.float64))
 
 
+def grape_tracking_kernel(waveform, ctrl: MRControl):
+    """(fidelity, grad) of trajectory tracking (GRAPETracking.jl:150-277):
+    weighted checkpoint fidelities averaged over the ensemble and state
+    pairs; the gradient of ctrl.grad_mode (the reference's co-state formula
+    for "ref_mr")."""
+    return ctrl.problem(tracking=True).eval(np.asarray(waveform, np.float64))
+
+
+def grape_phase_kernel(phi_profile, ctrl: MRControl, amplitudes=None):
+    """Phase-only kernel (GRAPEPhase.jl:52-93): (F, dF/dphi) with the
+    amplitude profile held fixed (default 1)."""
+    phi = np.asarray(phi_profile, np.float64)
+    n_ch, n_t = phi.shape
+    if len(ctrl.operators) != 2 * n_ch:
+        raise ValueError(f"grape_phase_kernel: ctrl has {len(ctrl.operators)} operators but phi_profile has "
+                         f"{n_ch} rows -- expected length(operators) == 2 x n_channels.")
+    amp = np.ones_like(phi) if amplitudes is None else np.asarray(amplitudes, np.float64)
+    if amp.shape != phi.shape:
+        raise ValueError(f"grape_phase_kernel: amplitudes {amp.shape} must match phi_profile {phi.shape}.")
+    if np.any(amp < 0):
+        raise ValueError("grape_phase_kernel: all amplitudes must be >= 0.")
+    return ctrl.problem().eval_phase(phi, amp)
+
+
 def fidelity_forward(waveform, ctrl) -> float:
     """Forward-only ensemble fidelity (GRAPEState.jl:434-566)."""
     return ctrl.problem().eval(np.asarray(waveform, np.float64), want_grad=False)[0]
@@ -1055,8 +1112,10 @@ def optimcon(ctrl, guess) -> OptimizationResult:
         raise ValueError(f"guess columns {n_t} != length(ctrl.pulse_dt) {len(ctrl.pulse_dt)}")
     if ctrl.method not in ("lbfgs", "grape"):
         raise ValueError(f"method :{ctrl.method} is not served on the device (:lbfgs, :grape)")
-    o = ctrl.problem().optimize(guess, "mr_lbfgs" if ctrl.method == "lbfgs" else "mr_grape",
-                                max_iter=ctrl.max_iter, gradient_norm_tol=ctrl.grad_tol,
-                                lbfgs_memory=ctrl.lbfgs_memory, l_bound=ctrl.l_bound,
-                                u_bound=ctrl.u_bound)
+    # a non-empty ctrl.tracking selects _optimcon_*_tracking (OptControl.jl:328-345):
+    # the same loops on the tracking kernel
+    prob = ctrl.problem(tracking=True) if getattr(ctrl, "tracking", None) else ctrl.problem()
+    o = prob.optimize(guess, "mr_lbfgs" if ctrl.method == "lbfgs" else "mr_grape", max_iter=ctrl.max_iter,
+                      gradient_norm_tol=ctrl.grad_tol, lbfgs_memory=ctrl.lbfgs_memory, l_bound=ctrl.l_bound,
+                      u_bound=ctrl.u_bound)
     return _result(o, "L-BFGS" if ctrl.method == "lbfgs" else "GRAPE")

@@ -30,6 +30,11 @@ struct ProbDev {
   const double2* target_op;  // gate: [Dp*Dp]
   const double2* psi_init;   // states: [n_pairs][Dp]
   const double2* psi_targ;   // states: [n_pairs][Dp]
+  // trajectory tracking (states targets): checkpoints in ascending step order
+  int n_ck;                  // 0 = the terminal objective
+  const int* ck_step;        // [n_ck] 1..n_t: the state after that many slices
+  const double* ck_weight;   // [n_ck]
+  const double2* ck_target;  // [n_ck][Dp*Dp] Hermitian target density matrices
   // mixed precision only: the same constants as df pairs
   // {re.hi, im.hi, re.lo, im.lo} (the first two floats are the FP32 rounding)
   const float4* drifts_df;   // [n_drifts][Dp*Dp]

@@ -226,6 +226,136 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chain_states_fwd(ProbDev p,
   if (tm.lane == 0) w.Fm[m] = Fm;
 }
 
+// Trajectory tracking (GRAPETracking.jl:166-277).  The reference propagates
+// density matrices rho[n+1] = U_n rho[n] U_n'; with rho[0] = psi0 psi0' that
+// is rho[n] = psi[n] psi[n]' exactly, so the chain carries the state vectors
+// (D^2 per slice instead of 2 D^3) and the objective of member m is
+//   F_m = sum_s sum_c w_c Re <psi_s[j_c]| rho_c |psi_s[j_c]>.
+// Every state is stored: the backward chain and the gradient read them.
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_track_fwd(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  const int np = p.n_pairs;
+  const int pan = np * D;
+  const int per_team = (2 * D * D > 2 * pan ? 2 * D * D : 2 * pan) + T;
+  double2 *base, *red;
+  team_slot<D>(smem, per_team, team, base, red);
+  double2* Ps = base;  // [np][D]
+  double2* Pm = w.psi + (size_t)m * (p.n_t + 1) * pan;
+  for (int e = tm.lane; e < pan; e += T) {
+    Ps[e] = p.psi_init[e];
+    Pm[e] = Ps[e];
+  }
+  tm.sync();
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  double Fm = 0.0;
+  int c = 0;
+  for (int k = 0; k < p.n_t; ++k) {
+    const double2* Uk = Um + (size_t)k * D * D;
+    double2 outv[(D * 8 + T - 1) / T > 0 ? (D * 8 + T - 1) / T : 1];
+    int cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      const int s = e / D, r = e % D;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int q = 0; q < D; ++q) acc = cmac(acc, Uk[r + D * q], Ps[s * D + q]);
+      if (cnt < (int)(sizeof(outv) / sizeof(outv[0]))) outv[cnt] = acc;
+    }
+    tm.sync();
+    cnt = 0;
+    double2* dst = Pm + (size_t)(k + 1) * pan;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      Ps[e] = outv[cnt];
+      dst[e] = outv[cnt];
+    }
+    tm.sync();
+    for (; c < p.n_ck && p.ck_step[c] == k + 1; ++c) {  // checkpoints after slice k
+      const double2* R = p.ck_target + (size_t)c * D * D;
+      double acc = 0.0;
+      for (int e = tm.lane; e < pan; e += T) {
+        const int s = e / D, r = e % D;
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < D; ++q) t = cmac(t, R[r + D * q], Ps[s * D + q]);
+        const double2 v = Ps[e];
+        acc = fma(v.x, t.x, fma(v.y, t.y, acc));  // Re(conj(psi_r) (rho psi)_r)
+      }
+      Fm = fma(p.ck_weight[c], team_sum<T>(tm, make_double2(acc, 0.0), red).x, Fm);
+    }
+  }
+  if (tm.lane == 0) w.Fm[m] = Fm;
+}
+
+// Tracking co-state as vectors: chi_s[k] = Lambda[k] psi_s[k], where the
+// reference's matrix co-state (Lambda += 2 w_c (rho_c - rho) at a checkpoint,
+// Lambda <- U' Lambda U) is the same for every pair, gives
+//   chi_s[k] = U_k' chi_s[k+1] + sum_{c: j_c = k} 2 w_c rho_c psi_s[k].
+// The -rho part of the reference's source adds -2 w_c |psi|^2 psi to chi,
+// whose contribution Im <psi|Op|psi> to the gradient is identically zero; it
+// is left out.  lam[k] = scale * chi[k]: scale = 2 w_m for the reference's
+// formula (its gradient is -dt Re(i Tr(Lambda' [H_k, rho])) = 2 dt Im <chi|H_k|psi>),
+// w_m for the exact gradient (d rho = dU rho U' + h.c. gives
+// Re Tr(L(A, psi[k] chi[k+1]') E_k)).
+template <int D>
+__global__ void __launch_bounds__(Cfg<D>::THREADS) k_track_bwd(ProbDev p, WorkDev w) {
+  using G = Cfg<D>;
+  constexpr int T = G::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * G::TPC + team;
+  if (m >= p.n_members) return;
+  const int np = p.n_pairs;
+  const int pan = np * D;
+  const int per_team = (2 * D * D > 2 * pan ? 2 * D * D : 2 * pan) + T;
+  double2 *base, *red;
+  team_slot<D>(smem, per_team, team, base, red);
+  double2* Ls = base;
+  const double scl = (p.grad_mode == GRAD_EXACT ? 1.0 : 2.0) * p.m_weight[m];
+  const double2* Pm = w.psi + (size_t)m * (p.n_t + 1) * pan;
+  double2* Lm = w.lam + (size_t)m * (p.n_t + 1) * pan;
+  const double2* Um = w.U + (size_t)m * p.n_t * D * D;
+  for (int e = tm.lane; e < pan; e += T) Ls[e] = make_double2(0.0, 0.0);
+  int c = p.n_ck - 1;
+  for (int k = p.n_t; k >= 1; --k) {
+    const double2* psk = Pm + (size_t)k * pan;
+    for (; c >= 0 && p.ck_step[c] == k; --c) {  // each lane updates the entries it owns
+      const double2* R = p.ck_target + (size_t)c * D * D;
+      const double tw = 2.0 * p.ck_weight[c];
+      for (int e = tm.lane; e < pan; e += T) {
+        const int s = e / D, r = e % D;
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < D; ++q) t = cmac(t, R[r + D * q], psk[s * D + q]);
+        Ls[e].x = fma(tw, t.x, Ls[e].x);
+        Ls[e].y = fma(tw, t.y, Ls[e].y);
+      }
+    }
+    tm.sync();
+    for (int e = tm.lane; e < pan; e += T) Lm[(size_t)k * pan + e] = make_double2(scl * Ls[e].x, scl * Ls[e].y);
+    const double2* Uk = Um + (size_t)(k - 1) * D * D;
+    double2 outv[(D * 8 + T - 1) / T > 0 ? (D * 8 + T - 1) / T : 1];
+    int cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) {
+      const int s = e / D, r = e % D;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int q = 0; q < D; ++q) acc = cmac_cj(acc, Uk[q + D * r], Ls[s * D + q]);
+      if (cnt < (int)(sizeof(outv) / sizeof(outv[0]))) outv[cnt] = acc;
+    }
+    tm.sync();
+    cnt = 0;
+    for (int e = tm.lane; e < pan; e += T, ++cnt) Ls[e] = outv[cnt];
+    tm.sync();
+  }
+  for (int e = tm.lane; e < pan; e += T) Lm[e] = make_double2(scl * Ls[e].x, scl * Ls[e].y);
+  (void)red;
+}
+
 // --------------------------------------------------------------------------
 // Stage 3: backward chains
 // --------------------------------------------------------------------------
@@ -372,7 +502,10 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_grad(ProbDev p, WorkDev w) 
       }
       for (int e = tm.lane; e < D * D; e += T) W.dB[e] = Mk[e];
     } else {
-      const double2* psi = w.psi + ((size_t)m * (p.n_t + 1) + k) * pan;
+      // tracking's reference formula pairs the co-state with the state after
+      // the slice (GRAPETracking.jl:256-262); every other form with the one before
+      const int pk = (p.n_ck > 0 && !exact) ? k + 1 : k;
+      const double2* psi = w.psi + ((size_t)m * (p.n_t + 1) + pk) * pan;
       const int li = (p.grad_mode == GRAD_REF_GRAPE) ? k : k + 1;
       const double2* lam = w.lam + ((size_t)m * (p.n_t + 1) + li) * pan;
       if (!exact) {
@@ -597,6 +730,9 @@ static cudaError_t do_chain_fwd(const ProbDev& p, const WorkDev& w, const Launch
   if (p.target == TGT_GATE) {
     ensure_smem(k_chain_gate_fwd<D>, smem);
     k_chain_gate_fwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w, store ? 1 : 0);
+  } else if (p.n_ck > 0) {
+    ensure_smem(k_track_fwd<D>, smem);
+    k_track_fwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
   } else {
     ensure_smem(k_chain_states_fwd<D>, smem);
     k_chain_states_fwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w, store ? 1 : 0);
@@ -617,6 +753,9 @@ static cudaError_t do_chain_bwd(const ProbDev& p, const WorkDev& w, const Launch
   if (p.target == TGT_GATE) {
     ensure_smem(k_chain_gate_bwd<D>, smem);
     k_chain_gate_bwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  } else if (p.n_ck > 0) {
+    ensure_smem(k_track_bwd<D>, smem);
+    k_track_bwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);
   } else {
     ensure_smem(k_chain_states_bwd<D>, smem);
     k_chain_states_bwd<D><<<grid, G::THREADS, smem, li.stream>>>(p, w);

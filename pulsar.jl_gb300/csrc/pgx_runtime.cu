@@ -691,7 +691,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
   mk.mark(PGX_STAGE_EXPM);
   if ((st = ctx_cuda(c, pgx::launch_expm(p->pd, w, li), "expm"))) return st;
   mk.mark(PGX_STAGE_CHAIN_FWD);
-  if (want_grad && p->split_grad_states) {
+  if (want_grad && p->split_grad_states && p->pd.n_ck == 0) {
     // F from states_init; gradient from grad_states_init (Gradients.jl:153-157).
     if ((st = ctx_cuda(c, pgx::launch_chain_fwd(p->pd, w, li, false), "chain_fwd(F)"))) return st;
     if ((st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, false), "reduce(F)"))) return st;
@@ -864,7 +864,7 @@ static int eval_residual(pgx_problem* p, bool had_grad, double* out, int32_t* ki
   }
   if (d.target == PGX_TARGET_GATE)
     kind = liou ? (N ? PGX_RESID_TRACE : PGX_RESID_NONE) : PGX_RESID_UNITARITY;
-  else if (had_grad)
+  else if (had_grad || p->pd.n_ck > 0)  // tracking stores its states on every evaluation
     kind = liou ? (N ? PGX_RESID_STATE_TRACE : PGX_RESID_NONE) : PGX_RESID_NORM;
   *kind_out = kind;
   *out = 0.0;
@@ -1111,6 +1111,116 @@ extern "C" int pgx_propagator(pgx_ctx* c, int32_t dim, int32_t generator, const 
     for (int r = 0; r < dim; ++r) {
       U[2 * (r + (size_t)dim * col)] = out[2 * (r + (size_t)Dp * col)];
       U[2 * (r + (size_t)dim * col) + 1] = out[2 * (r + (size_t)Dp * col) + 1];
+    }
+  return PGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// trajectory tracking and phase-only evaluation (MR/GRAPETracking.jl,
+// MR/GRAPEPhase.jl)
+// ---------------------------------------------------------------------------
+extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t* steps, const double* weights,
+                                        const double* targets) {
+  if (!p || n < 0 || (n > 0 && (!steps || !weights || !targets))) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  const pgx_problem_desc& d = p->desc;
+  if (n > 0 && (d.target != PGX_TARGET_STATES || d.generator != PGX_GEN_HERMITIAN))
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "tracking needs a Hermitian problem with state targets "
+                                            "(grape_tracking_kernel, GRAPETracking.jl:166-173)");
+  if (n > 0 && d.grad_mode == PGX_GRAD_REF_GRAPE)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "tracking has the MR first-order formula (PGX_GRAD_REF_MR) "
+                                            "or the exact gradient");
+  const int D = d.dim, Dp = p->Dp;
+  for (int i = 0; i < n; ++i) {
+    if (steps[i] < 1 || steps[i] > d.n_slices) {
+      char msg[96];
+      std::snprintf(msg, sizeof msg, "TrackingPoint.step=%d out of range [1, %d]", steps[i], d.n_slices);
+      return ctx_fail(c, PGX_ERR_INVALID, msg);  // GRAPETracking.jl:190-191
+    }
+    if (!std::isfinite(weights[i]) || !finite_all(targets + (size_t)i * 2 * D * D, (size_t)2 * D * D))
+      return ctx_fail(c, PGX_ERR_NONFINITE, "tracking weights and targets must be finite");
+    if (herm_dev(targets + (size_t)i * 2 * D * D, D) > 1e-10)
+      return ctx_fail(c, PGX_ERR_INVALID, "tracking target density matrices must be Hermitian");
+  }
+  cudaSetDevice(c->device);
+  // checkpoints in ascending step order; ties keep their given order
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return steps[a] < steps[b]; });
+  const size_t tb = (size_t)n * Dp * Dp * sizeof(double2);
+  const size_t off_w = ((size_t)n * sizeof(int) + 15) / 16 * 16;
+  const size_t off_t = off_w + ((size_t)n * sizeof(double) + 15) / 16 * 16;
+  const size_t bytes = off_t + tb;
+  std::vector<unsigned char> host(bytes, 0);
+  int* hs = reinterpret_cast<int*>(host.data());
+  double* hw = reinterpret_cast<double*>(host.data() + off_w);
+  for (int i = 0; i < n; ++i) {
+    hs[i] = steps[order[i]];
+    hw[i] = weights[order[i]];
+    const std::vector<double> t = pad_mats(targets + (size_t)order[i] * 2 * D * D, 1, D, Dp);
+    std::memcpy(host.data() + off_t + (size_t)i * Dp * Dp * sizeof(double2), t.data(), Dp * Dp * sizeof(double2));
+  }
+  int st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st) return st;
+  if (p->d_track) {  // the previous checkpoints
+    auto it = std::find(p->owned.begin(), p->owned.end(), p->d_track);
+    if (it != p->owned.end()) p->owned.erase(it);
+    if (c->pool) cudaFreeAsync(p->d_track, c->stream);
+    else cudaFree(p->d_track);
+    c->used -= p->track_bytes;
+    p->bytes -= p->track_bytes;
+    p->d_track = nullptr;
+    p->track_bytes = 0;
+  }
+  if (n > 0) {
+    if ((st = ctx_alloc(c, &p->d_track, bytes, p->owned, p->bytes))) return st;
+    p->track_bytes = bytes;
+    if ((st = ctx_cuda(c, cudaMemcpyAsync(p->d_track, host.data(), bytes, cudaMemcpyHostToDevice, c->stream),
+                       "H2D tracking")) ||
+        (st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync")))
+      return st;
+  }
+  unsigned char* base = static_cast<unsigned char*>(p->d_track);
+  for (pgx::ProbDev* pd : {&p->pd, &p->pd_grad}) {
+    pd->n_ck = n;
+    pd->ck_step = n ? reinterpret_cast<const int*>(base) : nullptr;
+    pd->ck_weight = n ? reinterpret_cast<const double*>(base + off_w) : nullptr;
+    pd->ck_target = n ? reinterpret_cast<const double2*>(base + off_t) : nullptr;
+  }
+  return PGX_OK;
+}
+
+extern "C" int pgx_eval_phase(pgx_problem* p, const double* phi, const double* amplitudes, double* F,
+                              double* G_phase) {
+  if (!p || !phi || !F) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  const int nc = p->desc.n_controls, nt = p->desc.n_slices;
+  if (nc % 2 != 0)
+    return ctx_fail(c, PGX_ERR_INVALID, "phase-only controls come in (x, y) pairs: n_controls must be even "
+                                        "(GRAPEPhase.jl:60-66)");
+  const int nch = nc / 2;
+  const size_t n = (size_t)nch * nt;
+  if (!finite_all(phi, n) || (amplitudes && !finite_all(amplitudes, n)))
+    return ctx_fail(c, PGX_ERR_NONFINITE, "phases and amplitudes must be finite");
+  for (size_t i = 0; amplitudes && i < n; ++i)
+    if (amplitudes[i] < 0.0) return ctx_fail(c, PGX_ERR_INVALID, "all amplitudes must be >= 0 (GRAPEPhase.jl:72)");
+  // polar -> Cartesian: w[2ch, k] = a cos(phi), w[2ch+1, k] = a sin(phi)
+  std::vector<double> u((size_t)nc * nt), G(G_phase ? (size_t)nc * nt : 0);
+  for (int k = 0; k < nt; ++k)
+    for (int ch = 0; ch < nch; ++ch) {
+      const size_t i = (size_t)ch + (size_t)nch * k;
+      const double a = amplitudes ? amplitudes[i] : 1.0;
+      u[(size_t)2 * ch + (size_t)nc * k] = a * std::cos(phi[i]);
+      u[(size_t)2 * ch + 1 + (size_t)nc * k] = a * std::sin(phi[i]);
+    }
+  const int st = eval_host(p, u.data(), F, G_phase ? G.data() : nullptr, nullptr);
+  if (st || !G_phase) return st;
+  // dF/dphi = -G_x sin(phi) + G_y cos(phi)   (GRAPEPhase.jl:86-90)
+  for (int k = 0; k < nt; ++k)
+    for (int ch = 0; ch < nch; ++ch) {
+      const size_t i = (size_t)ch + (size_t)nch * k;
+      G_phase[i] = -G[(size_t)2 * ch + (size_t)nc * k] * std::sin(phi[i]) +
+                   G[(size_t)2 * ch + 1 + (size_t)nc * k] * std::cos(phi[i]);
     }
   return PGX_OK;
 }

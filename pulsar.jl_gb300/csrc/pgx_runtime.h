@@ -46,6 +46,8 @@ struct pgx_problem {
   int team[pgx::kNumTunable] = {0, 0};  // tuned team sizes (0 = default)
   pgx_penalty* d_pen = nullptr;         // [PGX_MAX_PENALTIES] on the device
   int n_pen = 0;
+  void* d_track = nullptr;              // tracking checkpoints (steps | weights | targets)
+  uint64_t track_bytes = 0;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};
     for (int i = 0; i < pgx::kNumTunable; ++i) li.team[i] = team[i];

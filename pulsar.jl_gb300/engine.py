@@ -608,6 +608,40 @@ class Problem:
             arr[i].type, arr[i].weight, arr[i].l_bound, arr[i].u_bound = A.PENALTY[t], float(wgt), float(lo), float(hi)
         A.check(A.lib().pgx_problem_set_penalties(self._h, len(penalties), C.cast(arr, C.c_void_p)), self.ctx.handle)
 
+    def set_tracking(self, steps, weights, targets):
+        """Trajectory-tracking objective (pgx_problem_set_tracking,
+        GRAPETracking.jl): checkpoints at 1-based steps with weights and
+        target density matrices [n, D, D]; empty lists restore the terminal
+        objective."""
+        st = np.ascontiguousarray(np.asarray(steps, np.int64).astype(np.int32).ravel())
+        wt = np.ascontiguousarray(np.asarray(weights, np.float64).ravel())
+        n = int(st.size)
+        if wt.size != n:
+            raise ValueError("steps and weights must have the same length")
+        if n == 0:
+            A.check(A.lib().pgx_problem_set_tracking(self._h, 0, None, None, None), self.ctx.handle)
+            return
+        tg = np.asarray(targets, np.complex128)
+        if tg.shape != (n, self.D, self.D):
+            raise ValueError(f"targets have shape {tg.shape}, expected {(n, self.D, self.D)}")
+        tb = A.cmat_buf(tg)
+        A.check(A.lib().pgx_problem_set_tracking(self._h, n, st.ctypes.data_as(A.iptr), A.as_dptr(wt),
+                                                 A.as_dptr(tb)), self.ctx.handle)
+
+    def eval_phase(self, phi, amplitudes=None, want_grad: bool = True):
+        """Phase-only evaluation (pgx_eval_phase, GRAPEPhase.jl): phases and
+        amplitudes [n_c / 2, n_t]; returns (F, dF/dphi or None)."""
+        ph = np.asarray(phi, np.float64)
+        if ph.shape != (self.n_c // 2, self.n_t):
+            raise ValueError(f"phases have shape {ph.shape}, expected {(self.n_c // 2, self.n_t)}")
+        pb = np.ascontiguousarray(ph.T.ravel())
+        ab = None if amplitudes is None else np.ascontiguousarray(np.asarray(amplitudes, np.float64).T.ravel())
+        F = C.c_double()
+        G = np.zeros(pb.size) if want_grad else None
+        A.check(A.lib().pgx_eval_phase(self._h, A.as_dptr(pb), None if ab is None else A.as_dptr(ab), C.byref(F),
+                                       None if G is None else A.as_dptr(G)), self.ctx.handle)
+        return float(F.value), (None if G is None else G.reshape(self.n_t, self.n_c // 2).T.copy())
+
     @property
     def teams(self) -> tuple:
         """(expm, gradient) team sizes of the mixed kernels in use."""

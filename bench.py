@@ -11,6 +11,8 @@ Workloads (seeded synthetic inputs with the configurations' shapes):
   uneven512        512 independent problems, d in {2,4,8,16,32}, 50-2000 slices,
                    1-128 members, 2-6 controls; step = one batched GRAPE
                    iteration (one CUDA graph).
+  spin4_states     the spin4 system as an MR state-transfer ensemble (two
+                   basis-state pairs per member; grape_state_kernel's form).
   lindblad3q       3-qubit Lindblad gate (superoperator D = 64), 32 detuning
                    draws, 500 slices, exact gradient.
   serve            Poisson job stream through the continuous-batching server
@@ -63,22 +65,24 @@ TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
 DF_OPS_PER_CMAC = 46
 
 
-def flops_per_unit(stage: str, D: int, n_c: int, grad_mode: str) -> float:
+def flops_per_unit(stage: str, D: int, n_c: int, grad_mode: str, n_pairs: int = 0) -> float:
     """Algorithmic FLOPs per member-slice unit (complex MAC = 8 FLOPs), the
     conventional model W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 split by
     stage: expm K_exp products, forward chain 1, backward chain + costate 2,
-    gradient the Frechet terms 2 n_c K_exp products + n_c traces."""
+    gradient the Frechet terms 2 n_c K_exp products + n_c traces.  State
+    targets (n_pairs > 0) follow the state-vector model W_v = 8 D^3 K_exp
+    (1 + 2 n_c) + 8 D^2 (2 + n_c): matrix-vector chains, n_c contractions."""
     d3 = 8.0 * D ** 3
     if stage == "expm":
         return d3 * K_EXP
     if stage == "chain_fwd":
-        return d3
+        return d3 if not n_pairs else 8.0 * D ** 2
     if stage == "chain_bwd":
-        return 2 * d3
+        return 2 * d3 if not n_pairs else 8.0 * D ** 2
     if stage == "grad":
         return (d3 * K_EXP * 2 * n_c if grad_mode == "exact" else 0.0) + 8.0 * n_c * D ** 2
     if stage == "all":
-        return sum(flops_per_unit(s, D, n_c, grad_mode) for s in ("expm", "chain_fwd", "chain_bwd", "grad"))
+        return sum(flops_per_unit(s, D, n_c, grad_mode, n_pairs) for s in ("expm", "chain_fwd", "chain_bwd", "grad"))
     return 0.0
 
 
@@ -172,11 +176,14 @@ class Single:
         return K * self.units_per_step
 
     def stage_flops(self, stage):
-        return flops_per_unit(stage, self.prob.D, self.prob.n_c, self.grad_mode) * self.units_per_step
+        return flops_per_unit(stage, self.prob.D, self.prob.n_c, self.grad_mode, self.prob.n_pairs) * self.units_per_step
 
     def config(self):
-        return {"workload": self.name, "members": self.prob.n_members, "slices": self.prob.n_t,
-                "d": self.prob.D, "n_controls": self.prob.n_c, "generator": self.prob.generator}
+        cfg = {"workload": self.name, "members": self.prob.n_members, "slices": self.prob.n_t,
+               "d": self.prob.D, "n_controls": self.prob.n_c, "generator": self.prob.generator}
+        if self.prob.target != "gate":
+            cfg.update(target=self.prob.target, n_pairs=self.prob.n_pairs)
+        return cfg
 
     def cpu_sample(self, budget_s):
         return cpu_baseline_single(self.prob, self.u0, budget_s)
@@ -398,6 +405,10 @@ def make_workload(args, pg, ctx, torch, dev):
         prob, u0 = W.spin4_ensemble(n_t=args.slices or 1000)
         return Single(f"spin4_d16_231members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
                       args.precision, torch, dev, teams=args.teams)
+    if args.workload == "spin4_states":
+        prob, u0 = W.spin4_state_transfer(n_t=args.slices or 1000)
+        return Single(f"spin4_states_d16_231members_2pairs_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode,
+                      args.precision, torch, dev, teams=args.teams)
     if args.workload == "lindblad3q":
         prob, u0 = W.lindblad_3q(n_t=args.slices or 500)
         return Single(f"lindblad3q_D64_32members_{prob.n_t}slices", prob, u0, pg, ctx, args.grad_mode, args.precision,
@@ -467,7 +478,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spin4", choices=["spin4", "uneven512", "lindblad3q", "serve"])
+    ap.add_argument("--workload", default="spin4",
+                    choices=["spin4", "spin4_states", "uneven512", "lindblad3q", "serve"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--grad-mode", default="exact", choices=["exact", "ref_grape", "ref_mr"])
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)

@@ -59,7 +59,8 @@ enum { PGX_GRAD_REF_GRAPE = 0,  /* first-order formula of Gradients.jl:254-291,3
                                    GRAPELindblad.jl:183-195                            */
        PGX_GRAD_EXACT = 2       /* exact Frechet-derivative gradient                    */ };
 enum { PGX_PREC_FP64 = 0,       /* plain FP64 everywhere                                */
-       PGX_PREC_MIXED = 1       /* FP32 bulk, FP64 norm/overlap/chain (see design doc)  */ };
+       PGX_PREC_MIXED = 1       /* df32 propagators and forward chain, FP64 overlap and
+                                   objective, FP32 backward chain and gradient         */ };
 
 /* A problem is an ensemble of members.  Member m evolves under
  *   G_m(u_k) = drifts[member_drift[m]] + member_offset[m] * offset_op

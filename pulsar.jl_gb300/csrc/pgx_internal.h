@@ -158,7 +158,9 @@ cudaError_t launch_chain_bwd(const ProbDev& p, const WorkDev& w, const LaunchInf
 cudaError_t launch_grad(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_reduce(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool want_grad);
 // Largest PGX_RESID_* residual over members into *out (bits of a
-// non-negative double; *out must hold 0 before the launch).
+// non-negative double; *out must hold 0 before the launch).  kResidPairs:
+// the per-pair residuals the mixed state chain left in Utot[m np + s].
+constexpr int kResidPairs = 100;
 cudaError_t launch_residual(const ProbDev& p, const WorkDev& w, int kind, int N, unsigned long long* out,
                             const LaunchInfo& li);
 // G[q] = sum_i coef[i] Gm[idx[i]][q] (len = n_c n_t), in the order of idx.

@@ -608,6 +608,11 @@ __global__ void __launch_bounds__(kResidThreads) k_residual(ProbDev p, WorkDev w
       }
       keep(hypot(sx, sy));
     }
+  } else if (kind == kResidPairs) {
+    for (int s = threadIdx.x; s < p.n_pairs; s += blockDim.x) {
+      const double2 v = w.Utot[(size_t)m * p.n_pairs + s];
+      keep(hypot(v.x, v.y));
+    }
   } else {
     const size_t pan = (size_t)p.n_pairs * Dp;
     const double2* p0 = w.psi + (size_t)m * (p.n_t + 1) * pan;

@@ -26,8 +26,7 @@ static __constant__ df c_dfcoef[PGX_N_INVFACT] = PGX_INVFACT_DF_INIT;
 
 // Shared-memory layout of the team matrices (Lay<D, SW>).  Measured on GB300:
 // the XOR swizzle removes bank conflicts but its index arithmetic costs more
-// than the conflicts do, so the plain column-major layout is used.
-constexpr int kSwz = 0;
+// than the conflicts do, so it is not used.
 // The FP32 gradient is bound by shared-memory bandwidth, not FMAs: with
 // leading dimension D the columns a warp reads at one k share a bank.  It
 // keeps its Taylor workspace padded to leading dimension D + 1.
@@ -537,6 +536,193 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_fix_mx(ProbDev p, Wo
   }
 }
 
+// ---- state chains -----------------------------------------------------------------
+// State targets (pairs psi_s -> t_s; MR state transfer, Lindblad vec(rho)) carry
+// D^2 work per slice and pair: one warp per member.  The warp streams the next
+// slice's propagator (and, backward, the stored states) into a second
+// shared-memory buffer with cp.async while it computes the current slice, so
+// the sequential chain waits on shared memory, not on HBM.
+template <int D> struct StCfg {
+  static constexpr int TPC = D >= 64 ? 1 : 4;  // members (warps) per CTA
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// bytes (a multiple of 16) from global to shared, spread over the warp
+__device__ __forceinline__ void warp_copy_async(int lane, void* dst, const void* src, size_t bytes) {
+  const int n = (int)(bytes / 16);
+  for (int i = lane; i < n; i += 32)
+    cp_async16(static_cast<char*>(dst) + 16 * (size_t)i, static_cast<const char*>(src) + 16 * (size_t)i);
+  cp_async_commit();
+}
+
+template <int D> __host__ __device__ constexpr size_t st_fwd_team_bytes(int np) {
+  return (2 * (size_t)D * D + (size_t)np * D) * sizeof(float4);
+}
+template <int D> __host__ __device__ constexpr size_t st_bwd_team_bytes(int np) {
+  return 2 * (size_t)D * D * sizeof(float4) + (size_t)np * D * sizeof(float2);
+}
+
+// Forward in df: psi_s[k+1] = U_k psi_s[k], U_k the df propagator of the expm
+// stage.  The states are stored in FP32 for the gradient; z_s = <t_s|psi_s[n]>,
+// f(z_s) and kappa_s come from the df state in FP64, as the FP64 chain forms
+// them.  Utot[m np + s] receives the propagation residual of the pair in
+// FP64: |psi[n]|^2 - |psi[0]|^2 (Hermitian) or Tr rho[n] - Tr rho[0] (a
+// vectorised density matrix, N^2 = D).
+template <int D>
+__global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_fwd_mx(ProbDev p, WorkDev w, int store) {
+  constexpr int T = 32;
+  constexpr int NO = (8 * D + T - 1) / T;  // outputs per lane: at most 8 pairs
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * StCfg<D>::TPC + team;
+  if (m >= p.n_members) return;  // a whole warp: teams never share a barrier
+  const int np = p.n_pairs, pan = np * D;
+  float4* Ub = reinterpret_cast<float4*>(smem_raw + (size_t)team * st_fwd_team_bytes<D>(np));  // [2][D*D]
+  float4* Ps = Ub + 2 * D * D;                                                                   // [np][D]
+  float2* Pst = reinterpret_cast<float2*>(w.psi) + (size_t)m * (p.n_t + 1) * pan;
+  const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+  constexpr size_t UB = (size_t)D * D * sizeof(float4);
+  warp_copy_async(tm.lane, Ub, Um, UB);
+  for (int e = tm.lane; e < pan; e += T) {
+    Ps[e] = dfc_store(dfc_from(p.psi_init[e]));
+    if (store) Pst[e] = make_float2(Ps[e].x, Ps[e].y);
+  }
+  cp_async_wait_all();
+  tm.sync();
+  for (int k = 0; k < p.n_t; ++k) {
+    const float4* Uk = Ub + (size_t)(k & 1) * D * D;
+    if (k + 1 < p.n_t)  // the other buffer was last read at slice k - 1
+      warp_copy_async(tm.lane, Ub + (size_t)((k + 1) & 1) * D * D, Um + (size_t)(k + 1) * D * D, UB);
+    float4 outv[NO];
+#pragma unroll
+    for (int i = 0; i < NO; ++i) {
+      const int e = tm.lane + T * i;
+      if (e < pan) {
+        const int s = e / D, r = e % D;
+        DfAcc acc;
+        for (int q = 0; q < D; ++q) acc.mac(Uk[r + D * q], Ps[s * D + q]);
+        outv[i] = dfc_store(acc.result());
+      }
+    }
+    tm.sync();
+#pragma unroll
+    for (int i = 0; i < NO; ++i) {
+      const int e = tm.lane + T * i;
+      if (e < pan) {
+        Ps[e] = outv[i];
+        if (store) Pst[(size_t)(k + 1) * pan + e] = make_float2(outv[i].x, outv[i].y);
+      }
+    }
+    cp_async_wait_all();
+    tm.sync();
+  }
+  int N = (int)lrint(sqrt((double)p.D));
+  if (p.gen != GEN_LIOUV || N * N != p.D) N = 0;
+  double Fm = 0.0;
+  for (int s = 0; s < np; ++s) {
+    double2 acc = make_double2(0.0, 0.0), res = make_double2(0.0, 0.0);
+    for (int r = tm.lane; r < D; r += T) {
+      const double2 v = dfc_to(dfc_load(Ps[s * D + r]));
+      const double2 v0 = p.psi_init[s * D + r];
+      acc = cmac_cj(acc, p.psi_targ[s * D + r], v);
+      if (p.gen == GEN_HERM) {
+        res.x += (v.x * v.x + v.y * v.y) - (v0.x * v0.x + v0.y * v0.y);
+      } else if (N && r < N * N && r % (N + 1) == 0) {
+        res.x += v.x - v0.x;
+        res.y += v.y - v0.y;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      res.x += __shfl_xor_sync(0xffffffffu, res.x, o);
+      res.y += __shfl_xor_sync(0xffffffffu, res.y, o);
+    }
+    double f;
+    double2 kap;
+    fid_kappa(acc, p.fid, p.grad_mode, f, kap);
+    Fm += f;
+    if (tm.lane == 0) {
+      const double wgt = p.m_weight[m];
+      w.z[(size_t)m * np + s] = acc;
+      w.kap[(size_t)m * np + s] = make_double2(kap.x * wgt, kap.y * wgt);
+      w.Utot[(size_t)m * np + s] = res;
+    }
+  }
+  if (tm.lane == 0) w.Fm[m] = Fm;
+}
+
+// Backward in FP32: lambda_s[n] = conj(kappa_s) t_s, lambda_s[k] = U_k'
+// lambda_s[k+1] with U_k rounded to FP32; every lambda[k] is stored (FP32)
+// for the gradient kernel, which forms M_k = sum_s psi_s[k] lambda_s[k+1]'
+// (lambda_s[k] for the first-order GRAPE formula) itself.
+template <int D>
+__global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_bwd_mx(ProbDev p, WorkDev w) {
+  constexpr int T = 32;
+  constexpr int NO = (8 * D + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int team = threadIdx.x / T;
+  const Team<T> tm{(int)(threadIdx.x % T)};
+  const int m = blockIdx.x * StCfg<D>::TPC + team;
+  if (m >= p.n_members) return;
+  const int np = p.n_pairs, pan = np * D;
+  unsigned char* base = smem_raw + (size_t)team * st_bwd_team_bytes<D>(np);
+  float4* Ub = reinterpret_cast<float4*>(base);                                         // [2][D*D]
+  float2* Ls = reinterpret_cast<float2*>(base + 2 * (size_t)D * D * sizeof(float4));  // [np][D]
+  const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+  float2* Lm = reinterpret_cast<float2*>(w.lam) + (size_t)m * (p.n_t + 1) * pan;
+  constexpr size_t UB = (size_t)D * D * sizeof(float4);
+  const int k0 = p.n_t - 1;
+  warp_copy_async(tm.lane, Ub, Um + (size_t)k0 * D * D, UB);
+  for (int e = tm.lane; e < pan; e += T) {
+    const double2 kp = w.kap[(size_t)m * np + e / D];
+    const double2 v = cmul(make_double2(kp.x, -kp.y), p.psi_targ[e]);
+    Ls[e] = make_float2((float)v.x, (float)v.y);
+    Lm[(size_t)p.n_t * pan + e] = Ls[e];
+  }
+  cp_async_wait_all();
+  tm.sync();
+  for (int k = k0; k >= 0; --k) {
+    const int slot = (k0 - k) & 1;
+    const float4* Uk = Ub + (size_t)slot * D * D;
+    if (k > 0)  // the other buffer was last read at slice k + 1
+      warp_copy_async(tm.lane, Ub + (size_t)(slot ^ 1) * D * D, Um + (size_t)(k - 1) * D * D, UB);
+    float2 outv[NO];
+#pragma unroll
+    for (int i = 0; i < NO; ++i) {
+      const int e = tm.lane + T * i;
+      if (e < pan) {
+        const int s = e / D, r = e % D;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int q = 0; q < D; ++q) {
+          const float4 u = Uk[q + D * r];
+          acc = cmac_cj(acc, make_float2(u.x, u.y), Ls[s * D + q]);
+        }
+        outv[i] = acc;
+      }
+    }
+    tm.sync();
+#pragma unroll
+    for (int i = 0; i < NO; ++i) {
+      const int e = tm.lane + T * i;
+      if (e < pan) {
+        Ls[e] = outv[i];
+        Lm[(size_t)k * pan + e] = outv[i];
+      }
+    }
+    cp_async_wait_all();
+    tm.sync();
+  }
+}
+
 // ---- gradient in FP32 -----------------------------------------------------------
 // g_j = Re(c dt scale Tr(X C_j)).  The team's first warp sums in a fixed order
 // (stride-32 partial sums, then a fixed shuffle tree) so that the result does
@@ -580,12 +766,33 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
   for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
     double* Gout = w.Gm + ((size_t)m * p.n_t + k) * p.n_c;
-    const float2* Mk = reinterpret_cast<const float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
-    if (!exact) {
-      trace_controls32<D, T, 0>(tm, p, Mk, m, k, Gout, red);
-      continue;
+    if (p.target == TGT_GATE) {
+      const float2* Mk = reinterpret_cast<const float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
+      if (!exact) {
+        trace_controls32<D, T, 0>(tm, p, Mk, m, k, Gout, red);
+        continue;
+      }
+      for (int e = tm.lane; e < D * D; e += T) W.dB[L::idx(e % D, e / D)] = Mk[e];
+    } else {  // M_k = sum_s psi_s[k] lambda_s[li]'
+      const int np = p.n_pairs, pan = np * D;
+      const int li = (p.grad_mode == GRAD_REF_GRAPE) ? k : k + 1;
+      const float2* ps = reinterpret_cast<const float2*>(w.psi) + ((size_t)m * (p.n_t + 1) + k) * pan;
+      const float2* ls = reinterpret_cast<const float2*>(w.lam) + ((size_t)m * (p.n_t + 1) + li) * pan;
+      for (int e = tm.lane; e < D * D; e += T) {
+        const int r = e % D, c = e / D;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int s = 0; s < np; ++s) {
+          const float2 l = ls[s * D + c];
+          acc = cmac(acc, ps[s * D + r], make_float2(l.x, -l.y));
+        }
+        W.dB[L::idx(r, c)] = acc;
+      }
+      if (!exact) {
+        tm.sync();
+        trace_controls32<D, T, kSwzGrad>(tm, p, W.dB, m, k, Gout, red);
+        continue;
+      }
     }
-    for (int e = tm.lane; e < D * D; e += T) W.dB[L::idx(e % D, e / D)] = Mk[e];
     build_A32<D, T, kSwzGrad>(tm, p, w, m, k, W.B);
     tm.sync();
     const float nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<float*>(red));
@@ -693,6 +900,14 @@ cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
 template <int D>
 static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
   using G = Cfg<D>;
+  if (p.target != TGT_GATE) {
+    constexpr int TPC = StCfg<D>::TPC;
+    const size_t smem = (size_t)TPC * st_fwd_team_bytes<D>(p.n_pairs);
+    ensure_smem_mx(k_chain_states_fwd_mx<D>, smem);
+    k_chain_states_fwd_mx<D><<<(p.n_members + TPC - 1) / TPC, 32 * TPC, smem, li.stream>>>(p, w, store ? 1 : 0);
+    ++*li.launches;
+    return cudaGetLastError();
+  }
   if (w.pit_blocks <= 1) {
     const size_t smem = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
     ensure_smem_mx(k_chain_gate_fwd_mx<D>, smem);
@@ -725,6 +940,14 @@ cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Launch
 template <int D>
 static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = Cfg<D>;
+  if (p.target != TGT_GATE) {
+    constexpr int TPC = StCfg<D>::TPC;
+    const size_t smem = (size_t)TPC * st_bwd_team_bytes<D>(p.n_pairs);
+    ensure_smem_mx(k_chain_states_bwd_mx<D>, smem);
+    k_chain_states_bwd_mx<D><<<(p.n_members + TPC - 1) / TPC, 32 * TPC, smem, li.stream>>>(p, w);
+    ++*li.launches;
+    return cudaGetLastError();
+  }
   if (w.pit_blocks <= 1) {
     const size_t smem = (size_t)G::TPC * 2 * D * D * sizeof(float2);
     ensure_smem_mx(k_chain_gate_bwd_mx<D>, smem);

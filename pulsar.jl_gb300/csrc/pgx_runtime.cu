@@ -229,8 +229,6 @@ static int validate(pgx_ctx* c, const pgx_problem_desc* d) {
     return ctx_fail(c, PGX_ERR_INVALID, "unknown gradient mode");
   if (d->precision != PGX_PREC_FP64 && d->precision != PGX_PREC_MIXED)
     return ctx_fail(c, PGX_ERR_INVALID, "unknown precision mode");
-  if (d->precision == PGX_PREC_MIXED && d->target != PGX_TARGET_GATE)
-    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "mixed precision serves gate targets; use FP64 for state targets");
   if (!d->dt || !d->drifts || !d->controls)
     return ctx_fail(c, PGX_ERR_INVALID, "dt, drifts and controls are required");
   const size_t DD = (size_t)d->dim * d->dim;
@@ -296,8 +294,9 @@ static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
   const size_t nm = d->n_members, nt = d->n_slices;
   const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
   s.U = nm * nt * DD * sizeof(double2);
-  s.P = d->target == PGX_TARGET_GATE ? nm * nt * DD * sizeof(double2) : 0;
-  s.Utot = nm * DD * sizeof(double2);
+  s.P = d->target == PGX_TARGET_GATE ? nm * nt * DD * sizeof(double2) : 0;  // forward chain, then M_k
+  // U_total per member; mixed state targets keep one residual per pair there
+  s.Utot = nm * std::max<size_t>(DD, np) * sizeof(double2);
   s.psi = np ? nm * (nt + 1) * np * Dp * sizeof(double2) : 0;
   s.z = nm * std::max<size_t>(np, 1) * sizeof(double2);
   s.Fm = nm * sizeof(double);
@@ -671,11 +670,30 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
   const bool want_grad = d_G != nullptr;
   Marks mk(c, stream == nullptr);
   int st;
-  if (p->desc.precision == PGX_PREC_MIXED) {  // gate targets (validated at create)
+  if (p->desc.precision == PGX_PREC_MIXED) {
     mk.mark(PGX_STAGE_EXPM);
     if ((st = ctx_cuda(c, pgx::launch_prep_mx(p->pd, w, li), "prep_mx"))) return st;
     if ((st = ctx_cuda(c, pgx::launch_expm_mx(p->pd, w, li), "expm_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_FWD);
+    if (want_grad && p->split_grad_states) {
+      // F from states_init; gradient from grad_states_init (Gradients.jl:153-157)
+      if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, false), "chain_fwd_mx(F)")) ||
+          (st = ctx_cuda(c, pgx::launch_reduce(p->pd, w, li, false), "reduce(F)")))
+        return st;
+      WorkDev w2 = w;
+      w2.F = p->d_F + 1;  // scratch: the gradient pass's own objective
+      if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd_grad, w2, li, true), "chain_fwd_mx"))) return st;
+      mk.mark(PGX_STAGE_CHAIN_BWD);
+      if ((st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd_grad, w2, li), "chain_bwd_mx"))) return st;
+      mk.mark(PGX_STAGE_GRAD);
+      if ((st = ctx_cuda(c, pgx::launch_grad_mx(p->pd_grad, w2, li), "grad_mx"))) return st;
+      mk.mark(PGX_STAGE_REDUCE);
+      st = ctx_cuda(c, pgx::launch_reduce(p->pd_grad, w2, li, true), "reduce");
+      if (!st) st = apply_penalties(p, w, true, li);
+      mk.mark(PGX_N_STAGES);
+      mk.commit();
+      return st;
+    }
     if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, want_grad), "chain_fwd_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_BWD);
     if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd, w, li), "chain_bwd_mx"))) return st;
@@ -864,18 +882,21 @@ static int eval_residual(pgx_problem* p, bool had_grad, double* out, int32_t* ki
   }
   if (d.target == PGX_TARGET_GATE)
     kind = liou ? (N ? PGX_RESID_TRACE : PGX_RESID_NONE) : PGX_RESID_UNITARITY;
-  else if (had_grad || p->pd.n_ck > 0)  // tracking stores its states on every evaluation
+  else if (had_grad || p->pd.n_ck > 0 || d.precision == PGX_PREC_MIXED)
+    // FP64 states are stored when G is computed (tracking: always); the mixed
+    // state chain records each pair's residual on every evaluation
     kind = liou ? (N ? PGX_RESID_STATE_TRACE : PGX_RESID_NONE) : PGX_RESID_NORM;
   *kind_out = kind;
   *out = 0.0;
   if (kind == PGX_RESID_NONE) return PGX_OK;
+  const int dev_kind = (d.target == PGX_TARGET_STATES && d.precision == PGX_PREC_MIXED) ? pgx::kResidPairs : kind;
   unsigned long long* bits = reinterpret_cast<unsigned long long*>(p->d_F + 2);
   pgx::LaunchInfo li = p->launch_info();
   double* h = p->h_stage + 2 * (size_t)d.n_controls * d.n_slices + 1;
   int st;
   if ((st = ctx_cuda(c, cudaMemsetAsync(bits, 0, sizeof(double), c->stream), "memset")) ||
-      (st = ctx_cuda(c, pgx::launch_residual(p->split_grad_states && had_grad ? p->pd_grad : p->pd, p->w, kind, N,
-                                             bits, li), "residual")) ||
+      (st = ctx_cuda(c, pgx::launch_residual(p->split_grad_states && had_grad ? p->pd_grad : p->pd, p->w, dev_kind,
+                                             N, bits, li), "residual")) ||
       (st = ctx_cuda(c, cudaMemcpyAsync(h, bits, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H")) ||
       (st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync")))
     return st;
@@ -1127,6 +1148,8 @@ extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t
   if (n > 0 && (d.target != PGX_TARGET_STATES || d.generator != PGX_GEN_HERMITIAN))
     return ctx_fail(c, PGX_ERR_UNSUPPORTED, "tracking needs a Hermitian problem with state targets "
                                             "(grape_tracking_kernel, GRAPETracking.jl:166-173)");
+  if (n > 0 && d.precision != PGX_PREC_FP64)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "tracking runs in FP64");
   if (n > 0 && d.grad_mode == PGX_GRAD_REF_GRAPE)
     return ctx_fail(c, PGX_ERR_UNSUPPORTED, "tracking has the MR first-order formula (PGX_GRAD_REF_MR) "
                                             "or the exact gradient");

@@ -149,6 +149,18 @@ def spin4_ensemble(seed: int = 7, n_t: int = 1000, n_off: int = 21, n_b1: int = 
     return spec, u0
 
 
+def spin4_state_transfer(seed: int = 7, n_t: int = 1000, n_off: int = 21, n_b1: int = 11):
+    """The spin-4 broadband system as an MR state-transfer ensemble
+    (MRControl / grape_state_kernel, GRAPEState.jl:136-250): the same members,
+    controls and amplitudes, two basis-state pairs |0000> -> |1111> and
+    |0101> -> |1010>, square fidelity, weights 1 / (members x pairs)."""
+    spec, u0 = spin4_ensemble(seed, n_t, n_off, n_b1)
+    e = np.eye(16, dtype=C128)
+    spec.target, spec.fidelity, spec.target_op = "states", "square", None
+    spec.states_init, spec.states_target = np.stack([e[0], e[5]]), np.stack([e[15], e[10]])
+    return spec, u0
+
+
 def _rand_herm(rng, d, sigma):
     A = rng.normal(0.0, sigma, (d, d)) + 1j * rng.normal(0.0, sigma, (d, d))
     return (A + A.conj().T) / 2

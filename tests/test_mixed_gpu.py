@@ -8,7 +8,7 @@ import pytest
 
 from oracle import members as mb
 import fx
-from test_parity_gpu import random_gate_problem, to_gpu
+from test_parity_gpu import rand_herm, random_gate_problem, to_gpu
 
 pytestmark = pytest.mark.gpu
 
@@ -80,8 +80,117 @@ def test_autotune_keeps_results_bit_identical(pg, d):
     p.close()
 
 
-def test_mixed_states_target_is_refused(pg):
-    prob, u0 = fx.single_qubit_transfer()
-    with pytest.raises(pg._abi.PgxError) as ei:
-        to_gpu(pg, prob, "exact", precision="mixed")
-    assert ei.value.status == 6
+MODES = ("ref_grape", "ref_mr", "exact")
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("explicit", [False, True])
+def test_mixed_single_qubit_transfer(pg, mode, explicit):
+    """The reference's CPU-runnable case (1 qubit, 100 slices, state target),
+    legacy and explicit initial-state semantics."""
+    prob, u0 = fx.single_qubit_transfer(explicit_init=explicit)
+    p = to_gpu(pg, prob, mode, precision="mixed")
+    F, G = p.eval(u0)
+    Fo, Go = mb.eval_problem(prob, u0, mode)
+    check(F, G, Fo, Go)
+    p.close()
+
+
+def _state_pairs(rng, d, fid, n_t=9):
+    drifts = np.stack([rand_herm(rng, d, 0.5) for _ in range(3)])
+    ctrls = np.stack([rand_herm(rng, d, 0.5) for _ in range(2)])
+    si = np.stack([fx.haar_unitary(rng, d)[:, 0] for _ in range(3)])
+    st = np.stack([fx.haar_unitary(rng, d)[:, 0] for _ in range(3)])
+    prob = mb.Problem(drifts=drifts, controls=ctrls, dt=rng.uniform(0.05, 0.2, n_t),
+                      member_drift=np.repeat(np.arange(3), 2), member_scale=np.tile([0.8, 1.3], 3),
+                      n_members=6, target="states", fidelity=fid, states_init=si, states_target=st)
+    return prob, rng.uniform(-1, 1, (2, n_t))
+
+
+@pytest.mark.parametrize("fid", ["square", "real", "modulus"])
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("d", [2, 3, 6, 16, 40])
+def test_mixed_state_pairs(pg, fid, mode, d):
+    """MR state transfer (GRAPEState.jl:136-250) with three pairs per member,
+    drifts x pwr members; d = 40 pads to the D = 64 kernels."""
+    prob, u0 = _state_pairs(np.random.default_rng(11 * d), d, fid)
+    p = to_gpu(pg, prob, mode, precision="mixed")
+    F, G = p.eval(u0)
+    Fo, Go = mb.eval_problem(prob, u0, mode)
+    check(F, G, Fo, Go)
+    F1, _ = p.eval(u0, want_grad=False)
+    assert F1 == F
+    p.close()
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_mixed_lindblad_states(pg, mode):
+    from oracle import ref_semantics as rs
+    rng = np.random.default_rng(9)
+    SZ = np.diag([1.0, -1.0]).astype(complex)
+    SX = np.array([[0, 1], [1, 0]], complex)
+    SY = np.array([[0, -1j], [1j, 0]], complex)
+    sm = np.array([[0, 1], [0, 0]], complex)
+    Ls = np.stack([rs.build_drift_liouvillian(2 * np.pi * o * SZ / 2, [sm, SZ], [40.0, 15.0])
+                   for o in (-500.0, 0.0, 500.0)])
+    Lc = np.stack([rs.build_control_liouvillian(SX / 2), rs.build_control_liouvillian(SY / 2)])
+    prob = mb.Problem(drifts=Ls, controls=Lc, dt=np.full(15, 1e-5), generator="liouvillian",
+                      member_drift=np.arange(3), member_scale=np.full(3, 2 * np.pi * 1e4), n_members=3,
+                      target="states", fidelity="square",
+                      states_init=rs.pure_state_to_vec_rho([1, 0])[None],
+                      states_target=rs.pure_state_to_vec_rho([0, 1])[None])
+    u0 = rng.uniform(-1, 1, (2, 15))
+    p = to_gpu(pg, prob, mode, precision="mixed")
+    F, G, st = p.eval(u0, stats=True)
+    Fo, Go = mb.eval_problem(prob, u0, mode)
+    check(F, G, Fo, Go)
+    assert st["residual_kind"] == "state_trace" and st["residual"] <= 1e-12
+    p.close()
+
+
+def test_mixed_legacy_gradient_states(pg):
+    """grape_optimize's gradient runs from the target state while F uses
+    the initial state (Gradients.jl:153-157): both passes in mixed precision
+    against the FP64 path."""
+    prob, u0 = _state_pairs(np.random.default_rng(3), 4, "square")
+    gs = np.roll(prob.states_init, 1, axis=0)
+    kw = dict(grad_states_init=gs)
+    p64, pmx = to_gpu(pg, prob, "exact", **kw), to_gpu(pg, prob, "exact", precision="mixed", **kw)
+    (F, G), (Fm, Gm) = p64.eval(u0), pmx.eval(u0)
+    assert abs(Fm - F) <= F_TOL_MIXED
+    assert np.max(np.abs(Gm - G)) <= G_RTOL_MIXED * np.max(np.abs(G))
+    assert abs(Fm - pmx.eval(u0, want_grad=False)[0]) == 0.0
+    p64.close()
+    pmx.close()
+
+
+def test_mixed_states_residual_and_autotune(pg):
+    prob, u0 = _state_pairs(np.random.default_rng(5), 16, "real", n_t=20)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F1, G1, st = p.eval(u0, stats=True)
+    assert st["residual_kind"] == "norm" and st["residual"] <= 1e-12, st
+    report = p.autotune(u0, reps=1)
+    assert "expm_mx" in report and "grad_mx" in report
+    F2, G2 = p.eval(u0)
+    assert F1 == F2 and np.array_equal(G1, G2)
+    p.close()
+
+
+def test_mixed_states_full_size_mr_ensemble(pg):
+    """The benchmark system as an MR state-transfer ensemble (231 members x
+    1000 slices, d = 16, |0000> -> |1111> and a second pair): mixed against
+    the FP64 GPU path at the mixed bars."""
+    spec, u0 = fx.W.spin4_ensemble()
+    kw = spec.problem_kwargs("exact", "fp64")
+    e = np.eye(16, dtype=complex)
+    kw.update(target="states", fidelity="square", target_op=None, states_init=np.stack([e[0], e[5]]),
+              states_target=np.stack([e[15], e[10]]), member_weight=None)
+    p64 = pg.Problem(**kw)
+    pmx = pg.Problem(**dict(kw, precision="mixed"))
+    (F, G), (Fm, Gm) = p64.eval(u0), pmx.eval(u0)
+    print(f"mixed states vs FP64: |dF| = {abs(Fm - F):.3e}, "
+          f"grad rel = {np.max(np.abs(Gm - G)) / np.max(np.abs(G)):.3e}")
+    assert abs(Fm - F) <= F_TOL_MIXED
+    assert np.max(np.abs(Gm - G)) <= G_RTOL_MIXED * np.max(np.abs(G))
+    p64.close()
+    pmx.close()

@@ -408,8 +408,10 @@ int pgx_batch_iterate(pgx_batch* batch, int32_t n_iter, const pgx_opt_desc* opt,
  * solo run, so its result is bit-identical alone and in any mix.
  * PGX_OPT_ENSEMBLE_LBFGS jobs run grape_optimize_ensemble's L-BFGS
  * (GRAPE.jl:1012-1230) with the direction, line-search trial points and the
- * (s, y) history in HBM, one evaluation per step.  Other methods are refused
- * (PGX_ERR_UNSUPPORTED).  The server uses a private context on the
+ * (s, y) history in HBM, one evaluation per step; PGX_OPT_MR_LBFGS and
+ * PGX_OPT_MR_GRAPE jobs run optimcon's MR loops (OptControl.jl:380-561,
+ * 594-611: bounds, Armijo-like line search with its fall-back, max|G|-scaled
+ * ascent) the same way.  The server uses a private context on the
  * device of ctx; errors of pgx_submit are recorded on ctx.  No reference
  * counterpart: Pulsar.jl optimises one problem per call.                   */
 enum { PGX_JOB_QUEUED = 0, PGX_JOB_RUNNING = 1, PGX_JOB_DONE = 2, PGX_JOB_FAILED = 3,

@@ -129,7 +129,9 @@ struct Hasher {
 };
 
 bool exact_of(const Ckpt& c) { return (c.info.flags & PGX_CKPT_EXACT) != 0; }
-bool lbfgs_of(const Ckpt& c) { return c.info.opt.method == PGX_OPT_ENSEMBLE_LBFGS; }
+bool lbfgs_of(const Ckpt& c) {
+  return c.info.opt.method == PGX_OPT_ENSEMBLE_LBFGS || c.info.opt.method == PGX_OPT_MR_LBFGS;
+}
 
 }  // namespace
 
@@ -255,7 +257,7 @@ int ckpt_decode(const void* blob, uint64_t len, Ckpt* out, std::string* why) {
       o.method < PGX_OPT_GRAPE || o.method > PGX_OPT_MR_GRAPE)
     return bad("checkpoint header fields out of range");
   const bool exact = (I.flags & PGX_CKPT_EXACT) != 0;
-  const bool lb = o.method == PGX_OPT_ENSEMBLE_LBFGS;
+  const bool lb = o.method == PGX_OPT_ENSEMBLE_LBFGS || o.method == PGX_OPT_MR_LBFGS;
   if (I.lbfgs_pairs > 0 && !(exact && lb)) return bad("L-BFGS pairs in a checkpoint that cannot hold them");
   const uint64_t n = (uint64_t)I.n_controls * (uint64_t)I.n_timesteps;
   if (n > (1ull << 31)) return bad("checkpoint waveform too large");

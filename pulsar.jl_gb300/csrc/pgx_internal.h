@@ -110,14 +110,16 @@ struct StepArgs {
 // the n problems of `a`, one CTA each.
 cudaError_t launch_ascent_step(const StepArgs& a, cudaStream_t stream);
 
-// Device state of one L-BFGS job (grape_optimize_ensemble, GRAPE.jl:1012-1230)
-// run by the server.  dmax, gnorm and zero come first: the host reads them back
-// as one 24-byte block.
+// Device state of one L-BFGS job run by the server: grape_optimize_ensemble
+// (GRAPE.jl:1012-1230) or the MR L-BFGS of optimcon (OptControl.jl:380-482).
+// dmax, gnorm, zero and gnew come first: the host reads them back as one
+// 32-byte block.
 constexpr int kLbMaxMemory = 64;
 struct LbState {
   double dmax;    // max |d| of the last direction (before normalisation)
   double gnorm;   // ||g|| at the current controls
   double zero;    // 1.0 when dmax < 1e-14
+  double gnew;    // ||gn|| at the trial point of the last F-and-G evaluation (MR)
   double a;       // current trial step
   int head;       // next history slot
   int count;      // stored pairs (<= m)
@@ -134,12 +136,22 @@ struct LbArgs {
   double* ut;         // trial controls
   const double* gn;   // gradient at the accepted trial point
   double a0;          // first trial step
-  double lim;         // amplitude limit (clip when clip != 0)
+  double lo, hi;      // trial points are clamped to [lo, hi] when clip != 0
   int clip;
+  int mr;             // MR rules: s = ut - u, no 1e-14 floors in the recursion
+  int n;              // control count (n_c x n_t)
 };
+enum { kTrialFirst = 0, kTrialHalve = 1, kTrialZero = 2 };
 cudaError_t launch_lb_direction(const LbArgs& a, cudaStream_t stream);
-cudaError_t launch_lb_trial(const LbArgs& a, bool halve, cudaStream_t stream);
+cudaError_t launch_lb_trial(const LbArgs& a, int mode, cudaStream_t stream);
 cudaError_t launch_lb_accept(const LbArgs& a, cudaStream_t stream);
+// st->gnew = ||gn|| (fixed-order reduction)
+cudaError_t launch_lb_gnorm(const LbArgs& a, cudaStream_t stream);
+// MR gradient ascent step (OptControl.jl:513-518): u += 0.05 (hi - lo) / max|G|
+// G, clamped to [lo, hi] (no step when max|G| <= 1e-14)
+cudaError_t launch_mr_step(double* u, const double* G, int n, double lo, double hi, cudaStream_t stream);
+// *out = ||v|| (one CTA, fixed-order reduction)
+cudaError_t launch_norm(const double* v, int n, double* out, cudaStream_t stream);
 
 // Raises a kernel's dynamic shared-memory limit (once per kernel and device).
 void set_smem_once(const void* fn, size_t bytes);

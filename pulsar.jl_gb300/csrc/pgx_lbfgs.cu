@@ -1,7 +1,9 @@
-// Device-resident L-BFGS of grape_optimize_ensemble (GRAPE.jl:1012-1230) for
-// served jobs: the two-loop recursion (GRAPE.jl:1064-1084, with its 1e-14
-// floors), the normalised direction, the clipped trial point of the
-// backtracking line search (:1088-1104) and the (s, y) history update with its
+// Device-resident L-BFGS for served jobs, in the two forms the reference has:
+// grape_optimize_ensemble (GRAPE.jl:1012-1230: the two-loop recursion with its
+// 1e-14 floors, clipped trial points, s = a d) and the MR L-BFGS of optimcon
+// (OptControl.jl:380-482, 565-611: no floors, trial points clamped to the
+// bounds, s = w_new - w).  Both: the normalised direction, the trial points of
+// the backtracking line search and the (s, y) history update with its
 // curvature test.  Every vector of a job (controls, gradients, direction,
 // trial point, the m-entry history) stays in HBM; the host reads back only
 // (F, max|d|, ||g||) to steer the line search.  One CTA per call; every
@@ -70,7 +72,7 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_direction(LbArgs A) {
     const double* y = A.Y + (size_t)nw * n;
     const double sy = dotv(s, y, n, red);
     const double yy = dotv(y, y, n, red);
-    const double gam = sy / fmax(yy, 1e-14);
+    const double gam = sy / (A.mr ? yy : fmax(yy, 1e-14));
     for (int i = threadIdx.x; i < n; i += kLbThreads) d[i] *= gam;
   }
   __syncthreads();  // alpha[] written by thread 0
@@ -96,23 +98,24 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_direction(LbArgs A) {
   }
 }
 
-// ut = clip(u + a d); halve: a <- a / 2 first.
-__global__ void __launch_bounds__(kLbThreads) k_lb_trial(LbArgs A, int halve) {
+// ut = clamp(u + a d); kTrialHalve: a <- a / 2 first; kTrialZero: a <- 0
+// (the MR line search's fall-back to the current point).
+__global__ void __launch_bounds__(kLbThreads) k_lb_trial(LbArgs A, int mode) {
   LbState* st = A.st;
-  const double a = halve ? 0.5 * st->a : st->a;
+  const double a = mode == kTrialHalve ? 0.5 * st->a : mode == kTrialZero ? 0.0 : st->a;
   __syncthreads();  // every thread has read st->a
   if (threadIdx.x == 0) st->a = a;
   const int n = st->n;
   for (int i = threadIdx.x; i < n; i += kLbThreads) {
     double v = fma(a, A.d[i], A.u[i]);
-    if (A.clip) v = fmin(fmax(v, -A.lim), A.lim);
+    if (A.clip) v = fmin(fmax(v, A.lo), A.hi);
     A.ut[i] = v;
   }
 }
 
-// s = a d, y = gn - g; kept when y.s > 1e-14 ||s||^2 (the oldest pair drops
-// out beyond m).  Then u <- ut and g <- gn, so a job's buffers never move and
-// its steps can be replayed as CUDA graphs.
+// s = a d (MR: ut - u), y = gn - g; kept when y.s > 1e-14 ||s||^2 (the oldest
+// pair drops out beyond m).  Then u <- ut and g <- gn, so a job's buffers never
+// move and its steps can be replayed as CUDA graphs.
 __global__ void __launch_bounds__(kLbThreads) k_lb_accept(LbArgs A) {
   __shared__ double red[kLbThreads];
   LbState* st = A.st;
@@ -120,7 +123,7 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_accept(LbArgs A) {
   const double a = st->a;
   double ss = 0.0, ys = 0.0;
   for (int i = threadIdx.x; i < n; i += kLbThreads) {
-    const double si = a * A.d[i], yi = A.gn[i] - A.g[i];
+    const double si = A.mr ? A.ut[i] - A.u[i] : a * A.d[i], yi = A.gn[i] - A.g[i];
     ss = fma(si, si, ss);
     ys = fma(yi, si, ys);
   }
@@ -135,27 +138,58 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_accept(LbArgs A) {
   for (int i = threadIdx.x; i < n; i += kLbThreads) {
     const double gi = A.gn[i];
     if (keep) {
-      s[i] = a * A.d[i];
+      s[i] = A.mr ? A.ut[i] - u[i] : a * A.d[i];
       y[i] = gi - g[i];
     }
     g[i] = gi;
     u[i] = A.ut[i];
   }
   if (keep && threadIdx.x == 0) {
-    A.rho[head] = 1.0 / fmax(ys, 1e-14);
+    A.rho[head] = 1.0 / (A.mr ? ys : fmax(ys, 1e-14));
     st->head = (head + 1) % m;
     st->count = st->count < m ? st->count + 1 : m;
   }
 }
 
+// *out = ||v||
+__global__ void __launch_bounds__(kLbThreads) k_norm(const double* v, int n, double* out) {
+  __shared__ double red[kLbThreads];
+  const double s = dotv(v, v, n, red);
+  if (threadIdx.x == 0) *out = sqrt(s);
+}
+
+// One MR ascent step: u <- clamp(u + (0.05 (hi - lo) / max|G|) G).
+__global__ void __launch_bounds__(kLbThreads) k_mr_step(double* u, const double* G, int n, double lo, double hi) {
+  __shared__ double red[kLbThreads];
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += kLbThreads) mx = fmax(mx, fabs(G[i]));
+  const double gmax = block_max(mx, red);
+  if (!(gmax > 1e-14)) return;
+  const double step = 0.05 * (hi - lo) / gmax;
+  for (int i = threadIdx.x; i < n; i += kLbThreads) u[i] = fmin(fmax(u[i] + step * G[i], lo), hi);
+}
+
 }  // namespace
+
+cudaError_t launch_lb_gnorm(const LbArgs& a, cudaStream_t stream) {
+  k_norm<<<1, kLbThreads, 0, stream>>>(a.gn, a.n, &a.st->gnew);
+  return cudaGetLastError();
+}
+cudaError_t launch_mr_step(double* u, const double* G, int n, double lo, double hi, cudaStream_t stream) {
+  k_mr_step<<<1, kLbThreads, 0, stream>>>(u, G, n, lo, hi);
+  return cudaGetLastError();
+}
+cudaError_t launch_norm(const double* v, int n, double* out, cudaStream_t stream) {
+  k_norm<<<1, kLbThreads, 0, stream>>>(v, n, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_lb_direction(const LbArgs& a, cudaStream_t stream) {
   k_lb_direction<<<1, kLbThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
-cudaError_t launch_lb_trial(const LbArgs& a, bool halve, cudaStream_t stream) {
-  k_lb_trial<<<1, kLbThreads, 0, stream>>>(a, halve ? 1 : 0);
+cudaError_t launch_lb_trial(const LbArgs& a, int mode, cudaStream_t stream) {
+  k_lb_trial<<<1, kLbThreads, 0, stream>>>(a, mode);
   return cudaGetLastError();
 }
 cudaError_t launch_lb_accept(const LbArgs& a, cudaStream_t stream) {

@@ -69,12 +69,14 @@ struct Readback {
   double F;
   double gnorm;
   double step;
-  double lb[3];  // L-BFGS jobs: dmax, gnorm, zero of the last direction
+  double lb[4];  // L-BFGS jobs: dmax, gnorm, zero of the last direction, ||gn|| (MR)
 };
 
 // Phases of an L-BFGS job: the evaluation in flight is F and G at the initial
-// controls, F at a trial point, or F and G at the accepted point.
-enum { LB_INIT = 0, LB_TRIAL = 1, LB_ACCEPT = 2 };
+// controls, F at a trial point, F at the MR line search's last fall-back
+// point, or F and G at the accepted point.
+enum { LB_INIT = 0, LB_TRIAL = 1, LB_ACCEPT = 2, LB_FALLBACK = 3 };
+enum { G_START = 0, G_HALVE = 1, G_FG = 2, G_HALVE_FG = 3, G_ACC_START = 4, G_ZERO_FG = 5, G_COUNT = 6 };
 
 struct Slot {
   cudaStream_t stream = nullptr;
@@ -110,16 +112,16 @@ struct Job {
   double F = 0.0, bestF = -INFINITY, step = 0.0;
   bool converged = false;
   clk::time_point t_submit, t_start, t_end;
-  // L-BFGS jobs (PGX_OPT_ENSEMBLE_LBFGS)
-  bool lbfgs = false;
+  // L-BFGS jobs (PGX_OPT_ENSEMBLE_LBFGS, PGX_OPT_MR_LBFGS); MR rules (MR_LBFGS, MR_GRAPE)
+  bool lbfgs = false, mr = false, mrgrape = false;
   int lb_phase = LB_INIT, lb_bt = 0, lb_it = 0;
   bool lb_grad_eval = true;      // the evaluation in flight computes G
   double lb_gnorm = 0.0;         // ||g|| at the start of the current iteration
   pgx::LbState* lb = nullptr;
   double *S = nullptr, *Yh = nullptr, *rho = nullptr, *own_u = nullptr, *own_g = nullptr, *dvec = nullptr;
   double *ucur = nullptr, *utry = nullptr, *gcur = nullptr, *gtry = nullptr;
-  cudaGraphExec_t lb_exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  int64_t lb_kernels[5] = {0, 0, 0, 0, 0};
+  cudaGraphExec_t lb_exec[G_COUNT] = {};
+  int64_t lb_kernels[G_COUNT] = {};
   bool lb_boundary = false;      // an iteration ended and its successor is not enqueued yet
   // histories and resumption
   std::vector<double> gh;        // gradient-norm history
@@ -212,8 +214,12 @@ void release_device(pgx_server* s, Job& j) {
 }
 
 // Iterations a job reports: grape_optimize counts steps, grape_optimize_ensemble
-// the entries of its fidelity history (GRAPE.jl:1218).
-int own_iterations(const Job& j) { return j.lbfgs ? (int)j.fh.size() : std::max(j.round, 0); }
+// the entries of its fidelity history (GRAPE.jl:1218), optimcon one less
+// (OptControl.jl:476, 555).
+int own_iterations(const Job& j) {
+  if (j.mr) return std::max((int)j.fh.size() - 1, 0);
+  return j.lbfgs ? (int)j.fh.size() : std::max(j.round, 0);
+}
 
 template <class T>
 std::vector<T> joined(const std::vector<T>& a, const std::vector<T>& b) {
@@ -398,6 +404,15 @@ int admit(pgx_server* s, Job& j) {
   const int64_t l0 = c->launches;
   if ((st = run_pipeline(j.prob, j.prob->d_u, j.prob->d_F, j.prob->d_G, sl.stream))) return st;
   s->launches += c->launches - l0;
+  if (j.mrgrape) {  // ||G(u0)|| opens the gradient-norm history (OptControl.jl:501)
+    if (pgx::launch_norm(j.prob->d_G, (int)n, &j.dev->gnorm, sl.stream) != cudaSuccess ||
+        cudaMemcpyAsync(&sl.hb->gnorm, &j.dev->gnorm, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      return PGX_ERR_CUDA;
+    }
+    s->launches += 1;
+  }
   if (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) !=
           cudaSuccess ||
       cudaEventRecord(sl.done, sl.stream) != cudaSuccess) {
@@ -408,11 +423,14 @@ int admit(pgx_server* s, Job& j) {
   return PGX_OK;
 }
 
-// One iteration of a job as a graph: step, evaluation, read-back.
+// One iteration of a job as a graph: step, evaluation, read-back.  grape_optimize
+// reads back (F, ||G|| and step of the step); MR GRAPE (OptControl.jl:512-531)
+// steps by 0.05 (u - l) / max|G|, clamps, and reads back (F, ||G||) at the new point.
 int capture_iteration(pgx_server* s, Job& j) {
   pgx_ctx* c = s->ctx;
   const Slot& sl = s->slots[j.slot];
   JobDev* d = j.dev;
+  const int n = j.desc.n_controls * j.desc.n_slices;
   const pgx::StepArgs a{&d->u, &d->G, &d->F, &d->len, &d->st, nullptr, &d->F_out, &d->gnorm,
                         1, 0, j.opt.adapt_step_size, j.opt.min_step_size, j.opt.max_step_size};
   const int64_t l0 = c->launches;
@@ -421,15 +439,17 @@ int capture_iteration(pgx_server* s, Job& j) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
-  int st = pgx::launch_ascent_step(a, sl.stream) == cudaSuccess ? PGX_OK : PGX_ERR_CUDA;
+  int st = (j.mrgrape ? pgx::launch_mr_step(j.prob->d_u, j.prob->d_G, n, j.opt.l_bound, j.opt.u_bound, sl.stream)
+                      : pgx::launch_ascent_step(a, sl.stream)) == cudaSuccess ? PGX_OK : PGX_ERR_CUDA;
   if (!st) st = run_pipeline(j.prob, j.prob->d_u, j.prob->d_F, j.prob->d_G, sl.stream);
+  if (!st && j.mrgrape && pgx::launch_norm(j.prob->d_G, n, &d->gnorm, sl.stream) != cudaSuccess) st = PGX_ERR_CUDA;
   if (!st && (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) !=
                   cudaSuccess ||
               cudaMemcpyAsync(&sl.hb->gnorm, &d->gnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                               sl.stream) != cudaSuccess))
     st = PGX_ERR_CUDA;
   const cudaError_t e = cudaStreamEndCapture(sl.stream, &g);
-  j.iter_kernels = 1 + (c->launches - l0);
+  j.iter_kernels = (j.mrgrape ? 2 : 1) + (c->launches - l0);
   c->launches = l0;  // recorded, not launched: each replay counts them
   if (!st && e != cudaSuccess) st = PGX_ERR_CUDA;
   if (!st && cudaGraphInstantiate(&j.iter_exec, g, 0) != cudaSuccess) st = PGX_ERR_CUDA;
@@ -511,7 +531,50 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
   return !stop;
 }
 
-// ---- L-BFGS jobs (opt_ensemble_lbfgs semantics, GRAPE.jl:1012-1230) --------
+// A finished evaluation of an MR GRAPE job (_optimcon_grape, OptControl.jl:
+// 486-561): every evaluation enters both histories and the best-controls
+// bookkeeping; the stop rules apply from the first step on.
+bool advance_mrgrape(pgx_server* s, Job& j, const Readback& rb, const char** why, int* err) {
+  const Slot& sl = s->slots[j.slot];
+  j.round += 1;
+  j.F = rb.F;
+  if (!std::isfinite(rb.F)) {
+    *err = PGX_ERR_NONFINITE;
+    *why = "non-finite objective";
+    return false;
+  }
+  j.fh.push_back(rb.F);
+  j.gh.push_back(rb.gnorm);
+  if (rb.F > j.bestF) {
+    j.bestF = rb.F;
+    const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
+    if (cudaMemcpyAsync(j.d_best, j.prob->d_u, n * sizeof(double), cudaMemcpyDeviceToDevice, sl.stream) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      *err = PGX_ERR_CUDA;
+      *why = "best-controls copy failed";
+      return false;
+    }
+  }
+  if (j.round == 0) return true;
+  if (rb.F >= 1.0 - 1e-8) {
+    j.converged = true;
+    *why = "near-perfect fidelity";
+  } else if (rb.gnorm < j.opt.gradient_norm_tol) {
+    j.converged = true;
+    *why = "gradient norm below tolerance";
+  } else if (rb.F >= s->cfg.target_fidelity) {
+    j.converged = true;
+    *why = "target fidelity reached";
+  } else if (j.round >= j.opt.max_iter) {
+    *why = "max iterations reached";
+  } else {
+    return true;
+  }
+  return false;
+}
+
+// ---- L-BFGS jobs (GRAPE.jl:1012-1230; MR: OptControl.jl:380-482, 594-611) --
 // A job's buffers never move (the accept kernel copies ut -> u and gn -> g),
 // so each kind of step is captured once per job as a CUDA graph:
 //   start       direction, first trial point, F there, read-back
@@ -519,29 +582,49 @@ bool advance(pgx_server* s, Job& j, const Readback& rb, const char** why, int* e
 //   fg          F and G at the trial point, read-back
 //   halve_fg    halved trial point, F and G there, read-back (after 20 halvings)
 //   acc_start   accept (history, u, g), then as start
+//   zero_fg     trial point = u, F and G there (MR fall-back: no move)
+// MR jobs add ||gn|| at the trial point to every F-and-G read-back.
+
+// First trial step: grape_optimize_ensemble's step_size (x amplitude_limit
+// when clipping); MR's 0.05 (u - l) (OptControl.jl:418).
+double lb_a0(const Job& j) {
+  if (j.mr) return 0.05 * (j.opt.u_bound - j.opt.l_bound);
+  const double lim = j.opt.amplitude_limit;
+  return std::isfinite(lim) ? j.opt.step_size * lim : j.opt.step_size;
+}
 
 pgx::LbArgs lb_args(const Job& j) {
   const double lim = j.opt.amplitude_limit;
-  const bool clip = std::isfinite(lim);
-  return pgx::LbArgs{j.lb, j.S, j.Yh, j.rho, j.ucur, j.gcur, j.dvec, j.utry, j.gtry,
-                     clip ? j.opt.step_size * lim : j.opt.step_size, clip ? lim : 0.0, clip ? 1 : 0};
+  const bool clip = j.mr || std::isfinite(lim);
+  const double lo = j.mr ? j.opt.l_bound : -lim, hi = j.mr ? j.opt.u_bound : lim;
+  return pgx::LbArgs{j.lb, j.S, j.Yh, j.rho, j.ucur, j.gcur, j.dvec, j.utry, j.gtry, lb_a0(j),
+                     clip ? lo : 0.0, clip ? hi : 0.0, clip ? 1 : 0, j.mr ? 1 : 0,
+                     j.desc.n_controls * j.desc.n_slices};
 }
 
 // Evaluation at the trial point (with G when `grad`) and the read-back of
-// (F, dmax, gnorm, zero); *k counts the kernels enqueued outside the pipeline.
-int lb_enqueue_eval(pgx_server* s, Job& j, bool grad) {
+// (F, dmax, gnorm, zero, gnew); *extra counts the kernels enqueued outside
+// the pipeline.
+int lb_enqueue_eval(pgx_server* s, Job& j, bool grad, int* extra) {
   const Slot& sl = s->slots[j.slot];
   const int st = run_pipeline(j.prob, j.utry, j.prob->d_F, grad ? j.gtry : nullptr, sl.stream);
   if (st) return st;
+  if (grad && j.mr) {
+    if (pgx::launch_lb_gnorm(lb_args(j), sl.stream) != cudaSuccess) {
+      cudaGetLastError();
+      return PGX_ERR_CUDA;
+    }
+    ++*extra;
+  }
   if (cudaMemcpyAsync(&sl.hb->F, j.prob->d_F, sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
-      cudaMemcpyAsync(sl.hb->lb, j.lb, 3 * sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess) {
+      cudaMemcpyAsync(sl.hb->lb, j.lb, 4 * sizeof(double), cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
   return PGX_OK;
 }
 
-enum { G_START = 0, G_HALVE = 1, G_FG = 2, G_HALVE_FG = 3, G_ACC_START = 4, G_COUNT = 5 };
+bool lb_kind_grad(int kind) { return kind == G_FG || kind == G_HALVE_FG || kind == G_ZERO_FG; }
 
 int lb_enqueue_step(pgx_server* s, Job& j, int kind, int* extra) {
   const cudaStream_t stm = s->slots[j.slot].stream;
@@ -553,13 +636,14 @@ int lb_enqueue_step(pgx_server* s, Job& j, int kind, int* extra) {
   bool good = true;
   if (kind == G_ACC_START) good = ok(pgx::launch_lb_accept(a, stm));
   if (good && (kind == G_START || kind == G_ACC_START))
-    good = ok(pgx::launch_lb_direction(a, stm)) && ok(pgx::launch_lb_trial(a, false, stm));
-  if (good && (kind == G_HALVE || kind == G_HALVE_FG)) good = ok(pgx::launch_lb_trial(a, true, stm));
+    good = ok(pgx::launch_lb_direction(a, stm)) && ok(pgx::launch_lb_trial(a, pgx::kTrialFirst, stm));
+  if (good && (kind == G_HALVE || kind == G_HALVE_FG)) good = ok(pgx::launch_lb_trial(a, pgx::kTrialHalve, stm));
+  if (good && kind == G_ZERO_FG) good = ok(pgx::launch_lb_trial(a, pgx::kTrialZero, stm));
   if (!good) {
     cudaGetLastError();
     return PGX_ERR_CUDA;
   }
-  return lb_enqueue_eval(s, j, kind == G_FG || kind == G_HALVE_FG);
+  return lb_enqueue_eval(s, j, lb_kind_grad(kind), extra);
 }
 
 // Launches step `kind` of job j (capturing its graph on first use).
@@ -591,7 +675,7 @@ int lb_launch(pgx_server* s, Job& j, int kind) {
     return PGX_ERR_CUDA;
   }
   s->launches += j.lb_kernels[kind];
-  j.lb_grad_eval = (kind == G_FG || kind == G_HALVE_FG);
+  j.lb_grad_eval = lb_kind_grad(kind);
   return PGX_OK;
 }
 
@@ -643,9 +727,11 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       }
       if ((st = lb_launch(s, j, G_START)) || (st = lb_arm(s, j))) return fail(st, "launch failed");
       return true;
-    case LB_TRIAL:
+    case LB_TRIAL: {
       if (j.lb_bt == 0) {
-        j.gh.push_back(rb.lb[1]);  // ||g|| of the iteration (GRAPE.jl:1062)
+        // ||g|| of the iteration (GRAPE.jl:1062); MR records ||G|| at the
+        // initial point here and each accepted point's at the accept
+        if (!j.mr || j.gh.empty()) j.gh.push_back(rb.lb[1]);
         j.lb_gnorm = rb.lb[1];
         if (rb.lb[2] != 0.0) {
           j.converged = true;
@@ -653,15 +739,27 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
           return false;
         }
       }
-      if (rb.F >= j.F) {  // accepted: F and G there
+      // MR accepts F >= F0 - 1e-4 |a| (OptControl.jl:603), the ensemble F >= F0
+      const double a = lb_a0(j) * std::ldexp(1.0, -j.lb_bt);  // exact: the device halves the same way
+      if (j.mr ? rb.F >= j.F - 1e-4 * std::fabs(a) : rb.F >= j.F) {  // accepted: F and G there
         j.lb_phase = LB_ACCEPT;
         st = lb_launch(s, j, G_FG);
+      } else if (j.mr) {  // backtrack: 20 trials, then one more at a / 2 (OptControl.jl:600-610)
+        j.lb_bt += 1;
+        if (j.lb_bt >= 20) j.lb_phase = LB_FALLBACK;
+        st = lb_launch(s, j, G_HALVE);
       } else {  // backtrack: halve (20 halvings, then take the last one)
         j.lb_bt += 1;
         if (j.lb_bt >= 20) j.lb_phase = LB_ACCEPT;
         st = lb_launch(s, j, j.lb_bt >= 20 ? G_HALVE_FG : G_HALVE);
       }
       if (st || (st = lb_arm(s, j))) return fail(st, "launch failed");
+      return true;
+    }
+    case LB_FALLBACK:  // MR: keep the last trial point only if it improves F
+      j.lb_phase = LB_ACCEPT;
+      if ((st = lb_launch(s, j, rb.F > j.F ? G_FG : G_ZERO_FG)) || (st = lb_arm(s, j)))
+        return fail(st, "launch failed");
       return true;
     default: {  // LB_ACCEPT: F and G at the accepted point
       const double Fprev = j.F;
@@ -671,7 +769,26 @@ bool advance_lbfgs(pgx_server* s, Job& j, const Readback& rb, const char** why, 
       const bool improved = j.F > j.bestF;
       if (improved) j.bestF = j.F;
       bool stop = true;
-      if (j.lb_gnorm < j.opt.gradient_norm_tol) {
+      if (j.mr) {  // OptControl.jl:465-471
+        j.gh.push_back(rb.lb[3]);
+        if (j.F >= 1.0 - 1e-8) {
+          j.converged = true;
+          *why = "near-perfect fidelity";
+        } else if (rb.lb[3] < j.opt.gradient_norm_tol) {
+          j.converged = true;
+          *why = "gradient norm below tolerance";
+        } else if (std::fabs(j.F - Fprev) < 1e-9) {
+          j.converged = true;
+          *why = "fidelity stalled";
+        } else if (j.F >= s->cfg.target_fidelity) {
+          j.converged = true;
+          *why = "target fidelity reached";
+        } else if (++j.lb_it > j.opt.max_iter) {
+          *why = "max iterations reached";
+        } else {
+          stop = false;
+        }
+      } else if (j.lb_gnorm < j.opt.gradient_norm_tol) {
         j.converged = true;
         *why = "gradient norm below tolerance";
       } else if (j.F >= 1.0 - 1e-8) {
@@ -840,7 +957,9 @@ void worker_loop(pgx_server* s) {
         const Readback rb = *sl.hb;
         if (!j->lbfgs || j->lb_grad_eval) s->units += j->units;
         std::lock_guard<std::mutex> lk(s->mu);  // polls read what advance() updates
-        go = j->lbfgs ? advance_lbfgs(s, *j, rb, &why, &err) : advance(s, *j, rb, &why, &err);
+        go = j->lbfgs     ? advance_lbfgs(s, *j, rb, &why, &err)
+             : j->mrgrape ? advance_mrgrape(s, *j, rb, &why, &err)
+                          : advance(s, *j, rb, &why, &err);
         want_snap = j->snap_req;
       }
       // An iteration boundary: the job continues and nothing of it is in
@@ -1001,18 +1120,25 @@ int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, co
   if (o->struct_size < sizeof(pgx_opt_desc) || o->max_iter < 1 || o->step_size <= 0.0 ||
       o->min_step_size <= 0.0 || o->max_step_size < o->step_size)
     return ctx_fail(c, PGX_ERR_INVALID, "invalid optimiser settings (GRAPE.jl:108-119)");
-  if (o->method != PGX_OPT_GRAPE && o->method != PGX_OPT_ENSEMBLE_LBFGS)
-    return ctx_fail(c, PGX_ERR_UNSUPPORTED,
-                    "the server runs grape_optimize and grape_optimize_ensemble (L-BFGS) jobs");
+  if (o->method != PGX_OPT_GRAPE && o->method != PGX_OPT_ENSEMBLE_LBFGS && o->method != PGX_OPT_MR_LBFGS &&
+      o->method != PGX_OPT_MR_GRAPE)
+    return ctx_fail(c, PGX_ERR_UNSUPPORTED, "unknown optimisation method");
+  const bool mr = o->method == PGX_OPT_MR_LBFGS || o->method == PGX_OPT_MR_GRAPE;
   if (o->method == PGX_OPT_ENSEMBLE_LBFGS &&
       (o->lbfgs_memory < 1 || o->lbfgs_memory > pgx::kLbMaxMemory || !(o->amplitude_limit > 0.0)))
     return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory must be in [1, 64] and amplitude_limit positive");
+  if (mr && !(std::isfinite(o->l_bound) && std::isfinite(o->u_bound) && o->l_bound < o->u_bound))
+    return ctx_fail(c, PGX_ERR_INVALID, "MR methods need finite bounds l_bound < u_bound");
+  if (o->method == PGX_OPT_MR_LBFGS && (o->lbfgs_memory < 1 || o->lbfgs_memory > pgx::kLbMaxMemory))
+    return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory must be in [1, 64]");
   const size_t D = d->dim, DD = D * D, nc = d->n_controls, nt = d->n_slices, nm = d->n_members;
   const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
   for (size_t i = 0; i < nc * nt; ++i)
     if (!std::isfinite(u0[i])) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
   auto j = std::make_shared<Job>();
-  j->lbfgs = o->method == PGX_OPT_ENSEMBLE_LBFGS;
+  j->lbfgs = o->method == PGX_OPT_ENSEMBLE_LBFGS || o->method == PGX_OPT_MR_LBFGS;
+  j->mr = mr;
+  j->mrgrape = o->method == PGX_OPT_MR_GRAPE;
   j->footprint = problem_footprint(d, s->ctx->num_sms) + sizeof(JobDev) + nc * nt * sizeof(double);
   if (j->lbfgs)  // (s, y) history, rho, trial controls and gradient, direction
     j->footprint += sizeof(pgx::LbState) + sizeof(double) * ((2 * (size_t)o->lbfgs_memory + 3) * nc * nt +
@@ -1049,6 +1175,8 @@ int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, co
   j->desc.grad_states_init = P(j->sgrad);
   j->opt = *o;
   j->u.assign(u0, u0 + nc * nt);
+  if (mr)  // optimcon clamps the guess to the bounds first (OptControl.jl:384, 491)
+    for (double& x : j->u) x = std::min(std::max(x, o->l_bound), o->u_bound);
   *out = std::move(j);
   return PGX_OK;
 }
@@ -1117,7 +1245,7 @@ extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const
       return ctx_fail(c, PGX_ERR_INVALID, "the checkpoint was taken on a different problem");
     if (opt.method != I.opt.method)
       return ctx_fail(c, PGX_ERR_INVALID, "exact continuation keeps the checkpoint's method");
-    if (opt.method == PGX_OPT_ENSEMBLE_LBFGS && opt.lbfgs_memory < I.lbfgs_pairs)
+    if ((opt.method == PGX_OPT_ENSEMBLE_LBFGS || opt.method == PGX_OPT_MR_LBFGS) && opt.lbfgs_memory < I.lbfgs_pairs)
       return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory is below the checkpoint's stored pairs");
   }
   std::shared_ptr<Job> j;
@@ -1213,7 +1341,7 @@ extern "C" int pgx_fetch(pgx_server* s, uint64_t id, double* u, pgx_opt_result* 
     std::memset(res, 0, sizeof(*res));
     res->fidelity = j.bestF;
     res->total_time_s = secs(j.t_submit, j.t_end);
-    res->step_size_final = j.lbfgs ? j.opt.step_size : j.step;
+    res->step_size_final = j.mrgrape ? 0.05 : j.mr ? 0.0 : j.lbfgs ? j.opt.step_size : j.step;
     res->n_iterations = j.prior_iter + own_iterations(j);
     res->history_len = (int32_t)(j.prior_fh.size() + j.fh.size());
     res->gnorm_history_len = (int32_t)(j.prior_gh.size() + j.gh.size());

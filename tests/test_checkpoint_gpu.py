@@ -60,11 +60,15 @@ def _submit(srv, spec, u0, method, opt, precision):
     return srv.submit(u0=u0, opt=opt, method=method, **spec.problem_kwargs("exact", precision))
 
 
+MR_OPT = dict(max_iter=300, gradient_norm_tol=1e-15, lbfgs_memory=4)
+
+
 @pytest.mark.parametrize("method,precision", [("grape", "fp64"), ("grape", "mixed"), ("ensemble_lbfgs", "fp64"),
-                                              ("ensemble_lbfgs", "mixed")])
+                                              ("ensemble_lbfgs", "mixed"), ("mr_lbfgs", "mixed"),
+                                              ("mr_grape", "fp64")])
 def test_exact_continuation_is_bit_identical(pg, ctx, method, precision):
     spec, u0 = _job()
-    opt = GRAPE_OPT if method == "grape" else LB_OPT
+    opt = {"grape": GRAPE_OPT, "ensemble_lbfgs": LB_OPT}.get(method, MR_OPT)
     kw = spec.problem_kwargs("exact", precision)
     srv = pg.Server(ctx, max_inflight=4, target_fidelity=2.0)
     a = _submit(srv, spec, u0, method, opt, precision)          # never interrupted

@@ -230,7 +230,82 @@ def test_lbfgs_submit_validation(pg, ctx):
     with pytest.raises(pg._abi.PgxError) as e:
         srv.submit(u0=u0, opt=dict(lbfgs_memory=0), method="ensemble_lbfgs", **spec.problem_kwargs("exact", "fp64"))
     assert e.value.status == 1
-    with pytest.raises(pg._abi.PgxError) as e:
-        srv.submit(u0=u0, method="mr_lbfgs", **spec.problem_kwargs("exact", "fp64"))
-    assert e.value.status == 6
+    for bad in (dict(l_bound=1.0, u_bound=-1.0), dict(l_bound=-np.inf), dict(lbfgs_memory=65)):
+        with pytest.raises(pg._abi.PgxError) as e:   # MR methods need finite bounds l < u
+            srv.submit(u0=u0, opt=bad, method="mr_lbfgs", **spec.problem_kwargs("exact", "fp64"))
+        assert e.value.status == 1
     srv.close()
+
+
+def _mr_problem(seed=2, n_t=40):
+    """An MR state-transfer ensemble (drifts x pwr levels, two pairs), the
+    kind optimcon serves (OptControl.jl:137-259)."""
+    rng = np.random.default_rng(seed)
+    sx = np.array([[0, 1], [1, 0]], complex) / 2
+    sy = np.array([[0, -1j], [1j, 0]], complex) / 2
+    sz = np.diag([0.5, -0.5]).astype(complex)
+    drifts = np.stack([2 * np.pi * off * sz for off in (-400.0, 0.0, 300.0)])
+    pwr = np.array([2 * np.pi * 0.9e3, 2 * np.pi * 1.1e3])
+    kw = dict(drifts=drifts, controls=np.stack([sx, sy]), dt=np.full(n_t, 1.2e-5), target="states",
+              fidelity="real", member_drift=np.repeat(np.arange(3), 2), member_scale=np.tile(pwr, 3),
+              states_init=np.array([[1, 0], [0, 1]], complex), states_target=np.array([[0, 1], [1, 0]], complex),
+              grad_mode="ref_mr")
+    return kw, rng.uniform(-0.8, 0.8, (2, n_t))
+
+
+@pytest.mark.parametrize("method", ["mr_lbfgs", "mr_grape"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mr_jobs_follow_optimcon(pg, ctx, method, precision):
+    """Served MR L-BFGS / GRAPE against the solo optimiser's optimcon loops
+    (OptControl.jl:380-561): iteration count, stop rule, result and histories;
+    the two differ only in the order of the device's dot products."""
+    kw, u0 = _mr_problem()
+    kw["precision"] = precision
+    opt = dict(max_iter=25, gradient_norm_tol=1e-9, lbfgs_memory=5, l_bound=-1.0, u_bound=1.0)
+    p = pg.Problem(ctx=ctx, **kw)
+    ref = p.optimize(u0 * 1.5, method, **opt)       # the guess is clamped to the bounds first
+    p.close()
+    srv = pg.Server(ctx, max_inflight=2, target_fidelity=2.0)
+    jid = srv.submit(u0=u0 * 1.5, opt=opt, method=method, **kw)
+    assert srv.drain(timeout_s=300)
+    r = srv.fetch(jid)
+    srv.close()
+    assert r.state == "done"
+    assert r.n_iterations == ref.n_iterations, (r.n_iterations, ref.n_iterations)
+    assert r.termination_reason == ref.termination_reason, (r.termination_reason, ref.termination_reason)
+    assert r.converged == ref.converged
+    assert abs(r.fidelity - ref.fidelity) <= 1e-9, (r.fidelity, ref.fidelity)
+    assert np.max(np.abs(r.controls - ref.controls)) <= 1e-6
+    assert np.max(r.controls) <= 1.0 and np.min(r.controls) >= -1.0
+    assert len(r.fidelity_history) == len(ref.fidelity_history)
+    assert np.allclose(r.fidelity_history, ref.fidelity_history, rtol=0, atol=1e-9)
+    assert len(r.gradient_norm_history) == len(ref.gradient_norm_history)
+    assert np.allclose(r.gradient_norm_history, ref.gradient_norm_history, rtol=1e-7, atol=1e-12)
+
+
+def test_mr_jobs_identical_alone_and_in_the_mix(pg, ctx):
+    kw, u0 = _mr_problem(seed=5)
+    opt = dict(max_iter=15, lbfgs_memory=4)
+    solo = {}
+    for method in ("mr_lbfgs", "mr_grape"):
+        s = pg.Server(ctx, max_inflight=1, target_fidelity=2.0)
+        solo[method] = _run_one(s, kw, u0, method, opt)
+        s.close()
+    mix = pg.Server(ctx, max_inflight=8, target_fidelity=2.0)
+    ids = {m: mix.submit(u0=u0, opt=opt, method=m, **kw) for m in ("mr_lbfgs", "mr_grape")}
+    for spec, ux in _jobs()[:3]:
+        mix.submit(u0=ux, opt=OPT, **spec.problem_kwargs("exact", "mixed"))
+    assert mix.drain(timeout_s=300)
+    for m, jid in ids.items():
+        r = mix.fetch(jid)
+        a = solo[m]
+        assert r.n_iterations == a.n_iterations and r.fidelity == a.fidelity
+        assert np.array_equal(r.controls, a.controls)
+        assert r.fidelity_history == a.fidelity_history
+    mix.close()
+
+
+def _run_one(srv, kw, u0, method, opt):
+    jid = srv.submit(u0=u0, opt=opt, method=method, **kw)
+    assert srv.drain(timeout_s=300)
+    return srv.fetch(jid)

@@ -300,6 +300,17 @@ int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slice
                                  const double* d_gens, const double* d_dt, double* d_U_total,
                                  void* stream, char* err, size_t err_len);
 
+/* ---- drift ramps ----------------------------------------------------------- */
+/* Robust drift trajectories (sample_drift_trajectories, RobustOpt.jl:168-182;
+ * build_ensemble_from_perturbations(:drift), PerturbationBuilder.jl:52-133):
+ * member m adds tau[k] ops[member_op[m]] to its generator at slice k (ops
+ * [n_ops][D*D] complex, Hermitian for Hermitian problems; member_op
+ * [n_members] in -1..n_ops-1, -1 = none; tau [n_slices]).  The reference's
+ * linear ramp is tau[k] = k / max(1, n_slices - 1).  n_ops = 0 removes the
+ * ramp.  Calling it again redraws the ensemble in place.                    */
+int pgx_problem_set_drift_ramp(pgx_problem* prob, int32_t n_ops, const double* ops, const int32_t* member_op,
+                               const double* tau);
+
 /* ---- trajectory tracking and phase-only controls ------------------------ */
 /* Tracking (MR/GRAPETracking.jl:166-277): on a Hermitian state-target
  * problem, n > 0 checkpoints replace the terminal objective by

@@ -64,6 +64,10 @@ class Problem:
     states_init: Optional[np.ndarray] = None    # [n_pairs, D]
     states_target: Optional[np.ndarray] = None  # [n_pairs, D]
     n_members: int = 1
+    # per-slice drift ramp: member m adds tau[k] ramp_ops[member_ramp[m]] at slice k
+    ramp_ops: Optional[np.ndarray] = None       # [n_ops, D, D]
+    member_ramp: Optional[np.ndarray] = None    # [n_members], -1 = none
+    tau: Optional[np.ndarray] = None            # [n_t]
 
     @property
     def D(self) -> int:
@@ -92,11 +96,13 @@ class Problem:
             w = np.asarray(self.member_weight, float)
         return di, sc, of, w
 
-    def generator_of(self, m: int, uk: np.ndarray) -> np.ndarray:
+    def generator_of(self, m: int, uk: np.ndarray, k: Optional[int] = None) -> np.ndarray:
         di, sc, of, _ = self.members()
         G = self.drifts[di[m]].astype(C128).copy()
         if self.offset_op is not None and of[m] != 0.0:
             G = G + of[m] * self.offset_op
+        if self.ramp_ops is not None and k is not None and self.member_ramp[m] >= 0:
+            G = G + self.tau[k] * self.ramp_ops[self.member_ramp[m]]
         for j in range(self.n_c):
             G = G + (sc[m] * uk[j]) * self.controls[j]
         return G
@@ -171,7 +177,7 @@ def eval_problem(prob: Problem, u: np.ndarray, grad_mode: str = "exact", want_gr
     G = np.zeros((n_c, n_t))
     Fm_list = []
     for m in range(prob.n_members):
-        Gens = [prob.generator_of(m, u[:, k]) for k in range(n_t)]
+        Gens = [prob.generator_of(m, u[:, k], k) for k in range(n_t)]
         U = np.stack([_propagator(prob, Gens[k], float(prob.dt[k])) for k in range(n_t)]) \
             if n_t else np.zeros((0, D, D), C128)
         P = rs.forward_propagators(U)

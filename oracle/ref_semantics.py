@@ -776,6 +776,32 @@ def grape_state_kernel(waveform: np.ndarray, ctrl: MRControl):
     return fid / N_ens, grad / N_ens
 
 
+def sample_drift_trajectories(dH_finals, n_timesteps: int) -> list:
+    """sample_drift_trajectories (RobustOpt.jl:168-182): trajectory s is the
+    linear ramp (k-1)/max(1, n_t-1) dH_final_s, k = 1..n_t, with dH_final_s
+    drawn as sample_parametric_perturbations draws them (given here)."""
+    out = []
+    for dH in dH_finals:
+        out.append([((k - 1) / max(1, n_timesteps - 1)) * np.asarray(dH, C128) for k in range(1, n_timesteps + 1)])
+    return out
+
+
+def fidelity_with_perturbation(H0, H_ctrls, controls: np.ndarray, dt: float, U_tgt, perturbation) -> float:
+    """_fidelity_with_perturbation (RobustOpt.jl:739-761): H_k = H0 + dH_k +
+    sum_j u_jk H_j (dH_k = perturbation[k] for a trajectory, the matrix
+    itself otherwise), U = prod exp(-i dt H_k), F = clamp(|Tr(U_t' U)|^2 /
+    d^2, 0, 1)."""
+    H0 = np.asarray(H0, C128)
+    d = H0.shape[0]
+    U = np.eye(d, dtype=C128)
+    for k in range(controls.shape[1]):
+        dHk = perturbation[k] if isinstance(perturbation, list) else perturbation
+        H = H0 + dHk + sum(controls[j, k] * np.asarray(H_ctrls[j], C128) for j in range(len(H_ctrls)))
+        U = expm_neg_i(H, dt) @ U
+    F = abs(np.trace(np.asarray(U_tgt, C128).conj().T @ U)) ** 2 / d ** 2
+    return float(min(max(F, 0.0), 1.0))
+
+
 @dataclass
 class TrackingPoint:
     """GRAPETracking.jl:82-91: the density matrix after propagating through

@@ -27,6 +27,7 @@ from .api import (
     grape_gradient_check, lindblad_grad_prefactor, matrix_exponential_cuda, state_fidelity,
     penalty_gradient, penalty_value, penalty_value_and_gradient,
     PerturbationEnsemble, build_ensemble_from_perturbations, sample_parametric_perturbations,
+    drift_ramp_schedule, sample_drift_trajectories,
     TrackingPoint, grape_phase_kernel, grape_tracking_kernel,
 )
 

@@ -160,6 +160,7 @@ SIGNATURES = {
     "pgx_plan_clear": (C.c_int, []),
     "pgx_problem_set_tracking": (C.c_int, [C.c_void_p, C.c_int32, iptr, dptr, dptr]),
     "pgx_eval_phase": (C.c_int, [C.c_void_p, dptr, dptr, dptr, dptr]),
+    "pgx_problem_set_drift_ramp": (C.c_int, [C.c_void_p, C.c_int32, dptr, iptr, dptr]),
     "pgx_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "pgx_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -760,35 +760,60 @@ def sample_parametric_perturbations(system: QuantumSystem, n_samples: int, magni
     return out
 
 
+def drift_ramp_schedule(n_timesteps: int) -> np.ndarray:
+    """(k - 1) / max(1, n_t - 1), k = 1..n_t: the linear drift ramp of
+    sample_drift_trajectories (RobustOpt.jl:173-177)."""
+    return np.arange(n_timesteps, dtype=np.float64) / max(1, n_timesteps - 1)
+
+
+def sample_drift_trajectories(system: QuantumSystem, n_samples: int, magnitude: float, n_timesteps: int,
+                              rng: Optional[np.random.Generator] = None) -> list:
+    """RobustOpt.jl:168-182: trajectory s is the ramp tau_k dH_final_s over the
+    n_t slices, dH_final drawn as sample_parametric_perturbations draws."""
+    tau = drift_ramp_schedule(n_timesteps)
+    return [[t * dH for t in tau] for dH in sample_parametric_perturbations(system, n_samples, magnitude, rng)]
+
+
 class PerturbationEnsemble(EnsembleObjective):
-    """build_ensemble_from_perturbations (PerturbationBuilder.jl:52-133), the
-    :parametric kind: sample i evolves under H_drift + dH_i.  All samples are
-    members of one device problem; with resample=True the perturbations are
-    redrawn (seed + call count) before every value_and_grad.  The gradient is
-    the exact gradient of each sample's fidelity (the reference
-    differentiates by central differences, eps 1e-5)."""
+    """build_ensemble_from_perturbations (PerturbationBuilder.jl:52-133).
+    :parametric -- sample i evolves under H_drift + dH_i; :drift -- under
+    H_drift + tau_k dH_i, the linear ramp of sample_drift_trajectories, as a
+    per-slice drift ramp of the device problem.  All samples are members of
+    one device problem; with resample=True the perturbations are redrawn
+    (seed + call count) before every value_and_grad.  The gradient is the
+    exact gradient of each sample's fidelity (the reference differentiates by
+    central differences, eps 1e-5)."""
 
     def __init__(self, system: QuantumSystem, target: QuantumTarget, controls: ControlSequence, magnitude: float,
                  n_samples: int, aggregator: str, cvar_alpha: float, resample: bool, seed: int,
-                 grad_mode: str = "exact", precision: str = "fp64"):
+                 grad_mode: str = "exact", precision: str = "fp64", uncertainty_type: str = "parametric"):
         if target.type != "unitary":
             raise ValueError("perturbation ensembles score gate fidelities (RobustOpt.jl:739-761)")
         self.system, self.magnitude, self.resample, self.seed = system, float(magnitude), resample, int(seed)
+        self.kind = uncertainty_type
         self._calls = 0
-        pert = sample_parametric_perturbations(system, n_samples, magnitude, np.random.default_rng(seed))
-        drifts = np.stack([system.H_drift + dH for dH in pert])
         n_t = controls.n_steps
+        self._tau = drift_ramp_schedule(n_t)
+        pert = sample_parametric_perturbations(system, n_samples, magnitude, np.random.default_rng(seed))
+        drift_kind = self.kind == "drift"
+        drifts = system.H_drift[None] if drift_kind else np.stack([system.H_drift + dH for dH in pert])
         prob = Problem(drifts, np.stack(system.H_controls), _dt_vec(controls.dt, n_t),
-                       member_drift=np.arange(n_samples), member_weight=np.full(n_samples, 1.0 / n_samples),
+                       member_drift=np.zeros(n_samples, int) if drift_kind else np.arange(n_samples),
+                       member_weight=np.full(n_samples, 1.0 / n_samples), n_members=n_samples,
                        target="gate", fidelity="square", target_op=target.target_unitary, grad_mode=grad_mode,
                        precision=precision)
+        if drift_kind:
+            prob.set_drift_ramp(np.stack(pert), np.arange(n_samples), self._tau)
         super().__init__(prob, n_samples, system.n_controls, n_t, aggregator, cvar_alpha)
 
     def _redraw(self):
         self._calls += 1
         rng = np.random.default_rng(self.seed + self._calls)
         pert = sample_parametric_perturbations(self.system, self.n_samples, self.magnitude, rng)
-        self.problem.set_drifts(np.stack([self.system.H_drift + dH for dH in pert]))
+        if self.kind == "drift":
+            self.problem.set_drift_ramp(np.stack(pert), np.arange(self.n_samples), self._tau)
+        else:
+            self.problem.set_drifts(np.stack([self.system.H_drift + dH for dH in pert]))
 
     def batched_eval(self, theta):
         if self.resample:
@@ -802,16 +827,14 @@ def build_ensemble_from_perturbations(system: QuantumSystem, target: QuantumTarg
                                       uncertainty_type: str = "parametric", magnitude: float = 0.05,
                                       n_samples: int = 20, aggregator: str = "mean", cvar_alpha: float = 0.2,
                                       resample: bool = True, seed: int = 42, precision: str = "fp64"):
-    """PerturbationBuilder.jl:52-133 (:parametric)."""
+    """PerturbationBuilder.jl:52-133 (:parametric and :drift)."""
     if uncertainty_type not in ("parametric", "drift"):
         raise ValueError("uncertainty_type must be :parametric or :drift for this builder; use robust_optimize "
                          "for :noise")
-    if uncertainty_type == "drift":
-        raise ValueError("the :drift ramp dH_k = t_k dH is not served by the device problem model")
     if n_samples <= 0:
         raise ValueError("n_samples must be positive")
     return PerturbationEnsemble(system, target, controls, magnitude, n_samples, aggregator, cvar_alpha, resample,
-                                seed, precision=precision)
+                                seed, precision=precision, uncertainty_type=uncertainty_type)
 
 
 def grape_optimize_ensemble(systems, target: QuantumTarget, controls_init: ControlSequence,

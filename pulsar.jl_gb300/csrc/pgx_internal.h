@@ -30,6 +30,14 @@ struct ProbDev {
   const double2* target_op;  // gate: [Dp*Dp]
   const double2* psi_init;   // states: [n_pairs][Dp]
   const double2* psi_targ;   // states: [n_pairs][Dp]
+  // per-slice drift ramp (robust drift trajectories): member m adds
+  // tau[k] ramp_ops[m_ramp[m]] to its generator at slice k
+  int n_ramp;                  // 0 = none
+  const int* m_ramp;           // [n_members], -1 = no ramp
+  const double2* ramp_ops;     // [n_ramp][Dp*Dp]
+  const double* tau;           // [n_t]
+  const float4* ramp_ops_df;   // mixed: df copies
+  const float2* tau_df;        // mixed: [n_t] df pairs
   // trajectory tracking (states targets): checkpoints in ascending step order
   int n_ck;                  // 0 = the terminal objective
   const int* ck_step;        // [n_ck] 1..n_t: the state after that many slices

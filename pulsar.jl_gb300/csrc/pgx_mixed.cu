@@ -92,9 +92,13 @@ __device__ __forceinline__ void build_A_df(const Team<T>& tm, const ProbDev& p, 
   const bool has_off = off.hi != 0.f;
   const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
   const float2* uk = w.u_df + (size_t)k * p.n_c;
+  const int ro = p.n_ramp ? p.m_ramp[m] : -1;
+  const float4* Rm = ro >= 0 ? p.ramp_ops_df + (size_t)ro * D * D : nullptr;
+  const df tk = ro >= 0 ? df_ld(p.tau_df[k]) : df{0.f, 0.f};
   for (int q = tm.lane; q < D * D; q += T) {
     dfc v = dfc_load(Gd[q]);
     if (has_off) v = dfc_add(v, dfc_scale(dfc_load(p.offset_df[q]), off));
+    if (Rm) v = dfc_add(v, dfc_scale(dfc_load(Rm[q]), tk));
     for (int j = 0; j < p.n_c; ++j) {
       const df a = df_mul(sc, df_ld(uk[j]));
       v = dfc_add(v, dfc_scale(dfc_load(p.ctrls_df[(size_t)j * D * D + q]), a));
@@ -112,10 +116,17 @@ __device__ __forceinline__ void build_A32(const Team<T>& tm, const ProbDev& p, c
   const float dt = p.dt_df[k].x, sc = p.m_scale_df[m].x, off = p.m_offset_df[m].x;
   const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
   const float2* uk = w.u_df + (size_t)k * p.n_c;
+  const int ro = p.n_ramp ? p.m_ramp[m] : -1;
+  const float4* Rm = ro >= 0 ? p.ramp_ops_df + (size_t)ro * D * D : nullptr;
+  const float tk = ro >= 0 ? p.tau_df[k].x : 0.f;
   for (int q = tm.lane; q < D * D; q += T) {
     const float4 g = Gd[q];
     const float4 o = p.offset_df[q];
     float vx = fmaf(off, o.x, g.x), vy = fmaf(off, o.y, g.y);
+    if (Rm) {
+      vx = fmaf(tk, Rm[q].x, vx);
+      vy = fmaf(tk, Rm[q].y, vy);
+    }
     for (int j = 0; j < p.n_c; ++j) {
       const float a = sc * uk[j].x;
       const float4 c = p.ctrls_df[(size_t)j * D * D + q];

@@ -1140,6 +1140,20 @@ extern "C" int pgx_propagator(pgx_ctx* c, int32_t dim, int32_t generator, const 
 // trajectory tracking and phase-only evaluation (MR/GRAPETracking.jl,
 // MR/GRAPEPhase.jl)
 // ---------------------------------------------------------------------------
+// Frees an owned device buffer of a problem ahead of its destruction.
+static void release_owned(pgx_problem* p, void*& ptr, uint64_t& bytes) {
+  if (!ptr) return;
+  pgx_ctx* c = p->ctx;
+  auto it = std::find(p->owned.begin(), p->owned.end(), ptr);
+  if (it != p->owned.end()) p->owned.erase(it);
+  if (c->pool) cudaFreeAsync(ptr, c->stream);
+  else cudaFree(ptr);
+  c->used -= bytes;
+  p->bytes -= bytes;
+  ptr = nullptr;
+  bytes = 0;
+}
+
 extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t* steps, const double* weights,
                                         const double* targets) {
   if (!p || n < 0 || (n > 0 && (!steps || !weights || !targets))) return PGX_ERR_INVALID;
@@ -1185,16 +1199,7 @@ extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t
   }
   int st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
   if (st) return st;
-  if (p->d_track) {  // the previous checkpoints
-    auto it = std::find(p->owned.begin(), p->owned.end(), p->d_track);
-    if (it != p->owned.end()) p->owned.erase(it);
-    if (c->pool) cudaFreeAsync(p->d_track, c->stream);
-    else cudaFree(p->d_track);
-    c->used -= p->track_bytes;
-    p->bytes -= p->track_bytes;
-    p->d_track = nullptr;
-    p->track_bytes = 0;
-  }
+  release_owned(p, p->d_track, p->track_bytes);  // the previous checkpoints
   if (n > 0) {
     if ((st = ctx_alloc(c, &p->d_track, bytes, p->owned, p->bytes))) return st;
     p->track_bytes = bytes;
@@ -1209,6 +1214,69 @@ extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t
     pd->ck_step = n ? reinterpret_cast<const int*>(base) : nullptr;
     pd->ck_weight = n ? reinterpret_cast<const double*>(base + off_w) : nullptr;
     pd->ck_target = n ? reinterpret_cast<const double2*>(base + off_t) : nullptr;
+  }
+  return PGX_OK;
+}
+
+extern "C" int pgx_problem_set_drift_ramp(pgx_problem* p, int32_t n_ops, const double* ops, const int32_t* member_op,
+                                          const double* tau) {
+  if (!p || n_ops < 0 || (n_ops > 0 && (!ops || !member_op || !tau))) return PGX_ERR_INVALID;
+  pgx_ctx* c = p->ctx;
+  const pgx_problem_desc& d = p->desc;
+  const int D = d.dim, Dp = p->Dp, nm = d.n_members, nt = d.n_slices;
+  if (n_ops > 0) {
+    if (!finite_all(ops, 2 * (size_t)n_ops * D * D) || !finite_all(tau, nt))
+      return ctx_fail(c, PGX_ERR_NONFINITE, "ramp operators and schedule must be finite");
+    if (d.generator == PGX_GEN_HERMITIAN)
+      for (int i = 0; i < n_ops; ++i)
+        if (herm_dev(ops + 2 * (size_t)i * D * D, D) > 1e-10)
+          return ctx_fail(c, PGX_ERR_INVALID, "ramp operators of a Hermitian problem must be Hermitian");
+    for (int m = 0; m < nm; ++m)
+      if (member_op[m] < -1 || member_op[m] >= n_ops)
+        return ctx_fail(c, PGX_ERR_INVALID, "member ramp index out of range");
+  }
+  cudaSetDevice(c->device);
+  const bool mixed = d.precision == PGX_PREC_MIXED;
+  auto up16 = [](size_t b) { return (b + 15) / 16 * 16; };
+  const size_t off_tau = up16((size_t)nm * sizeof(int));
+  const size_t off_ops = off_tau + up16((size_t)nt * sizeof(double));
+  const size_t ops_bytes = (size_t)n_ops * Dp * Dp * sizeof(double2);
+  const size_t off_tdf = off_ops + ops_bytes;
+  const size_t off_odf = off_tdf + up16((size_t)nt * sizeof(float2));
+  const size_t bytes = mixed ? off_odf + (size_t)n_ops * Dp * Dp * sizeof(float4) : off_tdf;
+  std::vector<unsigned char> host(n_ops > 0 ? bytes : 0, 0);
+  std::vector<double> opsp;
+  if (n_ops > 0) {
+    std::memcpy(host.data(), member_op, (size_t)nm * sizeof(int));
+    std::memcpy(host.data() + off_tau, tau, (size_t)nt * sizeof(double));
+    opsp = pad_mats(ops, n_ops, D, Dp);
+    std::memcpy(host.data() + off_ops, opsp.data(), ops_bytes);
+    if (mixed) {
+      const std::vector<double> tv(tau, tau + nt);
+      const std::vector<float> tdf = to_df_scalars(tv), odf = to_df_pairs(opsp);
+      std::memcpy(host.data() + off_tdf, tdf.data(), tdf.size() * sizeof(float));
+      std::memcpy(host.data() + off_odf, odf.data(), odf.size() * sizeof(float));
+    }
+  }
+  int st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st) return st;
+  release_owned(p, p->d_ramp, p->ramp_bytes);
+  if (n_ops > 0) {
+    if ((st = ctx_alloc(c, &p->d_ramp, bytes, p->owned, p->bytes))) return st;
+    p->ramp_bytes = bytes;
+    if ((st = ctx_cuda(c, cudaMemcpyAsync(p->d_ramp, host.data(), bytes, cudaMemcpyHostToDevice, c->stream),
+                       "H2D ramp")) ||
+        (st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync")))
+      return st;
+  }
+  unsigned char* base = static_cast<unsigned char*>(p->d_ramp);
+  for (pgx::ProbDev* pd : {&p->pd, &p->pd_grad}) {
+    pd->n_ramp = n_ops;
+    pd->m_ramp = n_ops ? reinterpret_cast<const int*>(base) : nullptr;
+    pd->tau = n_ops ? reinterpret_cast<const double*>(base + off_tau) : nullptr;
+    pd->ramp_ops = n_ops ? reinterpret_cast<const double2*>(base + off_ops) : nullptr;
+    pd->tau_df = n_ops && mixed ? reinterpret_cast<const float2*>(base + off_tdf) : nullptr;
+    pd->ramp_ops_df = n_ops && mixed ? reinterpret_cast<const float4*>(base + off_odf) : nullptr;
   }
   return PGX_OK;
 }

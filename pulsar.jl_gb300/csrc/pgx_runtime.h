@@ -48,6 +48,8 @@ struct pgx_problem {
   int n_pen = 0;
   void* d_track = nullptr;              // tracking checkpoints (steps | weights | targets)
   uint64_t track_bytes = 0;
+  void* d_ramp = nullptr;               // drift ramp (member index | tau | operators | df copies)
+  uint64_t ramp_bytes = 0;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};
     for (int i = 0; i < pgx::kNumTunable; ++i) li.team[i] = team[i];

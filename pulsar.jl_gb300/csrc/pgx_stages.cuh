@@ -51,11 +51,18 @@ __device__ __forceinline__ void build_A(const Team<T>& tm, const ProbDev& p, con
   const double sc = p.m_scale[m], off = p.m_offset[m];
   const double2* Gd = p.drifts + (size_t)p.m_drift[m] * D * D;
   const double* uk = u + (size_t)k * p.n_c;
+  const int ro = p.n_ramp ? p.m_ramp[m] : -1;
+  const double2* Rm = ro >= 0 ? p.ramp_ops + (size_t)ro * D * D : nullptr;
+  const double tk = ro >= 0 ? p.tau[k] : 0.0;
   for (int e = tm.lane; e < D * D; e += T) {
     double2 v = Gd[e];
     const double2 o = p.offset_op[e];
     v.x = fma(off, o.x, v.x);
     v.y = fma(off, o.y, v.y);
+    if (Rm) {
+      v.x = fma(tk, Rm[e].x, v.x);
+      v.y = fma(tk, Rm[e].y, v.y);
+    }
     for (int j = 0; j < p.n_c; ++j) {
       const double a = sc * uk[j];
       const double2 c = p.ctrls[(size_t)j * D * D + e];

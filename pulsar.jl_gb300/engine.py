@@ -628,6 +628,23 @@ class Problem:
         A.check(A.lib().pgx_problem_set_tracking(self._h, n, st.ctypes.data_as(A.iptr), A.as_dptr(wt),
                                                  A.as_dptr(tb)), self.ctx.handle)
 
+    def set_drift_ramp(self, ops, member_op, tau):
+        """Per-slice drift ramp (pgx_problem_set_drift_ramp): member m adds
+        tau[k] ops[member_op[m]] at slice k; empty ops remove it."""
+        ops = np.asarray(ops, np.complex128)
+        if ops.size == 0:
+            A.check(A.lib().pgx_problem_set_drift_ramp(self._h, 0, None, None, None), self.ctx.handle)
+            return
+        if ops.ndim != 3 or ops.shape[1:] != (self.D, self.D):
+            raise ValueError(f"ops have shape {ops.shape}, expected (n, {self.D}, {self.D})")
+        mo = np.ascontiguousarray(np.asarray(member_op, np.int64).astype(np.int32).ravel())
+        tv = np.ascontiguousarray(np.asarray(tau, np.float64).ravel())
+        if mo.size != self.n_members or tv.size != self.n_t:
+            raise ValueError("member_op needs one entry per member and tau one per slice")
+        ob = A.cmat_buf(ops)
+        A.check(A.lib().pgx_problem_set_drift_ramp(self._h, ops.shape[0], A.as_dptr(ob), mo.ctypes.data_as(A.iptr),
+                                                   A.as_dptr(tv)), self.ctx.handle)
+
     def eval_phase(self, phi, amplitudes=None, want_grad: bool = True):
         """Phase-only evaluation (pgx_eval_phase, GRAPEPhase.jl): phases and
         amplitudes [n_c / 2, n_t]; returns (F, dF/dphi or None)."""

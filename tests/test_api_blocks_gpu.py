@@ -8,6 +8,7 @@ fidelities (Objectives.jl), finite differences and grape_gradient_check
 import numpy as np
 import pytest
 
+import fx
 from oracle import ref_semantics as rs
 
 pytestmark = pytest.mark.gpu
@@ -237,3 +238,74 @@ def test_parametric_perturbation_ensemble(pg, aggregator):
                                                 aggregator=aggregator, resample=True, seed=5)
     F2, g2 = obj2.value_and_grad(theta)
     assert F2 != F and g2.shape == g.shape
+
+
+@pytest.mark.parametrize("aggregator", ["mean", "worst_case", "cvar"])
+def test_drift_trajectory_ensemble(pg, aggregator):
+    """build_ensemble_from_perturbations(:drift): sample i evolves under
+    H_drift + tau_k dH_i (sample_drift_trajectories' linear ramp,
+    RobustOpt.jl:168-182).  Per-sample F against the reference's
+    _fidelity_with_perturbation on the trajectory (RobustOpt.jl:739-761) and
+    (F, exact G) against the oracle's member model, then the aggregator."""
+    from oracle import members as mb
+    rng = np.random.default_rng(41)
+    d, n_c, n_t, dt = 3, 2, 11, 0.1
+    Hd, Hc = _herm(rng, d), [_herm(rng, d) for _ in range(n_c)]
+    T = _unitary(rng, d)
+    sys_g = pg.quantum_system(Hd, Hc)
+    u = rng.uniform(-1, 1, (n_c, n_t))
+    cs = pg.ControlSequence.from_controls(u, dt)
+    obj = pg.build_ensemble_from_perturbations(sys_g, pg.unitary_target(T), cs, uncertainty_type="drift",
+                                               magnitude=0.3, n_samples=5, aggregator=aggregator, cvar_alpha=0.4,
+                                               resample=False, seed=7)
+    finals = pg.sample_parametric_perturbations(sys_g, 5, 0.3, np.random.default_rng(7))
+    trajs = pg.sample_drift_trajectories(sys_g, 5, 0.3, n_t, np.random.default_rng(7))
+    tau = pg.drift_ramp_schedule(n_t)
+    Fi, Gi = [], []
+    for dH, traj in zip(finals, trajs):
+        prob = mb.Problem(drifts=Hd[None], controls=np.stack(Hc), dt=np.full(n_t, dt), target="gate",
+                          fidelity="square", target_op=T, ramp_ops=dH[None], member_ramp=np.zeros(1, int), tau=tau)
+        F1, G1 = mb.eval_problem(prob, u, "exact")
+        assert abs(F1 - rs.fidelity_with_perturbation(Hd, Hc, u, dt, T, traj)) <= 1e-12
+        Fi.append(F1)
+        Gi.append(G1)
+    Fo, Go = rs.aggregate(Fi, Gi, aggregator, 0.4)
+    theta = u.reshape(-1, order="F")
+    F, g = obj.value_and_grad(theta)
+    assert abs(F - Fo) <= 1e-12
+    assert np.max(np.abs(g - Go.reshape(-1, order="F"))) <= 1e-9 * max(1.0, np.max(np.abs(Go)))
+    obj2 = pg.build_ensemble_from_perturbations(sys_g, pg.unitary_target(T), cs, uncertainty_type="drift",
+                                                magnitude=0.3, n_samples=5, aggregator=aggregator, seed=7)
+    F2, _ = obj2.value_and_grad(theta)       # resampled (seed + 1) before the evaluation
+    assert F2 != F
+
+
+def test_drift_ramp_mixed_and_validation(pg, ctx):
+    """The ramp in the df32 / FP32 generator assembly (mixed precision), on a
+    d = 16 ensemble, against the oracle; and the setter's validation."""
+    from oracle import members as mb
+    spec, u0 = fx.W.spin4_ensemble(n_t=12, n_off=3, n_b1=2)
+    rng = np.random.default_rng(3)
+    ops = np.stack([_herm(rng, 16) * 2e3 for _ in range(2)])
+    mo = np.array([0, 1, -1, 0, 1, -1])
+    tau = np.linspace(0.0, 1.0, 12)
+    prob = mb.Problem.from_spec(spec)
+    prob.ramp_ops, prob.member_ramp, prob.tau = ops, mo, tau
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    for precision, ftol, gtol in (("fp64", 1e-10, 1e-8), ("mixed", 1e-8, 1e-4)):
+        p = pg.Problem(ctx=ctx, **spec.problem_kwargs("exact", precision))
+        p.set_drift_ramp(ops, mo, tau)
+        F, G = p.eval(u0)
+        assert abs(F - Fo) <= ftol, (precision, F, Fo)
+        assert np.max(np.abs(G - Go)) <= gtol * np.max(np.abs(Go)), precision
+        p.set_drift_ramp([], [], [])                # removed: the plain problem again
+        F0, _ = p.eval(u0)
+        assert abs(F0 - mb.eval_problem(mb.Problem.from_spec(spec), u0, "exact")[0]) <= ftol
+        E = pg._abi.PgxError
+        with pytest.raises(E) as e:
+            p.set_drift_ramp(ops, [0, 1, 2, 0, 1, 0], tau)      # index beyond the operators
+        assert e.value.status == 1
+        with pytest.raises(E) as e:
+            p.set_drift_ramp(ops + 1j * np.eye(16), mo, tau)     # not Hermitian
+        assert e.value.status == 1
+        p.close()

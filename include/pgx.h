@@ -466,6 +466,26 @@ int pgx_server_destroy(pgx_server* server);
  * footprint alone exceeds the server budget.                                */
 int pgx_submit(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_desc* opt,
                const double* u0, uint64_t* job_id);
+/* What a job's problem carries beyond its descriptor, applied at admission
+ * with pgx_problem_set_penalties / _set_tracking / _set_drift_ramp (each
+ * part unused when its count is 0; arrays as those calls take them).  A
+ * part the problem refuses fails the job at admission with the reason.     */
+typedef struct pgx_job_extras {
+  uint32_t struct_size;
+  int32_t n_penalties;
+  const pgx_penalty* penalties;
+  int32_t n_tracking;
+  int32_t n_ramp_ops;
+  const int32_t* tracking_steps;
+  const double* tracking_weights;
+  const double* tracking_targets;  /* [n_tracking][D*D] complex                    */
+  const double* ramp_ops;          /* [n_ramp_ops][D*D] complex                    */
+  const int32_t* ramp_member_op;   /* [n_members]                                  */
+  const double* ramp_tau;          /* [n_slices]                                   */
+} pgx_job_extras;
+/* pgx_submit with extras (nullable).                                        */
+int pgx_submit_ex(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_desc* opt, const double* u0,
+                  const pgx_job_extras* extras, uint64_t* job_id);
 int pgx_poll(pgx_server* server, uint64_t job_id, pgx_job_status* status);
 /* Result of a finished job: best controls u ([n_c x n_t], nullable) and the
  * grape_optimize summary (nullable; history lengths filled, the traces come
@@ -544,10 +564,12 @@ int pgx_job_checkpoint_read(pgx_server* server, uint64_t job_id, void* blob, uin
  * n_controls must match desc, and n_timesteps its n_slices.  opt (nullable:
  * the checkpoint's own settings) gives the new run's settings; under
  * RESTART its max_iter is the number of additional iterations.  CONTINUE
- * also requires an exact checkpoint of the same problem (fingerprint), the
- * same method and, for L-BFGS, lbfgs_memory >= the stored pairs.            */
+ * also requires an exact checkpoint of the same problem (fingerprint of the
+ * descriptor and the extras), the same method and, for L-BFGS,
+ * lbfgs_memory >= the stored pairs.                                         */
 int pgx_submit_resume(pgx_server* server, const pgx_problem_desc* desc, const pgx_opt_desc* opt,
-                      const void* blob, uint64_t blob_len, int32_t mode, uint64_t* job_id);
+                      const pgx_job_extras* extras, const void* blob, uint64_t blob_len, int32_t mode,
+                      uint64_t* job_id);
 /* Host-only (no device work): parses and verifies a blob (magic, version,
  * sizes, checksum; PGX_ERR_INVALID otherwise) into info and, when non-null,
  * w_opt ([n_c x n_t]) and the histories (history_len / gnorm_history_len

@@ -104,6 +104,15 @@ class ServeStats(C.Structure):
     ]
 
 
+class JobExtras(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("n_penalties", C.c_int32), ("penalties", C.c_void_p),
+        ("n_tracking", C.c_int32), ("n_ramp_ops", C.c_int32), ("tracking_steps", iptr),
+        ("tracking_weights", dptr), ("tracking_targets", dptr), ("ramp_ops", dptr), ("ramp_member_op", iptr),
+        ("ramp_tau", dptr),
+    ]
+
+
 class CheckpointInfo(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32), ("version", C.c_int32), ("flags", C.c_int32),
@@ -187,8 +196,11 @@ SIGNATURES = {
                                   C.POINTER(C.c_int32)]),
     "pgx_job_checkpoint": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double, C.POINTER(C.c_uint64)]),
     "pgx_job_checkpoint_read": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
-    "pgx_submit_resume": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(OptDesc), C.c_void_p,
-                                    C.c_uint64, C.c_int32, C.POINTER(C.c_uint64)]),
+    "pgx_submit_ex": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(OptDesc), dptr,
+                                C.POINTER(JobExtras), C.POINTER(C.c_uint64)]),
+    "pgx_submit_resume": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(OptDesc),
+                                    C.POINTER(JobExtras), C.c_void_p, C.c_uint64, C.c_int32,
+                                    C.POINTER(C.c_uint64)]),
     "pgx_checkpoint_parse": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(CheckpointInfo), dptr, dptr, dptr]),
     "pgx_checkpoint_metadata": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]),
     "pgx_checkpoint_create": (C.c_int, [C.POINTER(CheckpointInfo), dptr, dptr, dptr, C.c_char_p, C.c_void_p,

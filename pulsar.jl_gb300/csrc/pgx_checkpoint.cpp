@@ -290,7 +290,7 @@ int ckpt_decode(const void* blob, uint64_t len, Ckpt* out, std::string* why) {
   return PGX_OK;
 }
 
-uint64_t problem_fingerprint(const pgx_problem_desc* d) {
+uint64_t problem_fingerprint(const pgx_problem_desc* d, const pgx_job_extras* x) {
   const size_t D = (size_t)d->dim, DD = D * D, nc = (size_t)d->n_controls, nt = (size_t)d->n_slices;
   const size_t nm = (size_t)d->n_members, nd = (size_t)d->n_drifts;
   const size_t np = d->target == PGX_TARGET_STATES ? (size_t)d->n_pairs : 0;
@@ -312,6 +312,27 @@ uint64_t problem_fingerprint(const pgx_problem_desc* d) {
   h.f64s(np ? d->states_init : nullptr, 2 * np * D);
   h.f64s(np ? d->states_target : nullptr, 2 * np * D);
   h.f64s(np ? d->grad_states_init : nullptr, 2 * np * D);
+  if (x && (x->n_penalties > 0 || x->n_tracking > 0 || x->n_ramp_ops > 0)) {
+    const uint8_t xt[4] = {'P', 'G', 'X', 'X'};
+    h.bytes(xt, 4);
+    h.i32(x->n_penalties);
+    for (int i = 0; i < x->n_penalties; ++i) {
+      h.i32(x->penalties[i].type);
+      h.f64s(&x->penalties[i].weight, 3);  // weight, l_bound, u_bound
+    }
+    h.i32(x->n_tracking);
+    if (x->n_tracking > 0) {
+      h.i32s(x->tracking_steps, (size_t)x->n_tracking);
+      h.f64s(x->tracking_weights, (size_t)x->n_tracking);
+      h.f64s(x->tracking_targets, 2 * DD * (size_t)x->n_tracking);
+    }
+    h.i32(x->n_ramp_ops);
+    if (x->n_ramp_ops > 0) {
+      h.f64s(x->ramp_ops, 2 * DD * (size_t)x->n_ramp_ops);
+      h.i32s(x->ramp_member_op, nm);
+      h.f64s(x->ramp_tau, nt);
+    }
+  }
   return h.h;
 }
 

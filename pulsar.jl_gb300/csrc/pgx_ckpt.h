@@ -31,7 +31,8 @@ struct Ckpt {
 std::vector<uint8_t> ckpt_encode(const Ckpt& c);
 // Decodes and verifies a blob; on failure returns PGX_ERR_INVALID and *why.
 int ckpt_decode(const void* blob, uint64_t len, Ckpt* out, std::string* why);
-uint64_t problem_fingerprint(const pgx_problem_desc* d);
+// FNV-1a-64 of a descriptor and, when any part is set, of the job extras.
+uint64_t problem_fingerprint(const pgx_problem_desc* d, const pgx_job_extras* x = nullptr);
 double unix_now();
 
 }  // namespace pgx

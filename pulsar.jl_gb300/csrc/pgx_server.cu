@@ -96,6 +96,10 @@ struct Job {
   pgx_problem_desc desc{};
   pgx_opt_desc opt{};
   std::vector<double> u;        // initial controls, then the result
+  // owned copies of the job extras (penalties, tracking, drift ramp)
+  std::vector<pgx_penalty> pens;
+  std::vector<int32_t> tr_steps, ramp_mo;
+  std::vector<double> tr_w, tr_t, ramp_ops, ramp_tau;
   uint64_t footprint = 0;
   int64_t units = 0;            // member-slice units per evaluation
   // device side (worker thread only)
@@ -352,6 +356,13 @@ int admit(pgx_server* s, Job& j) {
   OnStream on(s, sl.stream);
   int st = pgx_problem_create(c, &j.desc, &j.prob);
   if (st) return st;
+  if ((!j.pens.empty() && (st = pgx_problem_set_penalties(j.prob, (int32_t)j.pens.size(), j.pens.data()))) ||
+      (!j.tr_steps.empty() && (st = pgx_problem_set_tracking(j.prob, (int32_t)j.tr_steps.size(), j.tr_steps.data(),
+                                                             j.tr_w.data(), j.tr_t.data()))) ||
+      (!j.ramp_mo.empty() &&
+       (st = pgx_problem_set_drift_ramp(j.prob, (int32_t)(j.ramp_ops.size() / (2 * (size_t)j.desc.dim * j.desc.dim)),
+                                        j.ramp_ops.data(), j.ramp_mo.data(), j.ramp_tau.data()))))
+    return st;
   const size_t n = (size_t)j.desc.n_controls * j.desc.n_slices;
   if (cudaMallocFromPoolAsync((void**)&j.dev, sizeof(JobDev), s->pool, sl.stream) != cudaSuccess ||
       cudaMallocFromPoolAsync((void**)&j.d_best, n * sizeof(double), s->pool, sl.stream) != cudaSuccess) {
@@ -1113,7 +1124,7 @@ namespace {
 
 // Validates a submission and builds its job (owned copies of every array).
 int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
-             std::shared_ptr<Job>* out) {
+             const pgx_job_extras* x, std::shared_ptr<Job>* out) {
   pgx_ctx* c = s->user;
   int st = validate_desc(c, d);
   if (st) return st;
@@ -1135,6 +1146,11 @@ int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, co
   const size_t np = d->target == PGX_TARGET_STATES ? d->n_pairs : 0;
   for (size_t i = 0; i < nc * nt; ++i)
     if (!std::isfinite(u0[i])) return ctx_fail(c, PGX_ERR_NONFINITE, "controls must be finite");
+  if (x && (x->struct_size < sizeof(pgx_job_extras) || x->n_penalties < 0 || x->n_penalties > PGX_MAX_PENALTIES ||
+            x->n_tracking < 0 || x->n_ramp_ops < 0 || (x->n_penalties > 0 && !x->penalties) ||
+            (x->n_tracking > 0 && (!x->tracking_steps || !x->tracking_weights || !x->tracking_targets)) ||
+            (x->n_ramp_ops > 0 && (!x->ramp_ops || !x->ramp_member_op || !x->ramp_tau))))
+    return ctx_fail(c, PGX_ERR_INVALID, "invalid job extras");
   auto j = std::make_shared<Job>();
   j->lbfgs = o->method == PGX_OPT_ENSEMBLE_LBFGS || o->method == PGX_OPT_MR_LBFGS;
   j->mr = mr;
@@ -1146,7 +1162,18 @@ int make_job(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, co
   if (s->cfg.hbm_budget_bytes && j->footprint > s->cfg.hbm_budget_bytes)
     return ctx_fail(c, PGX_ERR_BUDGET, "job footprint exceeds the server's HBM budget");
   j->units = (int64_t)nm * (int64_t)nt;
-  j->fingerprint = pgx::problem_fingerprint(d);
+  j->fingerprint = pgx::problem_fingerprint(d, x);
+  if (x) {
+    j->pens = copy_of(x->penalties, (size_t)x->n_penalties);
+    j->tr_steps = copy_of(x->tracking_steps, (size_t)x->n_tracking);
+    j->tr_w = copy_of(x->tracking_weights, (size_t)x->n_tracking);
+    j->tr_t = copy_of(x->tracking_targets, 2 * DD * (size_t)x->n_tracking);
+    if (x->n_ramp_ops > 0) {
+      j->ramp_ops = copy_of(x->ramp_ops, 2 * DD * (size_t)x->n_ramp_ops);
+      j->ramp_mo = copy_of(x->ramp_member_op, nm);
+      j->ramp_tau = copy_of(x->ramp_tau, nt);
+    }
+  }
   j->dt = copy_of(d->dt, nt);
   j->drifts = copy_of(d->drifts, 2 * DD * d->n_drifts);
   j->controls = copy_of(d->controls, 2 * DD * nc);
@@ -1203,16 +1230,22 @@ std::shared_ptr<Job> find_job(pgx_server* s, uint64_t id) {
 
 }  // namespace
 
-extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
-                          uint64_t* job_id) {
+extern "C" int pgx_submit_ex(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
+                             const pgx_job_extras* x, uint64_t* job_id) {
   if (!s || !d || !o || !u0 || !job_id) return PGX_ERR_INVALID;
   std::shared_ptr<Job> j;
-  const int st = make_job(s, d, o, u0, &j);
+  const int st = make_job(s, d, o, u0, x, &j);
   return st ? st : enqueue(s, std::move(j), job_id);
 }
 
-extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const void* blob,
-                                 uint64_t blob_len, int32_t mode, uint64_t* job_id) {
+extern "C" int pgx_submit(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o, const double* u0,
+                          uint64_t* job_id) {
+  return pgx_submit_ex(s, d, o, u0, nullptr, job_id);
+}
+
+extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const pgx_opt_desc* o,
+                                 const pgx_job_extras* x, const void* blob, uint64_t blob_len, int32_t mode,
+                                 uint64_t* job_id) {
   if (!s || !d || !blob || !job_id) return PGX_ERR_INVALID;
   pgx_ctx* c = s->user;
   if (mode != PGX_RESUME_RESTART && mode != PGX_RESUME_CONTINUE)
@@ -1241,7 +1274,7 @@ extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const
     if (!(I.flags & PGX_CKPT_EXACT))
       return ctx_fail(c, PGX_ERR_INVALID, "exact continuation needs a snapshot of a running or cancelled job");
     if (validate_desc(c, d)) return PGX_ERR_INVALID;
-    if (pgx::problem_fingerprint(d) != I.fingerprint)
+    if (pgx::problem_fingerprint(d, x) != I.fingerprint)
       return ctx_fail(c, PGX_ERR_INVALID, "the checkpoint was taken on a different problem");
     if (opt.method != I.opt.method)
       return ctx_fail(c, PGX_ERR_INVALID, "exact continuation keeps the checkpoint's method");
@@ -1249,7 +1282,7 @@ extern "C" int pgx_submit_resume(pgx_server* s, const pgx_problem_desc* d, const
       return ctx_fail(c, PGX_ERR_INVALID, "lbfgs_memory is below the checkpoint's stored pairs");
   }
   std::shared_ptr<Job> j;
-  const int st = make_job(s, d, &opt, cont ? ck->u.data() : ck->w.data(), &j);
+  const int st = make_job(s, d, &opt, cont ? ck->u.data() : ck->w.data(), x, &j);
   if (st) return st;
   if (cont) {  // the run goes on: its own histories continue, earlier runs' stay ahead
     j->prior_iter = ck->prior_iteration;

@@ -301,6 +301,50 @@ def problem_fingerprint(drifts, controls, dt, **problem) -> int:
     return int(fp.value)
 
 
+def penalty_array(penalties):
+    """[(type, weight[, l_bound, u_bound]), ...] -> pgx_penalty array."""
+    arr = (A.Penalty * max(len(penalties), 1))()
+    for i, pen in enumerate(penalties):
+        t, wgt = pen[0], pen[1]
+        lo, hi = (pen[2], pen[3]) if len(pen) > 2 else (-1.0, 1.0)
+        if t not in A.PENALTY:
+            raise ValueError(f"Unknown penalty ':{t}'. Valid: {', '.join(A.PENALTY)}")
+        arr[i].type, arr[i].weight, arr[i].l_bound, arr[i].u_bound = A.PENALTY[t], float(wgt), float(lo), float(hi)
+    return arr
+
+
+def job_extras(D: int, penalties=None, tracking=None, drift_ramp=None):
+    """pgx_job_extras of a server job (None when nothing is set) and the
+    buffers it points into."""
+    if not penalties and tracking is None and drift_ramp is None:
+        return None, None
+    x = A.JobExtras()
+    x.struct_size = C.sizeof(A.JobExtras)
+    keep = []
+    if penalties:
+        arr = penalty_array(penalties)
+        keep.append(arr)
+        x.n_penalties, x.penalties = len(penalties), C.cast(arr, C.c_void_p)
+    if tracking is not None:
+        steps, weights, targets = tracking
+        st = np.ascontiguousarray(np.asarray(steps, np.int64).astype(np.int32).ravel())
+        wt = np.ascontiguousarray(np.asarray(weights, np.float64).ravel())
+        tg = A.cmat_buf(np.asarray(targets, np.complex128).reshape(-1, D, D))
+        keep += [st, wt, tg]
+        x.n_tracking = st.size
+        x.tracking_steps, x.tracking_weights, x.tracking_targets = st.ctypes.data_as(A.iptr), A.as_dptr(wt), \
+            A.as_dptr(tg)
+    if drift_ramp is not None:
+        ops, member_op, tau = drift_ramp
+        ob = A.cmat_buf(np.asarray(ops, np.complex128).reshape(-1, D, D))
+        mo = np.ascontiguousarray(np.asarray(member_op, np.int64).astype(np.int32).ravel())
+        tv = np.ascontiguousarray(np.asarray(tau, np.float64).ravel())
+        keep += [ob, mo, tv]
+        x.n_ramp_ops = np.asarray(ops).reshape(-1, D, D).shape[0]
+        x.ramp_ops, x.ramp_member_op, x.ramp_tau = A.as_dptr(ob), mo.ctypes.data_as(A.iptr), A.as_dptr(tv)
+    return x, keep
+
+
 class Server:
     """Continuous-batching GRAPE server (pgx_server): jobs are admitted by HBM
     footprint and iterate on the device, each at its own pace."""
@@ -328,25 +372,29 @@ class Server:
             pass
 
     def submit(self, drifts, controls, dt, u0, *, opt: Optional[dict] = None, method: str = "grape",
-               **problem) -> int:
-        """Queue one job: grape_optimize (method "grape") or the ensemble
-        L-BFGS of grape_optimize_ensemble ("ensemble_lbfgs").  ``problem``
-        takes Problem's keywords, ``opt`` opt_desc's (GRAPEConfig defaults).
-        Returns the job id."""
+               penalties=None, tracking=None, drift_ramp=None, **problem) -> int:
+        """Queue one job: grape_optimize ("grape"), the ensemble L-BFGS of
+        grape_optimize_ensemble ("ensemble_lbfgs") or optimcon's MR loops
+        ("mr_lbfgs", "mr_grape").  ``problem`` takes Problem's keywords, ``opt``
+        opt_desc's (GRAPEConfig defaults).  Optional job extras:
+        ``penalties`` as Problem.set_penalties, ``tracking`` = (steps, weights,
+        targets), ``drift_ramp`` = (ops, member_op, tau).  Returns the job id."""
         d, keep, (D, n_c, n_t, _, _) = problem_desc(drifts, controls, dt, **problem)
         u = np.asarray(u0, np.float64)
         if u.shape != (n_c, n_t):
             raise ValueError(f"controls have shape {u.shape}, expected {(n_c, n_t)}")
         ub = np.ascontiguousarray(u.T.ravel())
         o = opt_desc(method, **(opt or {}))
+        x, xkeep = job_extras(D, penalties, tracking, drift_ramp)
         jid = C.c_uint64()
-        A.check(A.lib().pgx_submit(self._h, C.byref(d), C.byref(o), A.as_dptr(ub), C.byref(jid)),
-                self.ctx.handle)
+        A.check(A.lib().pgx_submit_ex(self._h, C.byref(d), C.byref(o), A.as_dptr(ub),
+                                      C.byref(x) if x is not None else None, C.byref(jid)), self.ctx.handle)
         self._shape[int(jid.value)] = (n_c, n_t)
         return int(jid.value)
 
     def submit_resume(self, drifts, controls, dt, checkpoint: bytes, *, mode: str = "restart",
-                      opt: Optional[dict] = None, method: Optional[str] = None, **problem) -> int:
+                      opt: Optional[dict] = None, method: Optional[str] = None, penalties=None, tracking=None,
+                      drift_ramp=None, **problem) -> int:
         """Queue a job resumed from a checkpoint blob.  ``mode`` "restart" is
         resume_optimization (Checkpoint.jl:220-298): a fresh run from w_opt
         whose histories and iteration count follow the checkpoint's (opt's
@@ -362,9 +410,11 @@ class Server:
             kw = {k: v for k, v in base.items() if k != "method"}
             kw.update(opt or {})
             o = opt_desc(method or base["method"], **kw)
+        x, xkeep = job_extras(D, penalties, tracking, drift_ramp)
         jid = C.c_uint64()
-        A.check(A.lib().pgx_submit_resume(self._h, C.byref(d), C.byref(o) if o is not None else None, buf,
-                                          len(b), A.RESUME[mode], C.byref(jid)), self.ctx.handle)
+        A.check(A.lib().pgx_submit_resume(self._h, C.byref(d), C.byref(o) if o is not None else None,
+                                          C.byref(x) if x is not None else None, buf, len(b), A.RESUME[mode],
+                                          C.byref(jid)), self.ctx.handle)
         self._shape[int(jid.value)] = (n_c, n_t)
         return int(jid.value)
 
@@ -599,13 +649,7 @@ class Problem:
         """Subtract waveform penalties from every later evaluation:
         penalties = [(type, weight[, l_bound, u_bound]), ...] with type one of
         NS, SNS, SNSA, DNS, energy (Penalties.jl:197-330)."""
-        arr = (A.Penalty * max(len(penalties), 1))()
-        for i, pen in enumerate(penalties):
-            t, wgt = pen[0], pen[1]
-            lo, hi = (pen[2], pen[3]) if len(pen) > 2 else (-1.0, 1.0)
-            if t not in A.PENALTY:
-                raise ValueError(f"Unknown penalty ':{t}'. Valid: {', '.join(A.PENALTY)}")
-            arr[i].type, arr[i].weight, arr[i].l_bound, arr[i].u_bound = A.PENALTY[t], float(wgt), float(lo), float(hi)
+        arr = penalty_array(penalties)
         A.check(A.lib().pgx_problem_set_penalties(self._h, len(penalties), C.cast(arr, C.c_void_p)), self.ctx.handle)
 
     def set_tracking(self, steps, weights, targets):

@@ -43,7 +43,7 @@ def test_ctypes_layout_matches_c(tmp_path, pg):
               "pgx_opt_desc": A.OptDesc, "pgx_opt_result": A.OptResult,
               "pgx_server_desc": A.ServerDesc, "pgx_job_status": A.JobStatus,
               "pgx_serve_stats": A.ServeStats, "pgx_penalty": A.Penalty,
-              "pgx_checkpoint_info": A.CheckpointInfo}
+              "pgx_checkpoint_info": A.CheckpointInfo, "pgx_job_extras": A.JobExtras}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pgx.h"', "int main(void){"]
     for cname, py in fields.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

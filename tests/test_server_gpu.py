@@ -309,3 +309,78 @@ def _run_one(srv, kw, u0, method, opt):
     jid = srv.submit(u0=u0, opt=opt, method=method, **kw)
     assert srv.drain(timeout_s=300)
     return srv.fetch(jid)
+
+
+def _served_vs_solo(pg, ctx, kw, u0, method, opt, setup, extras, ftol=1e-9):
+    p = pg.Problem(ctx=ctx, **kw)
+    setup(p)
+    ref = p.optimize(u0, method, **opt)
+    p.close()
+    srv = pg.Server(ctx, max_inflight=2, target_fidelity=2.0)
+    jid = srv.submit(u0=u0, opt=opt, method=method, **extras, **kw)
+    assert srv.drain(timeout_s=300)
+    r = srv.fetch(jid)
+    srv.close()
+    assert r.state == "done", r.termination_reason
+    assert r.n_iterations == ref.n_iterations, (r.n_iterations, ref.n_iterations)
+    assert r.termination_reason == ref.termination_reason
+    assert abs(r.fidelity - ref.fidelity) <= ftol, (r.fidelity, ref.fidelity)
+    assert np.max(np.abs(r.controls - ref.controls)) <= 1e-6 * max(1.0, np.max(np.abs(ref.controls)))
+    assert np.allclose(r.fidelity_history, ref.fidelity_history, rtol=0, atol=ftol)
+    return r
+
+
+def test_served_mr_job_with_penalties(pg, ctx):
+    """An MR L-BFGS job with waveform penalties (GRAPEState.jl:571-584)."""
+    kw, u0 = _mr_problem(seed=8)
+    pens = [("SNS", 0.02, -0.6, 0.6), ("DNS", 0.01)]
+    opt = dict(max_iter=20, lbfgs_memory=5)
+    r = _served_vs_solo(pg, ctx, kw, u0, "mr_lbfgs", opt, lambda p: p.set_penalties(pens), dict(penalties=pens))
+    assert r.n_iterations > 2
+
+
+def test_served_tracking_job(pg, ctx):
+    """An MR GRAPE job on a trajectory-tracking objective (optimcon with
+    ctrl.tracking, OptControl.jl:328-345)."""
+    kw, u0 = _mr_problem(seed=9)
+    dn, up = np.array([0, 1], complex), np.array([1, 0], complex)
+    steps, weights = [10, 25, 40], [0.3, 0.3, 0.4]
+    targets = np.stack([np.outer(dn, dn), np.outer(up, up), np.outer(dn, dn)])
+    opt = dict(max_iter=15)
+    _served_vs_solo(pg, ctx, kw, u0, "mr_grape", opt, lambda p: p.set_tracking(steps, weights, targets),
+                    dict(tracking=(steps, weights, targets)))
+
+
+def test_served_drift_ramp_job_and_exact_resume(pg, ctx):
+    """A grape_optimize job on a drift-ramp ensemble; its exact snapshot
+    continues only with the same extras (they are part of the fingerprint)."""
+    rng = np.random.default_rng(12)
+    spec, u0 = W.uneven_problem(rng, d=8, n_t=60, n_members=3)
+    kw = spec.problem_kwargs("exact", "fp64")
+    A = rng.standard_normal((2, 8, 8)) + 1j * rng.standard_normal((2, 8, 8))
+    ops = 2 * np.pi * 1e5 * (A + np.conj(np.transpose(A, (0, 2, 1)))) / 2
+    ramp = (ops, [0, 1, -1], np.linspace(0.0, 1.0, 60))
+    opt = dict(max_iter=30, step_size=0.3, convergence_tol=1e-14)
+    r = _served_vs_solo(pg, ctx, kw, u0, "grape", opt, lambda p: p.set_drift_ramp(*ramp), dict(drift_ramp=ramp),
+                        ftol=1e-12)
+    srv = pg.Server(ctx, max_inflight=1, target_fidelity=2.0)
+    jid = srv.submit(u0=u0, opt=dict(opt, max_iter=400), drift_ramp=ramp, **kw)
+    import time
+    t0 = time.time()
+    while srv.poll(jid)["iterations"] < 3 and time.time() - t0 < 60:
+        time.sleep(0.001)
+    srv.cancel(jid)
+    assert srv.drain(timeout_s=300)
+    blob = srv.checkpoint(jid)
+    ref = srv.fetch(jid)
+    assert pg.checkpoint_parse(blob)["exact"]
+    with pytest.raises(pg._abi.PgxError):              # without its ramp: another problem
+        srv.submit_resume(checkpoint=blob, mode="continue", **kw)
+    full = srv.submit(u0=u0, opt=dict(opt, max_iter=400), drift_ramp=ramp, **kw)
+    cont = srv.submit_resume(checkpoint=blob, mode="continue", drift_ramp=ramp, **kw)
+    assert srv.drain(timeout_s=300)
+    a, b = srv.fetch(full), srv.fetch(cont)
+    assert a.n_iterations == b.n_iterations and a.fidelity == b.fidelity
+    assert np.array_equal(a.controls, b.controls) and a.fidelity_history == b.fidelity_history
+    srv.close()
+    assert ref.state == "cancelled" and r.n_iterations == 30

@@ -224,6 +224,98 @@ __device__ __forceinline__ void mm1_df(const Team<T>& tm, float4* out, const flo
   mm_df<D, T, false, SW>(tm, out, A, B, (const float4*)nullptr, (const float4*)nullptr, DfEpiNone{});
 }
 
+// Merge of two partial dot products held by lanes lane and lane ^ off of one
+// warp (both lanes end with the same sums: two_sum is exact, so its error term
+// does not depend on the operand order).
+__device__ __forceinline__ void dfacc_merge_xor(DfAcc& a, int off) {
+  const float sr = __shfl_xor_sync(0xffffffffu, a.sr, off), cr = __shfl_xor_sync(0xffffffffu, a.cr, off);
+  const float si = __shfl_xor_sync(0xffffffffu, a.si, off), ci = __shfl_xor_sync(0xffffffffu, a.ci, off);
+  float t, e;
+  two_sum(a.sr, sr, t, e);
+  a.sr = t;
+  a.cr = (a.cr + cr) + e;
+  two_sum(a.si, si, t, e);
+  a.si = t;
+  a.ci = (a.ci + ci) + e;
+}
+
+// Split of the k range of a triangular product: a power of two dividing D,
+// fixed per D so that every team size sums each entry in the same order.
+template <int D> struct TriSplit {
+  static constexpr int KS = (D >= 64) ? 1 : (D >= 32) ? 2 : 4;
+};
+
+// out = A*B in df for a product known to be Hermitian (anti = false) or
+// anti-Hermitian (anti = true) -- the powers of an anti-Hermitian matrix.
+// Only the D(D+1)/2 entries of the lower triangle are computed; the upper
+// triangle is written as their conjugates (negated when anti).
+//  - Entries are enumerated by row pairs: pair p (0 <= p < D/2) holds row
+//    D-1-p (columns 0..D-1-p) then row p (columns 0..p), D+1 entries each.
+//  - Each entry's dot product is split over KS consecutive lanes: lane q
+//    takes k = q, q + KS, ..., and the partial sums are merged by a fixed
+//    xor-shuffle tree.
+//  - Within each aligned block of 8 entries the groups are permuted so the
+//    8 lanes of one 128-bit shared-memory phase read KS consecutive k of
+//    columns KS apart: distinct banks for the B operand, a broadcast for A.
+// out must not alias A or B, and no lane may still read out from an earlier
+// step (each entry is stored as soon as its dot product completes).
+// Column-major layouts only (SW != 1).
+template <int D, int T, int SW = 0>
+__device__ __forceinline__ void mm_df_tri(const Team<T>& tm, float4* out, const float4* A, const float4* B,
+                                          bool anti) {
+  static_assert(SW != 1, "mm_df_tri indexes k linearly");
+  static_assert(T >= 32 && T % 32 == 0, "mm_df_tri shuffles within whole warps");
+  static_assert(D % 2 == 0 && D >= 8, "mm_df_tri pairs rows");
+  using L = Lay<D, SW>;
+  constexpr int KS = TriSplit<D>::KS, G = 8 / KS, KK = D / KS;
+  constexpr int NT = D * (D + 1) / 2, NTP = (NT + 7) / 8 * 8;
+  constexpr int NO = (NTP * KS + T - 1) / T;
+  constexpr int UNR = (D >= 64) ? 1 : (KK > 4 ? 2 : KK);
+  constexpr int PR = (NO < 2) ? NO : 2;
+  // rounds whose entries all lie in full blocks of 8 need no bounds test
+  constexpr int SAFE = (NT / 8) * 8 * KS / T;
+  const int q = tm.lane % KS;
+  const float sg = anti ? -1.f : 1.f;  // upper (c, r) = sg conj(lower (r, c))
+  // PR rounds at a time: their accumulators, merged and stored before the
+  // next ones start (out is not an operand, so no barrier is needed first)
+#pragma unroll
+  for (int i0 = 0; i0 < NO; i0 += PR) {
+    int ia[PR], ib[PR];  // storage index of (r, q) and of (q, c); ia = -1: no entry
+#pragma unroll
+    for (int u = 0; u < PR; ++u) {
+      const int i = i0 + u;
+      const int g = (tm.lane + T * i) / KS, x = g % 8;
+      const int e = (g - x) + x / G + KS * (x % G);
+      const int pr = e / (D + 1), j = e % (D + 1);
+      const bool lo_row = j < D - pr;
+      const int r = lo_row ? D - 1 - pr : pr, c = lo_row ? j : j - (D - pr);
+      const bool ok = i < NO && (i < SAFE || e < NT);
+      ia[u] = ok ? L::idx(r, q) : -1;
+      ib[u] = ok ? L::idx(q, c) : 0;
+    }
+    DfAcc acc[PR];
+#pragma unroll UNR
+    for (int j = 0; j < KK; ++j) {
+#pragma unroll
+      for (int u = 0; u < PR; ++u)
+        if ((i0 + u < SAFE) || ia[u] >= 0) acc[u].mac(A[ia[u] + L::LD * KS * j], B[ib[u] + KS * j]);
+    }
+#pragma unroll
+    for (int u = 0; u < PR; ++u) {
+      if (i0 + u >= NO) continue;  // uniform over the team
+#pragma unroll
+      for (int off = 1; off < KS; off <<= 1) dfacc_merge_xor(acc[u], off);
+      if (q != 0 || (i0 + u >= SAFE && ia[u] < 0)) continue;
+      const int r = ia[u], c = ib[u] / L::LD;  // q = 0: ia = r, ib = LD c
+      const float4 v = dfc_store(acc[u].result());
+      out[L::idx(r, c)] = v;
+      if (r != c)
+        out[L::idx(c, r)] = make_float4(sg * v.x, -sg * v.y, sg * v.z, -sg * v.w);
+    }
+  }
+  tm.sync();
+}
+
 // Taylor block C_i = c_{4i} I + c_{4i+1} B + c_{4i+2} B2 + c_{4i+3} B3 in df;
 // coef[k] = 1/k! as df.
 __device__ __forceinline__ dfc df_block(int i, int r, int c, const float4& b1, const float4& b2,
@@ -240,12 +332,24 @@ __device__ __forceinline__ dfc df_block(int i, int r, int c, const float4& b1, c
 // Horner steps i >= lo_from multiply B4 by a tail of size <= 1/(4(i+1))!; the
 // caller sets lo_from where D u32 ||B4||^(i+1) / (4(i+1))! is below df
 // precision, and those steps run in plain FP32.
-template <int D, int T, int SW = 0>
+// HERM (D >= 16, column-major layouts): B is anti-Hermitian, so B^2 and B^4
+// are Hermitian and B^3 anti-Hermitian, and their products run as triangular
+// ones.  The three power products share one call site (one copy of the
+// product's code: the kernel is instruction-cache bound otherwise).
+template <int D, int T, int SW = 0, bool HERM = false>
 __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* B3, float4* B4, float4* Y,
                               int m, int s, const df* coef, int lo_from = 1 << 30) {
-  mm1_df<D, T, SW>(tm, B2, B, B);
-  mm1_df<D, T, SW>(tm, B3, B2, B);
-  mm1_df<D, T, SW>(tm, B4, B2, B2);
+  constexpr bool TRI = HERM && D >= 16 && SW != 1;
+#pragma unroll 1
+  for (int st = 0; st < 3; ++st) {  // B2 = B B, B3 = B2 B, B4 = B2 B2
+    const float4* X = (st == 0) ? B : B2;
+    const float4* Z = (st == 2) ? B2 : B;
+    float4* out = (st == 0) ? B2 : (st == 1) ? B3 : B4;
+    if constexpr (TRI)
+      mm_df_tri<D, T, SW>(tm, out, X, Z, st == 1);
+    else
+      mm1_df<D, T, SW>(tm, out, X, Z);
+  }
   const int L = m / 4;
   for (int q = tm.lane; q < D * D; q += T) {
     const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);

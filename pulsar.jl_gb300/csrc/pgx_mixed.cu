@@ -186,8 +186,9 @@ __device__ __forceinline__ int lo_horner_from(float a, int L, int D) {
 }
 
 // ---- expm in df --------------------------------------------------------------
-template <int D, int T>
-__global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, WorkDev w) {
+// At D = 64 (workspace in global memory) two CTAs share an SM: 128 registers.
+template <int D, int T, bool HERM>
+__global__ void __launch_bounds__(CfgM<D, T>::THREADS, (D >= 64) ? 2 : 1) k_expm_mx(ProbDev p, WorkDev w) {
   using G = CfgM<D, T>;
   using L = Lay<D, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_expm_mx(ProbDev p, Work
       }
       tm.sync();
     }
-    taylor_exp_df<D, T, kSwzExpm>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef, lo_from);
+    taylor_exp_df<D, T, kSwzExpm, HERM>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef, lo_from);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
     for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
     tm.sync();
@@ -895,10 +896,12 @@ template <int D, int T>
 static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = CfgM<D, T>;
   const size_t smem = G::SMEM_E;
-  ensure_smem_mx(k_expm_mx<D, T>, smem);
-  const int grid = grid_for(k_expm_mx<D, T>, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC,
-                            li.num_sms, G::SLAB ? w.slab_teams : 0);
-  k_expm_mx<D, T><<<grid, G::THREADS, smem, li.stream>>>(p, w);
+  // Hermitian generators: an instance whose power products are triangular
+  const auto kern = (p.gen == GEN_HERM) ? k_expm_mx<D, T, true> : k_expm_mx<D, T, false>;
+  ensure_smem_mx(kern, smem);
+  const int grid = grid_for(kern, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC, li.num_sms,
+                            G::SLAB ? w.slab_teams : 0);
+  kern<<<grid, G::THREADS, smem, li.stream>>>(p, w);
   ++*li.launches;
   return cudaGetLastError();
 }

@@ -153,17 +153,13 @@ __device__ __forceinline__ float norm1f(const Team<T>& tm, const C* A, float* sc
     }
     best = fmaxf(best, s);
   }
-  if constexpr (T <= 32) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
-  } else {
-    scratch[tm.lane] = best;
+  for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if constexpr (T > 32) {  // max over the team's warps (exact in any order)
+    if (tm.lane % 32 == 0) scratch[tm.lane / 32] = best;
     tm.sync();
-    for (int w = T / 2; w > 0; w >>= 1) {
-      if (tm.lane < w) scratch[tm.lane] = fmaxf(scratch[tm.lane], scratch[tm.lane + w]);
-      tm.sync();
-    }
-    best = scratch[0];
+#pragma unroll
+    for (int w = 0; w < T / 32; ++w) best = fmaxf(best, scratch[w]);
     tm.sync();
   }
   return best * 1.00001f;
@@ -186,9 +182,15 @@ __device__ __forceinline__ int lo_horner_from(float a, int L, int D) {
 }
 
 // ---- expm in df --------------------------------------------------------------
-// At D = 64 (workspace in global memory) two CTAs share an SM: 128 registers.
+// Register budget: as many CTAs per SM as shared memory admits (at most 5;
+// two at D = 64, whose workspace lies in global memory).
+template <int D, int T> constexpr int expm_min_ctas() {
+  constexpr size_t kSmemSm = 227 * 1024;
+  constexpr size_t n = CfgM<D, T>::SLAB ? 2 : kSmemSm / CfgM<D, T>::SMEM_E;
+  return n < 1 ? 1 : n > 5 ? 5 : (int)n;
+}
 template <int D, int T, bool HERM>
-__global__ void __launch_bounds__(CfgM<D, T>::THREADS, (D >= 64) ? 2 : 1) k_expm_mx(ProbDev p, WorkDev w) {
+__global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_expm_mx(ProbDev p, WorkDev w) {
   using G = CfgM<D, T>;
   using L = Lay<D, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

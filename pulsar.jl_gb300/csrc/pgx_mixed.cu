@@ -181,6 +181,37 @@ __device__ __forceinline__ int lo_horner_from(float a, int L, int D) {
   return 1 << 30;
 }
 
+// Degree m and squarings s of the df expm.  Same thresholds as
+// choose_degree_f, but each candidate is costed by what it executes:
+//  - the three power products (weight kTriPowW each when triangular);
+//  - the df Horner steps (1 each);
+//  - the Horner steps lo_horner_from moves to FP32 (kLoHornerW each);
+//  - the s squarings (1 each).
+// Ties keep the lower degree.
+constexpr float kTriPowW = 0.8f, kLoHornerW = 0.25f;
+__device__ __forceinline__ void choose_degree_df(float nrm, int D, bool tri, int& m, int& s, int& lo_from) {
+  float best = 3.0e38f;
+  m = 4;
+  s = 0;
+  lo_from = 1 << 30;
+#pragma unroll
+  for (int i = 0; i < PGX_N_DEGREES; ++i) {
+    int si = 0;
+    float x = nrm;
+    while (x > c_thetadf[i] && si < 60) { x *= 0.5f; ++si; }
+    const int L = i + 1;
+    const int lo = lo_horner_from(x, L, D);
+    const int n_df = lo < L - 1 ? lo : L - 1;  // Horner steps i' = L-2 .. 0 below lo run in df
+    const float cost = 3.f * (tri ? kTriPowW : 1.f) + (float)n_df + kLoHornerW * (float)(L - 1 - n_df) + (float)si;
+    if (cost < best - 1e-3f) {
+      best = cost;
+      m = 4 * L;
+      s = si;
+      lo_from = lo;
+    }
+  }
+}
+
 // ---- expm in df --------------------------------------------------------------
 // Register budget: as many CTAs per SM as shared memory admits (at most 5;
 // two at D = 64, whose workspace lies in global memory).
@@ -213,9 +244,8 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
     build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
     tm.sync();
     const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
-    int deg, s;
-    choose_degree_f(nrm, c_thetadf, deg, s);
-    const int lo_from = lo_horner_from(ldexpf(nrm, -s), deg / 4, D);
+    int deg, s, lo_from;
+    choose_degree_df(nrm, D, HERM && D >= 16, deg, s, lo_from);
     if (s > 0) {  // B <- B / 2^s, exact in df
       const float sc = ldexpf(1.f, -s);
       for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df

@@ -52,9 +52,10 @@ template <int D, int T> struct CfgM {
   // expm kernel: five df matrices in the padded layout
   static constexpr size_t WSE = (size_t)5 * Lay<D, 2>::SIZE * sizeof(float4);
   static constexpr size_t SMEM_E = (SLAB ? 0 : TPC * WSE) + TPC * RED;
-  // gradient kernel: ten complex-float matrices in the padded layout; at
-  // D = 64 the six of the q = 2 form, which fit shared memory
-  static constexpr bool GRAD_Q2 = (D >= 64);
+  // gradient kernel: the q = 2 Paterson-Stockmeyer Frechet form, six
+  // complex-float matrices in the padded layout (fits shared memory at D = 64;
+  // at the norms of short slices it is also the cheaper form, below)
+  static constexpr bool GRAD_Q2 = true;
   static constexpr size_t WSG = (size_t)(GRAD_Q2 ? 6 : 10) * Lay<D, 2>::SIZE * sizeof(float2);
   static constexpr size_t SMEM_G = TPC * WSG + TPC * RED;
 };
@@ -209,6 +210,24 @@ __device__ __forceinline__ void choose_degree_df(float nrm, int D, bool tri, int
       s = si;
       lo_from = lo;
     }
+  }
+}
+
+// Degree m and squarings s of the q = 2 Frechet form: 3 (m/2 + s) product
+// units (X and dX, then per Horner step and per squaring dY and Y), fewest
+// first, ties to the lower degree.  At m = 4 this is 6 units against 9 for the
+// q = 4 form, which needs B^2, B^3, B^4 and their derivatives.
+__device__ __forceinline__ void choose_degree_q2(float nrm, const float* theta, int& m, int& s) {
+  int best = 1 << 30;
+  m = 4;
+  s = 0;
+#pragma unroll
+  for (int i = 0; i < PGX_N_DEGREES; ++i) {
+    int si = 0;
+    float x = nrm;
+    while (x > theta[i] && si < 60) { x *= 0.5f; ++si; }
+    const int cost = 2 * (i + 1) + si;  // m/2 + s
+    if (cost < best) { best = cost; m = 4 * (i + 1); s = si; }
   }
 }
 
@@ -841,7 +860,10 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
     tm.sync();
     const float nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<float*>(red));
     int deg, s;
-    choose_degree_f(nrm, c_theta32f, deg, s);
+    if constexpr (G::GRAD_Q2)
+      choose_degree_q2(nrm, c_theta32f, deg, s);
+    else
+      choose_degree_f(nrm, c_theta32f, deg, s);
     const float sc = ldexpf(1.f, -s);
     for (int q = tm.lane; q < D * D; q += T) {
       const int e = L::idx(q % D, q / D);

@@ -393,19 +393,52 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_combine_mx(ProbDev p
   chain_epilogue_mx<D, T>(tm, p, w, m, Pc, red);
 }
 
+// Fully parallel FP32 fix-up products of the chains: operands staged from
+// HBM into padded shared memory (each entry is read D times by the product),
+// teams sized for 2 x 2 register blocks at D = 16.
+template <int D> struct FixCfg {
+  static constexpr int T = (D <= 8) ? 32 : (D == 16) ? 64 : (D == 32) ? 128 : 256;
+  static constexpr int TPC = (T >= 256) ? 1 : 256 / T;
+  static constexpr int THREADS = T * TPC;
+};
+template <int D> __device__ __forceinline__ Team<FixCfg<D>::T> fix_team() {
+  constexpr int T = FixCfg<D>::T;
+  Team<T> tm{(int)(threadIdx.x % T)};
+  tm.bar = (T > 32 && FixCfg<D>::TPC > 1) ? 1 + (int)(threadIdx.x / T) : 0;
+  return tm;
+}
+// global column-major D x D <-> padded shared layout
+template <int D, int T>
+__device__ __forceinline__ void load_pad(const Team<T>& tm, float2* dst, const float2* src) {
+  for (int e = tm.lane; e < D * D; e += T) dst[Lay<D, 2>::idx(e % D, e / D)] = src[e];
+}
+template <int D, int T>
+__device__ __forceinline__ void store_pad(const Team<T>& tm, float2* dst, const float2* src) {
+  for (int e = tm.lane; e < D * D; e += T) dst[e] = src[Lay<D, 2>::idx(e % D, e / D)];
+}
+
+// P_k <- P_k T_b for every slice after the first block (FP32).
 template <int D>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_fix_mx(ProbDev p, WorkDev w) {
-  using G = Cfg<D>;
-  constexpr int T = G::T;
+__global__ void __launch_bounds__(FixCfg<D>::THREADS) k_chainf_fix_mx(ProbDev p, WorkDev w) {
+  using F = FixCfg<D>;
+  using L = Lay<D, 2>;
+  constexpr int T = F::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
-  const int L = w.pit_len, nk = p.n_t - L;
+  const Team<T> tm = fix_team<D>();
+  float2* A = reinterpret_cast<float2*>(smem_raw) + (size_t)team * 2 * L::SIZE;
+  float2* Tb = A + L::SIZE;
+  const int Lb = w.pit_len, nk = p.n_t - Lb;
   const long items = (long)p.n_members * (nk > 0 ? nk : 0);
-  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
-    const int m = (int)(it / nk), k = L + (int)(it % nk), b = k / L;
+  for (long it = (long)blockIdx.x * F::TPC + team; it < items; it += (long)gridDim.x * F::TPC) {
+    const int m = (int)(it / nk), k = Lb + (int)(it % nk), b = k / Lb;
     float2* Pk = reinterpret_cast<float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
-    const float2* Tb = w.pit_pre + ((size_t)m * w.pit_blocks + b) * D * D;
-    mm1<D, T>(tm, Pk, Pk, Tb);
+    load_pad<D, T>(tm, A, Pk);
+    load_pad<D, T>(tm, Tb, w.pit_pre + ((size_t)m * w.pit_blocks + b) * D * D);
+    tm.sync();
+    mm1<D, T, 2>(tm, A, A, Tb);
+    store_pad<D, T>(tm, Pk, A);
+    tm.sync();
   }
 }
 
@@ -573,29 +606,31 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_combine_mx(ProbDev p
 }
 
 template <int D>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_fix_mx(ProbDev p, WorkDev w) {
-  using G = Cfg<D>;
-  constexpr int T = G::T;
+__global__ void __launch_bounds__(FixCfg<D>::THREADS) k_chainb_fix_mx(ProbDev p, WorkDev w) {
+  using F = FixCfg<D>;
+  using L = Lay<D, 2>;
+  constexpr int T = F::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* smem = reinterpret_cast<float2*>(smem_raw);
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
-  float2* Lam = smem + (size_t)team * D * D;
+  const Team<T> tm = fix_team<D>();
+  float2* Lam = reinterpret_cast<float2*>(smem_raw) + (size_t)team * 3 * L::SIZE;
+  float2* R = Lam + L::SIZE;
+  float2* Pm = R + L::SIZE;
   const bool grape = (p.grad_mode == GRAD_REF_GRAPE);
   const long items = (long)p.n_members * p.n_t;
-  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
+  for (long it = (long)blockIdx.x * F::TPC + team; it < items; it += (long)gridDim.x * F::TPC) {
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t), b = k / w.pit_len;
     const int k1 = min(p.n_t, (b + 1) * w.pit_len);
     const int kk = grape ? k : k + 1;  // costate index the formula uses
-    const float2* lam_b = w.pit_lam + ((size_t)m * w.pit_blocks + b) * D * D;
-    if (kk == k1) {
-      for (int e = tm.lane; e < D * D; e += T) Lam[e] = lam_b[e];
-      tm.sync();
-    } else {
-      mm1<D, T>(tm, Lam, lam_b, w.pit_r + ((size_t)m * p.n_t + kk) * D * D);
-    }
     float2* Pk = reinterpret_cast<float2*>(w.P) + ((size_t)m * p.n_t + k) * D * D;
-    mm1<D, T>(tm, Pk, Pk, Lam);
+    load_pad<D, T>(tm, Lam, w.pit_lam + ((size_t)m * w.pit_blocks + b) * D * D);
+    load_pad<D, T>(tm, Pm, Pk);
+    if (kk != k1) load_pad<D, T>(tm, R, w.pit_r + ((size_t)m * p.n_t + kk) * D * D);
+    tm.sync();
+    if (kk != k1) mm1<D, T, 2>(tm, Lam, Lam, R);  // Lambda_kk = Lambda_k1 R_kk
+    mm1<D, T, 2>(tm, Pm, Pm, Lam);                 // M_k = P_k Lambda_kk
+    store_pad<D, T>(tm, Pk, Pm);
+    tm.sync();
   }
 }
 
@@ -993,9 +1028,12 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   k_chainf_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
   *li.launches += 2;
   if (store && p.n_t > w.pit_len) {
-    const int grid_f = grid_for(k_chainf_fix_mx<D>, G::THREADS, 0, (long)p.n_members * (p.n_t - w.pit_len), G::TPC,
-                                li.num_sms, 0);
-    k_chainf_fix_mx<D><<<grid_f, G::THREADS, 0, li.stream>>>(p, w);
+    using F = FixCfg<D>;
+    const size_t smem_f = (size_t)F::TPC * 2 * Lay<D, 2>::SIZE * sizeof(float2);
+    ensure_smem_mx(k_chainf_fix_mx<D>, smem_f);
+    const int grid_f = grid_for(k_chainf_fix_mx<D>, F::THREADS, smem_f, (long)p.n_members * (p.n_t - w.pit_len),
+                                F::TPC, li.num_sms, 0);
+    k_chainf_fix_mx<D><<<grid_f, F::THREADS, smem_f, li.stream>>>(p, w);
     ++*li.launches;
   }
   return cudaGetLastError();
@@ -1031,10 +1069,12 @@ static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   const size_t smem_c = (size_t)G::TPC * D * D * sizeof(float2);
   ensure_smem_mx(k_chainb_combine_mx<D>, smem_c);
   k_chainb_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w);
-  ensure_smem_mx(k_chainb_fix_mx<D>, smem_c);
-  const int grid_f = grid_for(k_chainb_fix_mx<D>, G::THREADS, smem_c, (long)p.n_members * p.n_t, G::TPC,
+  using F = FixCfg<D>;
+  const size_t smem_f = (size_t)F::TPC * 3 * Lay<D, 2>::SIZE * sizeof(float2);
+  ensure_smem_mx(k_chainb_fix_mx<D>, smem_f);
+  const int grid_f = grid_for(k_chainb_fix_mx<D>, F::THREADS, smem_f, (long)p.n_members * p.n_t, F::TPC,
                               li.num_sms, 0);
-  k_chainb_fix_mx<D><<<grid_f, G::THREADS, smem_c, li.stream>>>(p, w);
+  k_chainb_fix_mx<D><<<grid_f, F::THREADS, smem_f, li.stream>>>(p, w);
   *li.launches += 3;
   return cudaGetLastError();
 }

@@ -191,7 +191,10 @@ cudaError_t launch_select_sum(const double* Gm, const int* idx, const double* co
 // stack float2.
 cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store);
-cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+// skip_local: the in-block suffixes were already enqueued (launch_chain_bwd_local_mx,
+// gate targets with pit_blocks > 1; a no-op otherwise).
+cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool skip_local = false);
+cudaError_t launch_chain_bwd_local_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 // u -> w.u_df (df pairs), the first stage of a mixed evaluation.
 cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);

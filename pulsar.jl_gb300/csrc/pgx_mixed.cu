@@ -1043,8 +1043,23 @@ cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Launch
   return cudaSuccess;
 }
 
+// In-block suffix products of the parallel-in-time backward chain.  They need
+// only the U stack, so the pipeline may run them on a second stream while the
+// forward chain runs.
 template <int D>
-static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+static cudaError_t do_chain_bwd_local_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  using G = Cfg<D>;
+  const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float2);
+  ensure_smem_mx(k_chainb_local_mx<D>, smem_l);
+  const int grid_l = grid_for(k_chainb_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,
+                              li.num_sms, 0);
+  k_chainb_local_mx<D><<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
+template <int D>
+static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool skip_local) {
   using G = Cfg<D>;
   if (p.target != TGT_GATE) {
     constexpr int TPC = StCfg<D>::TPC;
@@ -1061,11 +1076,10 @@ static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Lau
     ++*li.launches;
     return cudaGetLastError();
   }
-  const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float2);
-  ensure_smem_mx(k_chainb_local_mx<D>, smem_l);
-  const int grid_l = grid_for(k_chainb_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,
-                              li.num_sms, 0);
-  k_chainb_local_mx<D><<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w);
+  if (!skip_local) {
+    const cudaError_t e = do_chain_bwd_local_mx<D>(p, w, li);
+    if (e != cudaSuccess) return e;
+  }
   const size_t smem_c = (size_t)G::TPC * D * D * sizeof(float2);
   ensure_smem_mx(k_chainb_combine_mx<D>, smem_c);
   k_chainb_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w);
@@ -1075,11 +1089,16 @@ static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   const int grid_f = grid_for(k_chainb_fix_mx<D>, F::THREADS, smem_f, (long)p.n_members * p.n_t, F::TPC,
                               li.num_sms, 0);
   k_chainb_fix_mx<D><<<grid_f, F::THREADS, smem_f, li.stream>>>(p, w);
-  *li.launches += 3;
+  *li.launches += 2;
   return cudaGetLastError();
 }
-cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  PGX_DISPATCH_MX(p.Dp, return do_chain_bwd_mx<D_>(p, w, li));
+cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool skip_local) {
+  PGX_DISPATCH_MX(p.Dp, return do_chain_bwd_mx<D_>(p, w, li, skip_local));
+  return cudaSuccess;
+}
+cudaError_t launch_chain_bwd_local_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  if (p.target != TGT_GATE || w.pit_blocks <= 1) return cudaSuccess;
+  PGX_DISPATCH_MX(p.Dp, return do_chain_bwd_local_mx<D_>(p, w, li));
   return cudaSuccess;
 }
 

@@ -588,6 +588,16 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
     pgx_problem_destroy(p);
     return st;
   }
+  if (d->precision == PGX_PREC_MIXED && d->target == PGX_TARGET_GATE && p->w.pit_blocks > 1) {
+    // second stream for the backward chain's in-block suffixes (run_pipeline)
+    if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      pgx_problem_destroy(p);
+      return ctx_fail(c, PGX_ERR_CUDA, "stream creation failed");
+    }
+  }
   if (d->precision == PGX_PREC_MIXED) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     const auto it = g_plans.find(plan_key(c->device, d));
@@ -621,6 +631,12 @@ extern "C" int pgx_problem_destroy(pgx_problem* p) {
     else cudaFree(q);
   }
   if (p->h_stage) cudaFreeHost(p->h_stage);
+  if (p->side) {
+    cudaStreamSynchronize(p->side);
+    cudaStreamDestroy(p->side);
+  }
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
   p->ctx->used -= p->bytes;
   delete p;
   return PGX_OK;
@@ -694,9 +710,23 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
       mk.commit();
       return st;
     }
+    // Gate targets in parallel in time: the backward chain's in-block
+    // suffixes need only U, so they run on the side stream beside the
+    // forward chain (FP32 latency-bound work beside issue-bound df work).
+    const bool fork = want_grad && p->side != nullptr;
+    if (fork) {
+      pgx::LaunchInfo ls = li;
+      ls.stream = p->side;
+      if ((st = ctx_cuda(c, cudaEventRecord(p->ev_fork, li.stream), "fork")) ||
+          (st = ctx_cuda(c, cudaStreamWaitEvent(p->side, p->ev_fork, 0), "fork")) ||
+          (st = ctx_cuda(c, pgx::launch_chain_bwd_local_mx(p->pd, w, ls), "chain_bwd_local_mx")) ||
+          (st = ctx_cuda(c, cudaEventRecord(p->ev_join, p->side), "join")))
+        return st;
+    }
     if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, want_grad), "chain_fwd_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_BWD);
-    if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd, w, li), "chain_bwd_mx"))) return st;
+    if (fork && (st = ctx_cuda(c, cudaStreamWaitEvent(li.stream, p->ev_join, 0), "join"))) return st;
+    if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd, w, li, fork), "chain_bwd_mx"))) return st;
     mk.mark(PGX_STAGE_GRAD);
     if (want_grad && (st = ctx_cuda(c, pgx::launch_grad_mx(p->pd, w, li), "grad_mx"))) return st;
     mk.mark(PGX_STAGE_REDUCE);

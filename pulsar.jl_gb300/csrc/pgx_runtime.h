@@ -50,6 +50,10 @@ struct pgx_problem {
   uint64_t track_bytes = 0;
   void* d_ramp = nullptr;               // drift ramp (member index | tau | operators | df copies)
   uint64_t ramp_bytes = 0;
+  // mixed gate problems in parallel in time: stream and fork/join events of
+  // the backward chain's in-block suffixes
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};
     for (int i = 0; i < pgx::kNumTunable; ++i) li.team[i] = team[i];

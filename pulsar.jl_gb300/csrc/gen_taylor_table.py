@@ -4,9 +4,11 @@ truncated Taylor series of exp of degree m has a tail below the unit roundoff.
 For ||B||_1 <= theta the remainder of T_m(B) = sum_{k<=m} B^k/k! obeys
     ||exp(B) - T_m(B)|| <= sum_{k>m} theta^k / k!  =: tail_m(theta),
 and theta_m is the largest theta with tail_m(theta) <= u (bisection).  The
-scaling-and-squaring driver picks, per slice, the degree m in {4,8,12,16,20}
-and squarings s with ||A||_1 / 2^s <= theta_m that minimise the number of
-matrix products (3 + m/4 - 1 for the degree, + s).  This is the standard
+scaling-and-squaring drivers pick, per slice, the degree m and squarings s
+with ||A||_1 / 2^s <= theta_m that minimise the matrix products: degrees
+{4,8,12,16,20} (3 + m/4 - 1 products, + s) in FP64 and FP32, and every degree
+m = q L with block size q in {2, 3, 4} in df (costed by the products it
+executes).  This is the standard
 forward-error bound of a truncated exponential series; the constants below are
 computed here, not taken from any library.
 
@@ -49,6 +51,10 @@ def main(out=sys.stdout):
     for name, u in (("PGX_THETA64_INIT", u64), ("PGX_THETA32_INIT", u32), ("PGX_THETADF_INIT", udf)):
         vals = ", ".join(f"{theta_for(m, u):.17g}" for m in DEGREES)
         print(f"#define {name} {{{vals}}}", file=out)
+    # every degree 1..20 in df, for the df expm's choice of Paterson-Stockmeyer
+    # block size q in {2, 3, 4} (degrees m = q L)
+    vals = ", ".join(f"{theta_for(m, udf):.17g}" for m in range(1, max(DEGREES) + 1))
+    print(f"#define PGX_THETADF_ALL_INIT {{{vals}}}  /* index m - 1 */", file=out)
     inv = ", ".join(f"{1.0 / math.factorial(k):.17g}" for k in range(max(DEGREES) + 1))
     print(f"#define PGX_N_INVFACT {max(DEGREES) + 1}", file=out)
     print(f"#define PGX_INVFACT_INIT {{{inv}}}", file=out)

@@ -316,32 +316,36 @@ __device__ __forceinline__ void mm_df_tri(const Team<T>& tm, float4* out, const 
   tm.sync();
 }
 
-// Taylor block C_i = c_{4i} I + c_{4i+1} B + c_{4i+2} B2 + c_{4i+3} B3 in df;
-// coef[k] = 1/k! as df.
-__device__ __forceinline__ dfc df_block(int i, int r, int c, const float4& b1, const float4& b2,
-                                        const float4& b3, const df* coef) {
-  dfc v = dfc_scale(dfc_load(b1), coef[4 * i + 1]);
-  v = dfc_add(v, dfc_scale(dfc_load(b2), coef[4 * i + 2]));
-  v = dfc_add(v, dfc_scale(dfc_load(b3), coef[4 * i + 3]));
-  if (r == c) v.re = df_add(v.re, coef[4 * i]);
+// Taylor block C_i = sum_{j<q} c_{qi+j} B^j in df at storage index e (B^0 =
+// I; b1, b2, b3 hold B, B^2, B^3); coef[k] = 1/k! as df.
+__device__ __forceinline__ dfc df_block(int i, int q, int r, int c, int e, const float4* b1, const float4* b2,
+                                        const float4* b3, const df* coef) {
+  const int o = q * i;
+  dfc v = dfc_scale(dfc_load(b1[e]), coef[o + 1]);
+  if (q >= 3) v = dfc_add(v, dfc_scale(dfc_load(b2[e]), coef[o + 2]));
+  if (q >= 4) v = dfc_add(v, dfc_scale(dfc_load(b3[e]), coef[o + 3]));
+  if (r == c) v.re = df_add(v.re, coef[o]);
   return v;
 }
 
-// Y = T_m(B)^(2^s) in df (B = A / 2^s on entry).  Same Paterson-Stockmeyer
-// schedule as taylor_exp: m = 4L costs 3 + (L - 1) products, then s squarings.
-// Horner steps i >= lo_from multiply B4 by a tail of size <= 1/(4(i+1))!; the
-// caller sets lo_from where D u32 ||B4||^(i+1) / (4(i+1))! is below df
-// precision, and those steps run in plain FP32.
+// Y = T_m(B)^(2^s) in df (B = A / 2^s on entry), Paterson-Stockmeyer with
+// block size q in {2, 3, 4} and m = q L:
+//   powers B^2 .. B^q (q - 1 products),
+//   Y = C_{L-1} + c_m B^q,  Y <- B^q Y + C_i for i = L-2 .. 0,
+// then s squarings.  Horner steps i >= lo_from multiply B^q by a tail of
+// size <= e^a / (q(i+1))!; the caller sets lo_from where that step's FP32
+// error, carried through i more factors B^q, stays below df precision, and
+// those steps run in plain FP32.
 // HERM (D >= 16, column-major layouts): B is anti-Hermitian, so B^2 and B^4
 // are Hermitian and B^3 anti-Hermitian, and their products run as triangular
-// ones.  The three power products share one call site (one copy of the
-// product's code: the kernel is instruction-cache bound otherwise).
+// ones.  The power products share one call site (one copy of the product's
+// code: the kernel is instruction-cache bound otherwise).
 template <int D, int T, int SW = 0, bool HERM = false>
 __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* B3, float4* B4, float4* Y,
-                              int m, int s, const df* coef, int lo_from = 1 << 30) {
+                              int m, int q, int s, const df* coef, int lo_from = 1 << 30) {
   constexpr bool TRI = HERM && D >= 16 && SW != 1;
 #pragma unroll 1
-  for (int st = 0; st < 3; ++st) {  // B2 = B B, B3 = B2 B, B4 = B2 B2
+  for (int st = 0; st < q - 1; ++st) {  // B2 = B B, B3 = B2 B, B4 = B2 B2
     const float4* X = (st == 0) ? B : B2;
     const float4* Z = (st == 2) ? B2 : B;
     float4* out = (st == 0) ? B2 : (st == 1) ? B3 : B4;
@@ -350,21 +354,22 @@ __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* 
     else
       mm1_df<D, T, SW>(tm, out, X, Z);
   }
-  const int L = m / 4;
-  for (int q = tm.lane; q < D * D; q += T) {
-    const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
-    dfc v = df_block(L - 1, r, c, B[e], B2[e], B3[e], coef);
-    Y[e] = dfc_store(dfc_add(v, dfc_scale(dfc_load(B4[e]), coef[4 * L])));
+  const float4* Bq = (q == 2) ? B2 : (q == 3) ? B3 : B4;
+  const int L = m / q;
+  for (int t = tm.lane; t < D * D; t += T) {
+    const int r = t % D, c = t / D, e = Lay<D, SW>::idx(r, c);
+    dfc v = df_block(L - 1, q, r, c, e, B, B2, B3, coef);
+    Y[e] = dfc_store(dfc_add(v, dfc_scale(dfc_load(Bq[e]), coef[m])));
   }
   tm.sync();
   for (int i = L - 2; i >= 0; --i) {
     const auto add_block = [=](int e, int r, int c, dfc v) {
-      return dfc_add(v, df_block(i, r, c, B[e], B2[e], B3[e], coef));
+      return dfc_add(v, df_block(i, q, r, c, e, B, B2, B3, coef));
     };
     if (i >= lo_from)
-      mm_df_lo<D, T, SW>(tm, Y, B4, Y, add_block);
+      mm_df_lo<D, T, SW>(tm, Y, Bq, Y, add_block);
     else
-      mm_df<D, T, false, SW>(tm, Y, B4, Y, (const float4*)nullptr, (const float4*)nullptr, add_block);
+      mm_df<D, T, false, SW>(tm, Y, Bq, Y, (const float4*)nullptr, (const float4*)nullptr, add_block);
   }
   for (int k = 0; k < s; ++k) mm1_df<D, T, SW>(tm, Y, Y, Y);
 }

@@ -166,51 +166,73 @@ __device__ __forceinline__ float norm1f(const Team<T>& tm, const C* A, float* sc
   return best * 1.00001f;
 }
 
-// First Horner step of the df Taylor polynomial that may run in FP32.  Step i
-// computes B4 * Y with ||B4|| <= a^4 and ||Y|| <= e^a / (4(i+1))!, and its
-// error reaches the result through i more factors B4: bound
-// D u32 a^(4(i+1)) e^a / (4(i+1))!, required below 2^-47.
-__device__ __forceinline__ int lo_horner_from(float a, int L, int D) {
-  const float a4 = (a * a) * (a * a);
-  float pw = a4, fact = 24.f;  // a^(4(i+1)), (4(i+1))! for i = 0
+// First Horner step of the df Taylor polynomial (block size q) that may run
+// in FP32.  Step i computes B^q Y with ||B^q|| <= a^q and ||Y|| <= e^a /
+// (q(i+1))!, and its error reaches the result through i more factors B^q:
+// bound D u32 a^(q(i+1)) e^a / (q(i+1))!, required below 2^-47.  Step 0 stays
+// in df.
+__device__ __forceinline__ int lo_horner_from(float a, int L, int D, int q) {
+  float aq = a;
+#pragma unroll 1
+  for (int j = 1; j < q; ++j) aq *= a;
+  float pw = aq, fact = 1.f;  // a^(q(i+1)), (q(i+1))! for i = 0
+#pragma unroll 1
+  for (int j = 2; j <= q; ++j) fact *= (float)j;
   const float lim = 7.1e-15f / (float)D / 5.96e-8f / __expf(a);
+#pragma unroll 1
   for (int i = 0; i < L - 1; ++i) {
     if (i >= 1 && pw / fact <= lim) return i;
-    pw *= a4;
-    fact *= (float)((4 * i + 5) * (4 * i + 6) * (4 * i + 7) * (4 * i + 8));
+    pw *= aq;
+#pragma unroll 1
+    for (int j = q * (i + 1) + 1; j <= q * (i + 2); ++j) fact *= (float)j;
   }
   return 1 << 30;
 }
 
-// Degree m and squarings s of the df expm.  Same thresholds as
-// choose_degree_f, but each candidate is costed by what it executes:
-//  - the three power products (weight kTriPowW each when triangular);
-//  - the df Horner steps (1 each);
-//  - the Horner steps lo_horner_from moves to FP32 (kLoHornerW each);
-//  - the s squarings (1 each).
-// Ties keep the lower degree.
-constexpr float kTriPowW = 0.8f, kLoHornerW = 0.25f;
-__device__ __forceinline__ void choose_degree_df(float nrm, int D, bool tri, int& m, int& s, int& lo_from) {
-  float best = 3.0e38f;
-  m = 4;
-  s = 0;
-  lo_from = 1 << 30;
-#pragma unroll
-  for (int i = 0; i < PGX_N_DEGREES; ++i) {
-    int si = 0;
-    float x = nrm;
-    while (x > c_thetadf[i] && si < 60) { x *= 0.5f; ++si; }
-    const int L = i + 1;
-    const int lo = lo_horner_from(x, L, D);
-    const int n_df = lo < L - 1 ? lo : L - 1;  // Horner steps i' = L-2 .. 0 below lo run in df
-    const float cost = 3.f * (tri ? kTriPowW : 1.f) + (float)n_df + kLoHornerW * (float)(L - 1 - n_df) + (float)si;
-    if (cost < best - 1e-3f) {
-      best = cost;
-      m = 4 * L;
-      s = si;
-      lo_from = lo;
+// Degree m = q L, block size q in {2, 3, 4} and squarings s of the df expm:
+// every degree whose df threshold theta_m (tail <= 2^-47) admits ||A|| / 2^s,
+// costed in twentieths of a df product by what it executes:
+//  - the q - 1 power products (16 each when triangular, else 20);
+//  - the df Horner steps (20 each);
+//  - the Horner steps lo_horner_from moves to FP32 (5 each);
+//  - the s squarings (20 each).
+// The 21 candidates (q = 4: L = 1..5, q = 3: L = 1..6, q = 2: L = 1..10, in
+// that order) are costed one per lane of the team's first warp; the exact
+// integer minimum, ties to the earlier candidate, is broadcast through
+// `scratch`.  Returns m | q << 5 | s << 8 | min(lo_from, 31) << 16.
+static __constant__ float c_thetadf_all[PGX_N_INVFACT - 1] = PGX_THETADF_ALL_INIT;
+constexpr int kTriPowCost = 16, kPowCost = 20, kLoHornerCost = 5;
+template <int T>
+__device__ __forceinline__ int choose_expm_df(const Team<T>& tm, float nrm, int D, bool tri, int* scratch) {
+  if (tm.lane < 32) {
+    const int t = tm.lane;
+    const int qq = (t < 5) ? 4 : (t < 11) ? 3 : 2;
+    const int L = (t < 5) ? t + 1 : (t < 11) ? t - 4 : t - 10;
+    long long key = 0x7fffffffffffffffLL;
+    int packed = 0;
+    if (t < 21) {
+      const int mm = qq * L;
+      int si = 0;
+      float x = nrm;
+      while (x > c_thetadf_all[mm - 1] && si < 60) { x *= 0.5f; ++si; }
+      const int lo = lo_horner_from(x, L, D, qq);
+      const int n_df = lo < L - 1 ? lo : L - 1;  // Horner steps i = L-2 .. 0 below lo run in df
+      const int cost = (qq - 1) * (tri ? kTriPowCost : kPowCost) + 20 * n_df + kLoHornerCost * (L - 1 - n_df) + 20 * si;
+      key = (long long)cost * 32 + t;
+      packed = mm | (qq << 5) | (si << 8) | ((lo < 31 ? lo : 31) << 16);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+      const int op = __shfl_xor_sync(0xffffffffu, packed, o);
+      if (ok < key) { key = ok; packed = op; }
+    }
+    if (t == 0) *scratch = packed;
   }
+  tm.sync();
+  const int r = *scratch;
+  tm.sync();
+  return r;
 }
 
 // Degree m and squarings s of the q = 2 Frechet form: 3 (m/2 + s) product
@@ -263,8 +285,9 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
     build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
     tm.sync();
     const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
-    int deg, s, lo_from;
-    choose_degree_df(nrm, D, HERM && D >= 16, deg, s, lo_from);
+    const int pk = choose_expm_df<T>(tm, nrm, D, HERM && D >= 16, reinterpret_cast<int*>(red));
+    const int deg = pk & 31, q = (pk >> 5) & 7, s = (pk >> 8) & 63;
+    const int lo_from = (pk >> 16) >= 31 ? 1 << 30 : (pk >> 16);
     if (s > 0) {  // B <- B / 2^s, exact in df
       const float sc = ldexpf(1.f, -s);
       for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df
@@ -274,7 +297,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
       }
       tm.sync();
     }
-    taylor_exp_df<D, T, kSwzExpm, HERM>(tm, B, B2, B3, B4, Y, deg, s, c_dfcoef, lo_from);
+    taylor_exp_df<D, T, kSwzExpm, HERM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
     for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
     tm.sync();

@@ -270,7 +270,7 @@ __device__ __forceinline__ void mm_df_tri(const Team<T>& tm, float4* out, const 
   constexpr int KS = TriSplit<D>::KS, G = 8 / KS, KK = D / KS;
   constexpr int NT = D * (D + 1) / 2, NTP = (NT + 7) / 8 * 8;
   constexpr int NO = (NTP * KS + T - 1) / T;
-  constexpr int UNR = (D >= 64) ? 1 : (KK > 4 ? 2 : KK);
+  constexpr int UNR = (D >= 64) ? 1 : 2;  // code size: the kernel is instruction-cache bound
   constexpr int PR = (NO < 2) ? NO : 2;
   // rounds whose entries all lie in full blocks of 8 need no bounds test
   constexpr int SAFE = (NT / 8) * 8 * KS / T;

@@ -316,6 +316,93 @@ __device__ __forceinline__ void mm_df_tri(const Team<T>& tm, float4* out, const 
   tm.sync();
 }
 
+// Hermiticity-preserving superoperators.  With vec(rho) indices a = i + d j
+// (D = d^2) and the swap sigma(i + d j) = j + d i, a Lindblad generator and
+// every polynomial in it satisfy X[a][b] = conj(X[sigma a][sigma b]).  So a
+// product of two such matrices is determined by its d(d+1)/2 columns
+// b = i + d j with i >= j; the other d(d-1)/2 columns are the conjugates of
+// permuted entries.
+template <int D> struct LSym {
+  static constexpr int d = (D == 64) ? 8 : (D == 16) ? 4 : (D == 4) ? 2 : 0;
+  static constexpr int NC = d * (d + 1) / 2;  // kept columns (i >= j)
+  static constexpr int NM = d * (d - 1) / 2;  // mirrored columns (i < j)
+};
+// t -> (r, c), r >= c, in row-major order of the lower triangle (diagonal
+// included when incl, else strictly below it).
+__device__ __forceinline__ void lower_decode(int t, bool incl, int& r, int& c) {
+  const int o = incl ? 0 : 1;  // strict: row r holds r entries
+  r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f) + o;
+  while ((r + 1 - o) * (r + 2 - o) / 2 <= t) ++r;
+  while ((r - o) * (r + 1 - o) / 2 > t) --r;
+  c = t - (r - o) * (r + 1 - o) / 2;
+}
+
+// out = A*B for Hermiticity-preserving superoperators (LSym), df (LO =
+// false) or plain FP32 from the leading halves (LO = true, as mm_df_lo), then
+// epi(e, r, c, value) on the kept entries.  Lane (r, g) = (lane % D, lane / D)
+// computes row r of the kept columns g, g + T/D, ...: the A reads of a warp
+// are one column (consecutive rows), the B reads broadcast.  The mirrored
+// columns are written after a barrier.  out may alias A or B.
+template <int D, int T, bool LO, int SW, class Epi>
+__device__ __forceinline__ void mm_df_lsym(const Team<T>& tm, float4* out, const float4* A, const float4* B,
+                                           Epi epi) {
+  using S = LSym<D>;
+  using L = Lay<D, SW>;
+  static_assert(S::d > 0 && T % D == 0 && S::NC % (T / D) == 0, "lsym blocking");
+  constexpr int NG = T / D, CB = S::NC / NG;
+  const int r = tm.lane % D, g = tm.lane / D;
+  int col[CB];
+#pragma unroll
+  for (int u = 0; u < CB; ++u) {
+    int i, j;
+    lower_decode(g + NG * u, true, i, j);
+    col[u] = i + S::d * j;
+  }
+  float4 res[CB];
+  if constexpr (LO) {
+    float2 acc[CB];
+#pragma unroll
+    for (int u = 0; u < CB; ++u) acc[u] = make_float2(0.f, 0.f);
+#pragma unroll 2
+    for (int k = 0; k < D; ++k) {
+      const float4 a = A[L::idx(r, k)];
+#pragma unroll
+      for (int u = 0; u < CB; ++u) {
+        const float4 b = B[L::idx(k, col[u])];
+        acc[u] = cmac(acc[u], make_float2(a.x, a.y), make_float2(b.x, b.y));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      const dfc v = {{acc[u].x, 0.f}, {acc[u].y, 0.f}};
+      res[u] = dfc_store(epi(L::idx(r, col[u]), r, col[u], v));
+    }
+  } else {
+    DfAcc acc[CB];
+#pragma unroll 1
+    for (int k = 0; k < D; ++k) {
+      const float4 a = A[L::idx(r, k)];
+#pragma unroll
+      for (int u = 0; u < CB; ++u) acc[u].mac(a, B[L::idx(k, col[u])]);
+    }
+#pragma unroll
+    for (int u = 0; u < CB; ++u) res[u] = dfc_store(epi(L::idx(r, col[u]), r, col[u], acc[u].result()));
+  }
+  tm.sync();
+#pragma unroll
+  for (int u = 0; u < CB; ++u) out[L::idx(r, col[u])] = res[u];
+  tm.sync();
+  for (int e = tm.lane; e < S::NM * D; e += T) {  // column b = i + d j (i < j) from (sigma a, sigma b)
+    const int a = e % D;
+    int jj, ii;
+    lower_decode(e / D, false, jj, ii);  // jj > ii
+    const int b = ii + S::d * jj, sb = jj + S::d * ii, sa = a / S::d + S::d * (a % S::d);
+    const float4 v = out[L::idx(sa, sb)];
+    out[L::idx(a, b)] = make_float4(v.x, -v.y, v.z, -v.w);
+  }
+  tm.sync();
+}
+
 // Taylor block C_i = sum_{j<q} c_{qi+j} B^j in df at storage index e (B^0 =
 // I; b1, b2, b3 hold B, B^2, B^3); coef[k] = 1/k! as df.
 __device__ __forceinline__ dfc df_block(int i, int q, int r, int c, int e, const float4* b1, const float4* b2,
@@ -340,7 +427,9 @@ __device__ __forceinline__ dfc df_block(int i, int q, int r, int c, int e, const
 // are Hermitian and B^3 anti-Hermitian, and their products run as triangular
 // ones.  The power products share one call site (one copy of the product's
 // code: the kernel is instruction-cache bound otherwise).
-template <int D, int T, int SW = 0, bool HERM = false>
+// LSYM: B is a Hermiticity-preserving superoperator (LSym<D>, T a multiple of
+// D): every product keeps d(d+1)/2 columns and mirrors the rest.
+template <int D, int T, int SW = 0, bool HERM = false, bool LSYM = false>
 __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* B3, float4* B4, float4* Y,
                               int m, int q, int s, const df* coef, int lo_from = 1 << 30) {
   constexpr bool TRI = HERM && D >= 16 && SW != 1;
@@ -351,6 +440,8 @@ __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* 
     float4* out = (st == 0) ? B2 : (st == 1) ? B3 : B4;
     if constexpr (TRI)
       mm_df_tri<D, T, SW>(tm, out, X, Z, st == 1);
+    else if constexpr (LSYM)
+      mm_df_lsym<D, T, false, SW>(tm, out, X, Z, DfEpiNone{});
     else
       mm1_df<D, T, SW>(tm, out, X, Z);
   }
@@ -366,12 +457,24 @@ __device__ void taylor_exp_df(const Team<T>& tm, float4* B, float4* B2, float4* 
     const auto add_block = [=](int e, int r, int c, dfc v) {
       return dfc_add(v, df_block(i, q, r, c, e, B, B2, B3, coef));
     };
-    if (i >= lo_from)
-      mm_df_lo<D, T, SW>(tm, Y, Bq, Y, add_block);
-    else
-      mm_df<D, T, false, SW>(tm, Y, Bq, Y, (const float4*)nullptr, (const float4*)nullptr, add_block);
+    if constexpr (LSYM) {
+      if (i >= lo_from)
+        mm_df_lsym<D, T, true, SW>(tm, Y, Bq, Y, add_block);
+      else
+        mm_df_lsym<D, T, false, SW>(tm, Y, Bq, Y, add_block);
+    } else {
+      if (i >= lo_from)
+        mm_df_lo<D, T, SW>(tm, Y, Bq, Y, add_block);
+      else
+        mm_df<D, T, false, SW>(tm, Y, Bq, Y, (const float4*)nullptr, (const float4*)nullptr, add_block);
+    }
   }
-  for (int k = 0; k < s; ++k) mm1_df<D, T, SW>(tm, Y, Y, Y);
+  for (int k = 0; k < s; ++k) {
+    if constexpr (LSYM)
+      mm_df_lsym<D, T, false, SW>(tm, Y, Y, Y, DfEpiNone{});
+    else
+      mm1_df<D, T, SW>(tm, Y, Y, Y);
+  }
 }
 
 }  // namespace pgx

@@ -16,6 +16,7 @@ struct ProbDev {
   int Dp;         // padded dimension
   int n_c, n_t, n_members, n_pairs;
   int gen;        // PGX_GEN_*
+  int lsym;       // Liouvillian pieces preserve Hermiticity: X[a][b] = conj(X[sigma a][sigma b])
   int target;     // PGX_TARGET_*
   int fid;        // PGX_FID_*
   int grad_mode;  // PGX_GRAD_*

@@ -261,8 +261,13 @@ template <int D, int T> constexpr int expm_min_ctas() {
   constexpr size_t n = CfgM<D, T>::SLAB ? 2 : kSmemSm / CfgM<D, T>::SMEM_E;
   return n < 1 ? 1 : n > 5 ? 5 : (int)n;
 }
-template <int D, int T, bool HERM>
+// KIND: kExpmFull (general generator), kExpmHerm (Hermitian: triangular
+// powers), kExpmLSym (Hermiticity-preserving superoperator at D = 64: half
+// of every product).
+enum { kExpmFull = 0, kExpmHerm = 1, kExpmLSym = 2 };
+template <int D, int T, int KIND>
 __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_expm_mx(ProbDev p, WorkDev w) {
+  constexpr bool HERM = KIND == kExpmHerm, LSYM = KIND == kExpmLSym;
   using G = CfgM<D, T>;
   using L = Lay<D, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -297,7 +302,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
       }
       tm.sync();
     }
-    taylor_exp_df<D, T, kSwzExpm, HERM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
+    taylor_exp_df<D, T, kSwzExpm, HERM, LSYM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
     for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
     tm.sync();
@@ -339,7 +344,9 @@ __device__ __forceinline__ void chain_epilogue_mx(const Team<T>& tm, const ProbD
 //           P_n = T_B gives U_total and z exactly as the sequential chain;
 //   fix     per (m, k), k >= pit_len: P_k <- Q_i T_b in FP32 (the gradient
 //           consumes P in FP32).
-template <int D>
+// LSYM (D = 64, Hermiticity-preserving superoperators): the prefix products
+// keep half of each product (mm_df_lsym).
+template <int D, bool LSYM>
 __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_local_mx(ProbDev p, WorkDev w, int store) {
   using G = Cfg<D>;
   constexpr int T = G::T;
@@ -382,7 +389,10 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_local_mx(ProbDev p, 
         }
       }
       tm.sync();
-      mm1_df<D, T>(tm, Pc, Ub, Pc);
+      if constexpr (LSYM)
+        mm_df_lsym<D, T, false, 0>(tm, Pc, Ub, Pc, DfEpiNone{});
+      else
+        mm1_df<D, T>(tm, Pc, Ub, Pc);
       if (store && k + 1 < k1)
         for (int e = tm.lane; e < D * D; e += T) Pst[(size_t)(k + 1) * D * D + e] = make_float2(Pc[e].x, Pc[e].y);
     }
@@ -1008,8 +1018,10 @@ template <int D, int T>
 static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   using G = CfgM<D, T>;
   const size_t smem = G::SMEM_E;
-  // Hermitian generators: an instance whose power products are triangular
-  const auto kern = (p.gen == GEN_HERM) ? k_expm_mx<D, T, true> : k_expm_mx<D, T, false>;
+  // an instance per generator structure
+  auto kern = (p.gen == GEN_HERM) ? k_expm_mx<D, T, kExpmHerm> : k_expm_mx<D, T, kExpmFull>;
+  if constexpr (D == 64 && T == 256)
+    if (p.lsym) kern = k_expm_mx<D, T, kExpmLSym>;
   ensure_smem_mx(kern, smem);
   const int grid = grid_for(kern, G::THREADS, smem, (long)p.n_members * p.n_t, G::TPC, li.num_sms,
                             G::SLAB ? w.slab_teams : 0);
@@ -1042,10 +1054,12 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
     return cudaGetLastError();
   }
   const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float4);
-  ensure_smem_mx(k_chainf_local_mx<D>, smem_l);
-  const int grid_l = grid_for(k_chainf_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,
-                              li.num_sms, 0);
-  k_chainf_local_mx<D><<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
+  auto local = k_chainf_local_mx<D, false>;
+  if constexpr (D == 64 && G::T == 256)
+    if (p.lsym) local = k_chainf_local_mx<D, true>;
+  ensure_smem_mx(local, smem_l);
+  const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
+  local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
   const size_t smem_c = (size_t)G::TPC * (D * D + G::T) * sizeof(float4);
   ensure_smem_mx(k_chainf_combine_mx<D>, smem_c);
   k_chainf_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);

@@ -193,6 +193,34 @@ double herm_dev(const double* m, int D) {
   return dev;
 }
 
+// Largest |X[a][b] - conj(X[sigma a][sigma b])| of a D x D superoperator,
+// D = d^2, sigma(i + d j) = j + d i: zero for Hermiticity-preserving maps
+// (every Lindblad generator).  Returns -1 when D is not a square.
+static double lsym_dev(const double* m, int D) {
+  int d = 1;
+  while (d * d < D) ++d;
+  if (d * d != D) return -1.0;
+  double dev = 0.0;
+  for (int a = 0; a < D; ++a)
+    for (int b = 0; b < D; ++b) {
+      const int sa = a / d + d * (a % d), sb = b / d + d * (b % d);
+      const cplx x(m[2 * (a + D * b)], m[2 * (a + D * b) + 1]);
+      const cplx y(m[2 * (sa + D * sb)], -m[2 * (sa + D * sb) + 1]);
+      dev = std::max(dev, std::abs(x - y));
+    }
+  return dev;
+}
+static bool lsym_all(const double* m, int n, int D) {
+  for (int i = 0; i < n; ++i) {
+    const double* x = m + 2 * (size_t)i * D * D;
+    double mx = 0.0;
+    for (size_t k = 0; k < 2 * (size_t)D * D; ++k) mx = std::max(mx, std::abs(x[k]));
+    const double dev = lsym_dev(x, D);
+    if (dev < 0.0 || dev > 1e-12 * std::max(mx, 1e-300)) return false;
+  }
+  return true;
+}
+
 static double unitarity_dev(const double* m, int D) {
   // ||U'U - I||_F / D  (Targets.jl:135-137)
   double s = 0.0;
@@ -530,6 +558,11 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   pd.n_members = nm;
   pd.n_pairs = np;
   pd.gen = d->generator;
+  // Liouvillians whose every generator piece preserves Hermiticity, at a
+  // dimension without padding: the mixed expm and forward chain keep half
+  // of each product (D = 64)
+  pd.lsym = d->generator == PGX_GEN_LIOUVILLIAN && Dp == D && lsym_all(d->drifts, d->n_drifts, D) &&
+            lsym_all(d->controls, d->n_controls, D) && (!d->offset_op || lsym_all(d->offset_op, 1, D));
   pd.target = d->target;
   pd.fid = d->fidelity;
   pd.grad_mode = d->grad_mode;
@@ -544,6 +577,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   pd.target_op = (const double2*)g_tg;
   pd.psi_init = (const double2*)g_pi;
   pd.psi_targ = (const double2*)g_pt;
+  p->lsym_base = pd.lsym != 0;
   p->pd_grad = pd;
   p->pd_grad.psi_init = (const double2*)g_pg;
 
@@ -1300,7 +1334,9 @@ extern "C" int pgx_problem_set_drift_ramp(pgx_problem* p, int32_t n_ops, const d
       return st;
   }
   unsigned char* base = static_cast<unsigned char*>(p->d_ramp);
+  const bool rsym = n_ops == 0 || lsym_all(ops, n_ops, D);  // the symmetric products need every piece symmetric
   for (pgx::ProbDev* pd : {&p->pd, &p->pd_grad}) {
+    pd->lsym = p->lsym_base && rsym;
     pd->n_ramp = n_ops;
     pd->m_ramp = n_ops ? reinterpret_cast<const int*>(base) : nullptr;
     pd->tau = n_ops ? reinterpret_cast<const double*>(base + off_tau) : nullptr;

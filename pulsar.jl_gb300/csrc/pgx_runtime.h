@@ -53,6 +53,7 @@ struct pgx_problem {
   // mixed gate problems in parallel in time: stream and fork/join events of
   // the backward chain's in-block suffixes
   cudaStream_t side = nullptr;
+  bool lsym_base = false;  // generator pieces given at creation preserve Hermiticity (ProbDev::lsym)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};

@@ -44,6 +44,53 @@ def test_mixed_lindblad_superoperator(pg):
     p.close()
 
 
+def test_mixed_lindblad_symmetric_products_parallel_in_time(pg):
+    """D = 64 Lindblad superoperators preserve Hermiticity, so the mixed expm
+    and forward chain keep half of each product and mirror the rest; 60
+    slices put the forward chain in its parallel-in-time form."""
+    prob, u0 = fx.lindblad_3q(n_t=60, n_draws=2)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F, G = p.eval(u0)
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    check(F, G, Fo, Go)
+    p.close()
+
+
+def test_mixed_lindblad_symmetric_path_matches_full_path(pg):
+    """A ramp operator that breaks the symmetry but enters with tau = 0 leaves
+    the generator unchanged and sends the evaluation through the full
+    products: both paths agree to df rounding."""
+    prob, u0 = fx.lindblad_3q(n_t=40, n_draws=2)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F1, G1 = p.eval(u0)
+    rng = np.random.default_rng(5)
+    D = prob.D
+    R = rng.standard_normal((1, D, D)) + 1j * rng.standard_normal((1, D, D))
+    p.set_drift_ramp(R, np.zeros(prob.n_members, int), np.zeros(prob.n_t))
+    F2, G2 = p.eval(u0)
+    assert abs(F1 - F2) <= 1e-12, (F1, F2)
+    assert np.max(np.abs(G1 - G2)) <= 1e-6 * np.max(np.abs(G1))
+    p.set_drift_ramp(np.zeros((0, D, D)), [], [])
+    F3, G3 = p.eval(u0)
+    assert F3 == F1 and np.array_equal(G3, G1)
+    p.close()
+
+
+def test_mixed_lindblad_asymmetric_generator(pg):
+    """A Liouvillian whose drift does not preserve Hermiticity (relative
+    defect 1e-6, far above the 1e-12 the symmetric path admits, small enough
+    to keep the dynamics bounded) takes the full products."""
+    prob, u0 = fx.lindblad_3q(n_t=6, n_draws=2)
+    rng = np.random.default_rng(8)
+    prob.drifts = prob.drifts + 1e-6 * np.abs(prob.drifts).max() * (
+        rng.standard_normal(prob.drifts.shape) + 1j * rng.standard_normal(prob.drifts.shape))
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F, G = p.eval(u0)
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    check(F, G, Fo, Go)
+    p.close()
+
+
 def test_mixed_needs_squarings(pg):
     rng = np.random.default_rng(11)
     prob, u0 = random_gate_problem(rng, 8, n_t=5, dt=0.9, scale=3.0)

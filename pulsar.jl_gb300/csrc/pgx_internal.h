@@ -165,9 +165,10 @@ cudaError_t launch_norm(const double* v, int n, double* out, cudaStream_t stream
 // Raises a kernel's dynamic shared-memory limit (once per kernel and device).
 void set_smem_once(const void* fn, size_t bytes);
 
-// Team sizes the mixed slice-parallel kernels admit at padded dimension Dp
-// (writes up to 4 values, returns the count), and the default choice.
-int mixed_variants(int Dp, int* out);
+// Team sizes the mixed slice-parallel kernel `kernel` (kTune*) admits at
+// padded dimension Dp (writes up to 4 values, returns the count), and the
+// default choice.
+int mixed_variants(int Dp, int kernel, int* out);
 int mixed_default_team(int Dp, int kernel);
 
 // Stage launchers (pgx_kernels.cu).  Each returns cudaGetLastError() after

@@ -860,7 +860,45 @@ __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_bwd_mx(Prob
 // not depend on the team size the autotuner picks.
 template <int D, int T, int SW>
 __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDev& p, const float2* X,
-                                                 int m, int k, double* Gout, float2*) {
+                                                 int m, int k, double* Gout, float2* red) {
+  if constexpr (D >= 32) {
+    // 256 fixed chunks (entries q = c, c + 256, ... summed in order), then a
+    // fixed tree: warp-sized groups by xor shuffles, the 8 group sums in
+    // order.  The order depends on D only, not on the team size; the scratch
+    // holds the 256 chunk sums (2T >= 256).
+    constexpr int NCH = 256, NGR = NCH / 32;
+    static_assert(T >= 32 && 2 * T >= NCH, "trace scratch holds the 256 chunk sums");
+    for (int j = 0; j < p.n_c; ++j) {
+      const float4* Cj = p.ctrls_df + (size_t)j * D * D;
+      for (int c = tm.lane; c < NCH; c += T) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int q = c; q < D * D; q += NCH) {
+          const int r = q % D, cc = q / D;
+          const float4 cv = Cj[cc + D * r];
+          acc = cmac(acc, X[Lay<D, SW>::idx(r, cc)], make_float2(cv.x, cv.y));
+        }
+        red[c] = acc;
+      }
+      tm.sync();
+      for (int gl = tm.lane; gl < NGR * 32; gl += T) {  // whole warps: gl / 32 is uniform in a warp
+        float2 v = red[gl];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (gl % 32 == 0) red[gl] = v;  // group sum over the group's first slot
+      }
+      tm.sync();
+      if (tm.lane == 0) {
+        float2 acc = red[0];
+        for (int g = 1; g < NGR; ++g) acc = make_float2(acc.x + red[32 * g].x, acc.y + red[32 * g].y);
+        Gout[j] = p.dt[k] * p.m_scale[m] * (double)(p.gen == GEN_HERM ? acc.y : acc.x);
+      }
+      tm.sync();
+    }
+    return;
+  }
   if (tm.lane < 32) {
     for (int j = 0; j < p.n_c; ++j) {
       const float4* Cj = p.ctrls_df + (size_t)j * D * D;
@@ -977,16 +1015,22 @@ static int grid_for(K kernel, int threads, size_t smem, long teams, int tpc, int
     default: return cudaErrorInvalidValue;            \
   }
 
-// Team sizes each D admits (register budget of the blocked df products).
-static int variants_for(int Dp, int* out) {
+// Team sizes each D admits (register budget of the blocked df products).  The
+// D = 64 gradient also runs as one 512-thread team per SM: its six FP32
+// matrices fill shared memory, so more threads per team is the only way to
+// more warps.
+static int variants_for(int Dp, int kernel, int* out) {
   int n = 0;
   if (Dp <= 8) out[n++] = 32;
   else if (Dp == 16) { out[n++] = 32; out[n++] = 64; out[n++] = 128; out[n++] = 256; }
   else if (Dp == 32) { out[n++] = 128; out[n++] = 256; }
-  else out[n++] = 256;
+  else {
+    out[n++] = 256;
+    if (kernel == kTuneGradMx) out[n++] = 512;
+  }
   return n;
 }
-int mixed_variants(int Dp, int* out) { return variants_for(Dp, out); }
+int mixed_variants(int Dp, int kernel, int* out) { return variants_for(Dp, kernel, out); }
 int mixed_default_team(int Dp, int kernel) {
   if (Dp == 16) return kernel == kTuneExpmMx ? 256 : 32;
   if (Dp == 32) return 256;
@@ -1159,6 +1203,7 @@ cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
 
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   const int t = li.team[kTuneGradMx] ? li.team[kTuneGradMx] : mixed_default_team(p.Dp, kTuneGradMx);
+  if (p.Dp == 64 && t == 512) return do_grad_mx<64, 512>(p, w, li);
   PGX_DISPATCH_MX_T(p.Dp, t, return (do_grad_mx<D_, T_>(p, w, li)));
   return cudaSuccess;
 }

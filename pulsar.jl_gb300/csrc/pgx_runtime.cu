@@ -830,7 +830,7 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
   for (int kern = 0; kern < pgx::kNumTunable; ++kern) {
     if (kern == pgx::kTuneGradMx && p->desc.grad_mode != PGX_GRAD_EXACT) continue;
     int vs[4];
-    const int nv = pgx::mixed_variants(p->Dp, vs);
+    const int nv = pgx::mixed_variants(p->Dp, kern, vs);
     double best_ms = 1e300;
     int best = vs[0];
     rep += std::string(rep.empty() ? "" : " | ") + names[kern] + "<" + std::to_string(p->Dp) + ">:";
@@ -869,7 +869,7 @@ extern "C" int pgx_problem_set_team(pgx_problem* p, int32_t kernel, int32_t team
   if (!p || kernel < 0 || kernel >= pgx::kNumTunable) return PGX_ERR_INVALID;
   if (team != 0) {
     int vs[4];
-    const int nv = pgx::mixed_variants(p->Dp, vs);
+    const int nv = pgx::mixed_variants(p->Dp, kernel, vs);
     if (std::find(vs, vs + nv, team) == vs + nv)
       return ctx_fail(p->ctx, PGX_ERR_INVALID, "team size not admitted at this dimension");
   }

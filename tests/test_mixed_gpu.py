@@ -114,7 +114,7 @@ def test_mixed_full_size_bench_workload(pg):
     pm.close()
 
 
-@pytest.mark.parametrize("d", [4, 16, 32])
+@pytest.mark.parametrize("d", [4, 16, 32, 40])
 def test_autotune_keeps_results_bit_identical(pg, d):
     rng = np.random.default_rng(500 + d)
     prob, u0 = random_gate_problem(rng, d, n_t=12, n_members=5, dt=0.3 / np.sqrt(d))

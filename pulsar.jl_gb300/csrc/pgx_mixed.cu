@@ -402,7 +402,10 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_local_mx(ProbDev p, 
   }
 }
 
-template <int D>
+// Per member, the block products in order: P <- T_b P in df, each T_b staged
+// in shared memory first (a latency-bound chain of few teams); LSYM as in
+// k_chainf_local_mx.
+template <int D, bool LSYM>
 __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_combine_mx(ProbDev p, WorkDev w, int store) {
   using G = Cfg<D>;
   constexpr int T = G::T;
@@ -412,16 +415,22 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_combine_mx(ProbDev p
   const Team<T> tm{(int)(threadIdx.x % T)};
   const int m = blockIdx.x * G::TPC + team;
   if (m >= p.n_members) return;
-  float4* Pc = smem + (size_t)team * (D * D + T);
-  double2* red = reinterpret_cast<double2*>(Pc + D * D);
+  float4* Pc = smem + (size_t)team * (2 * D * D + T);
+  float4* Tb = Pc + D * D;
+  double2* red = reinterpret_cast<double2*>(Tb + D * D);
   for (int e = tm.lane; e < D * D; e += T) Pc[e] = make_float4((e % D) == (e / D) ? 1.f : 0.f, 0.f, 0.f, 0.f);
-  tm.sync();
   for (int b = 0; b < w.pit_blocks; ++b) {
+    const float4* tot = w.pit_tot + ((size_t)m * w.pit_blocks + b) * D * D;
+    for (int e = tm.lane; e < D * D; e += T) Tb[e] = tot[e];
+    tm.sync();
     if (store) {
       float2* pre = w.pit_pre + ((size_t)m * w.pit_blocks + b) * D * D;
       for (int e = tm.lane; e < D * D; e += T) pre[e] = make_float2(Pc[e].x, Pc[e].y);
     }
-    mm1_df<D, T>(tm, Pc, w.pit_tot + ((size_t)m * w.pit_blocks + b) * D * D, Pc);
+    if constexpr (LSYM)
+      mm_df_lsym<D, T, false, 0>(tm, Pc, Tb, Pc, DfEpiNone{});
+    else
+      mm1_df<D, T>(tm, Pc, Tb, Pc);
   }
   chain_epilogue_mx<D, T>(tm, p, w, m, Pc, red);
 }
@@ -1104,9 +1113,12 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   ensure_smem_mx(local, smem_l);
   const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
   local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
-  const size_t smem_c = (size_t)G::TPC * (D * D + G::T) * sizeof(float4);
-  ensure_smem_mx(k_chainf_combine_mx<D>, smem_c);
-  k_chainf_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
+  const size_t smem_c = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
+  auto combine = k_chainf_combine_mx<D, false>;
+  if constexpr (D == 64 && G::T == 256)
+    if (p.lsym) combine = k_chainf_combine_mx<D, true>;
+  ensure_smem_mx(combine, smem_c);
+  combine<<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
   *li.launches += 2;
   if (store && p.n_t > w.pit_len) {
     using F = FixCfg<D>;

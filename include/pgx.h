@@ -261,7 +261,9 @@ int pgx_penalty_eval(pgx_ctx* ctx, int32_t n_controls, int32_t n_slices, const d
 int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report, size_t report_len);
 /* Sets the team sizes directly (a plan kept from an earlier pgx_autotune);
  * 0 = the built-in default.  Values the dimension does not admit are refused
- * with PGX_ERR_INVALID.  Kernel indices: 0 = mixed expm, 1 = mixed gradient. */
+ * with PGX_ERR_INVALID.  Kernel indices: 0 = mixed expm, 1 = mixed gradient.
+ * Admitted by padded dimension: 32 (<= 8); 32, 64, 128, 256 (16); 128, 256
+ * (32); 256 (64), plus 512 for the gradient at 64.                          */
 #define PGX_TUNE_EXPM 0
 #define PGX_TUNE_GRAD 1
 int pgx_problem_set_team(pgx_problem* prob, int32_t kernel, int32_t team);

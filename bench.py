@@ -201,11 +201,24 @@ class Uneven:
     def __init__(self, name, cases, pg, ctx, grad_mode, precision):
         self.name, self.cases, self.grad_mode, self.precision = name, cases, grad_mode, precision
         self.probs = [gpu_problem(pg, ctx, pr, grad_mode, precision) for pr, _ in cases]
+        # autotuned tiles: one problem per (d, n_controls) key is tuned at its
+        # own controls and the others take its plan (variants are bit-identical)
+        self.tune = "defaults (FP64 path: no tunable kernels)"
+        if precision == "mixed":
+            plans = {}
+            for p, (pr, u0) in zip(self.probs, cases):
+                key = (pr.D, pr.n_c)
+                if key not in plans:
+                    p.autotune(u0, reps=2)
+                    plans[key] = p.teams
+                else:
+                    p.set_teams(*plans[key])
+            self.tune = (f"autotuned per (d, n_controls) key at load time ({len(plans)} keys tuned, "
+                         f"{len(self.probs) - len(plans)} problems took the plan of their key)")
         self.batch = pg.Batch(self.probs, n_streams=16)
         for i, (_, u0) in enumerate(cases):
             self.batch.set_controls(i, u0)
         self.units_per_step = self.batch.units
-        self.tune = "defaults (per-problem autotuning skipped for the batch)"
         self.h2d = int(sum(u0.size * 8 for _, u0 in cases))
         self.d2h = int(sum(u0.size * 8 + 8 for _, u0 in cases))
 

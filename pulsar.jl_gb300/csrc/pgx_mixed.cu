@@ -1040,10 +1040,13 @@ static int variants_for(int Dp, int kernel, int* out) {
   return n;
 }
 int mixed_variants(int Dp, int kernel, int* out) { return variants_for(Dp, kernel, out); }
+// Defaults (problems that were never tuned: batches, served jobs) are the
+// autotuner's usual choice on GB300 at each dimension.
 int mixed_default_team(int Dp, int kernel) {
-  if (Dp == 16) return kernel == kTuneExpmMx ? 256 : 32;
-  if (Dp == 32) return 256;
-  return Dp <= 8 ? 32 : 256;
+  if (Dp <= 8) return 32;
+  if (Dp == 16) return kernel == kTuneExpmMx ? 128 : 32;
+  if (Dp == 32) return kernel == kTuneExpmMx ? 256 : 128;
+  return kernel == kTuneExpmMx ? 256 : 512;
 }
 
 #define PGX_DISPATCH_MX_T(DP, TT, CALL)                                                        \

@@ -701,11 +701,19 @@ __device__ __forceinline__ void warp_copy_async(int lane, void* dst, const void*
   cp_async_commit();
 }
 
+// The same copy into the padded layout (leading dimension D + 1): each
+// 16-byte chunk is one df entry (r, c), placed at r + (D + 1) c.
+template <int D>
+__device__ __forceinline__ void warp_copy_async_pad(int lane, float4* dst, const float4* src) {
+  for (int i = lane; i < D * D; i += 32) cp_async16(dst + (i % D) + (D + 1) * (i / D), src + i);
+  cp_async_commit();
+}
+
 template <int D> __host__ __device__ constexpr size_t st_fwd_team_bytes(int np) {
   return (2 * (size_t)D * D + (size_t)np * D) * sizeof(float4);
 }
 template <int D> __host__ __device__ constexpr size_t st_bwd_team_bytes(int np) {
-  return 2 * (size_t)D * D * sizeof(float4) + (size_t)np * D * sizeof(float2);
+  return 2 * (size_t)D * (D + 1) * sizeof(float4) + (size_t)np * D * sizeof(float2);
 }
 
 // Forward in df: psi_s[k+1] = U_k psi_s[k], U_k the df propagator of the expm
@@ -814,14 +822,16 @@ __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_bwd_mx(Prob
   const int m = blockIdx.x * StCfg<D>::TPC + team;
   if (m >= p.n_members) return;
   const int np = p.n_pairs, pan = np * D;
+  // U_k in the padded layout: lane r reads column r of U (U' lambda), and a
+  // leading dimension of D + 1 puts the lanes of one load in distinct banks
+  constexpr int UP = D * (D + 1);
   unsigned char* base = smem_raw + (size_t)team * st_bwd_team_bytes<D>(np);
-  float4* Ub = reinterpret_cast<float4*>(base);                                         // [2][D*D]
-  float2* Ls = reinterpret_cast<float2*>(base + 2 * (size_t)D * D * sizeof(float4));  // [np][D]
+  float4* Ub = reinterpret_cast<float4*>(base);                                    // [2][D*(D+1)]
+  float2* Ls = reinterpret_cast<float2*>(base + 2 * (size_t)UP * sizeof(float4));  // [np][D]
   const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
   float2* Lm = reinterpret_cast<float2*>(w.lam) + (size_t)m * (p.n_t + 1) * pan;
-  constexpr size_t UB = (size_t)D * D * sizeof(float4);
   const int k0 = p.n_t - 1;
-  warp_copy_async(tm.lane, Ub, Um + (size_t)k0 * D * D, UB);
+  warp_copy_async_pad<D>(tm.lane, Ub, Um + (size_t)k0 * D * D);
   for (int e = tm.lane; e < pan; e += T) {
     const double2 kp = w.kap[(size_t)m * np + e / D];
     const double2 v = cmul(make_double2(kp.x, -kp.y), p.psi_targ[e]);
@@ -832,9 +842,9 @@ __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_bwd_mx(Prob
   tm.sync();
   for (int k = k0; k >= 0; --k) {
     const int slot = (k0 - k) & 1;
-    const float4* Uk = Ub + (size_t)slot * D * D;
+    const float4* Uk = Ub + (size_t)slot * UP;
     if (k > 0)  // the other buffer was last read at slice k + 1
-      warp_copy_async(tm.lane, Ub + (size_t)(slot ^ 1) * D * D, Um + (size_t)(k - 1) * D * D, UB);
+      warp_copy_async_pad<D>(tm.lane, Ub + (size_t)(slot ^ 1) * UP, Um + (size_t)(k - 1) * D * D);
     float2 outv[NO];
 #pragma unroll
     for (int i = 0; i < NO; ++i) {
@@ -843,7 +853,7 @@ __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_bwd_mx(Prob
         const int s = e / D, r = e % D;
         float2 acc = make_float2(0.f, 0.f);
         for (int q = 0; q < D; ++q) {
-          const float4 u = Uk[q + D * r];
+          const float4 u = Uk[q + (D + 1) * r];
           acc = cmac_cj(acc, make_float2(u.x, u.y), Ls[s * D + q]);
         }
         outv[i] = acc;

@@ -722,6 +722,50 @@ template <int D> __host__ __device__ constexpr size_t st_bwd_team_bytes(int np) 
 // them.  Utot[m np + s] receives the propagation residual of the pair in
 // FP64: |psi[n]|^2 - |psi[0]|^2 (Hermitian) or Tr rho[n] - Tr rho[0] (a
 // vectorised density matrix, N^2 = D).
+// Overlaps z_s, f, the chain-rule coefficients and the norm / trace residual
+// of member m from its final df states Ps (one warp).
+template <int D>
+__device__ __forceinline__ void states_fwd_epilogue(int lane, const ProbDev& p, const WorkDev& w, int m,
+                                                   const float4* Ps) {
+  constexpr int T = 32;
+  const int np = p.n_pairs;
+  int N = (int)lrint(sqrt((double)p.D));
+  if (p.gen != GEN_LIOUV || N * N != p.D) N = 0;
+  double Fm = 0.0;
+  for (int s = 0; s < np; ++s) {
+    double2 acc = make_double2(0.0, 0.0), res = make_double2(0.0, 0.0);
+    for (int r = lane; r < D; r += T) {
+      const double2 v = dfc_to(dfc_load(Ps[s * D + r]));
+      const double2 v0 = p.psi_init[s * D + r];
+      acc = cmac_cj(acc, p.psi_targ[s * D + r], v);
+      if (p.gen == GEN_HERM) {
+        res.x += (v.x * v.x + v.y * v.y) - (v0.x * v0.x + v0.y * v0.y);
+      } else if (N && r < N * N && r % (N + 1) == 0) {
+        res.x += v.x - v0.x;
+        res.y += v.y - v0.y;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      res.x += __shfl_xor_sync(0xffffffffu, res.x, o);
+      res.y += __shfl_xor_sync(0xffffffffu, res.y, o);
+    }
+    double f;
+    double2 kap;
+    fid_kappa(acc, p.fid, p.grad_mode, f, kap);
+    Fm += f;
+    if (lane == 0) {
+      const double wgt = p.m_weight[m];
+      w.z[(size_t)m * np + s] = acc;
+      w.kap[(size_t)m * np + s] = make_double2(kap.x * wgt, kap.y * wgt);
+      w.Utot[(size_t)m * np + s] = res;
+    }
+  }
+  if (lane == 0) w.Fm[m] = Fm;
+}
+
 template <int D>
 __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_fwd_mx(ProbDev p, WorkDev w, int store) {
   constexpr int T = 32;
@@ -771,41 +815,81 @@ __global__ void __launch_bounds__(32 * StCfg<D>::TPC) k_chain_states_fwd_mx(Prob
     cp_async_wait_all();
     tm.sync();
   }
-  int N = (int)lrint(sqrt((double)p.D));
-  if (p.gen != GEN_LIOUV || N * N != p.D) N = 0;
-  double Fm = 0.0;
-  for (int s = 0; s < np; ++s) {
-    double2 acc = make_double2(0.0, 0.0), res = make_double2(0.0, 0.0);
-    for (int r = tm.lane; r < D; r += T) {
-      const double2 v = dfc_to(dfc_load(Ps[s * D + r]));
-      const double2 v0 = p.psi_init[s * D + r];
-      acc = cmac_cj(acc, p.psi_targ[s * D + r], v);
-      if (p.gen == GEN_HERM) {
-        res.x += (v.x * v.x + v.y * v.y) - (v0.x * v0.x + v0.y * v0.y);
-      } else if (N && r < N * N && r % (N + 1) == 0) {
-        res.x += v.x - v0.x;
-        res.y += v.y - v0.y;
+  states_fwd_epilogue<D>(tm.lane, p, w, m, Ps);
+}
+
+// D >= 16: the same chain with each member's dot products split over kStW
+// warps (k in [w D/kStW, (w+1) D/kStW) for warp w).  One member per CTA.  The
+// partial df sums are merged in warp order after a barrier.  One warp per
+// member leaves most SM sub-partitions idle (231 members, 608 of them), and a
+// 16-term df dot product is a long dependent chain.
+constexpr int kStW = 4;
+template <int D> __host__ __device__ constexpr size_t st_fwd_split_bytes(int np) {
+  return (2 * (size_t)D * D + (size_t)(1 + kStW) * np * D) * sizeof(float4);
+}
+template <int D>
+__global__ void __launch_bounds__(32 * kStW) k_chain_states_fwd_split_mx(ProbDev p, WorkDev w, int store) {
+  static_assert(D % kStW == 0, "k split");
+  constexpr int NT = 32 * kStW, KQ = D / kStW;
+  constexpr int NO = (8 * D + 31) / 32;  // outputs per lane: at most 8 pairs
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = blockIdx.x, tid = threadIdx.x, wp = tid / 32, lane = tid % 32;
+  const int np = p.n_pairs, pan = np * D;
+  float4* Ub = reinterpret_cast<float4*>(smem_raw);  // [2][D*D]
+  float4* Ps = Ub + 2 * D * D;                        // [np][D]
+  float4* part = Ps + pan;                            // [kStW][np * D] partial sums {sr, cr, si, ci}
+  float2* Pst = reinterpret_cast<float2*>(w.psi) + (size_t)m * (p.n_t + 1) * pan;
+  const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * D * D;
+  const auto copy_u = [&](float4* dst, const float4* src) {
+    for (int i = tid; i < D * D; i += NT) cp_async16(dst + i, src + i);
+    cp_async_commit();
+  };
+  copy_u(Ub, Um);
+  for (int e = tid; e < pan; e += NT) {
+    Ps[e] = dfc_store(dfc_from(p.psi_init[e]));
+    if (store) Pst[e] = make_float2(Ps[e].x, Ps[e].y);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  for (int k = 0; k < p.n_t; ++k) {
+    const float4* Uk = Ub + (size_t)(k & 1) * D * D;
+    if (k + 1 < p.n_t)  // the other buffer was last read at slice k - 1
+      copy_u(Ub + (size_t)((k + 1) & 1) * D * D, Um + (size_t)(k + 1) * D * D);
+#pragma unroll
+    for (int i = 0; i < NO; ++i) {
+      const int e = lane + 32 * i;
+      if (e < pan) {
+        const int s = e / D, r = e % D;
+        DfAcc acc;
+#pragma unroll
+        for (int q = wp * KQ; q < (wp + 1) * KQ; ++q) acc.mac(Uk[r + D * q], Ps[s * D + q]);
+        part[(size_t)wp * pan + e] = make_float4(acc.sr, acc.cr, acc.si, acc.ci);
       }
     }
+    __syncthreads();
+    for (int e = tid; e < pan; e += NT) {
+      const float4 v0 = part[e];
+      DfAcc acc;
+      acc.sr = v0.x; acc.cr = v0.y; acc.si = v0.z; acc.ci = v0.w;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-      res.x += __shfl_xor_sync(0xffffffffu, res.x, o);
-      res.y += __shfl_xor_sync(0xffffffffu, res.y, o);
+      for (int q = 1; q < kStW; ++q) {
+        const float4 v = part[(size_t)q * pan + e];
+        float t, er;
+        two_sum(acc.sr, v.x, t, er);
+        acc.sr = t;
+        acc.cr = (acc.cr + v.y) + er;
+        two_sum(acc.si, v.z, t, er);
+        acc.si = t;
+        acc.ci = (acc.ci + v.w) + er;
+      }
+      const float4 o = dfc_store(acc.result());
+      Ps[e] = o;
+      if (store) Pst[(size_t)(k + 1) * pan + e] = make_float2(o.x, o.y);
     }
-    double f;
-    double2 kap;
-    fid_kappa(acc, p.fid, p.grad_mode, f, kap);
-    Fm += f;
-    if (tm.lane == 0) {
-      const double wgt = p.m_weight[m];
-      w.z[(size_t)m * np + s] = acc;
-      w.kap[(size_t)m * np + s] = make_double2(kap.x * wgt, kap.y * wgt);
-      w.Utot[(size_t)m * np + s] = res;
-    }
+    cp_async_wait_all();
+    __syncthreads();
   }
-  if (tm.lane == 0) w.Fm[m] = Fm;
+  if (wp == 0) states_fwd_epilogue<D>(lane, p, w, m, Ps);
 }
 
 // Backward in FP32: lambda_s[n] = conj(kappa_s) t_s, lambda_s[k] = U_k'
@@ -1106,6 +1190,13 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   using G = Cfg<D>;
   if (p.target != TGT_GATE) {
     constexpr int TPC = StCfg<D>::TPC;
+    if constexpr (D >= 16) {
+      const size_t smem = st_fwd_split_bytes<D>(p.n_pairs);
+      ensure_smem_mx(k_chain_states_fwd_split_mx<D>, smem);
+      k_chain_states_fwd_split_mx<D><<<p.n_members, 32 * kStW, smem, li.stream>>>(p, w, store ? 1 : 0);
+      ++*li.launches;
+      return cudaGetLastError();
+    }
     const size_t smem = (size_t)TPC * st_fwd_team_bytes<D>(p.n_pairs);
     ensure_smem_mx(k_chain_states_fwd_mx<D>, smem);
     k_chain_states_fwd_mx<D><<<(p.n_members + TPC - 1) / TPC, 32 * TPC, smem, li.stream>>>(p, w, store ? 1 : 0);

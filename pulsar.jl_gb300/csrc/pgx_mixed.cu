@@ -55,8 +55,7 @@ template <int D, int T> struct CfgM {
   // gradient kernel: the q = 2 Paterson-Stockmeyer Frechet form, six
   // complex-float matrices in the padded layout (fits shared memory at D = 64;
   // at the norms of short slices it is also the cheaper form, below)
-  static constexpr bool GRAD_Q2 = true;
-  static constexpr size_t WSG = (size_t)(GRAD_Q2 ? 6 : 10) * Lay<D, 2>::SIZE * sizeof(float2);
+  static constexpr size_t WSG = (size_t)6 * Lay<D, 2>::SIZE * sizeof(float2);
   static constexpr size_t SMEM_G = TPC * WSG + TPC * RED;
 };
 
@@ -1031,7 +1030,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
   const Team<T> tm = team_of<D, T>();
   float2* base = reinterpret_cast<float2*>(smem_raw + (size_t)team * G::WSG);
   float2* red = reinterpret_cast<float2*>(smem_raw + G::TPC * G::WSG + (size_t)team * G::RED);
-  using Wk = std::conditional_t<G::GRAD_Q2, Work2<float2, D, L::SIZE>, Work<float2, D, L::SIZE>>;
+  using Wk = Work2<float2, D, L::SIZE>;
   const Wk W = Wk::at(base);
   const bool exact = (p.grad_mode == GRAD_EXACT);
   const long items = (long)p.n_members * p.n_t;
@@ -1069,10 +1068,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
     tm.sync();
     const float nrm = norm1f<D, T, kSwzGrad>(tm, W.B, reinterpret_cast<float*>(red));
     int deg, s;
-    if constexpr (G::GRAD_Q2)
-      choose_degree_q2(nrm, c_theta32f, deg, s);
-    else
-      choose_degree_f(nrm, c_theta32f, deg, s);
+    choose_degree_q2(nrm, c_theta32f, deg, s);
     const float sc = ldexpf(1.f, -s);
     for (int q = tm.lane; q < D * D; q += T) {
       const int e = L::idx(q % D, q / D);
@@ -1080,10 +1076,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
       W.dB[e] = cscale(W.dB[e], sc);
     }
     tm.sync();
-    if constexpr (G::GRAD_Q2)
-      taylor_exp_frechet2<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
-    else
-      taylor_exp_frechet<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
+    taylor_exp_frechet2<D, T, kSwzGrad>(tm, W, deg, s, c_invf32);
     trace_controls32<D, T, kSwzGrad>(tm, p, W.dY, m, k, Gout, red);
     tm.sync();
   }

@@ -104,28 +104,9 @@ __device__ __forceinline__ void team_slot(double2* smem, int per_team_elems, int
 }
 
 static __constant__ float c_invf32[PGX_N_INVFACT] = PGX_INVFACT32_INIT;
-static __constant__ double c_theta32[PGX_N_DEGREES] = PGX_THETA32_INIT;
-// The same thresholds in float for the mixed kernels, which choose the degree
-// without touching the FP64 pipe (the norm they compare carries a 1e-5
-// safety margin, far above the float rounding of a threshold).
-static __constant__ float c_theta64f[PGX_N_DEGREES] = PGX_THETA64_INIT;
+// The FP32 thresholds for the mixed gradient, which chooses its degree
+// without touching the FP64 pipe (the norm it compares carries a 1e-5 safety
+// margin, far above the float rounding of a threshold).
 static __constant__ float c_theta32f[PGX_N_DEGREES] = PGX_THETA32_INIT;
-static __constant__ float c_thetadf[PGX_N_DEGREES] = PGX_THETADF_INIT;
-
-// choose_degree in float (same cost model, same tie-breaking).
-__device__ __forceinline__ void choose_degree_f(float nrm, const float* theta, int& m, int& s) {
-  int best_cost = 1 << 30;
-  m = 4;
-  s = 0;
-#pragma unroll
-  for (int i = 0; i < PGX_N_DEGREES; ++i) {
-    int si = 0;
-    float x = nrm;
-    while (x > theta[i] && si < 60) { x *= 0.5f; ++si; }
-    const int mi = 4 * (i + 1);
-    const int cost = (3 + mi / 4 - 1) + si;
-    if (cost < best_cost) { best_cost = cost; m = mi; s = si; }
-  }
-}
 
 }  // namespace pgx

@@ -90,6 +90,7 @@ struct pgx_batch {
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;   // fork + one join per stream
   cudaGraphExec_t eval_exec = nullptr, iter_exec = nullptr;
+  std::vector<uint64_t> gens;        // the problems' generations the graphs were captured at
   // device tables
   double** d_u = nullptr;
   double** d_G = nullptr;
@@ -106,6 +107,19 @@ struct pgx_batch {
 };
 
 static int batch_cuda(pgx_batch* b, cudaError_t e, const char* where) { return ctx_cuda(b->ctx, e, where); }
+
+// Drops both graphs when a problem was changed (pgx_problem_set_*, autotune)
+// since they were captured; the next eval / iterate captures them again.
+static void drop_stale_graphs(pgx_batch* b) {
+  bool stale = b->gens.size() != b->probs.size();
+  for (size_t i = 0; !stale && i < b->probs.size(); ++i) stale = b->gens[i] != b->probs[i]->generation;
+  if (!stale) return;
+  if (b->eval_exec) cudaGraphExecDestroy(b->eval_exec);
+  if (b->iter_exec) cudaGraphExecDestroy(b->iter_exec);
+  b->eval_exec = b->iter_exec = nullptr;
+  b->gens.clear();
+  for (const pgx_problem* p : b->probs) b->gens.push_back(p->generation);
+}
 
 // Fork the context stream into the batch streams, enqueue every pipeline,
 // join; returns the captured graph instantiated.
@@ -267,6 +281,7 @@ extern "C" int pgx_batch_eval(pgx_batch* b, double* F) {
   pgx_ctx* c = b->ctx;
   cudaSetDevice(c->device);
   int st = PGX_OK;
+  drop_stale_graphs(b);
   if (!b->eval_exec) {
     // one plain pass first: sets kernel attributes outside the capture
     for (pgx_problem* p : b->probs)

@@ -114,6 +114,7 @@ extern "C" int pgx_problem_set_penalties(pgx_problem* p, int32_t n, const pgx_pe
     if (st2) return st2;
   }
   p->n_pen = n;
+  ++p->generation;
   return PGX_OK;
 }
 

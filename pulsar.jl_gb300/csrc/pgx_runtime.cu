@@ -561,8 +561,10 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   // Liouvillians whose every generator piece preserves Hermiticity, at a
   // dimension without padding: the mixed expm and forward chain keep half
   // of each product (D = 64)
-  pd.lsym = d->generator == PGX_GEN_LIOUVILLIAN && Dp == D && lsym_all(d->drifts, d->n_drifts, D) &&
-            lsym_all(d->controls, d->n_controls, D) && (!d->offset_op || lsym_all(d->offset_op, 1, D));
+  p->lsym_fixed = d->generator == PGX_GEN_LIOUVILLIAN && Dp == D && lsym_all(d->controls, d->n_controls, D) &&
+                  (!d->offset_op || lsym_all(d->offset_op, 1, D));
+  p->lsym_drift = p->lsym_fixed && lsym_all(d->drifts, d->n_drifts, D);
+  pd.lsym = (p->lsym_fixed && p->lsym_drift) ? 1 : 0;
   pd.target = d->target;
   pd.fid = d->fidelity;
   pd.grad_mode = d->grad_mode;
@@ -577,7 +579,6 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   pd.target_op = (const double2*)g_tg;
   pd.psi_init = (const double2*)g_pi;
   pd.psi_targ = (const double2*)g_pt;
-  p->lsym_base = pd.lsym != 0;
   p->pd_grad = pd;
   p->pd_grad.psi_init = (const double2*)g_pg;
 
@@ -855,6 +856,7 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
       if (per < best_ms) { best_ms = per; best = vs[i]; }
     }
     p->team[kern] = best;
+    ++p->generation;
     rep += " -> T=" + std::to_string(best);
   }
   {
@@ -874,6 +876,7 @@ extern "C" int pgx_problem_set_team(pgx_problem* p, int32_t kernel, int32_t team
       return ctx_fail(p->ctx, PGX_ERR_INVALID, "team size not admitted at this dimension");
   }
   p->team[kernel] = team;
+  ++p->generation;
   return PGX_OK;
 }
 
@@ -1091,9 +1094,16 @@ extern "C" int pgx_problem_set_drifts(pgx_problem* p, const double* drifts) {
       if (herm_dev(drifts + 2 * (size_t)i * D * D, D) > 1e-10)
         return ctx_fail(c, PGX_ERR_INVALID, "drift is not Hermitian (QuantumSystem.jl:318-341)");
   cudaSetDevice(c->device);
+  // the flag changes only after the stream has drained the evaluations that
+  // were enqueued with the old drifts
+  int st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st) return st;
+  p->lsym_drift = p->lsym_fixed && lsym_all(drifts, nd, D);
+  p->refresh_lsym();
+  ++p->generation;
   const std::vector<double> padded = pad_mats(drifts, nd, D, Dp);
-  int st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts, padded.data(), padded.size() * sizeof(double),
-                                       cudaMemcpyHostToDevice, c->stream), "H2D drifts");
+  st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts, padded.data(), padded.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream), "H2D drifts");
   if (!st && p->pd.drifts_df) {
     const std::vector<float> dfp = to_df_pairs(padded);
     st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts_df, dfp.data(), dfp.size() * sizeof(float),
@@ -1279,6 +1289,7 @@ extern "C" int pgx_problem_set_tracking(pgx_problem* p, int32_t n, const int32_t
     pd->ck_weight = n ? reinterpret_cast<const double*>(base + off_w) : nullptr;
     pd->ck_target = n ? reinterpret_cast<const double2*>(base + off_t) : nullptr;
   }
+  ++p->generation;
   return PGX_OK;
 }
 
@@ -1334,9 +1345,10 @@ extern "C" int pgx_problem_set_drift_ramp(pgx_problem* p, int32_t n_ops, const d
       return st;
   }
   unsigned char* base = static_cast<unsigned char*>(p->d_ramp);
-  const bool rsym = n_ops == 0 || lsym_all(ops, n_ops, D);  // the symmetric products need every piece symmetric
+  p->lsym_ramp = n_ops == 0 || lsym_all(ops, n_ops, D);  // the symmetric products need every piece symmetric
+  p->refresh_lsym();
+  ++p->generation;
   for (pgx::ProbDev* pd : {&p->pd, &p->pd_grad}) {
-    pd->lsym = p->lsym_base && rsym;
     pd->n_ramp = n_ops;
     pd->m_ramp = n_ops ? reinterpret_cast<const int*>(base) : nullptr;
     pd->tau = n_ops ? reinterpret_cast<const double*>(base + off_tau) : nullptr;

@@ -53,7 +53,16 @@ struct pgx_problem {
   // mixed gate problems in parallel in time: stream and fork/join events of
   // the backward chain's in-block suffixes
   cudaStream_t side = nullptr;
-  bool lsym_base = false;  // generator pieces given at creation preserve Hermiticity (ProbDev::lsym)
+  // ProbDev::lsym = lsym_fixed && lsym_drift && lsym_ramp: the controls and
+  // offset (and dimension) at creation, the current drifts, the current ramp
+  // operators each preserve Hermiticity
+  bool lsym_fixed = false, lsym_drift = false, lsym_ramp = true;
+  // bumped by every setter that changes what run_pipeline enqueues (kernel
+  // parameters, team sizes): graphs captured earlier (batches) are stale
+  uint64_t generation = 0;
+  void refresh_lsym() {
+    pd.lsym = pd_grad.lsym = (lsym_fixed && lsym_drift && lsym_ramp) ? 1 : 0;
+  }
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   pgx::LaunchInfo launch_info() const {
     pgx::LaunchInfo li{ctx->num_sms, ctx->stream, &ctx->launches};

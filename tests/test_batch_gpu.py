@@ -49,6 +49,30 @@ def test_batch_eval_bit_identical_to_solo(pg, precision):
         p.close()
 
 
+def test_batch_recaptures_after_a_member_changes(pg):
+    """A setter on a member problem (here a drift ramp) invalidates the batch's
+    captured graphs: the next batch evaluation matches the changed problem
+    evaluated alone."""
+    cases = _small_uneven(n=6, seed=23)
+    probs = [to_gpu(pg, prob, "exact", precision="mixed") for prob, _ in cases]
+    b = pg.Batch(probs, n_streams=2)
+    for i, (_, u0) in enumerate(cases):
+        b.set_controls(i, u0)
+    F1 = b.eval()
+    prob, u0 = cases[4]
+    rng = np.random.default_rng(9)
+    R = rng.standard_normal((1, prob.D, prob.D)) * 0.3
+    R = (R + R.transpose(0, 2, 1)) * np.abs(prob.drifts).max()
+    probs[4].set_drift_ramp(R, np.zeros(prob.n_members, int), np.linspace(0, 1, prob.n_t))
+    F2 = b.eval()
+    Fs, _ = probs[4].eval(u0)
+    assert F2[4] == Fs and F2[4] != F1[4]
+    assert np.array_equal(np.delete(F2, 4), np.delete(F1, 4))
+    b.close()
+    for p in probs:
+        p.close()
+
+
 def test_batch_iterate_follows_grape_step_rule(pg):
     cases = _small_uneven(n=6, seed=5)
     probs = [to_gpu(pg, prob, "exact", precision="mixed") for prob, _ in cases]

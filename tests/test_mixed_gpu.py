@@ -76,6 +76,26 @@ def test_mixed_lindblad_symmetric_path_matches_full_path(pg):
     p.close()
 
 
+def test_mixed_lindblad_set_drifts_updates_symmetry(pg):
+    """Replacing the drifts re-checks the symmetry: asymmetric drifts take the
+    full products (parity with the oracle), symmetric ones the halved ones."""
+    prob, u0 = fx.lindblad_3q(n_t=6, n_draws=2)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F0, G0 = p.eval(u0)
+    orig = prob.drifts.copy()
+    rng = np.random.default_rng(12)
+    pert = 1e-6 * np.abs(orig).max() * (rng.standard_normal(orig.shape) + 1j * rng.standard_normal(orig.shape))
+    prob.drifts = orig + pert
+    p.set_drifts(prob.drifts)
+    F1, G1 = p.eval(u0)
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    check(F1, G1, Fo, Go)
+    p.set_drifts(orig)
+    F2, G2 = p.eval(u0)
+    assert F2 == F0 and np.array_equal(G2, G0)
+    p.close()
+
+
 def test_mixed_lindblad_asymmetric_generator(pg):
     """A Liouvillian whose drift does not preserve Hermiticity (relative
     defect 1e-6, far above the 1e-12 the symmetric path admits, small enough

@@ -52,6 +52,11 @@ struct ProbDev {
   const float2* dt_df;       // [n_t] df pairs {hi, lo}
   const float2* m_scale_df;  // [n_members]
   const float2* m_offset_df; // [n_members]
+  // mixed precision only: the FP32 roundings (the leading halves of the df
+  // copies), read by the FP32 stages
+  const float2* drifts_f32;  // [n_drifts][Dp*Dp]
+  const float2* ctrls_f32;   // [n_c][Dp*Dp]
+  const float2* offset_f32;  // [Dp*Dp]
 };
 
 // Device work buffers of one evaluation.

@@ -109,19 +109,20 @@ __device__ __forceinline__ void build_A_df(const Team<T>& tm, const ProbDev& p, 
   }
 }
 
-// The same in FP32 from the leading halves of the df constants.
+// The same in FP32 from the FP32 copies of the constants (the leading halves
+// of the df copies).
 template <int D, int T, int SW>
 __device__ __forceinline__ void build_A32(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m,
                                           int k, float2* A) {
   const float dt = p.dt_df[k].x, sc = p.m_scale_df[m].x, off = p.m_offset_df[m].x;
-  const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
+  const float2* Gd = p.drifts_f32 + (size_t)p.m_drift[m] * D * D;
   const float2* uk = w.u_df + (size_t)k * p.n_c;
   const int ro = p.n_ramp ? p.m_ramp[m] : -1;
   const float4* Rm = ro >= 0 ? p.ramp_ops_df + (size_t)ro * D * D : nullptr;
   const float tk = ro >= 0 ? p.tau_df[k].x : 0.f;
   for (int q = tm.lane; q < D * D; q += T) {
-    const float4 g = Gd[q];
-    const float4 o = p.offset_df[q];
+    const float2 g = Gd[q];
+    const float2 o = p.offset_f32[q];
     float vx = fmaf(off, o.x, g.x), vy = fmaf(off, o.y, g.y);
     if (Rm) {
       vx = fmaf(tk, Rm[q].x, vx);
@@ -129,7 +130,7 @@ __device__ __forceinline__ void build_A32(const Team<T>& tm, const ProbDev& p, c
     }
     for (int j = 0; j < p.n_c; ++j) {
       const float a = sc * uk[j].x;
-      const float4 c = p.ctrls_df[(size_t)j * D * D + q];
+      const float2 c = p.ctrls_f32[(size_t)j * D * D + q];
       vx = fmaf(a, c.x, vx);
       vy = fmaf(a, c.y, vy);
     }
@@ -971,13 +972,12 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
     constexpr int NCH = 256, NGR = NCH / 32;
     static_assert(T >= 32 && 2 * T >= NCH, "trace scratch holds the 256 chunk sums");
     for (int j = 0; j < p.n_c; ++j) {
-      const float4* Cj = p.ctrls_df + (size_t)j * D * D;
+      const float2* Cj = p.ctrls_f32 + (size_t)j * D * D;
       for (int c = tm.lane; c < NCH; c += T) {
         float2 acc = make_float2(0.f, 0.f);
         for (int q = c; q < D * D; q += NCH) {
           const int r = q % D, cc = q / D;
-          const float4 cv = Cj[cc + D * r];
-          acc = cmac(acc, X[Lay<D, SW>::idx(r, cc)], make_float2(cv.x, cv.y));
+          acc = cmac(acc, X[Lay<D, SW>::idx(r, cc)], Cj[cc + D * r]);
         }
         red[c] = acc;
       }
@@ -1003,12 +1003,11 @@ __device__ __forceinline__ void trace_controls32(const Team<T>& tm, const ProbDe
   }
   if (tm.lane < 32) {
     for (int j = 0; j < p.n_c; ++j) {
-      const float4* Cj = p.ctrls_df + (size_t)j * D * D;
+      const float2* Cj = p.ctrls_f32 + (size_t)j * D * D;
       float2 acc = make_float2(0.f, 0.f);
       for (int q = tm.lane; q < D * D; q += 32) {
         const int r = q % D, c = q / D;
-        const float4 cv = Cj[c + D * r];
-        acc = cmac(acc, X[Lay<D, SW>::idx(r, c)], make_float2(cv.x, cv.y));
+        acc = cmac(acc, X[Lay<D, SW>::idx(r, c)], Cj[c + D * r]);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {

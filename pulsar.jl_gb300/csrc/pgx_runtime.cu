@@ -364,9 +364,10 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
   const size_t pit = pit_b > 1 ? (size_t)d->n_members * Dp * Dp *
                                      (pit_b * (sizeof(float4) + 2 * sizeof(float2)) + (size_t)d->n_slices * sizeof(float2))
                                : 0;
-  // mixed: df copies of the generator constants and scalars, df controls
+  // mixed: df and FP32 copies of the generator constants, df scalars and
+  // controls
   const size_t mixed = pit + (d->precision == PGX_PREC_MIXED
-                           ? DD * (d->n_drifts + d->n_controls + 1) +
+                           ? (DD + DD / 2) * (d->n_drifts + d->n_controls + 1) +
                                  sizeof(float2) * ((size_t)d->n_slices + 2 * (size_t)d->n_members) + s.u
                            : 0);
   return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
@@ -399,6 +400,14 @@ std::vector<double> pad_mats(const double* src, int n, int D, int Dp) {
         out[di] = src[si];
         out[di + 1] = src[si + 1];
       }
+  return out;
+}
+
+// Interleaved complex doubles -> their FP32 roundings (the leading halves of
+// the df pairs below).
+static std::vector<float> to_f32(const std::vector<double>& z) {
+  std::vector<float> out(z.size());
+  for (size_t i = 0; i < z.size(); ++i) out[i] = (float)z[i];
   return out;
 }
 
@@ -541,6 +550,16 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
     pd.drifts_df = (const float4*)f_dr;
     pd.ctrls_df = (const float4*)f_ct;
     pd.offset_df = (const float4*)f_of;
+    // FP32 copies for the FP32 stages (half the bytes of the df copies)
+    float *h_dr, *h_ct, *h_of;
+    if ((st = upload(p, &h_dr, to_f32(drifts))) || (st = upload(p, &h_ct, to_f32(ctrls))) ||
+        (st = upload(p, &h_of, to_f32(offs)))) {
+      pgx_problem_destroy(p);
+      return st;
+    }
+    pd.drifts_f32 = (const float2*)h_dr;
+    pd.ctrls_f32 = (const float2*)h_ct;
+    pd.offset_f32 = (const float2*)h_of;
     float *f_dt, *f_ms, *f_mo;
     if ((st = upload(p, &f_dt, to_df_scalars(dt))) || (st = upload(p, &f_ms, to_df_scalars(mscale))) ||
         (st = upload(p, &f_mo, to_df_scalars(moff)))) {
@@ -1105,9 +1124,12 @@ extern "C" int pgx_problem_set_drifts(pgx_problem* p, const double* drifts) {
   st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts, padded.data(), padded.size() * sizeof(double),
                                    cudaMemcpyHostToDevice, c->stream), "H2D drifts");
   if (!st && p->pd.drifts_df) {
-    const std::vector<float> dfp = to_df_pairs(padded);
+    const std::vector<float> dfp = to_df_pairs(padded), f32 = to_f32(padded);
     st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts_df, dfp.data(), dfp.size() * sizeof(float),
                                      cudaMemcpyHostToDevice, c->stream), "H2D drifts (df)");
+    if (!st)
+      st = ctx_cuda(c, cudaMemcpyAsync((void*)p->pd.drifts_f32, f32.data(), f32.size() * sizeof(float),
+                                       cudaMemcpyHostToDevice, c->stream), "H2D drifts (FP32)");
     if (!st) st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "sync");  // dfp lives on this stack
     return st;
   }

@@ -100,3 +100,29 @@ def test_plan_cache_is_host_side(pg):
     A = pg._abi
     t1, t2 = C.c_int32(), C.c_int32()
     assert A.lib().pgx_plan_lookup(0, None, C.byref(t1), C.byref(t2)) == 1
+
+
+def test_taylor_table_is_the_generators_output():
+    """csrc/taylor_table.h is exactly what csrc/gen_taylor_table.py prints
+    (the thresholds the expm kernels choose degrees with)."""
+    import io
+    import importlib.util
+    gen = ROOT / "pulsar.jl_gb300" / "csrc" / "gen_taylor_table.py"
+    spec = importlib.util.spec_from_file_location("gen_taylor_table", gen)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    buf = io.StringIO()
+    mod.main(out=buf)
+    assert buf.getvalue() == (ROOT / "pulsar.jl_gb300" / "csrc" / "taylor_table.h").read_text()
+
+
+def test_df_thresholds_bound_the_taylor_tail():
+    """Every df threshold theta_m (degrees 1..20) keeps the Taylor tail
+    sum_{k>m} theta^k/k! at or below 2^-47, and is increasing in m."""
+    import math
+    txt = (ROOT / "pulsar.jl_gb300" / "csrc" / "taylor_table.h").read_text()
+    vals = [float(v) for v in re.search(r"PGX_THETADF_ALL_INIT \{([^}]*)\}", txt).group(1).split(",")]
+    assert len(vals) == 20 and all(a < b for a, b in zip(vals, vals[1:]))
+    for m, th in enumerate(vals, start=1):
+        tail = sum(th ** k / math.factorial(k) for k in range(m + 1, m + 60))
+        assert tail <= 2.0 ** -47 * (1 + 1e-9), (m, th, tail)

@@ -24,7 +24,7 @@ def check(F, G, Fo, Go):
 
 
 @pytest.mark.parametrize("mode", ["ref_grape", "ref_mr", "exact"])
-@pytest.mark.parametrize("d", [2, 4, 7, 16, 32])
+@pytest.mark.parametrize("d", [2, 4, 7, 16, 32, 40])
 def test_mixed_random_gate(pg, mode, d):
     rng = np.random.default_rng(300 + d)
     prob, u0 = random_gate_problem(rng, d, n_t=8, n_members=3, dt=0.3 / np.sqrt(d))

@@ -53,12 +53,17 @@ METRIC = "ensemble-slice grads/s"
 UNIT = "units/s"
 K_EXP = 8  # conventional matrix-product count of one expm in the FLOP model
 
-# DRAM bytes per launch of the dominant kernel from ncu captures, scaled from
-# the captured 200-slice case to 1000 slices (one M_k read per unit: linear).
+# DRAM bytes per launch of the dominant kernel from ncu captures of a smaller
+# case (spin-4: 200 of 1000 slices; lindblad3q: 100 of 500), scaled by the
+# units a full launch processes (every unit reads or writes the same bytes).
 TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
-           ("spin4", "mixed", "expm"): 5 * (73.728000e6 + 127.458816e6),
-           ("spin4", "mixed", "grad"): 5 * (94.700032e6 + 2.850560e6),
-           ("spin4", "mixed", "chain_fwd"): 5 * (189.268736e6 + 67.549952e6)}
+           # k_expm_mx<16,128,Herm>, 200-slice capture: 0.1 MB read, the df U stack written
+           ("spin4", "mixed", "expm"): 5 * (0.095232e6 + 127.364352e6),
+           ("spin4", "mixed", "grad"): 5 * (94.700544e6 + 2.850816e6),
+           ("spin4", "mixed", "chain_fwd"): 5 * (189.268736e6 + 67.549952e6),
+           # k_expm_mx<64,256,LSym>, 100-slice capture: the per-team slab's L2
+           # write-backs come on top of the 210 MB U stack
+           ("lindblad3q", "mixed", "expm"): 5 * (70.671360e6 + 1.058322e9)}
 # FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
 # accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
 # busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).

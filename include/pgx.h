@@ -279,9 +279,9 @@ int pgx_plan_clear(void);
 
 /* ---- allocation-free total propagator ----------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory when they need a propagator (during CUDA-graph capture, in real-time
- * loops that forbid allocation after start-up, or inside hosts whose device
- * memory comes from their own pool): computes
+ * memory when they need a propagator (real-time loops that forbid allocation
+ * once started, or hosts whose device memory all comes from their own pool
+ * allocator): computes
  *   U_total = exp(c dt_{n-1} G_{n-1}) ... exp(c dt_0 G_0),
  * c = -i (PGX_GEN_HERMITIAN) or 1 (PGX_GEN_LIOUVILLIAN), with every piece of
  * working memory in one static device array of PGX_NOALLOC_SCRATCH_BYTES that
@@ -293,8 +293,8 @@ int pgx_plan_clear(void);
  * (n_slices * Dp^2 * 16 bytes, Dp = next power of two >= dim, plus 5 MiB of
  * Taylor workspace when Dp = 64) exceeds the array are rejected with
  * PGX_ERR_BUDGET and a message in err (err may be NULL).  The first call on a
- * device sets that device up (resolves the array's address); make it before
- * any stream capture.  All calls share the array: calls whose GPU work
+ * device sets that device up (resolves the array's address and loads every
+ * kernel the entry point uses); make it before any stream capture.  All calls share the array: calls whose GPU work
  * overlaps race and must be serialised by the caller.  Input contents are not
  * validated (Hermiticity, finiteness are the caller's responsibility).     */
 #define PGX_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)

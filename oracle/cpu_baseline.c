@@ -9,7 +9,11 @@
  *   - per slice H_k = drift + offset*O + scale*sum_j u_jk C_j
  *     (Propagators.jl:520-544, GRAPEState.jl:187-191);
  *   - U_k = V diag(exp(-i lambda dt)) V' from a Hermitian eigendecomposition
- *     (Propagators.jl:659-674; LAPACK zheevd there, cyclic complex Jacobi here);
+ *     (Propagators.jl:659-674: eigen(Hermitian(H)), which Julia's
+ *     LinearAlgebra runs as LAPACK zheevr, then mul!(out, tmp, V') = zgemm);
+ *     with pgx_cpu_set_lapack the same LAPACK zheevr and BLAS zgemm run here
+ *     (function pointers handed in by the caller, e.g. the OpenBLAS/LAPACK
+ *     that SciPy bundles), otherwise a cyclic complex Jacobi and plain loops;
  *   - forward chain, overlap, backward chain (Propagators.jl:309-406,
  *     GRAPEState.jl:201-217);
  *   - first-order gradients of Gradients.jl:254-291,357-399 ("ref_grape") and
@@ -36,6 +40,43 @@ typedef double complex cd;
 #define IDX(r, c, D) ((r) + (size_t)(D) * (c)) /* column-major */
 
 static cd ld(const double* buf, size_t i) { return buf[2 * i] + I * buf[2 * i + 1]; }
+
+/* Optional LAPACK/BLAS backend (Fortran calling convention, column-major). */
+typedef void (*zheevr_fn)(char* jobz, char* range, char* uplo, int* n, cd* a, int* lda, double* vl,
+                          double* vu, int* il, int* iu, double* abstol, int* m, double* w, cd* z,
+                          int* ldz, int* isuppz, cd* work, int* lwork, double* rwork, int* lrwork,
+                          int* iwork, int* liwork, int* info);
+typedef void (*zgemm_fn)(char* ta, char* tb, int* m, int* n, int* k, cd* alpha, cd* a, int* lda, cd* b,
+                         int* ldb, cd* beta, cd* c, int* ldc);
+static zheevr_fn g_zheevr = NULL;
+static zgemm_fn g_zgemm = NULL;
+
+/* Hands in LAPACK zheevr and BLAS zgemm; a NULL pointer selects the built-in
+ * routine instead (the Jacobi eigensolver, plain product loops). */
+int pgx_cpu_set_lapack(void* zheevr, void* zgemm) {
+  g_zheevr = (zheevr_fn)zheevr;
+  g_zgemm = (zgemm_fn)zgemm;
+  return PGX_OK;
+}
+/* Bit 0: LAPACK zheevr in use; bit 1: BLAS zgemm in use. */
+int pgx_cpu_backend(void) { return (g_zheevr != NULL) | ((g_zgemm != NULL) << 1); }
+
+/* Per-thread LAPACK workspace sizes for an n x n zheevr (JOBZ='V', RANGE='A'):
+ * generous fixed multiples of n, above the routine's documented minima. */
+#define EV_LWORK(n) (66 * (n) + 64)
+#define EV_LRWORK(n) (24 * (n) + 64)
+#define EV_LIWORK(n) (10 * (n) + 64)
+typedef struct {
+  cd* work;
+  double* rwork;
+  int* iwork;
+  int* isuppz;
+} EvWork;
+
+static void gemm(char ta, char tb, int n, const cd* A, const cd* B, cd* C) {
+  cd one = 1.0, zero = 0.0;
+  g_zgemm(&ta, &tb, &n, &n, &n, &one, (cd*)A, &n, (cd*)B, &n, &zero, C, &n);
+}
 
 /* Cyclic complex Jacobi: A (Hermitian, column-major, destroyed) -> eigenvalues
  * w and eigenvectors V (columns). */
@@ -83,6 +124,7 @@ static void jacobi_eigh(int n, cd* A, double* w, cd* V) {
 }
 
 static void matmul(int n, const cd* A, const cd* B, cd* C) { /* C = A B */
+  if (g_zgemm) { gemm('N', 'N', n, A, B, C); return; }
   for (int c = 0; c < n; ++c) {
     for (int r = 0; r < n; ++r) C[IDX(r, c, n)] = 0.0;
     for (int k = 0; k < n; ++k) {
@@ -94,6 +136,7 @@ static void matmul(int n, const cd* A, const cd* B, cd* C) { /* C = A B */
 
 /* C = A B' */
 static void matmul_nh(int n, const cd* A, const cd* B, cd* C) {
+  if (g_zgemm) { gemm('N', 'C', n, A, B, C); return; }
   for (int c = 0; c < n; ++c) {
     for (int r = 0; r < n; ++r) C[IDX(r, c, n)] = 0.0;
     for (int k = 0; k < n; ++k) {
@@ -105,11 +148,59 @@ static void matmul_nh(int n, const cd* A, const cd* B, cd* C) {
 
 /* C = A' B */
 static void matmul_hn(int n, const cd* A, const cd* B, cd* C) {
+  if (g_zgemm) { gemm('C', 'N', n, A, B, C); return; }
   for (int c = 0; c < n; ++c)
     for (int r = 0; r < n; ++r) {
       cd s = 0.0;
       for (int k = 0; k < n; ++k) s += conj(A[IDX(k, r, n)]) * B[IDX(k, c, n)];
       C[IDX(r, c, n)] = s;
+    }
+}
+
+/* Hermitian eigendecomposition of A (column-major, destroyed): zheevr with
+ * JOBZ='V', RANGE='A', UPLO='U', ABSTOL=-1 (the call Julia's
+ * eigen(Hermitian(A)) makes), or the Jacobi sweep without the backend. */
+static int eigh(int n, cd* A, double* w, cd* V, const EvWork* ew) {
+  if (!g_zheevr) {
+    jacobi_eigh(n, A, w, V);
+    return 0;
+  }
+  char jobz = 'V', range = 'A', uplo = 'U';
+  double vl = 0.0, vu = 0.0, abstol = -1.0;
+  int il = 0, iu = 0, m = 0, info = 0;
+  int lwork = EV_LWORK(n), lrwork = EV_LRWORK(n), liwork = EV_LIWORK(n);
+  g_zheevr(&jobz, &range, &uplo, &n, A, &n, &vl, &vu, &il, &iu, &abstol, &m, w, V, &n, ew->isuppz, ew->work,
+           &lwork, ew->rwork, &lrwork, ew->iwork, &liwork, &info);
+  return info;
+}
+
+/* H <- Gamma o H with Gamma_pq = e^{-i (t_p + t_q)/2} sinc((t_p - t_q)/2),
+ * t_p = lambda_p dt: the divided differences of exp(-i t) in the eigenbasis
+ * (the spectral Frechet derivative).  The phases and half-angle sines and
+ * cosines are formed once per eigenvalue: e^{-i(t_p+t_q)/2} = h_p h_q and
+ * sin((t_p - t_q)/2) = s_p c_q - c_p s_q; below |y| = 1/4 the sinc is its
+ * Taylor series to y^10 (truncation below 1e-17), which also avoids the
+ * cancellation of the difference formula. */
+static void apply_gamma(int D, const double* lam, double dt, cd* H) {
+  cd h[64];
+  double sn[64], cs[64], t[64];
+  for (int p = 0; p < D; ++p) {
+    t[p] = lam[p] * dt;
+    sn[p] = sin(0.5 * t[p]);
+    cs[p] = cos(0.5 * t[p]);
+    h[p] = cs[p] - I * sn[p];
+  }
+  for (int c = 0; c < D; ++c)
+    for (int r = 0; r < D; ++r) {
+      const double y = 0.5 * (t[r] - t[c]);
+      double sinc;
+      if (fabs(y) < 0.25) {
+        const double y2 = y * y;
+        sinc = 1.0 + y2 * (-1.0 / 6 + y2 * (1.0 / 120 + y2 * (-1.0 / 5040 + y2 * (1.0 / 362880 - y2 / 39916800.0))));
+      } else {
+        sinc = (sn[r] * cs[c] - cs[r] * sn[c]) / y;
+      }
+      H[IDX(r, c, D)] *= h[r] * h[c] * sinc;
     }
 }
 
@@ -120,7 +211,7 @@ typedef struct {
   int exact;
 } Ctx;
 
-static double member_eval(const Ctx* X, int m, double* Gm, cd* work) {
+static double member_eval(const Ctx* X, int m, double* Gm, cd* work, const EvWork* ew, int* err) {
   const pgx_problem_desc* d = X->d;
   const int D = X->D, nc = X->nc, nt = X->nt, np = X->np;
   const size_t DD = (size_t)D * D;
@@ -147,7 +238,7 @@ static double member_eval(const Ctx* X, int m, double* Gm, cd* work) {
       H[e] = h;
     }
     cd* Vk = V + k * DD;
-    jacobi_eigh(D, H, wv, Vk);
+    if (eigh(D, H, wv, Vk, ew) != 0) *err = 1;
     const double dt = d->dt[k];
     for (int c = 0; c < D; ++c) {
       lam[(size_t)k * D + c] = wv[c];
@@ -191,13 +282,7 @@ static double member_eval(const Ctx* X, int m, double* Gm, cd* work) {
           const double dt = d->dt[k];
           matmul_hn(D, Vk, T1, T3);
           matmul(D, T3, Vk, H);
-          for (int c = 0; c < D; ++c)
-            for (int r = 0; r < D; ++r) {
-              const double tp = lam[(size_t)k * D + r] * dt, tq = lam[(size_t)k * D + c] * dt;
-              const double y = 0.5 * (tp - tq);
-              const double sinc = fabs(y) < 1e-8 ? 1.0 - y * y / 6.0 : sin(y) / y;
-              H[IDX(r, c, D)] *= cexp(-I * 0.5 * (tp + tq)) * sinc;
-            }
+          apply_gamma(D, lam + (size_t)k * D, dt, H);
           matmul(D, Vk, H, T3);
           matmul_nh(D, T3, Vk, T1);
           Xk = T1;
@@ -274,13 +359,7 @@ static double member_eval(const Ctx* X, int m, double* Gm, cd* work) {
           const double dt = d->dt[k];
           matmul_hn(D, Vk, T1, T3);
           matmul(D, T3, Vk, H);
-          for (int c = 0; c < D; ++c)
-            for (int r = 0; r < D; ++r) {
-              const double tp = lam[(size_t)k * D + r] * dt, tq = lam[(size_t)k * D + c] * dt;
-              const double y = 0.5 * (tp - tq);
-              const double sinc = fabs(y) < 1e-8 ? 1.0 - y * y / 6.0 : sin(y) / y;
-              H[IDX(r, c, D)] *= cexp(-I * 0.5 * (tp + tq)) * sinc;
-            }
+          apply_gamma(D, lam + (size_t)k * D, dt, H);
           matmul(D, Vk, H, T3);
           matmul_nh(D, T3, Vk, T1);
           for (int j = 0; j < nc; ++j) {
@@ -306,10 +385,12 @@ static size_t work_elems(int D, int nt, int np) {
 
 /* (F, G) of a pgx_problem_desc at controls u ([n_c x n_t] column-major),
  * member-parallel on n_threads OpenMP threads (<= 0: all).  G may be NULL.
- * Returns 0 on success, PGX_ERR_UNSUPPORTED for Liouvillian generators.   */
+ * Returns 0 on success, PGX_ERR_UNSUPPORTED for Liouvillian generators,
+ * PGX_ERR_INVALID when zheevr reports a failure.                           */
 int pgx_cpu_eval(const pgx_problem_desc* d, const double* u, double* F, double* G, int n_threads) {
   if (!d || !u || !F) return PGX_ERR_INVALID;
   if (d->generator != PGX_GEN_HERMITIAN) return PGX_ERR_UNSUPPORTED;
+  if (d->dim < 1 || d->dim > 64) return PGX_ERR_DIMS;
   Ctx X = {d, u, d->dim, d->n_controls, d->n_slices, d->target == PGX_TARGET_STATES ? d->n_pairs : 0,
            d->grad_mode == PGX_GRAD_EXACT};
   const int nm = d->n_members;
@@ -318,11 +399,26 @@ int pgx_cpu_eval(const pgx_problem_desc* d, const double* u, double* F, double* 
   double* Gms = G ? (double*)calloc((size_t)nm * ng, sizeof(double)) : NULL;
   const size_t we = work_elems(X.D, X.nt, X.np);
   if (n_threads <= 0) n_threads = omp_get_max_threads();
+  int err = 0;
 #pragma omp parallel num_threads(n_threads)
   {
     cd* work = (cd*)malloc(sizeof(cd) * we);
+    EvWork ew;
+    ew.work = (cd*)malloc(sizeof(cd) * EV_LWORK(X.D));
+    ew.rwork = (double*)malloc(sizeof(double) * EV_LRWORK(X.D));
+    ew.iwork = (int*)malloc(sizeof(int) * EV_LIWORK(X.D));
+    ew.isuppz = (int*)malloc(sizeof(int) * 2 * X.D);
+    int terr = 0;
 #pragma omp for schedule(static)
-    for (int m = 0; m < nm; ++m) Fm[m] = member_eval(&X, m, Gms ? Gms + (size_t)m * ng : NULL, work);
+    for (int m = 0; m < nm; ++m) Fm[m] = member_eval(&X, m, Gms ? Gms + (size_t)m * ng : NULL, work, &ew, &terr);
+    if (terr) {
+#pragma omp atomic write
+      err = 1;
+    }
+    free(ew.work);
+    free(ew.rwork);
+    free(ew.iwork);
+    free(ew.isuppz);
     free(work);
   }
   double f = 0.0;
@@ -338,7 +434,7 @@ int pgx_cpu_eval(const pgx_problem_desc* d, const double* u, double* F, double* 
   }
   free(Fm);
   free(Gms);
-  return PGX_OK;
+  return err ? PGX_ERR_INVALID : PGX_OK;
 }
 
 int pgx_cpu_max_threads(void) { return omp_get_max_threads(); }

@@ -3,11 +3,23 @@
 TEST INFRASTRUCTURE ONLY: used by the tests as a second checker and by the
 CPU-baseline leg of bench.py.  It has its own copy of the pgx_problem_desc
 layout so that the oracle does not depend on the product package.
+
+The restatement runs the reference's arithmetic stack: LAPACK zheevr (what
+Julia's ``eigen(Hermitian(H))`` calls, Propagators.jl:663) and BLAS zgemm
+(``mul!``, :673), taken from the OpenBLAS/LAPACK that SciPy bundles through
+``scipy.linalg.cython_lapack`` / ``cython_blas``.  BLAS is pinned to one
+thread per OpenMP member thread, as GRAPEState.jl:168-174 pins it with
+``BLAS.set_num_threads(1)``.  Without SciPy it falls back to its own Jacobi
+eigensolver and loops (``backend()`` says which).
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
+
+# one BLAS thread inside each member thread; read when the OpenBLAS library loads
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 import numpy as np
 
@@ -32,6 +44,30 @@ class _Desc(C.Structure):
 
 
 _LIB = None
+_LAPACK = None
+
+
+def _capsule_ptr(capsule) -> int:
+    """Function pointer held by a Cython __pyx_capi__ capsule."""
+    api = C.pythonapi
+    api.PyCapsule_GetName.restype = C.c_char_p
+    api.PyCapsule_GetName.argtypes = [C.py_object]
+    api.PyCapsule_GetPointer.restype = C.c_void_p
+    api.PyCapsule_GetPointer.argtypes = [C.py_object, C.c_char_p]
+    return api.PyCapsule_GetPointer(capsule, api.PyCapsule_GetName(capsule))
+
+
+def lapack_pointers():
+    """(zheevr, zgemm) function pointers of SciPy's bundled LAPACK/BLAS, or None."""
+    global _LAPACK
+    if _LAPACK is None:
+        try:
+            from scipy.linalg import cython_blas, cython_lapack
+            _LAPACK = (_capsule_ptr(cython_lapack.__pyx_capi__["zheevr"]),
+                       _capsule_ptr(cython_blas.__pyx_capi__["zgemm"]))
+        except (ImportError, KeyError, AttributeError):
+            _LAPACK = ()
+    return _LAPACK or None
 
 
 def lib():
@@ -42,8 +78,65 @@ def lib():
         L.pgx_cpu_eval.restype = C.c_int
         L.pgx_cpu_eval.argtypes = [C.POINTER(_Desc), _dp, _dp, _dp, C.c_int]
         L.pgx_cpu_max_threads.restype = C.c_int
+        L.pgx_cpu_set_lapack.restype = C.c_int
+        L.pgx_cpu_set_lapack.argtypes = [C.c_void_p, C.c_void_p]
+        L.pgx_cpu_backend.restype = C.c_int
+        ptrs = lapack_pointers()
+        if ptrs:
+            L.pgx_cpu_set_lapack(ptrs[0], ptrs[1])
         _LIB = L
     return _LIB
+
+
+BACKENDS = {"lapack": (True, True), "zheevr": (True, False), "zgemm": (False, True), "jacobi": (False, False)}
+BACKEND_TEXT = {"lapack": "LAPACK zheevr + BLAS zgemm", "zheevr": "LAPACK zheevr + plain product loops",
+                "zgemm": "Jacobi eigensolver + BLAS zgemm", "jacobi": "Jacobi eigensolver + plain product loops"}
+
+
+def set_backend(name: str) -> None:
+    """'lapack' (SciPy's zheevr + zgemm), 'zheevr' or 'zgemm' (one of the two,
+    built-in code for the other), or 'jacobi' (built-in Jacobi and loops)."""
+    if name not in BACKENDS:
+        raise ValueError(name)
+    ev, gm = BACKENDS[name]
+    ptrs = lapack_pointers()
+    if (ev or gm) and not ptrs:
+        raise RuntimeError("SciPy's cython_lapack / cython_blas are not available")
+    lib().pgx_cpu_set_lapack(ptrs[0] if ev else None, ptrs[1] if gm else None)
+
+
+def backend() -> str:
+    b = lib().pgx_cpu_backend()
+    return {3: "lapack", 1: "zheevr", 2: "zgemm", 0: "jacobi"}[b]
+
+
+def calibrate(prob: Problem, u, grad_mode: str, threads: int, members: int = 0) -> str:
+    """Select the fastest backend for this host and thread count.
+
+    OpenBLAS serialises concurrent small calls on its buffer-pool lock, so on
+    some hosts LAPACK + BLAS from every member thread is slower than either
+    routine alone or than the built-in code.  Each backend evaluates the same
+    sub-problem (2 members per thread, up to 50 slices) once after a warm-up;
+    the fastest stays selected (best of two timings each), and its name is
+    returned."""
+    names = [n for n in BACKENDS if n == "jacobi" or lapack_pointers()]
+    nm = min(prob.n_members, members or 4 * max(threads, 1))
+    nt = min(prob.n_t, 50)
+    sub = prob.subproblem(nm, nt)
+    best, best_t = "jacobi", float("inf")
+    for n in names:
+        set_backend(n)
+        cp = CpuProblem(sub, grad_mode)
+        cp.eval(u[:, :nt], True, threads)
+        t = float("inf")
+        for _ in range(2):
+            t0 = time.perf_counter()
+            cp.eval(u[:, :nt], True, threads)
+            t = min(t, time.perf_counter() - t0)
+        if t < best_t:
+            best, best_t = n, t
+    set_backend(best)
+    return best
 
 
 def _mat(a):

@@ -2,20 +2,22 @@
 // that may not allocate device memory.
 //
 // Some hosts cannot call cudaMalloc at the point where they need a propagator:
-// code running while a CUDA graph is being captured (an allocation there is
-// illegal or breaks the capture), real-time control loops that forbid
-// allocation after start-up, and plugin hosts whose device memory belongs to
-// their own pool allocator.  For them this entry point keeps all of its
-// working memory -- the stack of slice propagators and, for 64 x 64
-// generators, the Taylor workspace -- in one file-scope device array of fixed
-// size.  The caller passes the generators, the slice durations and the output
-// in device memory it already owns.
+// real-time control loops that forbid allocation once they have started, and
+// plugin hosts whose device memory all belongs to their own pool allocator (a
+// cudaMalloc there fails or takes memory the host has promised elsewhere).
+// For them this entry point keeps all of its working memory -- the stack of
+// slice propagators and, for 64 x 64 generators, the Taylor workspace -- in
+// one file-scope device array of fixed size.  The caller passes the
+// generators, the slice durations and the output in device memory it already
+// owns.
 //
 // Set-up: the first call on a device (with that device current) resolves the
-// array's device address with cudaGetSymbolAddress and sets the kernels'
-// shared-memory limits; make that first call before any stream capture.  Every
-// GPU that loads the library holds the array until the process exits.  All
-// calls share the array: calls whose GPU work overlaps (other streams, other
+// array's device address with cudaGetSymbolAddress, sets the kernels'
+// shared-memory limits and queries every kernel instantiation, so that under
+// lazy module loading all of them are loaded then rather than at a later
+// first launch; make that first call before any stream capture.  Every GPU
+// that loads the library holds the array until the process exits.  All calls
+// share the array: calls whose GPU work overlaps (other streams, other
 // threads) race on it and must be serialised by the caller.  Each call writes
 // every scratch element it reads before reading it, so stale contents from an
 // earlier call never reach a result and nothing needs clearing.
@@ -132,12 +134,21 @@ static DeviceSetup g_setup[64];
 template <int D>
 constexpr size_t chain_smem() { return 2 * (size_t)D * D * sizeof(double2); }
 
+// Sets the shared-memory limit of the instantiations that need more than the
+// default 48 KB and queries the attributes of both kernels of dimension D,
+// which loads their code now (lazy module loading would otherwise load it at
+// the first launch).  Return codes are checked directly, so an error the
+// caller left pending is neither taken for this call's nor cleared.
 template <int D>
-static void set_limits() {
-  if (NaCfg<D>::SMEM > 48 * 1024)
-    cudaFuncSetAttribute(k_na_expm<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NaCfg<D>::SMEM);
-  if (chain_smem<D>() > 48 * 1024)
-    cudaFuncSetAttribute(k_na_chain<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chain_smem<D>());
+static cudaError_t prepare_kernels() {
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, k_na_expm<D>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, k_na_chain<D>);
+  if (e == cudaSuccess && NaCfg<D>::SMEM > 48 * 1024)
+    e = cudaFuncSetAttribute(k_na_expm<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NaCfg<D>::SMEM);
+  if (e == cudaSuccess && chain_smem<D>() > 48 * 1024)
+    e = cudaFuncSetAttribute(k_na_chain<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chain_smem<D>());
+  return e;
 }
 
 static cudaError_t setup_current_device(double2** scratch) {
@@ -149,10 +160,12 @@ static cudaError_t setup_current_device(double2** scratch) {
   if (!g_setup[dev].done) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return e;
-    set_limits<2>(); set_limits<4>(); set_limits<8>();
-    set_limits<16>(); set_limits<32>(); set_limits<64>();
-    e = cudaGetLastError();
+    if (e == cudaSuccess) e = prepare_kernels<2>();
+    if (e == cudaSuccess) e = prepare_kernels<4>();
+    if (e == cudaSuccess) e = prepare_kernels<8>();
+    if (e == cudaSuccess) e = prepare_kernels<16>();
+    if (e == cudaSuccess) e = prepare_kernels<32>();
+    if (e == cudaSuccess) e = prepare_kernels<64>();
     if (e != cudaSuccess) return e;
     g_setup[dev].scratch = static_cast<double2*>(p);
     g_setup[dev].done = true;
@@ -170,11 +183,14 @@ static cudaError_t run(int gen, int dim, int n, const double2* G, const double* 
   int grid = (n + Cf::TPC - 1) / Cf::TPC;
   if (Cf::SLAB && grid > kSlabTeams64) grid = kSlabTeams64;
   if (grid > 4096) grid = 4096;
+  // A launch-configuration error is reported by cudaPeekAtLastError without
+  // clearing it; the arguments here are validated, so any error seen is a
+  // real failure of this call (or one the caller left pending and still owns).
   k_na_expm<D><<<grid, Cf::THREADS, Cf::SMEM, st>>>(gen, dim, n, G, dt, Ustack, slab);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaPeekAtLastError();
   if (e != cudaSuccess) return e;
   k_na_chain<D><<<1, Cf::THREADS, chain_smem<D>(), st>>>(dim, n, Ustack, Utot);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 size_t scratch_needed(int Dp, int n) {

@@ -1,5 +1,10 @@
+import os
 import sys
 from pathlib import Path
+
+# the oracle's LAPACK/BLAS calls run one BLAS thread each (also in the spawned
+# workers of oracle.parallel); OpenBLAS reads this when it loads
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 import pytest
 

@@ -1,9 +1,10 @@
 """pgx_total_propagator_noalloc, the entry point for callers that cannot
-allocate device memory (graph capture, allocation-free real-time loops, hosts
-with their own device pools).  It must give the same U_total as the regular
-entry point (pgx_total_propagator through a problem) on two calls in a row --
-the second call reuses the static scratch the first one left behind -- and
-refuse sizes beyond its static scratch with a clear error.
+allocate device memory (real-time loops that forbid allocation once started,
+hosts whose device memory all belongs to their own pool allocator).  It must
+give the same U_total as the regular entry point (pgx_total_propagator through
+a problem) and as the oracle's product of slice exponentials, on two calls in
+a row -- the second call reuses the static scratch the first one left behind --
+and refuse sizes beyond its static scratch with a clear error.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test.
@@ -12,10 +13,14 @@ import ctypes as C
 
 import numpy as np
 import pytest
+import scipy.linalg as sla
+
+from oracle import ref_semantics as rs
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12
+TOL = 1e-12         # against the regular entry point (same Taylor method)
+ORACLE_TOL = 1e-10  # against the oracle (eigendecomposition / Pade slice exponentials)
 
 
 def _rand_herm(rng, d, s=1.0):
@@ -61,6 +66,14 @@ def test_noalloc_matches_regular_entry_point_twice(pg, dim, n_t, generator):
         assert st == 0, msg
         U_ref = prob.total_propagator(u, 0)
         assert np.max(np.abs(U - U_ref)) <= TOL * max(1.0, np.max(np.abs(U_ref))), call
+        # the oracle: U_total = U_{n-1} ... U_0 with eigendecomposition (Hermitian)
+        # or Pade (Liouvillian) slice exponentials
+        if generator == "hermitian":
+            props = rs.compute_propagators(gens, dt)
+        else:
+            props = np.stack([sla.expm(gens[k] * dt[k]) for k in range(n_t)])
+        U_or = rs.compute_total_propagator(props)
+        assert np.max(np.abs(U - U_or)) <= ORACLE_TOL * max(1.0, np.max(np.abs(U_or))), call
     prob.close()
 
 

@@ -460,7 +460,7 @@ def serve_capacity(pg, ctx, *, n_jobs: int = 64, max_iter: int = 50, slots: int 
     from pulsar_gb300 import workloads as W
     jobs = W.serve_stream(seed=9, rate=1000.0, duration_s=1.0, max_slices=200, max_members=16,
                           lindblad_slices=50, lindblad_draws=4)[:n_jobs]
-    opt = dict(max_iter=max_iter, step_size=0.01, convergence_tol=0.0, gradient_norm_tol=0.0)
+    opt = dict(max_iter=max_iter, step_size=0.01, convergence_tol=1e-300, gradient_norm_tol=1e-300)
     out = {"jobs": len(jobs), "iterations_per_job": max_iter, "method": "grape",
            "job_set": "first jobs of the served stream's distribution (up to 200 slices x 16 members, "
                       "20 % Lindblad 2-3 qubits x 50 slices x 4 draws), all submitted at t = 0"}
@@ -673,9 +673,12 @@ def extra_first_order(wl, pg, ctx, torch, dev, cpu_budget_s, with_cpu: bool):
 def extra_lbfgs200(wl):
     """grape_optimize_ensemble's L-BFGS (m = 10, GRAPE.jl:1012-1230) for 200
     iterations on the device, end to end through the optimiser call (host
-    controls in, optimised controls out)."""
+    controls in, optimised controls out).  The controls are in rad/s and the
+    gradient entries ~1e-6, so the stall and gradient-norm rules are off and
+    the run takes all 200 iterations."""
     t0 = time.perf_counter()
-    o = wl.p.optimize(wl.u0, "ensemble_lbfgs", max_iter=200, lbfgs_memory=10, step_size=0.01)
+    o = wl.p.optimize(wl.u0, "ensemble_lbfgs", max_iter=200, lbfgs_memory=10, step_size=0.01,
+                      convergence_tol=1e-300, gradient_norm_tol=1e-300)
     el = time.perf_counter() - t0
     return {"wall_s": el, "iterations": o.n_iterations, "gradient_evaluations": o.n_gradient_evaluations,
             "fidelity_only_evaluations": o.n_fidelity_evaluations, "F_initial": o.fidelity_history[0],

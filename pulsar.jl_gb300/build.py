@@ -21,7 +21,7 @@ BUILD = ROOT / "_build"
 LIB = PKG / "libpulsar_gb300.so"
 
 SOURCES = ["pgx_kernels.cu", "pgx_mixed.cu", "pgx_runtime.cu", "pgx_optimize.cu", "pgx_batch.cu",
-           "pgx_noalloc.cu", "pgx_server.cu", "pgx_stack.cu", "pgx_lbfgs.cu", "pgx_penalty.cu",
+           "pgx_noalloc.cu", "pgx_server.cu", "pgx_stack.cu", "pgx_lbfgs.cu", "pgx_penalty.cu", "pgx_tc.cu",
            "pgx_checkpoint.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]

@@ -257,15 +257,22 @@ int pgx_penalty_eval(pgx_ctx* ctx, int32_t n_controls, int32_t n_slices, const d
  * kernels at controls u, `reps` launches each, keeps the fastest for this
  * problem and writes a one-line report (nullable).  Variants only re-map work
  * to threads; every dot product is summed in the same order, so results are
- * bit-identical whatever is chosen.  The FP64 path has no variants.         */
+ * bit-identical whatever is chosen.  The FP64 path has no variants.  The
+ * D = 64 gradient of gate targets with the exact gradient has one candidate,
+ * the tensor-core engine (PGX_TEAM_TENSOR).                                 */
 int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report, size_t report_len);
 /* Sets the team sizes directly (a plan kept from an earlier pgx_autotune);
  * 0 = the built-in default.  Values the dimension does not admit are refused
  * with PGX_ERR_INVALID.  Kernel indices: 0 = mixed expm, 1 = mixed gradient.
  * Admitted by padded dimension: 32 (<= 8); 32, 64, 128, 256 (16); 128, 256
- * (32); 256 (64), plus 512 for the gradient at 64.                          */
+ * (32); 256 (64), plus 512 for the gradient at 64.  For the gradient at 64
+ * of gate targets with the exact gradient, PGX_TEAM_TENSOR (1) selects the
+ * tensor-core engine: 3xTF32 tcgen05 products, FP32-class like the CUDA-core
+ * teams but not bit-identical to them; it is that case's default.  The
+ * CUDA-core teams 256 and 512 stay admitted there for comparisons.         */
 #define PGX_TUNE_EXPM 0
 #define PGX_TUNE_GRAD 1
+#define PGX_TEAM_TENSOR 1
 int pgx_problem_set_team(pgx_problem* prob, int32_t kernel, int32_t team);
 int pgx_problem_get_team(const pgx_problem* prob, int32_t kernel, int32_t* team);
 /* Plans: pgx_autotune records its choice process-wide under (device, padded
@@ -307,10 +314,14 @@ int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slice
  * C_i = P_i Q_i (i < n; each matrix column-major interleaved re/im, FP64 on the
  * host, rounded to FP32) through the tensor-core (tcgen05) product engine that
  * the D = 64 mixed gradient uses: 3xTF32 with FP32 accumulation (passes = 3)
- * or plain TF32 (passes = 1).  Synchronous, on the current device; allocates
- * its own device buffers.  PGX_ERR_TIMEOUT when an MMA-completion wait gave
- * up.  For tests and profiling of the engine alone.                          */
-int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes);
+ * or plain TF32 (passes = 1), the left factor as an expanded operand in
+ * shared memory (mode 0) or in tensor memory (mode 1); or 3xFP16 with the
+ * left factor in tensor memory (mode 2, passes = 3: the gradient's path).
+ * Synchronous, on the current device; allocates its own device buffers.
+ * PGX_ERR_TIMEOUT when an MMA-completion wait gave up.  For tests and
+ * profiling of the engine alone.                                             */
+int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes,
+                          int32_t mode);
 
 /* ---- drift ramps ----------------------------------------------------------- */
 /* Robust drift trajectories (sample_drift_trajectories, RobustOpt.jl:168-182;

@@ -173,8 +173,18 @@ void set_smem_once(const void* fn, size_t bytes);
 // Team sizes the mixed slice-parallel kernel `kernel` (kTune*) admits at
 // padded dimension Dp (writes up to 4 values, returns the count), and the
 // default choice.
-int mixed_variants(int Dp, int kernel, int* out);
-int mixed_default_team(int Dp, int kernel);
+// Team values of the tunable mixed kernels: candidates the autotuner times,
+// values pgx_problem_set_team admits, and the default.  kTeamTensor (1)
+// selects the tensor-core engine of the D = 64 gate-target exact gradient.
+constexpr int kTeamTensor = 1;
+bool grad_tc_eligible(const ProbDev& p);
+int mixed_variants(const ProbDev& p, int kernel, int* out);
+int mixed_admitted(const ProbDev& p, int kernel, int* out);
+int mixed_default_team(const ProbDev& p, int kernel);
+// Error bits of the tensor-core gradient since the last call (the flag is
+// cleared): 1 = an MMA-completion wait gave up, 2 = a value beyond the FP16
+// operand limit; 0 = none, -1 = the flag cannot be read.
+int grad_tc_check();
 
 // Stage launchers (pgx_kernels.cu).  Each returns cudaGetLastError() after
 // launching on li.stream.

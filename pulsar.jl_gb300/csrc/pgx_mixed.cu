@@ -1081,6 +1081,13 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
   }
 }
 
+}  // namespace pgx
+
+// the D = 64 tensor-core gradient (uses choose_degree_q2 and the tables above)
+#include "pgx_grad_tc.cuh"
+
+namespace pgx {
+
 // ---- launchers ---------------------------------------------------------------------
 template <class K>
 static void ensure_smem_mx(K kernel, size_t bytes) {
@@ -1113,7 +1120,14 @@ static int grid_for(K kernel, int threads, size_t smem, long teams, int tpc, int
 // Team sizes each D admits (register budget of the blocked df products).  The
 // D = 64 gradient also runs as one 512-thread team per SM: its six FP32
 // matrices fill shared memory, so more threads per team is the only way to
-// more warps.
+// more warps.  For gate targets with the exact gradient the D = 64 gradient
+// has a third form, the tensor-core engine (kTeamTensor): the default and the
+// only one the autotuner times (its products are 3xTF32, not bit-identical
+// to the CUDA-core teams, and several times faster); the CUDA-core teams stay
+// selectable with pgx_problem_set_team.
+bool grad_tc_eligible(const ProbDev& p) {
+  return p.Dp == 64 && p.target == TGT_GATE && p.grad_mode == GRAD_EXACT;
+}
 static int variants_for(int Dp, int kernel, int* out) {
   int n = 0;
   if (Dp <= 8) out[n++] = 32;
@@ -1125,13 +1139,26 @@ static int variants_for(int Dp, int kernel, int* out) {
   }
   return n;
 }
-int mixed_variants(int Dp, int kernel, int* out) { return variants_for(Dp, kernel, out); }
+int mixed_variants(const ProbDev& p, int kernel, int* out) {
+  if (kernel == kTuneGradMx && grad_tc_eligible(p)) {
+    out[0] = kTeamTensor;
+    return 1;
+  }
+  return variants_for(p.Dp, kernel, out);
+}
+int mixed_admitted(const ProbDev& p, int kernel, int* out) {
+  int n = variants_for(p.Dp, kernel, out);
+  if (kernel == kTuneGradMx && grad_tc_eligible(p)) out[n++] = kTeamTensor;
+  return n;
+}
 // Defaults (problems that were never tuned: batches, served jobs) are the
 // autotuner's usual choice on GB300 at each dimension.
-int mixed_default_team(int Dp, int kernel) {
+int mixed_default_team(const ProbDev& p, int kernel) {
+  const int Dp = p.Dp;
   if (Dp <= 8) return 32;
   if (Dp == 16) return kernel == kTuneExpmMx ? 128 : 32;
   if (Dp == 32) return kernel == kTuneExpmMx ? 256 : 128;
+  if (kernel == kTuneGradMx && grad_tc_eligible(p)) return kTeamTensor;
   return kernel == kTuneExpmMx ? 256 : 512;
 }
 
@@ -1172,7 +1199,7 @@ static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchIn
   return cudaGetLastError();
 }
 cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  const int t = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p.Dp, kTuneExpmMx);
+  const int t = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p, kTuneExpmMx);
   PGX_DISPATCH_MX_T(p.Dp, t, return (do_expm_mx<D_, T_>(p, w, li)));
   return cudaSuccess;
 }
@@ -1309,8 +1336,32 @@ cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
   return cudaGetLastError();
 }
 
+static cudaError_t do_grad_tc64(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  const size_t smem = 2 * tc::kBBytesF16 + 4 * gtc::kMatBytes + tc::kSmemAlign;
+  ensure_smem_mx(k_grad_tc64, smem);
+  const long items = (long)p.n_members * p.n_t;
+  const int grid = items < li.num_sms ? (int)items : li.num_sms;  // one CTA per SM: TMEM and shared memory
+  k_grad_tc64<<<grid, tc::kThreads, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+
+int grad_tc_check() {
+  int flag = 0;
+  if (cudaMemcpyFromSymbol(&flag, g_grad_tc_timeout, sizeof(int)) != cudaSuccess) return -1;
+  if (flag) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_grad_tc_timeout, &zero, sizeof(int));
+  }
+  return flag;
+}
+
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  const int t = li.team[kTuneGradMx] ? li.team[kTuneGradMx] : mixed_default_team(p.Dp, kTuneGradMx);
+  const int t = li.team[kTuneGradMx] ? li.team[kTuneGradMx] : mixed_default_team(p, kTuneGradMx);
+  if (t == kTeamTensor) {
+    if (!grad_tc_eligible(p)) return cudaErrorInvalidValue;
+    return do_grad_tc64(p, w, li);
+  }
   if (p.Dp == 64 && t == 512) return do_grad_mx<64, 512>(p, w, li);
   PGX_DISPATCH_MX_T(p.Dp, t, return (do_grad_mx<D_, T_>(p, w, li)));
   return cudaSuccess;

@@ -850,7 +850,7 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
   for (int kern = 0; kern < pgx::kNumTunable; ++kern) {
     if (kern == pgx::kTuneGradMx && p->desc.grad_mode != PGX_GRAD_EXACT) continue;
     int vs[4];
-    const int nv = pgx::mixed_variants(p->Dp, kern, vs);
+    const int nv = pgx::mixed_variants(p->pd, kern, vs);
     double best_ms = 1e300;
     int best = vs[0];
     rep += std::string(rep.empty() ? "" : " | ") + names[kern] + "<" + std::to_string(p->Dp) + ">:";
@@ -890,7 +890,7 @@ extern "C" int pgx_problem_set_team(pgx_problem* p, int32_t kernel, int32_t team
   if (!p || kernel < 0 || kernel >= pgx::kNumTunable) return PGX_ERR_INVALID;
   if (team != 0) {
     int vs[4];
-    const int nv = pgx::mixed_variants(p->Dp, kernel, vs);
+    const int nv = pgx::mixed_admitted(p->pd, kernel, vs);
     if (std::find(vs, vs + nv, team) == vs + nv)
       return ctx_fail(p->ctx, PGX_ERR_INVALID, "team size not admitted at this dimension");
   }
@@ -901,7 +901,7 @@ extern "C" int pgx_problem_set_team(pgx_problem* p, int32_t kernel, int32_t team
 
 extern "C" int pgx_problem_get_team(const pgx_problem* p, int32_t kernel, int32_t* team) {
   if (!p || !team || kernel < 0 || kernel >= pgx::kNumTunable) return PGX_ERR_INVALID;
-  *team = p->team[kernel] ? p->team[kernel] : pgx::mixed_default_team(p->Dp, kernel);
+  *team = p->team[kernel] ? p->team[kernel] : pgx::mixed_default_team(p->pd, kernel);
   return PGX_OK;
 }
 
@@ -1015,6 +1015,13 @@ int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_st
     return st;
   if ((st = ctx_cuda(c, cudaEventRecord(c->ev1, c->stream), "event"))) return st;
   if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "eval sync"))) return st;
+  if (G && p->desc.precision == PGX_PREC_MIXED && pgx::grad_tc_eligible(p->pd)) {
+    const int tcf = pgx::grad_tc_check();
+    if (tcf & 2)
+      return ctx_fail(c, PGX_ERR_NONFINITE, "tensor-core gradient: an operand exceeded the FP16 range (select the "
+                                            "CUDA-core gradient team with pgx_problem_set_team)");
+    if (tcf != 0) return ctx_fail(c, PGX_ERR_TIMEOUT, "tensor-core gradient: an MMA-completion wait gave up");
+  }
   if (G) std::memcpy(G, hG, n * sizeof(double));
   if (F) *F = *hF;
   if (stats) {

@@ -11,13 +11,16 @@
 namespace pgx {
 namespace tc {
 
-// One persistent CTA per SM.  Per item: P and Q are loaded into TMEM in the
-// stacked layout (columns 0..63 and 64..127), read back and staged as the A
-// and B operands, multiplied into columns 128..191 and written out.  The TMEM
-// round trip is the path the gradient takes for every product.
+// One persistent CTA per SM.  Per item: Q is loaded into TMEM in the stacked
+// layout (columns 64..127), read back and staged as the B operand; P is
+// loaded into TMEM (columns 0..63) and staged as the expanded A operand in
+// shared memory, or (a_tmem) copied into shared memory compact and expanded
+// into TMEM columns 256..511.  The product lands in columns 128..191 and is
+// written out.  mode 2 runs the 3xFP16 form (fp16 parts, A in TMEM), the
+// gradient's path; passes is then 3.
 __global__ void __launch_bounds__(kThreads, 1)
 k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* __restrict__ C, int n, int passes,
-           int* err) {
+           int a_tmem, int* err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint32_t s_tmem;
   __shared__ __align__(8) uint64_t s_bar;
@@ -44,6 +47,10 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
     const float* Pf = reinterpret_cast<const float*>(P + (size_t)it * 4096);
     const float* Qf = reinterpret_cast<const float*>(Q + (size_t)it * 4096);
     float v[32];
+    if (a_tmem) {
+      float2* Pc = reinterpret_cast<float2*>(a_hi);  // compact copy of P
+      for (int e = threadIdx.x; e < 4096; e += kThreads) Pc[e] = P[(size_t)it * 4096 + e];
+    }
 #pragma unroll
     for (int c = 0; c < 32; ++c) v[c] = Pf[2 * (l.i + 64 * (l.c0 + c)) + l.im];
     tmem_st32(my + 0, v);
@@ -54,16 +61,35 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    tmem_ld32(my + 0, v);
-    stage_A(a_hi, a_lo, l, v);
+    if (a_tmem == 2) {
+      __syncthreads();  // the compact copy of P is complete
+      stage_A_tmem_f16(tmem + l.lane_addr + 256, tmem + l.lane_addr + 256 + kAColsF16,
+                       reinterpret_cast<const float2*>(a_hi), l.L, l.c0 / 32);
+      tmem_st_wait();
+    } else if (a_tmem) {
+      __syncthreads();  // the compact copy of P is complete
+      stage_A_tmem(tmem + l.lane_addr + 256, tmem + l.lane_addr + 384, reinterpret_cast<const float2*>(a_hi), l.L,
+                   l.c0 / 32);
+      tmem_st_wait();
+    } else {
+      tmem_ld32(my + 0, v);
+      stage_A(a_hi, a_lo, l, v);
+    }
     tmem_ld32(my + 64, v);
-    stage_B(b_hi, b_lo, l, v);
+    if (a_tmem == 2) stage_B_f16(b_hi, b_hi + kBBytesF16, l, v);
+    else stage_B(b_hi, b_lo, l, v);
     fence_smem_to_async();
     fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0) {
       fence_after_sync();
-      issue_product(tmem + 128, smem_u32(a_hi), smem_u32(a_lo), smem_u32(b_hi), smem_u32(b_lo), 0, mbar, passes);
+      if (a_tmem == 2)
+        issue_product_f16(tmem + 128, tmem + 256, tmem + 256 + kAColsF16, smem_u32(b_hi),
+                          smem_u32(b_hi + kBBytesF16), 0, mbar);
+      else if (a_tmem)
+        issue_product_ta(tmem + 128, tmem + 256, tmem + 384, smem_u32(b_hi), smem_u32(b_lo), 0, mbar, passes);
+      else
+        issue_product(tmem + 128, smem_u32(a_hi), smem_u32(a_lo), smem_u32(b_hi), smem_u32(b_lo), 0, mbar, passes);
     }
     if (!mbar_wait(mbar, phase)) s_abort = 1;
     phase ^= 1;
@@ -93,9 +119,11 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
 }  // namespace tc
 }  // namespace pgx
 
-extern "C" int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes) {
+extern "C" int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes,
+                                     int32_t mode) {
   using namespace pgx::tc;
-  if (!P || !Q || !C || n < 1 || (passes != 1 && passes != 3)) return PGX_ERR_INVALID;
+  if (!P || !Q || !C || n < 1 || (passes != 1 && passes != 3) || mode < 0 || mode > 2 || (mode == 2 && passes != 3))
+    return PGX_ERR_INVALID;
   const size_t elems = (size_t)n * 4096;
   std::vector<float> hP(2 * elems), hQ(2 * elems), hC(2 * elems);
   for (size_t e = 0; e < 2 * elems; ++e) {
@@ -120,7 +148,7 @@ extern "C" int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C
     e = cudaFuncSetAttribute(k_tc_cmm64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) {
     const int grid = n < sms ? n : sms;
-    k_tc_cmm64<<<grid, kThreads, smem>>>(dP, dQ, dC, n, passes, dErr);
+    k_tc_cmm64<<<grid, kThreads, smem>>>(dP, dQ, dC, n, passes, mode, dErr);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();

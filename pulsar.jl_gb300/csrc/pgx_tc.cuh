@@ -27,6 +27,7 @@
 // 64-column matrix.  One elected thread issues the MMAs; completion is tracked
 // by an mbarrier that all threads wait on with a clock bound.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -221,6 +222,59 @@ __device__ __forceinline__ void stage_B(uint8_t* b_hi, uint8_t* b_lo, const Lane
   }
 }
 
+// tcgen05.mma with the A operand in tensor memory: A (M = 128 rows, one
+// per lane; K = 8 tf32 values in 8 consecutive 32-bit columns from a_tmem).
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}"
+      ::"r"(d_tmem), "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+// Expanded left operand in TMEM: 128 lanes x 128 columns per part (hi at
+// a_hi, lo at a_lo = a_hi + 128).  Thread (lane L, column half h) writes
+// columns 64 h .. 64 h + 63 of its lane from the compact complex matrix P
+// (64 x 64 float2, column-major, anywhere in shared memory):
+//   lane i < 64:  [Pr | -Pi],   lane 64 + i:  [Pi | Pr]   (row i).
+__device__ __forceinline__ void stage_A_tmem(uint32_t a_hi_lane, uint32_t a_lo_lane, const float2* P, int L,
+                                             int h) {
+  const int i = L & 63, im = L >> 6;
+  const bool take_im = (h == 0) ? (im == 1) : (im == 0);  // h = 0: own part; h = 1: the other part
+  const float sg = (h == 1 && im == 0) ? -1.f : 1.f;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float hv[32], lv[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const float2 e = P[i + 64 * (32 * half + c)];
+      const float x = sg * (take_im ? e.y : e.x);
+      hv[c] = tf32_hi(x);
+      lv[c] = x - hv[c];
+    }
+    tmem_st32(a_hi_lane + (uint32_t)(64 * h + 32 * half), hv);
+    tmem_st32(a_lo_lane + (uint32_t)(64 * h + 32 * half), lv);
+  }
+}
+
+// One elected thread: D = (accumulate ? D : 0) + A B in 3xTF32 with A in TMEM
+// (hi at a_hi, lo at a_lo: 128 columns each) and B in shared memory.
+__device__ __forceinline__ void issue_product_ta(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                                 uint32_t b_lo, uint32_t accumulate, uint32_t mbar, int passes = 3) {
+  const uint32_t pa[3] = {a_lo, a_hi, a_hi};
+  const uint32_t pb[3] = {b_hi, b_lo, b_hi};
+  uint32_t acc = accumulate;
+  for (int ps = 3 - passes; ps < 3; ++ps) {
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const uint64_t db = make_desc(pb[ps] + (uint32_t)((t >> 2) * (64 * 128) + (t & 3) * 32));
+      mma_tf32_ta(d_tmem, pa[ps] + (uint32_t)(8 * t), db, acc);
+      acc = 1;
+    }
+  }
+  commit(mbar);
+}
+
 // One elected thread: D (64 TMEM columns at d_tmem) = (accumulate ? D : 0) +
 // A B in 3xTF32 (passes = 3: lo*hi, hi*lo, hi*hi) or plain TF32 (passes = 1),
 // K = 128 in 16 steps of 8; then commits the group to the mbarrier.
@@ -235,6 +289,103 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t a_hi, ui
       const uint64_t da = make_desc(pa[ps] + (uint32_t)((t >> 2) * (128 * 128) + (t & 3) * 32));
       const uint64_t db = make_desc(pb[ps] + (uint32_t)((t >> 2) * (64 * 128) + (t & 3) * 32));
       mma_tf32(d_tmem, da, db, acc);
+      acc = 1;
+    }
+  }
+  commit(mbar);
+}
+
+// ---- 3xFP16 variant: the same products with fp16 operand parts -------------
+// FP16 has TF32's 11-bit significand, and kind::f16 MMAs take K = 16 per
+// instruction at the same issue cost (measured on GB300: an M = 128, N = 64
+// MMA takes 48 cycles in either kind), so a product needs half the
+// instructions and half the staging bytes.  Its exponent range is narrow:
+// callers keep every staged value below kF16Limit in magnitude (the gradient
+// scales the derivative family by a power of two per unit); values whose lo
+// part falls below FP16's normal range keep an absolute error of 2^-25.
+constexpr uint32_t kIdescF16 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);  // F32 += F16 x F16
+constexpr uint32_t kBBytesF16 = 64u * 128u * 2u;  // one part of B: 64 n-rows x 128 k fp16
+constexpr uint32_t kAColsF16 = 64;                // TMEM columns of one part of the expanded A (2 fp16 each)
+constexpr float kF16Limit = 32768.f;
+
+// Byte offset of fp16 element (row, k) in a K-major, 128-byte-swizzled tile
+// (64 values per 128-byte row, k blocks of 64).
+__device__ __forceinline__ uint32_t sw128_off16(int row, int k, int rows) {
+  const int blk = k >> 6, kk = k & 63;
+  return (uint32_t)(blk * rows * 128 + (row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 3) ^ (row & 7)) << 4) +
+                    ((kk & 7) << 1));
+}
+
+// x = hi + lo to about 2^-22 relative: hi = fp16(x), lo = fp16(x - hi).
+// Returns false when x is beyond kF16Limit.
+__device__ __forceinline__ bool split_f16(float x, __half& hi, __half& lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
+  return fabsf(x) < kF16Limit;
+}
+
+// As stage_B: this thread's 32 values into the right operand [Qr; Qi] (k = l.L,
+// n = c0..c0+31), hi and lo fp16 parts.  Returns false if a value is out of range.
+__device__ __forceinline__ bool stage_B_f16(uint8_t* b_hi, uint8_t* b_lo, const Lane& l, const float (&v)[32]) {
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const uint32_t off = sw128_off16(l.c0 + c, l.L, 64);
+    __half h, o;
+    ok &= split_f16(v[c], h, o);
+    *reinterpret_cast<__half*>(b_hi + off) = h;
+    *reinterpret_cast<__half*>(b_lo + off) = o;
+  }
+  return ok;
+}
+
+// As stage_A_tmem with fp16 parts: TMEM columns hold two consecutive k
+// values each (the lower k in the low half), so one part of the expanded
+// operand is 128 lanes x 64 columns; thread (L, h) writes columns
+// 32 h .. 32 h + 31 (k = 64 h .. 64 h + 63).  Returns false if out of range.
+__device__ __forceinline__ bool stage_A_tmem_f16(uint32_t a_hi_lane, uint32_t a_lo_lane, const float2* P, int L,
+                                                 int h) {
+  const int i = L & 63, im = L >> 6;
+  const bool take_im = (h == 0) ? (im == 1) : (im == 0);
+  const float sg = (h == 1 && im == 0) ? -1.f : 1.f;
+  float hv[32], lv[32];
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const float2 e0 = P[i + 64 * (2 * c)], e1 = P[i + 64 * (2 * c + 1)];
+    __half h0, l0, h1, l1;
+    ok &= split_f16(sg * (take_im ? e0.y : e0.x), h0, l0);
+    ok &= split_f16(sg * (take_im ? e1.y : e1.x), h1, l1);
+    hv[c] = __uint_as_float((uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16));
+    lv[c] = __uint_as_float((uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16));
+  }
+  tmem_st32(a_hi_lane + (uint32_t)(32 * h), hv);
+  tmem_st32(a_lo_lane + (uint32_t)(32 * h), lv);
+  return ok;
+}
+
+__device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+      ::"r"(d_tmem), "r"(a_tmem), "l"(b), "r"(kIdescF16), "r"(accumulate)
+      : "memory");
+}
+
+// One elected thread: D = (accumulate ? D : 0) + A B in 3xFP16 (lo*hi, hi*lo,
+// hi*hi), A in TMEM (kAColsF16 columns per part), B in shared memory, K = 128
+// in 8 steps of 16; then commits the group to the mbarrier.
+__device__ __forceinline__ void issue_product_f16(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                                  uint32_t b_lo, uint32_t accumulate, uint32_t mbar) {
+  const uint32_t pa[3] = {a_lo, a_hi, a_hi};
+  const uint32_t pb[3] = {b_hi, b_lo, b_hi};
+  uint32_t acc = accumulate;
+#pragma unroll
+  for (int ps = 0; ps < 3; ++ps) {
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const uint64_t db = make_desc(pb[ps] + (uint32_t)((t >> 2) * (64 * 128) + (t & 3) * 32));
+      mma_f16_ta(d_tmem, pa[ps] + (uint32_t)(8 * t), db, acc);
       acc = 1;
     }
   }

@@ -14,16 +14,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _cmm(pg, P, Q, passes):
+def _cmm(pg, P, Q, passes, a_in_tmem=0):
     A = pg._abi
     n = P.shape[0]
     f = A.lib().pgx_diag_tc_cmatmul64
     f.restype = C.c_int
-    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     buf = lambda M: np.ascontiguousarray(np.swapaxes(M, -1, -2)).astype(np.complex128)  # column-major
     Pb, Qb = buf(P), buf(Q)
     Cb = np.zeros_like(Pb)
-    st = f(Pb.ctypes.data, Qb.ctypes.data, Cb.ctypes.data, n, passes)
+    st = f(Pb.ctypes.data, Qb.ctypes.data, Cb.ctypes.data, n, passes, a_in_tmem)
     assert st == 0, st
     return np.swapaxes(Cb, -1, -2)
 
@@ -32,7 +32,9 @@ def _rel(Cg, Cr):
     return np.max(np.abs(Cg - Cr), axis=(1, 2)) / np.max(np.abs(Cr), axis=(1, 2))
 
 
-def test_tc_cmatmul64_3xtf32_is_fp32_accurate(pg):
+@pytest.mark.parametrize("a_in_tmem", [0, 1])
+def test_tc_cmatmul64_3xtf32_is_fp32_accurate(pg, a_in_tmem):
+    """modes 0 and 1: 3xTF32 with the left factor in shared memory / in TMEM"""
     rng = np.random.default_rng(64)
     n = 300
     P = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
@@ -44,20 +46,106 @@ def test_tc_cmatmul64_3xtf32_is_fp32_accurate(pg):
     P32 = P.astype(np.complex64).astype(np.complex128)
     Q32 = Q.astype(np.complex64).astype(np.complex128)
     ref = P32 @ Q32
-    C3 = _cmm(pg, P, Q, 3)
+    C3 = _cmm(pg, P, Q, 3, a_in_tmem)
     e3 = _rel(C3, ref)
     assert np.all(np.isfinite(C3))
     assert e3.max() <= 5e-6, e3.max()
-    C1 = _cmm(pg, P, Q, 1)
+    C1 = _cmm(pg, P, Q, 1, a_in_tmem)
     e1 = _rel(C1, ref)
     assert 1e-5 <= np.median(e1) <= 2e-2, np.median(e1)
     print(f"3xTF32 max rel {e3.max():.2e}, TF32 median rel {np.median(e1):.2e}")
 
 
+def test_tc_cmatmul64_3xfp16_is_fp32_accurate(pg):
+    """mode 2, the gradient's path: 3xFP16 with the left factor in TMEM"""
+    rng = np.random.default_rng(65)
+    n = 300
+    P = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    Q = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    P[:8] = np.eye(64) + 0.01 * P[:8]
+    Q[:8] = np.eye(64) + 0.03 * Q[:8]
+    P32 = P.astype(np.complex64).astype(np.complex128)
+    Q32 = Q.astype(np.complex64).astype(np.complex128)
+    ref = P32 @ Q32
+    C3 = _cmm(pg, P, Q, 3, 2)
+    e3 = _rel(C3, ref)
+    assert np.all(np.isfinite(C3))
+    assert e3.max() <= 5e-6, e3.max()
+    print(f"3xFP16 max rel {e3.max():.2e}")
+
+
 def test_tc_cmatmul64_rejects_bad_arguments(pg):
     f = pg._abi.lib().pgx_diag_tc_cmatmul64
     f.restype = C.c_int
-    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     buf = np.zeros(2 * 4096)
-    assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 2) == 1
-    assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 0, 3) == 1
+    assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 2, 0) == 1
+    assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 0, 3, 0) == 1
+    assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 1, 2) == 1
+
+
+# ---- the D = 64 exact gradient on the tensor-core engine -------------------
+
+from oracle import members as mb  # noqa: E402
+import fx  # noqa: E402
+from test_parity_gpu import random_gate_problem, to_gpu  # noqa: E402
+
+G_RTOL_MIXED = 1e-4     # the mixed path's gradient bar against the FP64 oracle
+G_RTOL_ENGINES = 2e-5   # tensor-core (3xTF32) against CUDA-core (FP32) gradients
+
+
+def _rel_g(G, Go):
+    return np.max(np.abs(G - Go)) / np.max(np.abs(Go))
+
+
+def test_tc_gradient_lindblad_vs_cuda_core_and_oracle(pg):
+    prob, u0 = fx.lindblad_3q(n_t=40, n_draws=4)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    assert p.teams[1] == 1                      # the tensor-core engine is the default here
+    F_tc, G_tc = p.eval(u0)
+    p.set_teams(0, 512)                         # the CUDA-core FP32 team
+    F_cc, G_cc = p.eval(u0)
+    p.close()
+    assert F_tc == F_cc                         # F does not depend on the gradient kernel
+    assert _rel_g(G_tc, G_cc) <= G_RTOL_ENGINES, _rel_g(G_tc, G_cc)
+    Fo, Go = mb.eval_gate_exact_adjoint(prob, u0)
+    assert abs(F_tc - Fo) <= 1e-8
+    assert _rel_g(G_tc, Go) <= G_RTOL_MIXED, _rel_g(G_tc, Go)
+    print(f"lindblad D=64: tc vs cuda-core {_rel_g(G_tc, G_cc):.2e}, tc vs oracle {_rel_g(G_tc, Go):.2e}, "
+          f"cuda-core vs oracle {_rel_g(G_cc, Go):.2e}")
+
+
+@pytest.mark.parametrize("d", [40, 64])
+def test_tc_gradient_hermitian_padded_vs_oracle(pg, d):
+    rng = np.random.default_rng(900 + d)
+    prob, u0 = random_gate_problem(rng, d, n_t=10, n_members=3, dt=0.3 / np.sqrt(d))
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    assert p.teams[1] == 1
+    F, G = p.eval(u0)
+    p.close()
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    assert abs(F - Fo) <= 1e-8
+    assert _rel_g(G, Go) <= G_RTOL_MIXED, _rel_g(G, Go)
+
+
+def test_tc_gradient_runs_twice_bit_identically(pg):
+    """Persistent CTAs reuse TMEM, the staging buffers and the barrier phase
+    across units and launches: a second evaluation reproduces the first."""
+    prob, u0 = fx.lindblad_3q(n_t=200, n_draws=2)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F1, G1 = p.eval(u0)
+    F2, G2 = p.eval(u0)
+    p.close()
+    assert F1 == F2 and np.array_equal(G1, G2)
+
+
+def test_state_targets_at_64_keep_the_cuda_core_gradient(pg):
+    rng = np.random.default_rng(77)
+    prob, u0 = random_gate_problem(rng, 40, n_t=6, n_members=2, dt=0.05)
+    kw = dict(generator=prob.generator, target="states", fidelity="square",
+              states_init=np.eye(40)[:2], states_target=np.eye(40)[2:4], grad_mode="exact", precision="mixed")
+    p = pg.Problem(prob.drifts, prob.controls, prob.dt, **kw)
+    assert p.teams[1] == 512
+    with pytest.raises(pg._abi.PgxError):
+        p.set_teams(0, 1)                        # not admitted for state targets
+    p.close()

@@ -62,7 +62,8 @@ struct ProbDev {
 // Device work buffers of one evaluation.
 struct WorkDev {
   double2* U;       // [n_members][n_t][Dp*Dp] slice propagators
-  double2* P;       // gate: [n_members][n_t][Dp*Dp] forward chain, then M_k
+  double2* P;       // gate: [n_members][n_t][Dp*Dp] forward chain, then M_k (then, for the
+                    // tensor-core gradient, L(A_k, M_k))
   double2* Utot;    // [n_members][Dp*Dp]
   double2* psi;     // states: [n_members][n_t+1][n_pairs][Dp]
   double2* lam;     // states: [n_members][n_t+1][n_pairs][Dp]

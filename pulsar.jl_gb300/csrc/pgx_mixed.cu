@@ -1337,11 +1337,19 @@ cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo&
 }
 
 static cudaError_t do_grad_tc64(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  const size_t smem = 2 * tc::kBBytesF16 + 4 * gtc::kMatBytes + tc::kSmemAlign;
+  const size_t smem = 4 * tc::kBBytesF16 + 3 * gtc::kMatBytes + gtc::kMkBytes + tc::kSmemAlign;
   ensure_smem_mx(k_grad_tc64, smem);
   const long items = (long)p.n_members * p.n_t;
   const int grid = items < li.num_sms ? (int)items : li.num_sms;  // one CTA per SM: TMEM and shared memory
   k_grad_tc64<<<grid, tc::kThreads, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int nj = p.n_c < kTraceCtrls ? p.n_c : kTraceCtrls;
+  const size_t tsmem = (size_t)nj * 64 * 64 * sizeof(float2);
+  ensure_smem_mx(k_trace_tc64, tsmem);
+  const long tgrid = (items + 7) / 8;
+  k_trace_tc64<<<tgrid < li.num_sms ? (int)tgrid : li.num_sms, 256, tsmem, li.stream>>>(p, w);
   ++*li.launches;
   return cudaGetLastError();
 }

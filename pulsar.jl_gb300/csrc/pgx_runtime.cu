@@ -854,6 +854,12 @@ extern "C" int pgx_autotune(pgx_problem* p, const double* u, int32_t reps, char*
     double best_ms = 1e300;
     int best = vs[0];
     rep += std::string(rep.empty() ? "" : " | ") + names[kern] + "<" + std::to_string(p->Dp) + ">:";
+    if (nv == 1) {  // nothing to choose (and the tensor-core gradient consumes its input in place)
+      rep += " T=" + std::to_string(best) + " (single candidate) -> T=" + std::to_string(best);
+      p->team[kern] = best;
+      ++p->generation;
+      continue;
+    }
     for (int i = 0; i < nv; ++i) {
       pgx::LaunchInfo li = p->launch_info();
       li.team[kern] = vs[i];

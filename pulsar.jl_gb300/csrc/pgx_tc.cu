@@ -47,7 +47,14 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
     const float* Pf = reinterpret_cast<const float*>(P + (size_t)it * 4096);
     const float* Qf = reinterpret_cast<const float*>(Q + (size_t)it * 4096);
     float v[32];
-    if (a_tmem) {
+    if (a_tmem == 2) {  // planar, row-padded compact copy of P
+      float* Pc = reinterpret_cast<float*>(a_hi);
+      for (int e = threadIdx.x; e < 4096; e += kThreads) {
+        const float2 x = P[(size_t)it * 4096 + e];  // column-major: row e % 64, column e / 64
+        Pc[(e % 64) * kLdp + e / 64] = x.x;
+        Pc[kPlaneFloats + (e % 64) * kLdp + e / 64] = x.y;
+      }
+    } else if (a_tmem) {
       float2* Pc = reinterpret_cast<float2*>(a_hi);  // compact copy of P
       for (int e = threadIdx.x; e < 4096; e += kThreads) Pc[e] = P[(size_t)it * 4096 + e];
     }
@@ -64,7 +71,7 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
     if (a_tmem == 2) {
       __syncthreads();  // the compact copy of P is complete
       stage_A_tmem_f16(tmem + l.lane_addr + 256, tmem + l.lane_addr + 256 + kAColsF16,
-                       reinterpret_cast<const float2*>(a_hi), l.L, l.c0 / 32);
+                       reinterpret_cast<const float*>(a_hi), l.L, l.c0 / 32);
       tmem_st_wait();
     } else if (a_tmem) {
       __syncthreads();  // the compact copy of P is complete

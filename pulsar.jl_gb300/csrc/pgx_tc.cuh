@@ -115,6 +115,16 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// TMA bulk copy (cp.async.bulk) of `bytes` (a multiple of 16, both addresses
+// 16-byte aligned) from global to this CTA's shared memory, completing on
+// `mbar`, whose expected transaction count the same thread raises first.
+__device__ __forceinline__ void tma_bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
 // Waits for the barrier phase `parity` to complete, at most kWaitCycles.
 // Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
@@ -303,17 +313,29 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t a_hi, ui
 // callers keep every staged value below kF16Limit in magnitude (the gradient
 // scales the derivative family by a power of two per unit); values whose lo
 // part falls below FP16's normal range keep an absolute error of 2^-25.
-constexpr uint32_t kIdescF16 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);  // F32 += F16 x F16
+// F32 += F16 x F16, A K-major (from TMEM), B MN-major (bit 16)
+constexpr uint32_t kIdescF16 = (1u << 4) | (1u << 16) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr uint32_t kBBytesF16 = 64u * 128u * 2u;  // one part of B: 64 n-rows x 128 k fp16
 constexpr uint32_t kAColsF16 = 64;                // TMEM columns of one part of the expanded A (2 fp16 each)
 constexpr float kF16Limit = 32768.f;
 
-// Byte offset of fp16 element (row, k) in a K-major, 128-byte-swizzled tile
-// (64 values per 128-byte row, k blocks of 64).
-__device__ __forceinline__ uint32_t sw128_off16(int row, int k, int rows) {
-  const int blk = k >> 6, kk = k & 63;
-  return (uint32_t)(blk * rows * 128 + (row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 3) ^ (row & 7)) << 4) +
-                    ((kk & 7) << 1));
+// Byte offset of fp16 element (k, n) of the right operand in an MN-major,
+// 128-byte-swizzled tile: one 128-byte row of 64 n values per k, 8-row
+// groups of 1024 bytes along k, the 16-byte chunks of a row XOR-permuted by
+// k mod 8.  An MMA step (K = 16) reads two groups: 2048 bytes.
+__device__ __forceinline__ uint32_t sw128_mn16(int k, int n) {
+  return (uint32_t)((k >> 3) * 1024 + (k & 7) * 128 + (((n >> 3) ^ (k & 7)) << 4) + ((n & 7) << 1));
+}
+// Descriptor of an MN-major 128-byte-swizzled tile: the 8-row groups along K
+// are 1024 bytes apart; N = 64 fits one swizzle atom, so the atom stride along
+// N is never used (both byte offsets are set to 1024).
+__device__ __forceinline__ uint64_t make_desc_mn(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(1024u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
 }
 
 // x = hi + lo to about 2^-22 relative: hi = fp16(x), lo = fp16(x - hi).
@@ -324,40 +346,65 @@ __device__ __forceinline__ bool split_f16(float x, __half& hi, __half& lo) {
   return fabsf(x) < kF16Limit;
 }
 
+// Two values at once: hi = fp16x2(x), lo = fp16x2(x - hi), packed as the MMA
+// reads them (the first value in the low half).  Returns false when a value
+// is beyond kF16Limit.
+__device__ __forceinline__ bool split_f16x2(float x0, float x1, uint32_t& hw, uint32_t& lw) {
+  const __half2 h = __floats2half2_rn(x0, x1);
+  const float2 hf = __half22float2(h);
+  const __half2 o = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+  hw = *reinterpret_cast<const uint32_t*>(&h);
+  lw = *reinterpret_cast<const uint32_t*>(&o);
+  return fmaxf(fabsf(x0), fabsf(x1)) < kF16Limit;
+}
+
 // As stage_B: this thread's 32 values into the right operand [Qr; Qi] (k = l.L,
-// n = c0..c0+31), hi and lo fp16 parts.  Returns false if a value is out of range.
+// n = c0..c0+31), hi and lo fp16 parts, MN-major: eight consecutive n per
+// 16-byte store.  Returns false if a value is out of range.
 __device__ __forceinline__ bool stage_B_f16(uint8_t* b_hi, uint8_t* b_lo, const Lane& l, const float (&v)[32]) {
   bool ok = true;
 #pragma unroll
-  for (int c = 0; c < 32; ++c) {
-    const uint32_t off = sw128_off16(l.c0 + c, l.L, 64);
-    __half h, o;
-    ok &= split_f16(v[c], h, o);
-    *reinterpret_cast<__half*>(b_hi + off) = h;
-    *reinterpret_cast<__half*>(b_lo + off) = o;
+  for (int j = 0; j < 4; ++j) {
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) ok &= split_f16x2(v[8 * j + 2 * e], v[8 * j + 2 * e + 1], hw[e], lw[e]);
+    const uint32_t off = sw128_mn16(l.L, l.c0 + 8 * j);
+    *reinterpret_cast<uint4*>(b_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(b_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
   return ok;
 }
 
-// As stage_A_tmem with fp16 parts: TMEM columns hold two consecutive k
-// values each (the lower k in the low half), so one part of the expanded
-// operand is 128 lanes x 64 columns; thread (L, h) writes columns
-// 32 h .. 32 h + 31 (k = 64 h .. 64 h + 63).  Returns false if out of range.
-__device__ __forceinline__ bool stage_A_tmem_f16(uint32_t a_hi_lane, uint32_t a_lo_lane, const float2* P, int L,
+// Compact complex 64 x 64 matrices in shared memory as two row-major planes
+// (real, then imaginary) with rows padded to kLdp floats: a warp's 16-byte
+// row accesses (lanes = consecutive rows) fall in distinct banks.
+constexpr int kLdp = 68;
+constexpr uint32_t kPlaneFloats = 64u * kLdp;
+
+// As stage_A_tmem with fp16 parts, from a planar compact matrix P: TMEM
+// columns hold two consecutive k values each (the lower k in the low half),
+// so one part of the expanded operand is 128 lanes x 64 columns; thread
+// (L, h) writes columns 32 h .. 32 h + 31 (k = 64 h .. 64 h + 63): row i of
+// one plane, read as 16-byte vectors.  Returns false if out of range.
+__device__ __forceinline__ bool stage_A_tmem_f16(uint32_t a_hi_lane, uint32_t a_lo_lane, const float* P, int L,
                                                  int h) {
   const int i = L & 63, im = L >> 6;
   const bool take_im = (h == 0) ? (im == 1) : (im == 0);
   const float sg = (h == 1 && im == 0) ? -1.f : 1.f;
+  const float4* row = reinterpret_cast<const float4*>(P + (take_im ? kPlaneFloats : 0u) + (uint32_t)i * kLdp);
   float hv[32], lv[32];
   bool ok = true;
 #pragma unroll
-  for (int c = 0; c < 32; ++c) {
-    const float2 e0 = P[i + 64 * (2 * c)], e1 = P[i + 64 * (2 * c + 1)];
-    __half h0, l0, h1, l1;
-    ok &= split_f16(sg * (take_im ? e0.y : e0.x), h0, l0);
-    ok &= split_f16(sg * (take_im ? e1.y : e1.x), h1, l1);
-    hv[c] = __uint_as_float((uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16));
-    lv[c] = __uint_as_float((uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16));
+  for (int q = 0; q < 16; ++q) {
+    const float4 r = row[q];
+    const float x[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      uint32_t hw, lw;
+      ok &= split_f16x2(sg * x[2 * e], sg * x[2 * e + 1], hw, lw);
+      hv[2 * q + e] = __uint_as_float(hw);
+      lv[2 * q + e] = __uint_as_float(lw);
+    }
   }
   tmem_st32(a_hi_lane + (uint32_t)(32 * h), hv);
   tmem_st32(a_lo_lane + (uint32_t)(32 * h), lv);
@@ -373,8 +420,25 @@ __device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uin
 }
 
 // One elected thread: D = (accumulate ? D : 0) + A B in 3xFP16 (lo*hi, hi*lo,
-// hi*hi), A in TMEM (kAColsF16 columns per part), B in shared memory, K = 128
-// in 8 steps of 16; then commits the group to the mbarrier.
+// hi*hi), A in TMEM (kAColsF16 columns per part), B MN-major in shared
+// memory, K = 128 in 8 steps of 16.  Not committed: several products are
+// issued back to back and committed together.
+__device__ __forceinline__ void mma_product_f16(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                                uint32_t b_lo, uint32_t accumulate) {
+  const uint32_t pa[3] = {a_lo, a_hi, a_hi};
+  const uint32_t pb[3] = {b_hi, b_lo, b_hi};
+  uint32_t acc = accumulate;
+#pragma unroll
+  for (int ps = 0; ps < 3; ++ps) {
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      mma_f16_ta(d_tmem, pa[ps] + (uint32_t)(8 * t), make_desc_mn(pb[ps] + (uint32_t)(2048 * t)), acc);
+      acc = 1;
+    }
+  }
+}
+
+// As mma_product_f16, then commits the group to the mbarrier.
 __device__ __forceinline__ void issue_product_f16(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
                                                   uint32_t b_lo, uint32_t accumulate, uint32_t mbar) {
   const uint32_t pa[3] = {a_lo, a_hi, a_hi};
@@ -384,7 +448,7 @@ __device__ __forceinline__ void issue_product_f16(uint32_t d_tmem, uint32_t a_hi
   for (int ps = 0; ps < 3; ++ps) {
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
-      const uint64_t db = make_desc(pb[ps] + (uint32_t)((t >> 2) * (64 * 128) + (t & 3) * 32));
+      const uint64_t db = make_desc_mn(pb[ps] + (uint32_t)(2048 * t));
       mma_f16_ta(d_tmem, pa[ps] + (uint32_t)(8 * t), db, acc);
       acc = 1;
     }

@@ -214,6 +214,10 @@ cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Launch
 cudaError_t launch_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool skip_local = false);
 cudaError_t launch_chain_bwd_local_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
+// FP64 re-unitarisation of U_total after the mixed forward chain (Hermitian
+// gate problems; a no-op otherwise): z, f and kappa from the refined U.
+bool refine_applies(const ProbDev& p);
+cudaError_t launch_refine_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 // u -> w.u_df (df pairs), the first stage of a mixed evaluation.
 cudaError_t launch_prep_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li);
 // Global slab size (in double2 elements) the Dp = 64 path needs.

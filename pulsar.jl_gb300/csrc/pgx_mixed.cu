@@ -336,6 +336,55 @@ __device__ __forceinline__ void chain_epilogue_mx(const Team<T>& tm, const ProbD
   }
 }
 
+// FP64 refinement of the chained propagator (Hermitian gate problems).  The
+// df chain leaves U_total unitary to about 1e-13; one Newton-Schulz step of
+// the polar decomposition, U' = U (3I - U'U) / 2, projects it back onto the
+// unitary matrices (its non-unitary error goes from e to O(e^2)), all in FP64.
+// The overlap z = Tr(T'U')/D, f and the chain-rule coefficient are then
+// recomputed from U', so F and the gradient's costate seed both use the
+// refined propagator.  U_total itself stays as the chain produced it: the
+// oracle-free residual ||U'U - I|| of pgx_eval_stats reports the defect the
+// refinement removed.  One CTA per member; sums in a fixed order.
+constexpr int kRefThreads = 256;
+template <int D>
+__global__ void __launch_bounds__(kRefThreads) k_refine_unitary_mx(ProbDev p, WorkDev w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* U = reinterpret_cast<double2*>(smem_raw);
+  double2* S = U + D * D;
+  double2* red = S + D * D;
+  const int m = blockIdx.x;
+  const Team<kRefThreads> tm{(int)threadIdx.x};
+  const double2* Ut = w.Utot + (size_t)m * D * D;
+  for (int e = threadIdx.x; e < D * D; e += kRefThreads) U[e] = Ut[e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < D * D; e += kRefThreads) {  // S = (3I - U'U) / 2
+    const int r = e % D, c = e / D;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = 0; k < D; ++k) acc = cmac_cj(acc, U[k + D * r], U[k + D * c]);
+    S[e] = make_double2(0.5 * ((r == c ? 3.0 : 0.0) - acc.x), -0.5 * acc.y);
+  }
+  __syncthreads();
+  double2 z = make_double2(0.0, 0.0);
+  for (int e = threadIdx.x; e < D * D; e += kRefThreads) {  // z = sum conj(T) (U S)
+    const int r = e % D, c = e / D;
+    double2 v = make_double2(0.0, 0.0);
+    for (int k = 0; k < D; ++k) v = cmac(v, U[r + D * k], S[k + D * c]);
+    z = cmac_cj(z, p.target_op[e], v);
+  }
+  z = team_sum<kRefThreads>(tm, z, red);
+  if (threadIdx.x == 0) {
+    z.x /= p.D;
+    z.y /= p.D;
+    double f;
+    double2 kap;
+    fid_kappa(z, p.fid, p.grad_mode, f, kap);
+    const double sc = p.m_weight[m] / p.D;
+    w.z[m] = z;
+    w.kap[m] = make_double2(kap.x * sc, kap.y * sc);
+    w.Fm[m] = f;
+  }
+}
+
 // Parallel in time (members with few teams each would leave SMs idle): the
 // slices of member m fall into pit_blocks blocks of pit_len.
 //   local   per (m, b): local prefixes Q_i = U_{k0+i-1} ... U_{k0} in df,
@@ -1362,6 +1411,21 @@ int grad_tc_check() {
     cudaMemcpyToSymbol(g_grad_tc_timeout, &zero, sizeof(int));
   }
   return flag;
+}
+
+template <int D>
+static cudaError_t do_refine_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  const size_t smem = (2 * (size_t)D * D + kRefThreads) * sizeof(double2);
+  ensure_smem_mx(k_refine_unitary_mx<D>, smem);
+  k_refine_unitary_mx<D><<<p.n_members, kRefThreads, smem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+bool refine_applies(const ProbDev& p) { return p.gen == GEN_HERM && p.target == TGT_GATE; }
+cudaError_t launch_refine_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  if (!refine_applies(p)) return cudaSuccess;
+  PGX_DISPATCH_MX(p.Dp, return (do_refine_mx<D_>(p, w, li)));
+  return cudaSuccess;
 }
 
 cudaError_t launch_grad_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {

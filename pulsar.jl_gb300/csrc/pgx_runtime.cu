@@ -778,6 +778,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
         return st;
     }
     if ((st = ctx_cuda(c, pgx::launch_chain_fwd_mx(p->pd, w, li, want_grad), "chain_fwd_mx"))) return st;
+    if ((st = ctx_cuda(c, pgx::launch_refine_mx(p->pd, w, li), "refine_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_BWD);
     if (fork && (st = ctx_cuda(c, cudaStreamWaitEvent(li.stream, p->ev_join, 0), "join"))) return st;
     if (want_grad && (st = ctx_cuda(c, pgx::launch_chain_bwd_mx(p->pd, w, li, fork), "chain_bwd_mx"))) return st;

@@ -179,6 +179,8 @@ void set_smem_once(const void* fn, size_t bytes);
 // selects the tensor-core engine of the D = 64 gate-target exact gradient.
 constexpr int kTeamTensor = 1;
 bool grad_tc_eligible(const ProbDev& p);
+// The D = 64 gate chains' fix-up products run on the tensor cores as well.
+bool tc_kernels_used(const ProbDev& p);
 int mixed_variants(const ProbDev& p, int kernel, int* out);
 int mixed_admitted(const ProbDev& p, int kernel, int* out);
 int mixed_default_team(const ProbDev& p, int kernel);

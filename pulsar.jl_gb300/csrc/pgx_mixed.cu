@@ -1134,6 +1134,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
 
 // the D = 64 tensor-core gradient (uses choose_degree_q2 and the tables above)
 #include "pgx_grad_tc.cuh"
+#include "pgx_fix_tc.cuh"
 
 namespace pgx {
 
@@ -1293,6 +1294,14 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   combine<<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
   *li.launches += 2;
   if (store && p.n_t > w.pit_len) {
+    if constexpr (D == 64) {  // tensor cores (pgx_fix_tc.cuh)
+      const size_t smem = 2 * tc::kBBytes + 3 * D * D * sizeof(float2) + tc::kSmemAlign;
+      ensure_smem_mx(k_fix_tc64<0>, smem);
+      const long items = (long)p.n_members * (p.n_t - w.pit_len);
+      k_fix_tc64<0><<<items < li.num_sms ? (int)items : li.num_sms, tc::kThreads, smem, li.stream>>>(p, w);
+      ++*li.launches;
+      return cudaGetLastError();
+    }
     using F = FixCfg<D>;
     const size_t smem_f = (size_t)F::TPC * 2 * Lay<D, 2>::SIZE * sizeof(float2);
     ensure_smem_mx(k_chainf_fix_mx<D>, smem_f);
@@ -1348,6 +1357,14 @@ static cudaError_t do_chain_bwd_mx(const ProbDev& p, const WorkDev& w, const Lau
   const size_t smem_c = (size_t)G::TPC * D * D * sizeof(float2);
   ensure_smem_mx(k_chainb_combine_mx<D>, smem_c);
   k_chainb_combine_mx<D><<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w);
+  if constexpr (D == 64) {  // tensor cores (pgx_fix_tc.cuh)
+    const size_t smem = 2 * tc::kBBytes + 3 * D * D * sizeof(float2) + tc::kSmemAlign;
+    ensure_smem_mx(k_fix_tc64<1>, smem);
+    const long items = (long)p.n_members * p.n_t;
+    k_fix_tc64<1><<<items < li.num_sms ? (int)items : li.num_sms, tc::kThreads, smem, li.stream>>>(p, w);
+    *li.launches += 2;
+    return cudaGetLastError();
+  }
   using F = FixCfg<D>;
   const size_t smem_f = (size_t)F::TPC * 3 * Lay<D, 2>::SIZE * sizeof(float2);
   ensure_smem_mx(k_chainb_fix_mx<D>, smem_f);
@@ -1422,6 +1439,7 @@ static cudaError_t do_refine_mx(const ProbDev& p, const WorkDev& w, const Launch
   return cudaGetLastError();
 }
 bool refine_applies(const ProbDev& p) { return p.gen == GEN_HERM && p.target == TGT_GATE; }
+bool tc_kernels_used(const ProbDev& p) { return p.Dp == 64 && p.target == TGT_GATE; }
 cudaError_t launch_refine_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   if (!refine_applies(p)) return cudaSuccess;
   PGX_DISPATCH_MX(p.Dp, return (do_refine_mx<D_>(p, w, li)));

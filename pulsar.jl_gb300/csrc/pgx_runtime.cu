@@ -1022,12 +1022,12 @@ int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_st
     return st;
   if ((st = ctx_cuda(c, cudaEventRecord(c->ev1, c->stream), "event"))) return st;
   if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "eval sync"))) return st;
-  if (G && p->desc.precision == PGX_PREC_MIXED && pgx::grad_tc_eligible(p->pd)) {
+  if (G && p->desc.precision == PGX_PREC_MIXED && pgx::tc_kernels_used(p->pd)) {
     const int tcf = pgx::grad_tc_check();
     if (tcf & 2)
       return ctx_fail(c, PGX_ERR_NONFINITE, "tensor-core gradient: an operand exceeded the FP16 range (select the "
                                             "CUDA-core gradient team with pgx_problem_set_team)");
-    if (tcf != 0) return ctx_fail(c, PGX_ERR_TIMEOUT, "tensor-core gradient: an MMA-completion wait gave up");
+    if (tcf != 0) return ctx_fail(c, PGX_ERR_TIMEOUT, "tensor-core kernel: a completion wait gave up");
   }
   if (G) std::memcpy(G, hG, n * sizeof(double));
   if (F) *F = *hF;

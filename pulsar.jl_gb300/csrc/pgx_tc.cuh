@@ -125,6 +125,18 @@ __device__ __forceinline__ void tma_bulk_g2s(uint32_t dst, const void* src, uint
                : "memory");
 }
 
+// The same in two steps, for several copies completing on one barrier: the
+// issuing thread arms the barrier once with the total byte count, then issues
+// each copy.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
 // Waits for the barrier phase `parity` to complete, at most kWaitCycles.
 // Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {

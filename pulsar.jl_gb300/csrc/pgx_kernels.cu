@@ -20,6 +20,7 @@
 // polynomial in A with scalar coefficients, so ONE Frechet derivative per
 // slice serves all n_c controls.
 #include <mutex>
+#include <map>
 #include <set>
 #include <utility>
 
@@ -668,17 +669,23 @@ static void ensure_smem(K kernel, size_t bytes) {
   set_smem_once((const void*)kernel, bytes);
 }
 
-// The dynamic shared-memory limit is set once per kernel and device, so that
-// launches recorded into a CUDA graph never need to change function attributes.
+// The dynamic shared-memory limit of a kernel on a device only grows: it is
+// raised when a launch needs more than any earlier one (kernels whose shared
+// memory depends on the problem -- state pairs, control counts -- meet larger
+// needs later), and never lowered, so launches already recorded into a CUDA
+// graph stay valid.
 void set_smem_once(const void* fn, size_t bytes) {
   if (bytes <= 48 * 1024) return;
   static std::mutex mu;
-  static std::set<std::pair<const void*, int>> done;
+  static std::map<std::pair<const void*, int>, size_t> limit;
   int dev = 0;
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lk(mu);
-  if (done.insert({fn, dev}).second)
+  size_t& cur = limit[{fn, dev}];
+  if (bytes > cur) {
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cur = bytes;
+  }
 }
 
 template <class K>

@@ -304,7 +304,13 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
     }
     taylor_exp_df<D, T, kSwzExpm, HERM, LSYM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
     float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
-    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
+    if constexpr (G::SLAB) {
+      // the U stack streams out (gigabytes, read back from DRAM by the
+      // chains): evict-first stores keep the per-CTA Taylor slab in L2
+      for (int e = tm.lane; e < D * D; e += T) __stcs(out + e, Y[L::idx(e % D, e / D)]);
+    } else {
+      for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
+    }
     tm.sync();
   }
 }

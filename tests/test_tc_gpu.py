@@ -149,3 +149,26 @@ def test_state_targets_at_64_keep_the_cuda_core_gradient(pg):
     with pytest.raises(pg._abi.PgxError):
         p.set_teams(0, 1)                        # not admitted for state targets
     p.close()
+
+
+def test_kernel_shared_memory_limits_grow_with_later_problems():
+    """A fresh process evaluates a D = 64 problem with 2 controls, then one with
+    6: kernels whose shared memory depends on the problem (the trace pass
+    holds the controls) must accept the larger launch after the smaller one."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    code = (
+        "import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+        "import numpy as np, __graft_entry__ as ge\n"
+        "pg = ge.load_package()\n"
+        "import fx\n"
+        "from test_parity_gpu import random_gate_problem, to_gpu\n"
+        "prob, u0 = random_gate_problem(np.random.default_rng(1), 40, n_t=4, n_members=2, dt=0.05)\n"
+        "p = to_gpu(pg, prob, 'exact', precision='mixed'); p.eval(u0); p.close()\n"
+        "prob, u0 = fx.lindblad_3q(n_t=4, n_draws=2)\n"
+        "p = to_gpu(pg, prob, 'exact', precision='mixed'); F, G = p.eval(u0); p.close()\n"
+        "assert np.all(np.isfinite(G)); print('ok')\n" % (str(root), str(root / "tests")))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]

@@ -1008,10 +1008,19 @@ void worker_loop(pgx_server* s) {
       s->done_cv.notify_all();
     }
     if (!progress) {
-      // new submissions wake the loop at once; device progress is polled
-      std::unique_lock<std::mutex> lk(s->mu);
-      s->cv.wait_for(lk, std::chrono::microseconds(20),
-                     [&] { return s->stop || (!s->queue.empty() && !s->free_slots.empty()); });
+      // Device progress is polled.  While any job is on the device the loop
+      // only yields between sweeps: a timed sleep here (with the kernel's
+      // timer slack) would add its wake-up latency to every step of every
+      // small job.  With nothing in flight it sleeps until a submission.
+      bool any_inflight = false;
+      for (const auto& j : s->running) any_inflight |= j->inflight;
+      if (any_inflight) {
+        std::this_thread::yield();
+      } else {
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->cv.wait_for(lk, std::chrono::microseconds(200),
+                       [&] { return s->stop || (!s->queue.empty() && !s->free_slots.empty()); });
+      }
     }
   }
 }

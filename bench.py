@@ -76,9 +76,9 @@ TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
            ("spin4", "mixed", "expm"): 5 * (0.095232e6 + 127.364352e6),
            ("spin4", "mixed", "grad"): 5 * (94.700544e6 + 2.850816e6),
            ("spin4", "mixed", "chain_fwd"): 5 * (189.268736e6 + 67.549952e6),
-           # k_expm_mx<64,256,LSym>, 100-slice capture: the per-team slab's L2
+           # k_expm_mx<64,256,LSym>, 100-slice capture: the per-CTA slabs' L2
            # write-backs come on top of the 210 MB U stack
-           ("lindblad3q", "mixed", "expm"): 5 * (70.671360e6 + 1.058322e9)}
+           ("lindblad3q", "mixed", "expm"): 5 * (46.415360e6 + 964.345600e6)}
 # FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
 # accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
 # busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).

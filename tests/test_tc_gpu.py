@@ -172,3 +172,26 @@ def test_kernel_shared_memory_limits_grow_with_later_problems():
         "assert np.all(np.isfinite(G)); print('ok')\n" % (str(root), str(root / "tests")))
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
+
+
+def test_tc_gradient_refuses_values_beyond_fp16_range(pg):
+    """A (non-physical) D = 64 Liouvillian that grows by e^24 per slice drives
+    the squarings past the FP16 operand limit (the last squaring's factor
+    exp(A/2) reaches e^12 ~ 1.6e5 > 32768; F ~ e^48 and G stay finite in FP32
+    and FP64): the tensor-core gradient
+    reports PGX_ERR_NONFINITE instead of returning a wrong gradient, and the
+    CUDA-core team evaluates the same problem."""
+    D = 64
+    rng = np.random.default_rng(3)
+    drift = 24.0 * np.eye(D, dtype=complex)
+    ctrl = 0.01 * (rng.standard_normal((1, D, D)) + 1j * rng.standard_normal((1, D, D)))
+    kw = dict(generator="liouvillian", target="gate", target_op=np.eye(D), grad_mode="exact", precision="mixed")
+    p = pg.Problem(drift[None], ctrl, np.array([1.0]), **kw)
+    assert p.teams[1] == 1
+    with pytest.raises(pg._abi.PgxError) as ei:
+        p.eval(np.zeros((1, 1)))
+    assert ei.value.status == 10          # PGX_ERR_NONFINITE
+    p.set_teams(0, 512)                   # the CUDA-core FP32 gradient
+    F, G = p.eval(np.zeros((1, 1)))
+    assert np.isfinite(F) and np.all(np.isfinite(G))
+    p.close()

@@ -322,6 +322,17 @@ int pgx_total_propagator_noalloc(int32_t dim, int32_t generator, int32_t n_slice
  * profiling of the engine alone.                                             */
 int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes,
                           int32_t mode);
+/* The same batched products in df (double-float, ~48-bit) arithmetic, the
+ * precision of the mixed expm: engine 0 = the CUDA-core df product of the
+ * D = 64 expm (FP32 pipe); engine 1 = the tensor-core form, each operand cut
+ * into six exact 8-bit bf16 slices whose 21 slice pairs of levels 0..5 are
+ * accumulated exactly in FP32 TMEM and summed in df; engine 2 = the same
+ * with level 6 (26 pairs).  Inputs are rounded to df from FP64.  The kernel
+ * runs reps times after one warm-up launch; *ms (may be NULL) receives the
+ * mean time per launch.  PGX_ERR_TIMEOUT when an MMA-completion wait gave
+ * up.                                                                          */
+int pgx_diag_dfcmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t engine, int32_t reps,
+                         float* ms);
 
 /* ---- drift ramps ----------------------------------------------------------- */
 /* Robust drift trajectories (sample_drift_trajectories, RobustOpt.jl:168-182;

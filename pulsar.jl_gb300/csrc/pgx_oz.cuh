@@ -1,0 +1,200 @@
+// df-class complex 64 x 64 products on the tcgen05 tensor cores by exact
+// integer slicing (the Ozaki scheme, with bf16 slices and FP32 accumulation).
+//
+// A df operand (hi + lo, ~48 significant bits) is scaled by a power of two 2^e
+// so that every entry lies in [-1/2, 1/2], then cut into six slices of 8 bits:
+//     x = 2^e sum_i s_i 2^(-8 (i + 1)),   s_i integers,
+//     |s_0|, |s_1|, |s_2|, |s_4|, |s_5| <= 128,   |s_3| <= 256.
+// s_0..s_2 come from hi alone; lo joins the remainder before s_3 (one FP32
+// rounding at 2^-49 of the scale).  Every slice is exact in bf16 (8
+// significant bits).
+//
+// A complex product is the real MMA [Cr; Ci] = [Pr -Pi; Pi Pr] [Qr; Qi]
+// (M = 128, N = 64, K = 128).  With S_i, T_j the slices of the two real
+// operands,
+//     C = 2^(eA + eB) sum_l 2^(-8 (l + 2)) L_l,   L_l = sum_{i + j = l} S_i T_j.
+// Each level L_l is accumulated in its own FP32 TMEM accumulator.  Slice
+// products are integers, and with K = 128 the bounds above keep every level's
+// partial sums at most 2^24 in magnitude (level 5: 2 pairs with s_3 at 2^22
+// plus 4 pairs at 2^21), so the FP32 accumulation is exact.  Levels 0..5 take
+// 21 slice pairs; level 6 (5 more pairs, also exact) is optional.  The levels
+// are summed in df on the CUDA cores, smallest first.  What is dropped (levels
+// beyond the last, the slicing remainder) stays below 2^-44 of K max|A| max|B|
+// in the worst case of aligned signs.
+//
+// Measured on GB300: an M = 128, N = 64 MMA takes 48 cycles, so the 21 pairs
+// (168 MMAs of K = 16) of one product take ~8,100 cycles of one SM's tensor
+// pipe, against ~48,000 FP32-pipe cycles for the same product in df
+// arithmetic (~23 FP32 instructions per complex multiply-add).
+//
+// Layouts (128-byte swizzle, 1024-byte aligned tiles):
+//   - the expanded left operand of one slice, K-major: 128 rows x 128 k bf16,
+//     two 64-k column blocks of 16 KB (the 3xTF32 engine's byte layout, with
+//     64 bf16 instead of 32 tf32 per 128-byte row);
+//   - the right operand of one slice, MN-major: 128 k x 64 n bf16 (the 3xFP16
+//     engine's layout).
+#pragma once
+#include <cuda_bf16.h>
+
+#include "pgx_df.cuh"
+#include "pgx_tc.cuh"
+
+namespace pgx {
+namespace oz {
+
+using tc::Lane;
+
+constexpr int kSlices = 6;
+constexpr uint32_t kASlice = 128u * 128u * 2u;  // 32 KB
+constexpr uint32_t kBSlice = 128u * 64u * 2u;   // 16 KB
+// F32 += BF16 x BF16: D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 =
+// 1), A K-major, B MN-major (bit 16), N = 64, M = 128.
+constexpr uint32_t kIdescBF16 =
+    (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+// Byte offset of bf16 element (row, k) of a K-major, 128-byte-swizzled tile of
+// 128 rows: k blocks of 64 values (128 rows x 128 bytes each), 8-row groups at
+// 1024 bytes, the 16-byte chunks of a row XOR-permuted by the row mod 8.
+__device__ __forceinline__ uint32_t sw128_k16(int row, int k) {
+  const int blk = k >> 6, kk = k & 63;
+  return (uint32_t)(blk * 16384 + (row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 3) ^ (row & 7)) << 4) +
+                    ((kk & 7) << 1));
+}
+
+// The exponent e of the operand scale: the smallest power of two with
+// 2^e >= 2 max|x| (entries of x 2^-e then lie in [-1/2, 1/2]; lo adds at most
+// a relative 2^-24, which the rounding of slice 0 absorbs).  0 for a zero
+// operand.
+__device__ __forceinline__ int scale_exp(float maxabs) {
+  if (!(maxabs > 0.f)) return 0;
+  int ex;
+  frexpf(maxabs, &ex);  // maxabs = f 2^ex, f in [1/2, 1)
+  return ex + 1;
+}
+
+// Slice i of a scaled df value: h holds the remainder (hi's part, from slice 3
+// on with lo joined), l the scaled lo.  Returns s_i and advances h.
+__device__ __forceinline__ float next_slice(float& h, float l, int i) {
+  if (i == 3) h = fmaf(l, 16777216.f, h);  // lo in units of slice 2's remainder (2^-24)
+  const float s = rintf(h * 256.f);
+  h = fmaf(h, 256.f, -s);  // exact: s is the integer nearest to 256 h
+  return s;
+}
+
+// 32 slice values of this thread (row l.i of the real or imaginary part,
+// columns c0..c0+31) into the expanded left operand: its own row and the
+// partner row of [Pr -Pi; Pi Pr], 16-byte stores.
+__device__ __forceinline__ void stage_A(uint8_t* a, const Lane& l, const float (&s)[32]) {
+  const int r1 = l.im ? 64 + l.i : l.i;
+  const int r2 = l.im ? l.i : 64 + l.i;
+  const float sg = l.im ? -1.f : 1.f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t w1[4], w2[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 p = __floats2bfloat162_rn(s[8 * q + 2 * e], s[8 * q + 2 * e + 1]);
+      const __nv_bfloat162 m = __floats2bfloat162_rn(sg * s[8 * q + 2 * e], sg * s[8 * q + 2 * e + 1]);
+      w1[e] = *reinterpret_cast<const uint32_t*>(&p);
+      w2[e] = *reinterpret_cast<const uint32_t*>(&m);
+    }
+    *reinterpret_cast<uint4*>(a + sw128_k16(r1, l.c0 + 8 * q)) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    *reinterpret_cast<uint4*>(a + sw128_k16(r2, 64 + l.c0 + 8 * q)) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+  }
+}
+
+// 32 slice values of this thread (k = l.L, n = c0..c0+31) into the right
+// operand, MN-major.
+__device__ __forceinline__ void stage_B(uint8_t* b, const Lane& l, const float (&s)[32]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 p = __floats2bfloat162_rn(s[8 * q + 2 * e], s[8 * q + 2 * e + 1]);
+      w[e] = *reinterpret_cast<const uint32_t*>(&p);
+    }
+    *reinterpret_cast<uint4*>(b + tc::sw128_mn16(l.L, l.c0 + 8 * q)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(d_tmem), "l"(a), "l"(b), "r"(kIdescBF16), "r"(accumulate)
+      : "memory");
+}
+
+// One elected thread: the slice pairs (i, j) of left slice I (in shared
+// memory at a) with every right slice j (at b + j kBSlice) whose level I + j
+// is below LEVELS, each into the level's accumulator (64 TMEM columns at
+// acc + 64 (I + j)); the first pair of a level overwrites it.  Straight-line
+// code: the descriptors of the K steps are the base descriptors plus
+// immediate offsets (a start address below 256 KB keeps the 14-bit address
+// field from carrying), so the single issuing thread keeps ahead of the
+// tensor pipe.
+template <int LEVELS, int I>
+__device__ __forceinline__ void issue_slice_i(uint32_t acc, uint64_t da0, uint64_t db0) {
+#pragma unroll
+  for (int j = 0; j < kSlices; ++j) {
+    if (I + j < LEVELS) {
+      const int lv = I + j;
+      const int first_i = lv > kSlices - 1 ? lv - (kSlices - 1) : 0;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const uint64_t da = da0 + (uint64_t)(((t >> 2) * 16384 + (t & 3) * 32) >> 4);
+        const uint64_t db = db0 + (uint64_t)(((uint32_t)j * kBSlice + 2048u * t) >> 4);
+        mma_bf16(acc + 64u * (uint32_t)lv, da, db, (I != first_i || t != 0) ? 1u : 0u);
+      }
+    }
+  }
+}
+template <int LEVELS>
+__device__ __forceinline__ void issue_slice(uint32_t acc, uint32_t a, uint32_t b, int i) {
+  const uint64_t da0 = tc::make_desc(a), db0 = tc::make_desc_mn(b);
+  switch (i) {
+    case 0: issue_slice_i<LEVELS, 0>(acc, da0, db0); break;
+    case 1: issue_slice_i<LEVELS, 1>(acc, da0, db0); break;
+    case 2: issue_slice_i<LEVELS, 2>(acc, da0, db0); break;
+    case 3: issue_slice_i<LEVELS, 3>(acc, da0, db0); break;
+    case 4: issue_slice_i<LEVELS, 4>(acc, da0, db0); break;
+    default: issue_slice_i<LEVELS, 5>(acc, da0, db0); break;
+  }
+}
+
+// Loads 8 consecutive columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// sum_l 2^(-8 l) L_l (levels exact FP32 integers) as df, smallest levels
+// first: levels 4.. in FP32 (their rounding is below 2^-56 of level 0's
+// scale), levels 3, 2, 1, 0 joined by error-free sums.  (Rounding level 3 in
+// FP32 as well would cost 2^-24 of its size, ~2^-43 of the product.)
+template <int LEVELS>
+__device__ __forceinline__ void combine_levels(const float (&L)[LEVELS], float& hi, float& lo) {
+  float t = 0.f;
+#pragma unroll
+  for (int lv = LEVELS - 1; lv >= 4; --lv) t = fmaf(L[lv], ldexpf(1.f, -8 * lv), t);
+  float s, e;
+  two_sum(L[3] * 0x1p-24f, t, s, lo);
+  two_sum(L[2] * 0x1p-16f, s, s, e);
+  lo += e;
+  two_sum(L[1] * 0x1p-8f, s, s, e);
+  lo += e;
+  two_sum(L[0], s, s, e);
+  lo += e;
+  fast_two_sum(s, lo, hi, lo);
+}
+
+}  // namespace oz
+}  // namespace pgx

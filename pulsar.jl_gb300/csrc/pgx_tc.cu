@@ -1,11 +1,16 @@
 // pgx_diag_tc_cmatmul64: batched complex 64 x 64 products C_i = P_i Q_i
 // through the tcgen05 product engine of pgx_tc.cuh (the engine the D = 64
 // mixed gradient runs on), for tests and profiling of the engine alone.
+// pgx_diag_dfcmatmul64: the same products in df (double-float) arithmetic,
+// on the CUDA cores (the df expm's product) or on the tensor cores by exact
+// bf16 slicing (pgx_oz.cuh), timed.
 #include <cuda_runtime.h>
 
 #include <vector>
 
 #include "pgx.h"
+#include "pgx_df.cuh"
+#include "pgx_oz.cuh"
 #include "pgx_tc.cuh"
 
 namespace pgx {
@@ -124,6 +129,214 @@ k_tc_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
 }
 
 }  // namespace tc
+
+namespace oz {
+
+// Batched df products on the tensor cores: one persistent CTA per SM.  Per
+// item the right factor's six slices are staged (96 KB), then the left
+// factor's slices one at a time into two alternating 32 KB buffers; the pairs
+// of slice i are issued while slice i + 1 is cut.  Operands and results are
+// planar df: [item][re, im][64 x 64 column-major] float2 {hi, lo}.
+template <int LEVELS>
+__global__ void __launch_bounds__(tc::kThreads, 1)
+k_oz_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* __restrict__ C, int n, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ float s_red[2][8];
+  const uint32_t pad = (tc::kSmemAlign - (tc::smem_u32(smem_raw) & (tc::kSmemAlign - 1))) & (tc::kSmemAlign - 1);
+  uint8_t* bsl = smem_raw + pad;            // kSlices right-operand slices
+  uint8_t* abuf = bsl + kSlices * kBSlice;  // two left-operand slice buffers
+  const Lane l = tc::lane_of();
+  const int warp = threadIdx.x >> 5;
+  uint32_t bar[2] = {tc::smem_u32(&s_bar[0]), tc::smem_u32(&s_bar[1])};
+  if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kTmemCols);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(bar[0]);
+    tc::mbar_init(bar[1]);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  uint32_t ph[2] = {0, 0};
+  int pend[2] = {0, 0};
+  bool abort = false;
+  for (int it = blockIdx.x; it < n && !abort; it += gridDim.x) {
+    // this thread's values: row l.i of the real (l.im = 0) or imaginary part,
+    // columns c0..c0+31; for the right factor the same entries are row k = l.L
+    // of [Qr; Qi]
+    const size_t base = ((size_t)it * 2 + l.im) * 4096 + l.i;
+    float h[32], lo[32];
+    float mx = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const float2 v = Q[base + 64 * (l.c0 + c)];
+      h[c] = v.x;
+      lo[c] = v.y;
+      mx = fmaxf(mx, fabsf(v.x));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_red[1][warp] = mx;
+    __syncthreads();
+    mx = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) mx = fmaxf(mx, s_red[1][w]);
+    const int eB = scale_exp(mx);
+    {
+      const float sc = ldexpf(1.f, -eB);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        h[c] *= sc;
+        lo[c] *= sc;
+      }
+#pragma unroll 1
+      for (int j = 0; j < kSlices; ++j) {
+        float s[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) s[c] = next_slice(h[c], lo[c], j);
+        stage_B(bsl + j * kBSlice, l, s);
+      }
+    }
+    mx = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const float2 v = P[base + 64 * (l.c0 + c)];
+      h[c] = v.x;
+      lo[c] = v.y;
+      mx = fmaxf(mx, fabsf(v.x));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_red[0][warp] = mx;
+    __syncthreads();
+    mx = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) mx = fmaxf(mx, s_red[0][w]);
+    const int eA = scale_exp(mx);
+    {
+      const float sc = ldexpf(1.f, -eA);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        h[c] *= sc;
+        lo[c] *= sc;
+      }
+    }
+#pragma unroll 1
+    for (int i = 0; i < kSlices; ++i) {
+      const int b = i & 1;
+      bool ok = true;
+      if (i >= 2) {  // the pairs of slice i - 2 have read buffer b
+        ok = tc::mbar_wait(bar[b], ph[b]);
+        if (ok) {
+          ph[b] ^= 1;
+          --pend[b];
+        }
+      }
+      if (__syncthreads_or(!ok)) {
+        abort = true;
+        break;
+      }
+      float s[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) s[c] = next_slice(h[c], lo[c], i);
+      stage_A(abuf + b * kASlice, l, s);
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        issue_slice<LEVELS>(tmem, tc::smem_u32(abuf + b * kASlice), tc::smem_u32(bsl), i);
+        tc::commit(bar[b]);
+      }
+      ++pend[b];
+    }
+    if (abort) break;
+    bool ok = true;
+    for (int b = 0; b < 2; ++b) {
+      if (tc::mbar_wait(bar[b], ph[b])) {
+        ph[b] ^= 1;
+        --pend[b];
+      } else {
+        ok = false;
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      abort = true;
+      break;
+    }
+    tc::fence_after_sync();
+    const float sc = ldexpf(1.f, eA + eB - 16);
+    float2* out = C + base;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+      float Lv[LEVELS][8];
+#pragma unroll
+      for (int lv = 0; lv < LEVELS; ++lv)
+        tmem_ld8(tmem + l.lane_addr + (uint32_t)(64 * lv + l.c0 + 8 * q), Lv[lv]);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        float L[LEVELS];
+#pragma unroll
+        for (int lv = 0; lv < LEVELS; ++lv) L[lv] = Lv[lv][c];
+        float hi, lw;
+        combine_levels<LEVELS>(L, hi, lw);
+        out[64 * (l.c0 + 8 * q + c)] = make_float2(hi * sc, lw * sc);
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // TMEM read and the buffers free before the next item's MMAs
+  }
+  if (abort && threadIdx.x == 0) {
+    atomicExch(err, 1);
+    for (int b = 0; b < 2; ++b)  // bounded: let the groups in flight finish before TMEM is freed
+      while (pend[b] > 0 && tc::mbar_wait(bar[b], ph[b])) {
+        ph[b] ^= 1;
+        --pend[b];
+      }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, tc::kTmemCols);
+  }
+}
+
+}  // namespace oz
+
+// The df product of the CUDA-core expm (mm1_df, one 256-thread team per CTA,
+// two CTAs per SM, operands in a per-CTA global workspace as the D = 64 expm
+// keeps them), batched, for comparison with the tensor-core form.
+__global__ void __launch_bounds__(256, 2)
+k_df_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* __restrict__ C, int n,
+           float4* __restrict__ slab) {
+  using L = Lay<64, 2>;
+  const Team<256> tm{(int)threadIdx.x};
+  float4* A = slab + (size_t)blockIdx.x * 3 * L::SIZE;
+  float4* B = A + L::SIZE;
+  float4* O = B + L::SIZE;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const float2* Pr = P + (size_t)it * 2 * 4096;
+    const float2* Qr = Q + (size_t)it * 2 * 4096;
+    for (int e = tm.lane; e < 4096; e += 256) {
+      const float2 pr = Pr[e], pi = Pr[4096 + e], qr = Qr[e], qi = Qr[4096 + e];
+      A[L::idx(e % 64, e / 64)] = make_float4(pr.x, pi.x, pr.y, pi.y);
+      B[L::idx(e % 64, e / 64)] = make_float4(qr.x, qi.x, qr.y, qi.y);
+    }
+    tm.sync();
+    mm1_df<64, 256, 2>(tm, O, A, B);
+    float2* Cr = C + (size_t)it * 2 * 4096;
+    for (int e = tm.lane; e < 4096; e += 256) {
+      const float4 v = O[L::idx(e % 64, e / 64)];
+      Cr[e] = make_float2(v.x, v.z);
+      Cr[4096 + e] = make_float2(v.y, v.w);
+    }
+    tm.sync();
+  }
+}
+
 }  // namespace pgx
 
 extern "C" int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t passes,
@@ -168,6 +381,83 @@ extern "C" int pgx_diag_tc_cmatmul64(const double* P, const double* Q, double* C
   cudaFree(dP);
   cudaFree(dQ);
   cudaFree(dC);
+  cudaFree(dErr);
+  return st;
+}
+
+extern "C" int pgx_diag_dfcmatmul64(const double* P, const double* Q, double* C, int32_t n, int32_t engine,
+                                    int32_t reps, float* ms) {
+  using namespace pgx;
+  if (!P || !Q || !C || n < 1 || engine < 0 || engine > 2 || reps < 1) return PGX_ERR_INVALID;
+  const size_t elems = (size_t)n * 4096;
+  // planar df: [item][re, im][4096] {hi, lo}
+  std::vector<float2> hP(2 * elems), hQ(2 * elems), hC(2 * elems);
+  for (size_t it = 0; it < (size_t)n; ++it)
+    for (int part = 0; part < 2; ++part)
+      for (int e = 0; e < 4096; ++e) {
+        const size_t src = (it * 4096 + e) * 2 + part, dst = (it * 2 + part) * 4096 + e;
+        const double p = P[src], q = Q[src];
+        const float ph = (float)p, qh = (float)q;
+        hP[dst] = make_float2(ph, (float)(p - (double)ph));
+        hQ[dst] = make_float2(qh, (float)(q - (double)qh));
+      }
+  float2 *dP = nullptr, *dQ = nullptr, *dC = nullptr;
+  float4* dSlab = nullptr;
+  int* dErr = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = PGX_OK, dev = 0, sms = 0, herr = 0;
+  const size_t smem = (size_t)oz::kSlices * oz::kBSlice + 2 * oz::kASlice + tc::kSmemAlign;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid_oz = n < sms ? n : sms, grid_df = n < 2 * sms ? n : 2 * sms;
+  if (e == cudaSuccess) e = cudaMalloc(&dP, 2 * elems * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&dQ, 2 * elems * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&dC, 2 * elems * sizeof(float2));
+  if (e == cudaSuccess && engine == 0)
+    e = cudaMalloc(&dSlab, (size_t)grid_df * 3 * Lay<64, 2>::SIZE * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&dErr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dP, hP.data(), 2 * elems * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dQ, hQ.data(), 2 * elems * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dErr, 0, sizeof(int));
+  if (e == cudaSuccess && engine == 1)
+    e = cudaFuncSetAttribute(oz::k_oz_cmm64<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && engine == 2)
+    e = cudaFuncSetAttribute(oz::k_oz_cmm64<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  auto launch = [&]() {
+    if (engine == 0) k_df_cmm64<<<grid_df, 256>>>(dP, dQ, dC, n, dSlab);
+    else if (engine == 1) oz::k_oz_cmm64<6><<<grid_oz, tc::kThreads, smem>>>(dP, dQ, dC, n, dErr);
+    else oz::k_oz_cmm64<7><<<grid_oz, tc::kThreads, smem>>>(dP, dQ, dC, n, dErr);
+    return cudaGetLastError();
+  };
+  if (e == cudaSuccess) e = launch();  // warm-up (module load, first touch)
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaEventRecord(e0);
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch();
+  if (e == cudaSuccess) e = cudaEventRecord(e1);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float t = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dErr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hC.data(), dC, 2 * elems * sizeof(float2), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) st = e == cudaErrorMemoryAllocation ? PGX_ERR_NOMEM : PGX_ERR_CUDA;
+  else if (herr) st = PGX_ERR_TIMEOUT;
+  if (st == PGX_OK) {
+    if (ms) *ms = t / (float)reps;
+    for (size_t it = 0; it < (size_t)n; ++it)
+      for (int part = 0; part < 2; ++part)
+        for (int i = 0; i < 4096; ++i) {
+          const float2 v = hC[(it * 2 + part) * 4096 + i];
+          C[(it * 4096 + i) * 2 + part] = (double)v.x + (double)v.y;
+        }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(dP);
+  cudaFree(dQ);
+  cudaFree(dC);
+  cudaFree(dSlab);
   cudaFree(dErr);
   return st;
 }

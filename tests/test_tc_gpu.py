@@ -84,6 +84,92 @@ def test_tc_cmatmul64_rejects_bad_arguments(pg):
     assert f(buf.ctypes.data, buf.ctypes.data, buf.ctypes.data, 1, 1, 2) == 1
 
 
+# ---- df-class products: CUDA-core df against tensor-core slicing ----------
+
+def _dfcmm(pg, P, Q, engine, reps=1):
+    f = pg._abi.lib().pgx_diag_dfcmatmul64
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
+    buf = lambda M: np.ascontiguousarray(np.swapaxes(M, -1, -2)).astype(np.complex128)
+    Pb, Qb = buf(P), buf(Q)
+    Cb = np.zeros_like(Pb)
+    ms = C.c_float(0.0)
+    st = f(Pb.ctypes.data, Qb.ctypes.data, Cb.ctypes.data, P.shape[0], engine, reps, C.byref(ms))
+    assert st == 0, st
+    return np.swapaxes(Cb, -1, -2), ms.value
+
+
+def _df_inputs(rng, n):
+    """Random Gaussian factors, near-identity factors (Taylor terms), unitary
+    factors (squarings), and factors with every entry of one sign and near
+    the slicing range's edge (every level sum near its bound)."""
+    P = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    Q = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    P[:8] = np.eye(64) + 0.01 * P[:8]
+    Q[:8] = np.eye(64) + 0.03 * Q[:8]
+    for k in range(8, 16):
+        P[k] = np.linalg.qr(P[k])[0]
+        Q[k] = P[k]
+    P[16:24] = rng.uniform(0.45, 0.5, (8, 64, 64)) * (1 + 1j)
+    Q[16:24] = rng.uniform(0.45, 0.5, (8, 64, 64)) * (1 - 1j)
+    return P, Q
+
+
+def _df_ref(P, Q):
+    """The FP64 product of the df roundings of the inputs (the kernels'
+    input); its own rounding is ~1e-16."""
+    def rdf(x):
+        hi = x.astype(np.float32).astype(np.float64)
+        return hi + (x - hi).astype(np.float32).astype(np.float64)
+    rd = lambda M: rdf(M.real) + 1j * rdf(M.imag)
+    return rd(P) @ rd(Q)
+
+
+# Errors relative to each product's largest entry.  The CUDA-core df product
+# (compensated dot products, ~2^-42 here) is the bar the expm was built on;
+# the sliced forms drop the levels beyond the last and the bits below slice 5
+# (2^-47 of the operand scale): about 2^-41 with levels 0..5 for
+# near-identity factors, about 2^-45 with level 6 (numpy emulation of the
+# slicing, exact level sums and the FP32 combine: 5.0e-13 and 2.2e-14).
+DF_REL = {0: 5e-13, 1: 1e-12, 2: 5e-14}
+
+
+def test_df_product_engines_reach_df_accuracy(pg):
+    """engine 0: the df expm's CUDA-core product; 1, 2: the tensor-core
+    product by exact bf16 slicing (levels 0..5, 0..6), on the same inputs."""
+    rng = np.random.default_rng(640)
+    P, Q = _df_inputs(rng, 300)
+    ref = _df_ref(P, Q)
+    errs = {}
+    for engine in (0, 1, 2):
+        Cg, _ = _dfcmm(pg, P, Q, engine)
+        assert np.all(np.isfinite(Cg))
+        err = np.max(np.abs(Cg - ref), axis=(1, 2)) / np.max(np.abs(ref), axis=(1, 2))
+        errs[engine] = err
+        print(f"df product engine {engine}: max rel {err.max():.2e}, median {np.median(err):.2e}")
+    for engine, err in errs.items():
+        assert err.max() <= DF_REL[engine], (engine, err.max(), int(err.argmax()))
+    assert errs[2].max() < errs[0].max()
+
+
+def test_df_product_tensor_core_is_faster_and_deterministic(pg):
+    """Times both engines on the same batch (8 products per SM): the
+    tensor-core form must beat the CUDA-core df product and reproduce its own
+    bits on a rerun."""
+    rng = np.random.default_rng(77)
+    n = 1216
+    P = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    Q = rng.standard_normal((n, 64, 64)) + 1j * rng.standard_normal((n, 64, 64))
+    C0, ms0 = _dfcmm(pg, P, Q, 0, reps=10)
+    C1, ms1 = _dfcmm(pg, P, Q, 1, reps=10)
+    C1b, _ = _dfcmm(pg, P, Q, 1, reps=1)
+    C2, ms2 = _dfcmm(pg, P, Q, 2, reps=10)
+    assert np.array_equal(C1, C1b)
+    print(f"df products, {n} per launch: CUDA-core {ms0:.3f} ms, tensor-core 21 pairs {ms1:.3f} ms, "
+          f"26 pairs {ms2:.3f} ms; speed-up {ms0 / ms1:.2f}x / {ms0 / ms2:.2f}x")
+    assert ms1 < ms0
+
+
 # ---- the D = 64 exact gradient on the tensor-core engine -------------------
 
 from oracle import members as mb  # noqa: E402

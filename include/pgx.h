@@ -127,7 +127,11 @@ typedef struct pgx_problem pgx_problem;
 int pgx_abi_version(void);
 const char* pgx_status_string(int status);
 
-/* Context on one device with an HBM budget (0 = no limit).  Owns one stream. */
+/* Context on one device with an HBM budget (0 = no limit).  Owns one stream.
+ * pgx_ctx_destroy on a context that still has live problems only marks it
+ * closing: the last pgx_problem_destroy releases it (no problem outlives the
+ * context it points to).  Destroying a closing context again is
+ * PGX_ERR_INVALID. */
 int pgx_ctx_create(int device, uint64_t hbm_budget_bytes, pgx_ctx** out);
 int pgx_ctx_destroy(pgx_ctx* ctx);
 int pgx_last_error(const pgx_ctx* ctx, char* buf, size_t len);

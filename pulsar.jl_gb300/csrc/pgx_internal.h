@@ -73,6 +73,7 @@ struct WorkDev {
   double* Gm;       // [n_members][n_t][n_c] per-member weighted gradient
   double2* slab;    // global Taylor workspace for Dp = 64: [slab_teams][10][Dp*Dp]
   int slab_teams;
+  int* expm_plan;   // mixed, Dp = 64: [n_members][n_t] degree choice of each slice's expm
   const double* u;  // [n_t][n_c]  (column-major [n_c x n_t])
   double* G;        // [n_t][n_c]
   double* F;        // [1]
@@ -176,17 +177,19 @@ void set_smem_once(const void* fn, size_t bytes);
 // default choice.
 // Team values of the tunable mixed kernels: candidates the autotuner times,
 // values pgx_problem_set_team admits, and the default.  kTeamTensor (1)
-// selects the tensor-core engine of the D = 64 gate-target exact gradient.
+// selects the tensor-core engine: of the D = 64 gate-target exact gradient,
+// and of the D = 64 df expm.
 constexpr int kTeamTensor = 1;
 bool grad_tc_eligible(const ProbDev& p);
-// The D = 64 gate chains' fix-up products run on the tensor cores as well.
+// Whether an evaluation may run tensor-core kernels (the D = 64 expm, the
+// gate chains' fix-up products, the gradient).
 bool tc_kernels_used(const ProbDev& p);
 int mixed_variants(const ProbDev& p, int kernel, int* out);
 int mixed_admitted(const ProbDev& p, int kernel, int* out);
 int mixed_default_team(const ProbDev& p, int kernel);
-// Error bits of the tensor-core gradient since the last call (the flag is
+// Error bits of the tensor-core kernels since the last call (the flags are
 // cleared): 1 = an MMA-completion wait gave up, 2 = a value beyond the FP16
-// operand limit; 0 = none, -1 = the flag cannot be read.
+// operand limit of the gradient; 0 = none, -1 = a flag cannot be read.
 int grad_tc_check();
 
 // Stage launchers (pgx_kernels.cu).  Each returns cudaGetLastError() after

@@ -1141,6 +1141,7 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS) k_grad_gate_mx(ProbDev p,
 // the D = 64 tensor-core gradient (uses choose_degree_q2 and the tables above)
 #include "pgx_grad_tc.cuh"
 #include "pgx_fix_tc.cuh"
+#include "pgx_expm_oz.cuh"
 
 namespace pgx {
 
@@ -1180,10 +1181,14 @@ static int grid_for(K kernel, int threads, size_t smem, long teams, int tpc, int
 // has a third form, the tensor-core engine (kTeamTensor): the default and the
 // only one the autotuner times (its products are 3xTF32, not bit-identical
 // to the CUDA-core teams, and several times faster); the CUDA-core teams stay
-// selectable with pgx_problem_set_team.
+// selectable with pgx_problem_set_team.  The D = 64 df expm has a tensor-core
+// form as well (every product by exact bf16 slicing, pgx_expm_oz.cuh) for every
+// generator and target: the default and the autotuner's only candidate there,
+// the CUDA-core team (256) selectable.
 bool grad_tc_eligible(const ProbDev& p) {
   return p.Dp == 64 && p.target == TGT_GATE && p.grad_mode == GRAD_EXACT;
 }
+static bool expm_tc_eligible(const ProbDev& p) { return p.Dp == 64; }
 static int variants_for(int Dp, int kernel, int* out) {
   int n = 0;
   if (Dp <= 8) out[n++] = 32;
@@ -1195,8 +1200,11 @@ static int variants_for(int Dp, int kernel, int* out) {
   }
   return n;
 }
+static bool tc_eligible(const ProbDev& p, int kernel) {
+  return kernel == kTuneGradMx ? grad_tc_eligible(p) : expm_tc_eligible(p);
+}
 int mixed_variants(const ProbDev& p, int kernel, int* out) {
-  if (kernel == kTuneGradMx && grad_tc_eligible(p)) {
+  if (tc_eligible(p, kernel)) {
     out[0] = kTeamTensor;
     return 1;
   }
@@ -1204,7 +1212,7 @@ int mixed_variants(const ProbDev& p, int kernel, int* out) {
 }
 int mixed_admitted(const ProbDev& p, int kernel, int* out) {
   int n = variants_for(p.Dp, kernel, out);
-  if (kernel == kTuneGradMx && grad_tc_eligible(p)) out[n++] = kTeamTensor;
+  if (tc_eligible(p, kernel)) out[n++] = kTeamTensor;
   return n;
 }
 // Defaults (problems that were never tuned: batches, served jobs) are the
@@ -1214,7 +1222,7 @@ int mixed_default_team(const ProbDev& p, int kernel) {
   if (Dp <= 8) return 32;
   if (Dp == 16) return kernel == kTuneExpmMx ? 128 : 32;
   if (Dp == 32) return kernel == kTuneExpmMx ? 256 : 128;
-  if (kernel == kTuneGradMx && grad_tc_eligible(p)) return kTeamTensor;
+  if (tc_eligible(p, kernel)) return kTeamTensor;
   return kernel == kTuneExpmMx ? 256 : 512;
 }
 
@@ -1254,8 +1262,30 @@ static cudaError_t do_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchIn
   ++*li.launches;
   return cudaGetLastError();
 }
+// The tensor-core expm: one CTA per SM (its slice buffers and accumulators
+// fill shared memory and TMEM), at most one per slab workspace.
+static cudaError_t do_expm_oz64(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  if (!w.expm_plan) return cudaErrorInvalidValue;
+  const long items = (long)p.n_members * p.n_t;
+  ensure_smem_mx(k_expm_prep_oz64, kExpmPrepSmem);
+  const int pgrid = grid_for(k_expm_prep_oz64, 256, kExpmPrepSmem, items, 1, li.num_sms, 0);
+  k_expm_prep_oz64<<<pgrid, 256, kExpmPrepSmem, li.stream>>>(p, w);
+  ++*li.launches;
+  if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) return e;
+  ensure_smem_mx(k_expm_oz64, oz::kExpmSmem);
+  long grid = li.num_sms;
+  if (grid > items) grid = items;
+  if (grid > w.slab_teams) grid = w.slab_teams;
+  k_expm_oz64<<<(int)grid, oz::kExpmThreads, oz::kExpmSmem, li.stream>>>(p, w);
+  ++*li.launches;
+  return cudaGetLastError();
+}
 cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   const int t = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p, kTuneExpmMx);
+  if (t == kTeamTensor) {
+    if (!expm_tc_eligible(p)) return cudaErrorInvalidValue;
+    return do_expm_oz64(p, w, li);
+  }
   PGX_DISPATCH_MX_T(p.Dp, t, return (do_expm_mx<D_, T_>(p, w, li)));
   return cudaSuccess;
 }
@@ -1427,13 +1457,14 @@ static cudaError_t do_grad_tc64(const ProbDev& p, const WorkDev& w, const Launch
 }
 
 int grad_tc_check() {
-  int flag = 0;
-  if (cudaMemcpyFromSymbol(&flag, g_grad_tc_timeout, sizeof(int)) != cudaSuccess) return -1;
-  if (flag) {
-    const int zero = 0;
-    cudaMemcpyToSymbol(g_grad_tc_timeout, &zero, sizeof(int));
-  }
-  return flag;
+  int flag = 0, ex = 0;
+  if (cudaMemcpyFromSymbol(&flag, g_grad_tc_timeout, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyFromSymbol(&ex, g_expm_tc_timeout, sizeof(int)) != cudaSuccess)
+    return -1;
+  const int zero = 0;
+  if (flag) cudaMemcpyToSymbol(g_grad_tc_timeout, &zero, sizeof(int));
+  if (ex) cudaMemcpyToSymbol(g_expm_tc_timeout, &zero, sizeof(int));
+  return flag | (ex ? 1 : 0);
 }
 
 template <int D>
@@ -1445,7 +1476,7 @@ static cudaError_t do_refine_mx(const ProbDev& p, const WorkDev& w, const Launch
   return cudaGetLastError();
 }
 bool refine_applies(const ProbDev& p) { return p.gen == GEN_HERM && p.target == TGT_GATE; }
-bool tc_kernels_used(const ProbDev& p) { return p.Dp == 64 && p.target == TGT_GATE; }
+bool tc_kernels_used(const ProbDev& p) { return p.Dp == 64; }
 cudaError_t launch_refine_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
   if (!refine_applies(p)) return cudaSuccess;
   PGX_DISPATCH_MX(p.Dp, return (do_refine_mx<D_>(p, w, li)));

@@ -22,10 +22,12 @@
 // beyond the last, the slicing remainder) stays below 2^-44 of K max|A| max|B|
 // in the worst case of aligned signs.
 //
-// Measured on GB300: an M = 128, N = 64 MMA takes 48 cycles, so the 21 pairs
-// (168 MMAs of K = 16) of one product take ~8,100 cycles of one SM's tensor
-// pipe, against ~48,000 FP32-pipe cycles for the same product in df
-// arithmetic (~23 FP32 instructions per complex multiply-add).
+// Measured on GB300: an M = 128 MMA of K = 16 takes 46-48 cycles at N = 64
+// and 64 at N = 128; pairs that share a left slice go two at a time, so the 26
+// pairs of levels 0..6 (12 MMA groups of N = 128, 2 of N = 64, K = 128 each)
+// take ~7,000 cycles of one SM's tensor pipe, against ~48,000 FP32-pipe
+// cycles for the same product in df arithmetic (~23 FP32 instructions per
+// complex multiply-add).
 //
 // Layouts (128-byte swizzle, 1024-byte aligned tiles):
 //   - the expanded left operand of one slice, K-major: 128 rows x 128 k bf16,
@@ -118,49 +120,79 @@ __device__ __forceinline__ void stage_B(uint8_t* b, const Lane& l, const float (
   }
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+// Right-operand descriptor of two adjacent slices read as one N = 128
+// operand: the second 64-wide swizzle atom along N is the next slice, kBSlice
+// bytes on (the leading byte offset of an MN-major layout); 8-row groups along
+// K at 1024 bytes.
+__device__ __forceinline__ uint64_t make_desc_mn2(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(kBSlice >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+constexpr uint32_t kIdescBF16N128 =
+    (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16_n(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                           uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(d_tmem), "l"(a), "l"(b), "r"(kIdescBF16), "r"(accumulate)
+      ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
-// One elected thread: the slice pairs (i, j) of left slice I (in shared
+// One elected thread: the slice pairs (I, j) of left slice I (in shared
 // memory at a) with every right slice j (at b + j kBSlice) whose level I + j
-// is below LEVELS, each into the level's accumulator (64 TMEM columns at
-// acc + 64 (I + j)); the first pair of a level overwrites it.  Straight-line
-// code: the descriptors of the K steps are the base descriptors plus
-// immediate offsets (a start address below 256 KB keeps the 14-bit address
-// field from carrying), so the single issuing thread keeps ahead of the
-// tensor pipe.
+// is below LEVELS, into the level accumulators (64 TMEM columns each at
+// acc + 64 level).  Adjacent right slices j, j + 1 go as one N = 128 MMA
+// (its two halves land in the accumulators of levels I + j and I + j + 1):
+// an M = 128 MMA takes 46-48 cycles at N = 64 and 64 at N = 128 (measured on
+// GB300), so a pair costs 32 cycles instead of 48.  Slice 0's MMAs overwrite
+// (at the first K step); every later one accumulates, so a level first
+// reached after slice 0 (level 6, from slice 1 on) must be zeroed by the
+// caller.  Straight-line code: the descriptors of the K steps are the base
+// descriptors plus immediate offsets (a start address below 256 KB keeps the
+// 14-bit address field from carrying).
 template <int LEVELS, int I>
-__device__ __forceinline__ void issue_slice_i(uint32_t acc, uint64_t da0, uint64_t db0) {
+__device__ __forceinline__ void issue_slice_i(uint32_t acc, uint32_t a, uint32_t b) {
+  constexpr int NJ = (LEVELS - I < kSlices) ? LEVELS - I : kSlices;  // right slices j = 0 .. NJ-1
+  const uint64_t da0 = tc::make_desc(a);
 #pragma unroll
-  for (int j = 0; j < kSlices; ++j) {
-    if (I + j < LEVELS) {
-      const int lv = I + j;
-      const int first_i = lv > kSlices - 1 ? lv - (kSlices - 1) : 0;
+  for (int j = 0; j < NJ; j += 2) {
+    const bool two = j + 1 < NJ;
+    const uint64_t db0 = two ? make_desc_mn2(b + (uint32_t)j * kBSlice) : tc::make_desc_mn(b + (uint32_t)j * kBSlice);
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const uint64_t da = da0 + (uint64_t)(((t >> 2) * 16384 + (t & 3) * 32) >> 4);
-        const uint64_t db = db0 + (uint64_t)(((uint32_t)j * kBSlice + 2048u * t) >> 4);
-        mma_bf16(acc + 64u * (uint32_t)lv, da, db, (I != first_i || t != 0) ? 1u : 0u);
-      }
+    for (int t = 0; t < 8; ++t) {
+      const uint64_t da = da0 + (uint64_t)(((t >> 2) * 16384 + (t & 3) * 32) >> 4);
+      const uint64_t db = db0 + (uint64_t)((2048u * t) >> 4);
+      mma_bf16_n(acc + 64u * (uint32_t)(I + j), da, db, two ? kIdescBF16N128 : kIdescBF16,
+                 (I != 0 || t != 0) ? 1u : 0u);
     }
   }
 }
 template <int LEVELS>
 __device__ __forceinline__ void issue_slice(uint32_t acc, uint32_t a, uint32_t b, int i) {
-  const uint64_t da0 = tc::make_desc(a), db0 = tc::make_desc_mn(b);
   switch (i) {
-    case 0: issue_slice_i<LEVELS, 0>(acc, da0, db0); break;
-    case 1: issue_slice_i<LEVELS, 1>(acc, da0, db0); break;
-    case 2: issue_slice_i<LEVELS, 2>(acc, da0, db0); break;
-    case 3: issue_slice_i<LEVELS, 3>(acc, da0, db0); break;
-    case 4: issue_slice_i<LEVELS, 4>(acc, da0, db0); break;
-    default: issue_slice_i<LEVELS, 5>(acc, da0, db0); break;
+    case 0: issue_slice_i<LEVELS, 0>(acc, a, b); break;
+    case 1: issue_slice_i<LEVELS, 1>(acc, a, b); break;
+    case 2: issue_slice_i<LEVELS, 2>(acc, a, b); break;
+    case 3: issue_slice_i<LEVELS, 3>(acc, a, b); break;
+    case 4: issue_slice_i<LEVELS, 4>(acc, a, b); break;
+    default: issue_slice_i<LEVELS, 5>(acc, a, b); break;
   }
+}
+
+// Zeroes this thread's 32 columns (c0 ..) of the level-6 accumulator in its
+// TMEM lane (levels beyond slice 0's reach start from zero).
+__device__ __forceinline__ void zero_level6(uint32_t tmem, const Lane& l) {
+  float z[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) z[c] = 0.f;
+  tc::tmem_st32(tmem + l.lane_addr + (uint32_t)(64 * 6 + l.c0), z);
+  tc::tmem_st_wait();
 }
 
 // Loads 8 consecutive columns of this thread's TMEM lane.

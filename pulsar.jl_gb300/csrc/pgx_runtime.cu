@@ -105,8 +105,7 @@ extern "C" int pgx_ctx_create(int device, uint64_t hbm_budget_bytes, pgx_ctx** o
   return PGX_OK;
 }
 
-extern "C" int pgx_ctx_destroy(pgx_ctx* c) {
-  if (!c) return PGX_ERR_INVALID;
+static void ctx_release(pgx_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaEventDestroy(c->ev0);
@@ -118,6 +117,15 @@ extern "C" int pgx_ctx_destroy(pgx_ctx* c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
+}
+
+extern "C" int pgx_ctx_destroy(pgx_ctx* c) {
+  if (!c || c->closing) return PGX_ERR_INVALID;
+  if (c->live > 0) {  // released by the last pgx_problem_destroy
+    c->closing = true;
+    return PGX_OK;
+  }
+  ctx_release(c);
   return PGX_OK;
 }
 
@@ -313,7 +321,7 @@ static int validate(pgx_ctx* c, const pgx_problem_desc* d) {
 }
 
 struct Sizes {
-  size_t U, P, Utot, psi, z, Fm, Gm, slab, u, G;
+  size_t U, P, Utot, psi, z, Fm, Gm, slab, u, G, plan;
 };
 
 static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
@@ -330,6 +338,7 @@ static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
   s.Fm = nm * sizeof(double);
   s.Gm = nm * nt * d->n_controls * sizeof(double);
   s.slab = pgx::slab_elems(Dp, num_sms) * sizeof(double2);
+  s.plan = (Dp >= 64 && d->precision == PGX_PREC_MIXED) ? nm * nt * sizeof(int) : 0;
   s.u = nt * d->n_controls * sizeof(double);
   s.G = s.u;
   return s;
@@ -370,7 +379,7 @@ static uint64_t footprint(const pgx_problem_desc* d, int num_sms) {
                            ? (DD + DD / 2) * (d->n_drifts + d->n_controls + 1) +
                                  sizeof(float2) * ((size_t)d->n_slices + 2 * (size_t)d->n_members) + s.u
                            : 0);
-  return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.u + s.G +
+  return s.U + s.P + s.Utot + 2 * s.psi + 2 * s.z + s.Fm + s.Gm + s.slab + s.plan + s.u + s.G +
          3 * sizeof(double) + consts + mixed;
 }
 
@@ -501,6 +510,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   pgx_problem* p = new (std::nothrow) pgx_problem();
   if (!p) return ctx_fail(c, PGX_ERR_NOMEM, "host allocation failed");
   p->ctx = c;
+  ++c->live;  // every later failure path releases p through pgx_problem_destroy
   p->desc = *d;
   const int D = d->dim, Dp = pad_dim(D);
   p->Dp = Dp;
@@ -621,6 +631,7 @@ extern "C" int pgx_problem_create(pgx_ctx* c, const pgx_problem_desc* d, pgx_pro
   w.Gm = (double*)A(s.Gm);
   w.slab = (double2*)A(s.slab);
   w.slab_teams = pgx::slab_team_count(Dp, c->num_sms);
+  w.expm_plan = (int*)A(s.plan);
   p->d_u = (double*)A(s.u);
   p->d_G = (double*)A(s.G);
   p->d_F = (double*)A(3 * sizeof(double));  // objective, gradient-pass scratch, residual bits
@@ -691,8 +702,10 @@ extern "C" int pgx_problem_destroy(pgx_problem* p) {
   }
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
-  p->ctx->used -= p->bytes;
+  pgx_ctx* c = p->ctx;
+  c->used -= p->bytes;
   delete p;
+  if (--c->live == 0 && c->closing) ctx_release(c);
   return PGX_OK;
 }
 
@@ -1022,7 +1035,7 @@ int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_st
     return st;
   if ((st = ctx_cuda(c, cudaEventRecord(c->ev1, c->stream), "event"))) return st;
   if ((st = ctx_cuda(c, cudaStreamSynchronize(c->stream), "eval sync"))) return st;
-  if (G && p->desc.precision == PGX_PREC_MIXED && pgx::tc_kernels_used(p->pd)) {
+  if (p->desc.precision == PGX_PREC_MIXED && pgx::tc_kernels_used(p->pd)) {
     const int tcf = pgx::grad_tc_check();
     if (tcf & 2)
       return ctx_fail(c, PGX_ERR_NONFINITE, "tensor-core gradient: an operand exceeded the FP16 range (select the "

@@ -25,6 +25,10 @@ struct pgx_ctx {
   bool stage_timing = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::vector<cudaEvent_t>> stage_marks;  // one vector of 6 events per evaluation
+  // Problems alive on this context; pgx_ctx_destroy with live problems only
+  // marks it closing, and the last pgx_problem_destroy releases it.
+  int live = 0;
+  bool closing = false;
 };
 
 struct pgx_problem {

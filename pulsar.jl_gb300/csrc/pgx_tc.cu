@@ -223,6 +223,7 @@ k_oz_cmm64(const float2* __restrict__ P, const float2* __restrict__ Q, float2* _
         lo[c] *= sc;
       }
     }
+    if (LEVELS > kSlices) zero_level6(tmem, l);  // the previous item's accumulators are read
 #pragma unroll 1
     for (int i = 0; i < kSlices; ++i) {
       const int b = i & 1;

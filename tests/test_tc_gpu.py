@@ -281,3 +281,52 @@ def test_tc_gradient_refuses_values_beyond_fp16_range(pg):
     F, G = p.eval(np.zeros((1, 1)))
     assert np.isfinite(F) and np.all(np.isfinite(G))
     p.close()
+
+
+# ---- the D = 64 df expm on the tensor cores -------------------------------
+
+@pytest.mark.parametrize("dt", [0.002, 0.02, 0.1, 0.5])
+def test_tc_expm_matches_cuda_core_expm_and_oracle(pg, dt):
+    """Hermitian D = 64 gate problems whose slice norms (~0.1 .. ~25) select
+    different degrees, block sizes and squaring counts: the tensor-core expm
+    (the default at D = 64) against the CUDA-core df expm (team 256) and the
+    FP64 oracle."""
+    rng = np.random.default_rng(int(dt * 1000) + 11)
+    prob, u0 = random_gate_problem(rng, 64, n_t=6, n_members=2, dt=dt)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    assert p.teams[0] == 1
+    F_tc, G_tc = p.eval(u0)
+    p.set_teams(256, 0)
+    F_cc, G_cc = p.eval(u0)
+    p.close()
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    assert abs(F_tc - F_cc) <= 1e-11, (F_tc, F_cc)
+    assert abs(F_tc - Fo) <= 1e-8
+    assert _rel_g(G_tc, Go) <= G_RTOL_MIXED, _rel_g(G_tc, Go)
+    print(f"dt {dt}: |F_tc - F_cc| {abs(F_tc - F_cc):.1e}, |F_tc - F_oracle| {abs(F_tc - Fo):.1e}")
+
+
+def test_tc_expm_lindblad_and_state_targets(pg):
+    """The 3-qubit Lindblad gate (non-Hermitian superoperators) and a D = 64
+    state-transfer problem: the tensor-core expm against the CUDA-core expm
+    and the oracle."""
+    prob, u0 = fx.lindblad_3q(n_t=30, n_draws=2)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F_tc, G_tc = p.eval(u0)
+    p.set_teams(256, 0)
+    F_cc, _ = p.eval(u0)
+    p.close()
+    Fo, Go = mb.eval_gate_exact_adjoint(prob, u0)
+    assert abs(F_tc - F_cc) <= 1e-11 and abs(F_tc - Fo) <= 1e-8
+    assert _rel_g(G_tc, Go) <= G_RTOL_MIXED
+    rng = np.random.default_rng(78)
+    gp, u1 = random_gate_problem(rng, 64, n_t=5, n_members=2, dt=0.04)
+    kw = dict(generator=gp.generator, target="states", fidelity="square", states_init=np.eye(64)[:2],
+              states_target=np.eye(64)[2:4], grad_mode="exact", precision="mixed")
+    ps = pg.Problem(gp.drifts, gp.controls, gp.dt, **kw)
+    assert ps.teams[0] == 1
+    F1, _ = ps.eval(u1)
+    ps.set_teams(256, 0)
+    F2, _ = ps.eval(u1)
+    ps.close()
+    assert abs(F1 - F2) <= 1e-11, (F1, F2)

@@ -216,30 +216,36 @@ __device__ __forceinline__ void issue_loop(Engine& g) {
   }
 }
 
-// This worker's part of the Horner block C_i = sum_{j<q} c_{qi+j} B^j at its
-// entry c (B^0 = I), from the own-value copies of B, B^2, B^3.
-__device__ __forceinline__ df block_part(int i, int q, bool diag, bool real, const float2* own, int c,
-                                         const df* coef) {
+// This worker's part of the Horner block C_i = sum_{j<q} c_{qi+j} B^j at two
+// of its entries (columns c0 + 2 cp, + 1; B^0 = I), from the own-value copies
+// of B, B^2, B^3 (float4 {hi, lo, hi, lo} per entry pair): v0, v1.
+__device__ __forceinline__ void block_pair(int i, int q, int row, int c0, bool real, const float4* own, int cp,
+                                           const df* coef, df& v0, df& v1) {
   const int o = q * i;
-  const float2 b1 = own[c * kWorkers + threadIdx.x];
-  df v = df_mul(df{b1.x, b1.y}, coef[o + 1]);
+  const float4 b1 = __ldcg(own + cp * kWorkers + threadIdx.x);
+  const float4 b2 = q >= 3 ? __ldcg(own + (16 + cp) * kWorkers + threadIdx.x) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 b3 = q >= 4 ? __ldcg(own + (32 + cp) * kWorkers + threadIdx.x) : make_float4(0.f, 0.f, 0.f, 0.f);
+  v0 = df_mul(df{b1.x, b1.y}, coef[o + 1]);
+  v1 = df_mul(df{b1.z, b1.w}, coef[o + 1]);
   if (q >= 3) {
-    const float2 b2 = own[(32 + c) * kWorkers + threadIdx.x];
-    v = df_add(v, df_mul(df{b2.x, b2.y}, coef[o + 2]));
+    v0 = df_add(v0, df_mul(df{b2.x, b2.y}, coef[o + 2]));
+    v1 = df_add(v1, df_mul(df{b2.z, b2.w}, coef[o + 2]));
   }
   if (q >= 4) {
-    const float2 b3 = own[(64 + c) * kWorkers + threadIdx.x];
-    v = df_add(v, df_mul(df{b3.x, b3.y}, coef[o + 3]));
+    v0 = df_add(v0, df_mul(df{b3.x, b3.y}, coef[o + 3]));
+    v1 = df_add(v1, df_mul(df{b3.z, b3.w}, coef[o + 3]));
   }
-  if (diag && real) v = df_add(v, coef[o]);
-  return v;
+  if (real && row == c0 + 2 * cp) v0 = df_add(v0, coef[o]);
+  if (real && row == c0 + 2 * cp + 1) v1 = df_add(v1, coef[o]);
 }
 
 // Writes this worker's values as matrix `mat` (0: B, 1: B^2, 2: B^3) of the
-// own-value copies.
-__device__ __forceinline__ void store_own(float2* own, int mat, const float (&h)[32], const float (&lo)[32]) {
+// own-value copies: thread-major float4 {hi, lo, hi, lo} per entry pair, so a
+// warp's loads are 512 contiguous bytes.
+__device__ __forceinline__ void store_own(float4* own, int mat, const float (&h)[32], const float (&lo)[32]) {
 #pragma unroll
-  for (int c = 0; c < 32; ++c) own[(32 * mat + c) * kWorkers + threadIdx.x] = make_float2(h[c], lo[c]);
+  for (int cp = 0; cp < 16; ++cp)
+    own[(16 * mat + cp) * kWorkers + threadIdx.x] = make_float4(h[2 * cp], lo[2 * cp], h[2 * cp + 1], lo[2 * cp + 1]);
 }
 
 }  // namespace oz
@@ -272,8 +278,8 @@ __global__ void __launch_bounds__(256) k_expm_prep_oz64(ProbDev p, WorkDev w) {
     float2* out = reinterpret_cast<float2*>(w.U) + (size_t)it * 8192;
     for (int e = tm.lane; e < 4096; e += 256) {
       const float4 v = A[L::idx(e % 64, e / 64)];
-      out[e] = make_float2(v.x * sc, v.z * sc);
-      out[4096 + e] = make_float2(v.y * sc, v.w * sc);
+      __stcs(out + e, make_float2(v.x * sc, v.z * sc));  // read once, by the expm
+      __stcs(out + 4096 + e, make_float2(v.y * sc, v.w * sc));
     }
     if (tm.lane == 0) w.expm_plan[it] = pk;
     tm.sync();  // A is rebuilt by the next unit
@@ -319,7 +325,7 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
     __syncwarp();
   } else {
     const Lane l = tc::lane_of();
-    float2* own = reinterpret_cast<float2*>(w.slab) + (size_t)blockIdx.x * 3 * 32 * kWorkers;  // B, B^2, B^3
+    float4* own = reinterpret_cast<float4*>(w.slab) + (size_t)blockIdx.x * 3 * 16 * kWorkers;  // B, B^2, B^3
     const auto nop = [] {};
     const long items = (long)p.n_members * p.n_t;
     long it = blockIdx.x;
@@ -334,7 +340,7 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
         const float2* Bp = reinterpret_cast<const float2*>(w.U) + (size_t)it * 8192 + l.im * 4096 + l.i;
 #pragma unroll
         for (int c = 0; c < 32; ++c) {
-          const float2 v = Bp[64 * (l.c0 + c)];
+          const float2 v = __ldcs(Bp + 64 * (l.c0 + c));
           xh[c] = v.x;
           xl[c] = v.y;
         }
@@ -355,10 +361,12 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
         if (st == 2 && q == 4) {  // B^4 = B^2 B^2
           store_own(own, 2, xh, xl);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const float2 v = own[(32 + c) * kWorkers + threadIdx.x];
-            xh[c] = v.x;
-            xl[c] = v.y;
+          for (int cp = 0; cp < 16; ++cp) {
+            const float4 v = own[(16 + cp) * kWorkers + threadIdx.x];
+            xh[2 * cp] = v.x;
+            xl[2 * cp] = v.y;
+            xh[2 * cp + 1] = v.z;
+            xl[2 * cp + 1] = v.w;
           }
           eR = stage_right(g, l, xh, xl);
         }
@@ -367,11 +375,15 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
           if (q == 3) store_own(own, 2, xh, xl);
           eR = stage_right(g, l, xh, xl);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const df v = df_add(block_part(nL - 1, q, l.i == l.c0 + c, l.im == 0, own, c, c_dfcoef),
-                                df_mul(df{xh[c], xl[c]}, c_dfcoef[deg]));
-            xh[c] = v.hi;
-            xl[c] = v.lo;
+          for (int cp = 0; cp < 16; ++cp) {
+            df v0, v1;
+            block_pair(nL - 1, q, l.i, l.c0, l.im == 0, own, cp, c_dfcoef, v0, v1);
+            v0 = df_add(v0, df_mul(df{xh[2 * cp], xl[2 * cp]}, c_dfcoef[deg]));
+            v1 = df_add(v1, df_mul(df{xh[2 * cp + 1], xl[2 * cp + 1]}, c_dfcoef[deg]));
+            xh[2 * cp] = v0.hi;
+            xl[2 * cp] = v0.lo;
+            xh[2 * cp + 1] = v1.hi;
+            xl[2 * cp + 1] = v1.lo;
           }
         }
         if (st == n_steps) break;
@@ -379,10 +391,12 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
         if (st >= n_pow && st < n_pow + n_hor) {
           const int i = n_pow + n_hor - 1 - st;
           const auto park = [&] {  // C_i into shared memory while the MMAs run
-#pragma unroll 8
-            for (int c = 0; c < 32; ++c) {
-              const df v = block_part(i, q, l.i == l.c0 + c, l.im == 0, own, c, c_dfcoef);
-              g.ci[c * kWorkers + threadIdx.x] = make_float2(v.hi, v.lo);
+#pragma unroll 4
+            for (int cp = 0; cp < 16; ++cp) {
+              df v0, v1;
+              block_pair(i, q, l.i, l.c0, l.im == 0, own, cp, c_dfcoef, v0, v1);
+              g.ci[(2 * cp) * kWorkers + threadIdx.x] = make_float2(v0.hi, v0.lo);
+              g.ci[(2 * cp + 1) * kWorkers + threadIdx.x] = make_float2(v1.hi, v1.lo);
             }
           };
           ok = product(g, l, xh, xl, eR, true, park);

@@ -104,8 +104,9 @@ typedef struct pgx_problem_desc {
  *              the trace-preservation defect of Phi = U_total
  *   NORM       states, Hermitian:    max_s | ||psi_s(T)||^2 - ||psi_s(0)||^2 |
  *   STATE_TRACE states, Liouvillian: max_s |Tr rho_s(T) - Tr rho_s(0)|
- * (state targets: evaluations that compute G; NONE otherwise).  The mixed
- * path has no refinement step, so this is its only a-posteriori check.     */
+ * (state targets: evaluations that compute G; NONE otherwise).  For mixed
+ * Hermitian gate problems it is measured before the FP64 Newton-Schulz
+ * refinement of U_total, so it reports the defect the refinement removed. */
 enum { PGX_RESID_NONE = 0, PGX_RESID_UNITARITY = 1, PGX_RESID_TRACE = 2, PGX_RESID_NORM = 3,
        PGX_RESID_STATE_TRACE = 4 };
 
@@ -261,19 +262,24 @@ int pgx_penalty_eval(pgx_ctx* ctx, int32_t n_controls, int32_t n_slices, const d
  * kernels at controls u, `reps` launches each, keeps the fastest for this
  * problem and writes a one-line report (nullable).  Variants only re-map work
  * to threads; every dot product is summed in the same order, so results are
- * bit-identical whatever is chosen.  The FP64 path has no variants.  The
- * D = 64 gradient of gate targets with the exact gradient has one candidate,
- * the tensor-core engine (PGX_TEAM_TENSOR).                                 */
+ * bit-identical whatever is chosen.  The FP64 path has no variants.  At
+ * padded dimension 64 the expm, and the gradient of gate targets with the
+ * exact gradient, have one candidate each: the tensor-core engine
+ * (PGX_TEAM_TENSOR).                                                        */
 int pgx_autotune(pgx_problem* prob, const double* u, int32_t reps, char* report, size_t report_len);
 /* Sets the team sizes directly (a plan kept from an earlier pgx_autotune);
  * 0 = the built-in default.  Values the dimension does not admit are refused
  * with PGX_ERR_INVALID.  Kernel indices: 0 = mixed expm, 1 = mixed gradient.
  * Admitted by padded dimension: 32 (<= 8); 32, 64, 128, 256 (16); 128, 256
- * (32); 256 (64), plus 512 for the gradient at 64.  For the gradient at 64
- * of gate targets with the exact gradient, PGX_TEAM_TENSOR (1) selects the
- * tensor-core engine: 3xTF32 tcgen05 products, FP32-class like the CUDA-core
- * teams but not bit-identical to them; it is that case's default.  The
- * CUDA-core teams 256 and 512 stay admitted there for comparisons.         */
+ * (32); 256 (64), plus 512 for the gradient at 64.  PGX_TEAM_TENSOR (1)
+ * selects a tensor-core engine, the default where it exists:
+ *   - the expm at 64 (every generator and target): df products by exact bf16
+ *     slicing (six 8-bit slices per operand, levels 0..6 accumulated exactly
+ *     in FP32), df-class like the CUDA-core team 256 but not bit-identical;
+ *   - the gradient at 64 of gate targets with the exact gradient: 3xFP16
+ *     tcgen05 products, FP32-class like the CUDA-core teams but not
+ *     bit-identical to them.
+ * The CUDA-core teams stay admitted there for comparisons.                   */
 #define PGX_TUNE_EXPM 0
 #define PGX_TUNE_GRAD 1
 #define PGX_TEAM_TENSOR 1

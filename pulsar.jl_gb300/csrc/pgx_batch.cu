@@ -8,8 +8,11 @@
 // several streams -- largest problems first -- so small problems fill the GPU
 // while large ones run, and the whole iteration (fork, pipelines, join, the
 // step kernel) is captured once into a CUDA graph and relaunched; the host
-// reads nothing between iterations.  Each problem runs exactly the kernels of
-// a solo evaluation, so batched results are bit-identical to solo ones.
+// reads nothing between iterations.  Each problem runs the kernels of a solo
+// evaluation, except that mixed problems of padded dimension 2 get their slice
+// propagators from one shared launch (the register-resident expm over every
+// (problem, member, slice) item of the class, whose per-slice arithmetic is
+// the solo launch's), so batched results are bit-identical to solo ones.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -104,6 +107,20 @@ struct pgx_batch {
   double opt_key[4] = {0, 0, 0, 0};  // settings baked into iter_exec
   int64_t units = 0;
   int64_t kernels_eval = 0, kernels_iter = 0;  // kernel nodes in each graph
+  // Mixed problems of padded dimension 2 take their slice propagators from
+  // one shared launch of the register-resident expm, walking every (problem,
+  // member, slice) item of the class.
+  struct Small {
+    int Dp = 0;
+    std::vector<int> idx;  // problems of the class
+    pgx::ProbDev* d_p = nullptr;
+    pgx::WorkDev* d_w = nullptr;
+    long* d_first = nullptr;
+  };
+  std::vector<Small> small;
+  std::vector<char> shared_expm;  // per problem
+  cudaStream_t s_small = nullptr;
+  cudaEvent_t ev_small = nullptr;
 };
 
 static int batch_cuda(pgx_batch* b, cudaError_t e, const char* where) { return ctx_cuda(b->ctx, e, where); }
@@ -136,19 +153,58 @@ static int capture(pgx_batch* b, bool with_step, cudaGraphExec_t* out) {
   } count{b, c, l0, with_step};
   cudaStream_t s0 = c->stream;
   cudaGraph_t g = nullptr;
-  int st = batch_cuda(b, cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal), "begin capture");
+  int st = PGX_OK;
+  for (const auto& cl : b->small) {  // the problems' current device descriptors
+    const int n = (int)cl.idx.size();
+    std::vector<pgx::ProbDev> hp(n);
+    std::vector<pgx::WorkDev> hw(n);
+    std::vector<long> first(n + 1, 0);
+    for (int a = 0; a < n; ++a) {
+      const pgx_problem* p = b->probs[cl.idx[a]];
+      hp[a] = p->pd;
+      hw[a] = p->w;
+      hw[a].u = p->d_u;
+      // each problem's items start where the shared launch needs them
+      const long spw = pgx::expm_small_align(cl.Dp);
+      const long n_items = (long)p->desc.n_members * p->desc.n_slices;
+      first[a + 1] = first[a] + (n_items + spw - 1) / spw * spw;
+    }
+    if (!st) st = batch_cuda(b, cudaMemcpy(cl.d_p, hp.data(), sizeof(pgx::ProbDev) * n, cudaMemcpyHostToDevice), "upload");
+    if (!st) st = batch_cuda(b, cudaMemcpy(cl.d_w, hw.data(), sizeof(pgx::WorkDev) * n, cudaMemcpyHostToDevice), "upload");
+    if (!st) st = batch_cuda(b, cudaMemcpy(cl.d_first, first.data(), sizeof(long) * (n + 1), cudaMemcpyHostToDevice), "upload");
+  }
+  if (st) return st;
+  st = batch_cuda(b, cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal), "begin capture");
   if (st) return st;
   const int K = (int)b->streams.size();
   cudaEventRecord(b->events[0], s0);
   for (int k = 0; k < K; ++k) cudaStreamWaitEvent(b->streams[k], b->events[0], 0);
+  if (!b->small.empty()) {  // the shared small-dimension expm launches
+    cudaStreamWaitEvent(b->s_small, b->events[0], 0);
+    pgx::LaunchInfo li{c->num_sms, b->s_small, &c->launches};
+    for (const auto& cl : b->small) {
+      const long spw = pgx::expm_small_align(cl.Dp);
+      long items = 0;
+      for (int i : cl.idx)
+        items += ((long)b->probs[i]->desc.n_members * b->probs[i]->desc.n_slices + spw - 1) / spw * spw;
+      if (!st)
+        st = batch_cuda(b, pgx::launch_expm_small_set(cl.Dp, cl.d_p, cl.d_w, cl.d_first, (int)cl.idx.size(), items, li),
+                        "shared expm");
+    }
+    cudaEventRecord(b->ev_small, b->s_small);
+  }
   for (size_t j = 0; j < b->order.size() && !st; ++j) {
-    pgx_problem* p = b->probs[b->order[j]];
-    st = run_pipeline(p, p->d_u, p->d_F, p->d_G, b->streams[j % K]);
+    const int i = b->order[j];
+    pgx_problem* p = b->probs[i];
+    const bool shared = b->shared_expm[i] != 0;
+    if (shared) cudaStreamWaitEvent(b->streams[j % K], b->ev_small, 0);
+    st = run_pipeline(p, p->d_u, p->d_F, p->d_G, b->streams[j % K], shared);
   }
   for (int k = 0; k < K; ++k) {
     cudaEventRecord(b->events[1 + k], b->streams[k]);
     cudaStreamWaitEvent(s0, b->events[1 + k], 0);
   }
+  if (!b->small.empty()) cudaStreamWaitEvent(s0, b->ev_small, 0);
   const int n = (int)b->probs.size();
   if (!st) {
     if (with_step) k_ascent_step<<<n, kStepThreads, 0, s0>>>(b->step_args);
@@ -198,6 +254,24 @@ extern "C" int pgx_batch_create(pgx_ctx* c, int32_t n, pgx_problem* const* probl
     if (!st) st = batch_cuda(b, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
   for (auto& e : b->events)
     if (!st) st = batch_cuda(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  b->shared_expm.assign(n, 0);
+  for (int Dp : {2}) {  // the dimensions whose batches share the expm launch
+    pgx_batch::Small cl;
+    cl.Dp = Dp;
+    for (int i = 0; i < n; ++i)
+      if (problems[i]->desc.precision == PGX_PREC_MIXED && problems[i]->Dp == Dp) cl.idx.push_back(i);
+    if (cl.idx.empty()) continue;
+    const size_t k = cl.idx.size();
+    if (!st) st = batch_cuda(b, cudaMalloc((void**)&cl.d_p, sizeof(pgx::ProbDev) * k), "alloc");
+    if (!st) st = batch_cuda(b, cudaMalloc((void**)&cl.d_w, sizeof(pgx::WorkDev) * k), "alloc");
+    if (!st) st = batch_cuda(b, cudaMalloc((void**)&cl.d_first, sizeof(long) * (k + 1)), "alloc");
+    for (int i : cl.idx) b->shared_expm[i] = 1;
+    b->small.push_back(cl);
+  }
+  if (!b->small.empty()) {
+    if (!st) st = batch_cuda(b, cudaStreamCreateWithFlags(&b->s_small, cudaStreamNonBlocking), "stream");
+    if (!st) st = batch_cuda(b, cudaEventCreateWithFlags(&b->ev_small, cudaEventDisableTiming), "event");
+  }
   std::vector<double*> hu(n), hG(n), hF(n);
   std::vector<int> hl(n);
   for (int i = 0; i < n; ++i) {
@@ -235,6 +309,13 @@ extern "C" int pgx_batch_destroy(pgx_batch* b) {
     if (s) cudaStreamDestroy(s);
   for (auto e : b->events)
     if (e) cudaEventDestroy(e);
+  for (auto& cl : b->small) {
+    cudaFree(cl.d_p);
+    cudaFree(cl.d_w);
+    cudaFree(cl.d_first);
+  }
+  if (b->s_small) cudaStreamDestroy(b->s_small);
+  if (b->ev_small) cudaEventDestroy(b->ev_small);
   cudaFree(b->d_u);
   cudaFree(b->d_G);
   cudaFree(b->d_F);

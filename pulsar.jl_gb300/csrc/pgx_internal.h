@@ -187,6 +187,14 @@ bool tc_kernels_used(const ProbDev& p);
 int mixed_variants(const ProbDev& p, int kernel, int* out);
 int mixed_admitted(const ProbDev& p, int kernel, int* out);
 int mixed_default_team(const ProbDev& p, int kernel);
+// The df expm over the items of n mixed problems of padded dimension Dp = 2
+// (the only one batches share; device tables ps, ws; problem i's members x
+// slices items start at first[i], a multiple of expm_small_align(Dp);
+// items = first[n]): one launch for a batch's class, each unit computed as in
+// the problem's solo launch (the register-resident kernel).
+int expm_small_align(int Dp);
+cudaError_t launch_expm_small_set(int Dp, const ProbDev* ps, const WorkDev* ws, const long* first, int n,
+                                  long items, const LaunchInfo& li);
 // Error bits of the tensor-core kernels since the last call (the flags are
 // cleared): 1 = an MMA-completion wait gave up, 2 = a value beyond the FP16
 // operand limit of the gradient; 0 = none, -1 = a flag cannot be read.

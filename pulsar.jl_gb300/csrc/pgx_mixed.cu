@@ -84,29 +84,33 @@ __global__ void k_prep_mx(const double* u, float2* u_df, int n) {
 __device__ __forceinline__ df df_ld(const float2 v) { return {v.x, v.y}; }
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
 
-// A = c dt_k (drift + off O + scale sum_j u_jk C_j) in df.
+// Entry q (= r + D c) of A = c dt_k (drift + off O + tau_k R + scale
+// sum_j u_jk C_j) in df for member m, slice k; u(j) gives control j of slice
+// k as df.
+template <int D, class U>
+__device__ __forceinline__ dfc gen_entry_df(const ProbDev& p, int m, int k, int q, U u) {
+  const df dt = df_ld(p.dt_df[k]), sc = df_ld(p.m_scale_df[m]), off = df_ld(p.m_offset_df[m]);
+  const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
+  const int ro = p.n_ramp ? p.m_ramp[m] : -1;
+  dfc v = dfc_load(Gd[q]);
+  if (off.hi != 0.f) v = dfc_add(v, dfc_scale(dfc_load(p.offset_df[q]), off));
+  if (ro >= 0) v = dfc_add(v, dfc_scale(dfc_load(p.ramp_ops_df[(size_t)ro * D * D + q]), df_ld(p.tau_df[k])));
+  for (int j = 0; j < p.n_c; ++j) {
+    const df a = df_mul(sc, u(j));
+    v = dfc_add(v, dfc_scale(dfc_load(p.ctrls_df[(size_t)j * D * D + q]), a));
+  }
+  v = dfc_scale(v, dt);
+  if (p.gen == GEN_HERM) v = {v.im, df_neg(v.re)};  // times -i
+  return v;
+}
+
+// The whole A into a team's matrix (layout SW).
 template <int D, int T, int SW>
 __device__ __forceinline__ void build_A_df(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m,
                                            int k, float4* A) {
-  const df dt = df_ld(p.dt_df[k]), sc = df_ld(p.m_scale_df[m]), off = df_ld(p.m_offset_df[m]);
-  const bool has_off = off.hi != 0.f;
-  const float4* Gd = p.drifts_df + (size_t)p.m_drift[m] * D * D;
   const float2* uk = w.u_df + (size_t)k * p.n_c;
-  const int ro = p.n_ramp ? p.m_ramp[m] : -1;
-  const float4* Rm = ro >= 0 ? p.ramp_ops_df + (size_t)ro * D * D : nullptr;
-  const df tk = ro >= 0 ? df_ld(p.tau_df[k]) : df{0.f, 0.f};
-  for (int q = tm.lane; q < D * D; q += T) {
-    dfc v = dfc_load(Gd[q]);
-    if (has_off) v = dfc_add(v, dfc_scale(dfc_load(p.offset_df[q]), off));
-    if (Rm) v = dfc_add(v, dfc_scale(dfc_load(Rm[q]), tk));
-    for (int j = 0; j < p.n_c; ++j) {
-      const df a = df_mul(sc, df_ld(uk[j]));
-      v = dfc_add(v, dfc_scale(dfc_load(p.ctrls_df[(size_t)j * D * D + q]), a));
-    }
-    v = dfc_scale(v, dt);
-    if (p.gen == GEN_HERM) v = {v.im, df_neg(v.re)};  // times -i
-    A[Lay<D, SW>::idx(q % D, q / D)] = dfc_store(v);
-  }
+  const auto u = [=](int j) { return df_ld(uk[j]); };
+  for (int q = tm.lane; q < D * D; q += T) A[Lay<D, SW>::idx(q % D, q / D)] = dfc_store(gen_entry_df<D>(p, m, k, q, u));
 }
 
 // The same in FP32 from the FP32 copies of the constants (the leading halves
@@ -265,9 +269,56 @@ template <int D, int T> constexpr int expm_min_ctas() {
 // powers), kExpmLSym (Hermiticity-preserving superoperator at D = 64: half
 // of every product).
 enum { kExpmFull = 0, kExpmHerm = 1, kExpmLSym = 2 };
+// One unit (member m, slice k) of the df expm by one team; its five
+// workspace matrices at `base`, reduction scratch `red`.  U_DOUBLE: the
+// controls come from w.u (FP64) rounded to df here, with the same values as
+// the prologue's df copy w.u_df.
+template <int D, int T, int KIND, bool U_DOUBLE>
+__device__ __forceinline__ void expm_unit(const Team<T>& tm, const ProbDev& p, const WorkDev& w, int m, int k,
+                                          float4* base, float4* red) {
+  constexpr bool HERM = KIND == kExpmHerm, LSYM = KIND == kExpmLSym;
+  using G = CfgM<D, T>;
+  using L = Lay<D, kSwzExpm>;
+  float4* B = base;
+  float4* B2 = base + L::SIZE;
+  float4* B3 = base + 2 * L::SIZE;
+  float4* B4 = base + 3 * L::SIZE;
+  float4* Y = base + 4 * L::SIZE;
+  if constexpr (U_DOUBLE) {
+    const double* uk = w.u + (size_t)k * p.n_c;
+    const auto u = [=](int c) { return df_from(uk[c]); };
+    for (int q = tm.lane; q < D * D; q += T) B[L::idx(q % D, q / D)] = dfc_store(gen_entry_df<D>(p, m, k, q, u));
+  } else {
+    build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
+  }
+  tm.sync();
+  const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
+  const int pk = choose_expm_df<T>(tm, nrm, D, HERM && D >= 16, reinterpret_cast<int*>(red));
+  const int deg = pk & 31, q = (pk >> 5) & 7, s = (pk >> 8) & 63;
+  const int lo_from = (pk >> 16) >= 31 ? 1 << 30 : (pk >> 16);
+  if (s > 0) {  // B <- B / 2^s, exact in df
+    const float sc = ldexpf(1.f, -s);
+    for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry above
+      const int e = L::idx(q % D, q / D);
+      const float4 a = B[e];
+      B[e] = make_float4(a.x * sc, a.y * sc, a.z * sc, a.w * sc);
+    }
+    tm.sync();
+  }
+  taylor_exp_df<D, T, kSwzExpm, HERM, LSYM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
+  float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
+  if constexpr (G::SLAB) {
+    // the U stack streams out (gigabytes, read back from DRAM by the
+    // chains): evict-first stores keep the per-CTA Taylor slab in L2
+    for (int e = tm.lane; e < D * D; e += T) __stcs(out + e, Y[L::idx(e % D, e / D)]);
+  } else {
+    for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
+  }
+  tm.sync();
+}
+
 template <int D, int T, int KIND>
 __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_expm_mx(ProbDev p, WorkDev w) {
-  constexpr bool HERM = KIND == kExpmHerm, LSYM = KIND == kExpmLSym;
   using G = CfgM<D, T>;
   using L = Lay<D, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -279,41 +330,17 @@ __global__ void __launch_bounds__(CfgM<D, T>::THREADS, expm_min_ctas<D, T>()) k_
   else
     base = reinterpret_cast<float4*>(smem_raw + (size_t)team * G::WSE);
   float4* red = reinterpret_cast<float4*>(smem_raw + (G::SLAB ? 0 : G::TPC * G::WSE) + (size_t)team * G::RED);
-  float4* B = base;
-  float4* B2 = base + L::SIZE;
-  float4* B3 = base + 2 * L::SIZE;
-  float4* B4 = base + 3 * L::SIZE;
-  float4* Y = base + 4 * L::SIZE;
   const long items = (long)p.n_members * p.n_t;
-  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC) {
-    const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
-    build_A_df<D, T, kSwzExpm>(tm, p, w, m, k, B);
-    tm.sync();
-    const float nrm = norm1f<D, T, kSwzExpm>(tm, B, reinterpret_cast<float*>(red));
-    const int pk = choose_expm_df<T>(tm, nrm, D, HERM && D >= 16, reinterpret_cast<int*>(red));
-    const int deg = pk & 31, q = (pk >> 5) & 7, s = (pk >> 8) & 63;
-    const int lo_from = (pk >> 16) >= 31 ? 1 << 30 : (pk >> 16);
-    if (s > 0) {  // B <- B / 2^s, exact in df
-      const float sc = ldexpf(1.f, -s);
-      for (int q = tm.lane; q < D * D; q += T) {  // same lane wrote this entry in build_A_df
-        const int e = L::idx(q % D, q / D);
-        const float4 a = B[e];
-        B[e] = make_float4(a.x * sc, a.y * sc, a.z * sc, a.w * sc);
-      }
-      tm.sync();
-    }
-    taylor_exp_df<D, T, kSwzExpm, HERM, LSYM>(tm, B, B2, B3, B4, Y, deg, q, s, c_dfcoef, lo_from);
-    float4* out = reinterpret_cast<float4*>(w.U) + ((size_t)m * p.n_t + k) * D * D;
-    if constexpr (G::SLAB) {
-      // the U stack streams out (gigabytes, read back from DRAM by the
-      // chains): evict-first stores keep the per-CTA Taylor slab in L2
-      for (int e = tm.lane; e < D * D; e += T) __stcs(out + e, Y[L::idx(e % D, e / D)]);
-    } else {
-      for (int e = tm.lane; e < D * D; e += T) out[e] = Y[L::idx(e % D, e / D)];
-    }
-    tm.sync();
-  }
+  for (long it = (long)blockIdx.x * G::TPC + team; it < items; it += (long)gridDim.x * G::TPC)
+    expm_unit<D, T, KIND, false>(tm, p, w, (int)(it / p.n_t), (int)(it % p.n_t), base, red);
 }
+
+}  // namespace pgx
+
+// register-resident expm for D <= 8 (uses gen_entry_df, choose's tables, DfAcc)
+#include "pgx_small.cuh"
+
+namespace pgx {
 
 // ---- forward chain in df -------------------------------------------------------
 // U_total = P_n in FP64 from the df chain, the overlap z = Tr(T'U)/D in FP64,
@@ -1280,7 +1307,51 @@ static cudaError_t do_expm_oz64(const ProbDev& p, const WorkDev& w, const Launch
   ++*li.launches;
   return cudaGetLastError();
 }
+// The register-resident expm (D <= 8): 256-thread blocks walking the items in
+// warp-sized groups of slices, as many blocks as are resident at once.
+template <int D, bool MULTI>
+static cudaError_t do_expm_small(const sm::Set& set, const LaunchInfo& li) {
+  constexpr long kPerBlock = (sm::kSmallThreads / 32) * sm::Grp<D>::SPW;
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sm::k_expm_small<D, MULTI>, sm::kSmallThreads, 0);
+  long blocks = (set.items + kPerBlock - 1) / kPerBlock;
+  const long cap = (long)li.num_sms * (per_sm < 1 ? 1 : per_sm);
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  sm::k_expm_small<D, MULTI><<<(int)blocks, sm::kSmallThreads, 0, li.stream>>>(set);
+  ++*li.launches;
+  return cudaGetLastError();
+}
+// The register-resident kernel runs at D = 2 only.  Measured on GB300 in the
+// uneven batch's classes (one evaluation of all problems of a dimension):
+//   - D = 2: 4.3 -> 2.8 ms, with one shared launch for the class;
+//   - D = 4 and 8 lose: 5.7 -> 6.6 and 14.5 -> 85.7 ms.  A shuffle moves 4
+//     bytes per lane and instruction where a shared-memory broadcast moves
+//     16, and at D = 8 its 230 registers leave one block per SM.
+// The shared-memory teams of D = 4 and 8 in one shared launch per class were
+// slower as well (6.2 and 15.9 ms): the class's pipelines then wait for all
+// of its propagators instead of overlapping on the batch's streams.  So
+// batches share a launch only at D = 2.
+int expm_small_align(int Dp) { return Dp == 2 ? sm::Grp<2>::SPW : 1; }
+cudaError_t launch_expm_small_set(int Dp, const ProbDev* ps, const WorkDev* ws, const long* first, int n,
+                                  long items, const LaunchInfo& li) {
+  if (Dp != 2) return cudaErrorInvalidValue;
+  sm::Set set{};
+  set.ps = ps;
+  set.ws = ws;
+  set.first = first;
+  set.n = n;
+  set.items = items;
+  return do_expm_small<2, true>(set, li);
+}
 cudaError_t launch_expm_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
+  if (p.Dp == 2) {
+    sm::Set set{};
+    set.p0 = p;
+    set.w0 = w;
+    set.items = (long)p.n_members * p.n_t;
+    return do_expm_small<2, false>(set, li);
+  }
   const int t = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p, kTuneExpmMx);
   if (t == kTeamTensor) {
     if (!expm_tc_eligible(p)) return cudaErrorInvalidValue;

@@ -742,7 +742,7 @@ static int apply_penalties(pgx_problem* p, const WorkDev& w, bool want_grad, con
                   "penalties");
 }
 
-int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream) {
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream, bool skip_expm) {
   pgx_ctx* c = p->ctx;
   pgx::LaunchInfo li = p->launch_info();
   if (stream) li.stream = stream;  // batches enqueue on their own (captured) streams
@@ -756,7 +756,7 @@ int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cu
   if (p->desc.precision == PGX_PREC_MIXED) {
     mk.mark(PGX_STAGE_EXPM);
     if ((st = ctx_cuda(c, pgx::launch_prep_mx(p->pd, w, li), "prep_mx"))) return st;
-    if ((st = ctx_cuda(c, pgx::launch_expm_mx(p->pd, w, li), "expm_mx"))) return st;
+    if (!skip_expm && (st = ctx_cuda(c, pgx::launch_expm_mx(p->pd, w, li), "expm_mx"))) return st;
     mk.mark(PGX_STAGE_CHAIN_FWD);
     if (want_grad && p->split_grad_states) {
       // F from states_init; gradient from grad_states_init (Gradients.jl:153-157)

@@ -93,5 +93,8 @@ cudaError_t launch_penalties(const pgx_penalty* d_pens, int n_pen, const double*
                              int n_t, double* F, double* G, const LaunchInfo& li);
 }  // namespace pgx
 // Enqueues one evaluation; stream = nullptr means the context stream.
-int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream = nullptr);
+// skip_expm: the slice propagators of d_u are already in p->w.U (a batch's
+// shared launch wrote them).
+int run_pipeline(pgx_problem* p, const double* d_u, double* d_F, double* d_G, cudaStream_t stream = nullptr,
+                 bool skip_expm = false);
 int eval_host(pgx_problem* p, const double* u, double* F, double* G, pgx_eval_stats* stats);

@@ -35,14 +35,16 @@ def test_mixed_random_gate(pg, mode, d):
     p.close()
 
 
+@pytest.mark.parametrize("d", [2, 8, 16])
 @pytest.mark.parametrize("target_norm", [0.004, 0.03, 0.1, 0.16, 0.4, 1.5, 6.0])
-def test_mixed_expm_schedules_across_norms(pg, target_norm):
+def test_mixed_expm_schedules_across_norms(pg, target_norm, d):
     """The df expm picks its Paterson-Stockmeyer block size (2, 3, 4), degree
     and squarings per slice from ||A||_1: these norms walk through each kind
     of schedule (q = 2 at the smallest, q = 3 degree 9, q = 4 degree 12 / 16,
-    squarings at the largest).  F stays at df accuracy against the oracle."""
-    rng = np.random.default_rng(int(1e4 * target_norm))
-    d = 16
+    squarings at the largest).  F stays at df accuracy against the oracle,
+    for the register-resident kernel (d = 2, 8: one slice per 2 and per 16
+    lanes) and the shared-memory teams (d = 16)."""
+    rng = np.random.default_rng(int(1e4 * target_norm) + d)
     prob, u0 = random_gate_problem(rng, d, n_t=12, n_members=2, dt=1.0)
     A = [prob.drifts[0] + sum(u0[j, k] * prob.controls[j] for j in range(prob.n_c)) for k in range(prob.n_t)]
     nrm = max(np.abs(a).sum(axis=0).max() for a in A)
@@ -53,6 +55,18 @@ def test_mixed_expm_schedules_across_norms(pg, target_norm):
     dF, _ = check(F, G, Fo, Go)
     assert dF <= 1e-12, dF
     p.close()
+
+
+def test_mixed_one_qubit_lindblad_register_path(pg):
+    """A 1-qubit Lindblad gate (D = 4 superoperators, non-Hermitian): the
+    register-resident expm against the FP64 oracle."""
+    prob, u0 = fx.lindblad_gate(n_qubits=1, n_t=20, n_draws=3)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F, G = p.eval(u0)
+    p.close()
+    Fo, Go = mb.eval_problem(prob, u0, "exact")
+    dF, dG = check(F, G, Fo, Go)
+    print(f"1-qubit Lindblad mixed: |dF| = {dF:.2e}, grad rel = {dG:.2e}")
 
 
 def test_mixed_lindblad_superoperator(pg):

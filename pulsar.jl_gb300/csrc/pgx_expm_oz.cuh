@@ -438,4 +438,138 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
   }
 }
 
+// The parallel-in-time forward chain's in-block prefix products at D = 64 on
+// the same engine: per (member m, block b of slices k0 .. k1-1) P_k0 = I,
+// P_{k+1} = U_k P_k in df; with `store` the FP32 rounding of every P_k
+// (k0 <= k < k1) for the gradient; the block product P_k1 into pit_tot.
+// P_{k0+1} = U_k0 is taken as is.  Each step stages P_k as the right factor
+// and multiplies U_k (left, this worker's values) into it; U_{k+1} is parked
+// in shared memory while the step's MMAs run.  Same CTA shape, barriers and
+// bounded waits as k_expm_oz64; a CTA that gives up NaN-poisons the block
+// products of its remaining items.
+__global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbDev p, WorkDev w, int store) {
+  using namespace oz;
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_bar[4];
+  __shared__ float s_red[16];
+  __shared__ int s_cmd[2];
+  const uint32_t pad = (tc::kSmemAlign - (tc::smem_u32(smem_raw) & (tc::kSmemAlign - 1))) & (tc::kSmemAlign - 1);
+  Engine g;
+  g.bsl = smem_raw + pad;
+  g.abuf = g.bsl + kSlices * kBSlice;
+  g.ci = reinterpret_cast<float2*>(g.abuf + 2 * kASlice);  // here: the parked U_{k+1}
+  g.red = s_red;
+  g.cmd = s_cmd;
+  g.par = 0;
+  g.seq = 0;
+  g.abort = false;
+  g.eph[0] = g.eph[1] = 0;
+  g.pend[0] = g.pend[1] = 0;
+  for (int b = 0; b < 2; ++b) {
+    g.full[b] = tc::smem_u32(&s_bar[b]);
+    g.empty[b] = tc::smem_u32(&s_bar[2 + b]);
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(&s_tmem, tc::kTmemCols);
+  if (threadIdx.x == 0)
+    for (int b = 0; b < 4; ++b) tc::mbar_init(tc::smem_u32(&s_bar[b]));
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  g.tmem = s_tmem;
+  if (threadIdx.x >= kWorkers) {
+    if (threadIdx.x == kWorkers) issue_loop(g);
+    __syncwarp();
+  } else {
+    const Lane l = tc::lane_of();
+    const long items = (long)p.n_members * w.pit_blocks;
+    // this worker's entries e = i + 64 c of a 4096-entry matrix
+    const auto entry = [&](int c) { return (size_t)(l.i + 64 * (l.c0 + c)); };
+    long it = blockIdx.x;
+    for (; it < items; it += gridDim.x) {
+      const int m = (int)(it / w.pit_blocks), b = (int)(it % w.pit_blocks);
+      const int k0 = b * w.pit_len, k1 = min(p.n_t, k0 + w.pit_len);
+      const float4* Um = reinterpret_cast<const float4*>(w.U) + (size_t)m * p.n_t * 4096;
+      float* Pst = reinterpret_cast<float*>(w.P) + (size_t)m * p.n_t * 4096 * 2;  // float2 {re, im} per entry
+      float xh[32], xl[32], uh[32], ul[32];
+      if (store) {  // P_k0 = I
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          Pst[((size_t)k0 * 4096 + entry(c)) * 2 + l.im] = (l.im == 0 && l.i == l.c0 + c) ? 1.f : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {  // x = P_{k0+1} = U_k0
+        const float4 v = Um[(size_t)k0 * 4096 + entry(c)];
+        xh[c] = l.im ? v.y : v.x;
+        xl[c] = l.im ? v.w : v.z;
+      }
+      bool ok = true;
+      bool parked = false;
+#pragma unroll 1
+      for (int k = k0 + 1; k <= k1 && ok; ++k) {  // x holds P_k
+        if (store && k < k1)
+#pragma unroll
+          for (int c = 0; c < 32; ++c) Pst[((size_t)k * 4096 + entry(c)) * 2 + l.im] = xh[c];
+        if (k == k1) break;
+        const int eR = stage_right(g, l, xh, xl);  // P_k
+        if (parked) {
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            const float2 v = g.ci[c * kWorkers + threadIdx.x];
+            uh[c] = v.x;
+            ul[c] = v.y;
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            const float4 v = Um[(size_t)k * 4096 + entry(c)];
+            uh[c] = l.im ? v.y : v.x;
+            ul[c] = l.im ? v.w : v.z;
+          }
+        }
+        parked = k + 1 < k1;
+        const auto park = [&] {  // U_{k+1} into shared memory while the MMAs run
+          if (k + 1 < k1)
+#pragma unroll 8
+            for (int c = 0; c < 32; ++c) {
+              const float4 v = Um[(size_t)(k + 1) * 4096 + entry(c)];
+              g.ci[c * kWorkers + threadIdx.x] = l.im ? make_float2(v.y, v.w) : make_float2(v.x, v.z);
+            }
+        };
+        ok = product(g, l, uh, ul, eR, false, park);  // U_k P_k
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          xh[c] = uh[c];
+          xl[c] = ul[c];
+        }
+      }
+      if (!ok) break;
+      float* tot = reinterpret_cast<float*>(w.pit_tot + ((size_t)m * w.pit_blocks + b) * 4096);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        tot[entry(c) * 4 + l.im] = xh[c];
+        tot[entry(c) * 4 + 2 + l.im] = xl[c];
+      }
+    }
+    if (g.abort) {
+      const float nan = __int_as_float(0x7fffffff);
+      for (; it < items; it += gridDim.x) {
+        float* tot = reinterpret_cast<float*>(w.pit_tot + (size_t)it * 4096);
+        for (int e = threadIdx.x; e < 4096 * 4; e += kWorkers) tot[e] = nan;
+      }
+      if (threadIdx.x == 0) atomicOr(&g_expm_tc_timeout, 1);
+    }
+    wsync();
+    if (threadIdx.x == 0) hand_over(g, -1);
+    drain(g, 0);
+    drain(g, 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(g.tmem, tc::kTmemCols);
+  }
+}
+
 }  // namespace pgx

@@ -1386,13 +1386,22 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
     ++*li.launches;
     return cudaGetLastError();
   }
-  const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float4);
-  auto local = k_chainf_local_mx<D, false>;
-  if constexpr (D == 64 && G::T == 256)
-    if (p.lsym) local = k_chainf_local_mx<D, true>;
-  ensure_smem_mx(local, smem_l);
-  const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
-  local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
+  const int expm_team = li.team[kTuneExpmMx] ? li.team[kTuneExpmMx] : mixed_default_team(p, kTuneExpmMx);
+  if (D == 64 && expm_team == kTeamTensor) {
+    // the in-block prefixes on the tensor-core expm's engine (pgx_expm_oz.cuh)
+    ensure_smem_mx(k_chainf_local_oz64, oz::kExpmSmem);
+    const long items = (long)p.n_members * w.pit_blocks;
+    k_chainf_local_oz64<<<items < li.num_sms ? (int)items : li.num_sms, oz::kExpmThreads, oz::kExpmSmem,
+                          li.stream>>>(p, w, store);
+  } else {
+    const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float4);
+    auto local = k_chainf_local_mx<D, false>;
+    if constexpr (D == 64 && G::T == 256)
+      if (p.lsym) local = k_chainf_local_mx<D, true>;
+    ensure_smem_mx(local, smem_l);
+    const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
+    local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
+  }
   const size_t smem_c = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
   auto combine = k_chainf_combine_mx<D, false>;
   if constexpr (D == 64 && G::T == 256)

@@ -76,9 +76,12 @@ TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
            ("spin4", "mixed", "expm"): 5 * (0.095232e6 + 127.364352e6),
            ("spin4", "mixed", "grad"): 5 * (94.700544e6 + 2.850816e6),
            ("spin4", "mixed", "chain_fwd"): 5 * (189.268736e6 + 67.549952e6),
-           # k_expm_mx<64,256,LSym>, 100-slice capture: the per-CTA slabs' L2
-           # write-backs come on top of the 210 MB U stack
-           ("lindblad3q", "mixed", "expm"): 5 * (46.415360e6 + 964.345600e6)}
+           # k_expm_oz64 (tensor cores), 100-slice capture: the prologue's planar
+           # generator read once, the df U stack written once
+           ("lindblad3q", "mixed", "expm"): 5 * (210.639104e6 + 194.420224e6)}
+# Slice pairs of one df product on the sliced-bf16 tensor-core engine (levels
+# 0..6): the tensor pipe executes this many times the product's model FLOPs.
+OZ_PAIRS = 26
 # FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
 # accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
 # busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).
@@ -844,9 +847,14 @@ def main():
             dom_ms = stages[dom] / max(n_rec, 1)
             achieved = wl.stage_flops(dom) / (dom_ms * 1e-3)
             share = {k: round(v / max(sum(stages.values()), 1e-30), 4) for k, v in stages.items()}
+            # at padded dimension 64 the mixed expm runs on the tensor cores by
+            # default (team 1): the prologue plus the sliced-bf16 kernel
+            tc_expm = pipe == "fp32" and dom == "expm" and wl.p.teams[0] == 1
             kname = ("k_" + dom) if pipe == "fp64" else {"expm": "k_expm_mx", "chain_fwd": "k_chain_gate_fwd_mx",
                                                          "chain_bwd": "k_chain_gate_bwd_mx",
                                                          "grad": "k_grad_gate_mx", "reduce": "k_reduce"}[dom]
+            if tc_expm:
+                kname = "k_expm_prep_oz64 + k_expm_oz64"
             roof = {"kernel": kname, "ms_per_launch": dom_ms, "stage_share": share,
                     "traffic": TRAFFIC.get((args.workload, args.precision, dom))}
             pr = wl.prob
@@ -858,6 +866,7 @@ def main():
                           "note": "model = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 (K_exp = 8); executed "
                                   "counts the one Frechet derivative per slice the gradient runs"}
         else:
+            tc_expm = False
             achieved = wl.total_flops() * (units / wl.units_per_step) / (ms * 1e-3)
             roof = {"kernel": "whole batched iteration (CUDA graph)", "ms_per_launch": ms / (args.steps + 1),
                     "traffic": None}
@@ -871,7 +880,13 @@ def main():
                                             f"{pipe.upper()} pipe",
                      "flop_model": "conventional per-unit W = 8 D^3 (K_exp (1 + 2 n_c) + 3) + 8 n_c D^2 "
                                    "(K_exp = 8) split by stage"})
-        if args.precision == "mixed" and single and dom in ("expm", "chain_fwd"):
+        if single and tc_expm:
+            roof.update({"pipe": "tensor cores (tcgen05, df products by exact bf16 slicing)",
+                         "tensor_executed_tflops": achieved * OZ_PAIRS / 1e12,
+                         "tensor_executed_frac": achieved * OZ_PAIRS / peak,
+                         "tensor_note": f"each df product is {OZ_PAIRS} bf16 slice-pair products on the tensor "
+                                        "pipe: tensor_executed = achieved model FLOP/s x that count"})
+        elif args.precision == "mixed" and single and dom in ("expm", "chain_fwd"):
             # df32 stages: each model FLOP costs DF_OPS_PER_CMAC / 8 FP32 operations
             eff = pipe_peak / (DF_OPS_PER_CMAC / 8.0)
             roof.update({"df32_effective_peak": eff / 1e12, "frac_of_df32_effective": achieved / eff,

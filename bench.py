@@ -79,9 +79,9 @@ TRAFFIC = {("spin4", "fp64", "grad"): 5 * (190.615296e6 + 4.743936e6),
            # k_expm_oz64 (tensor cores), 100-slice capture: the prologue's planar
            # generator read once, the df U stack written once
            ("lindblad3q", "mixed", "expm"): 5 * (210.639104e6 + 194.420224e6)}
-# Slice pairs of one df product on the sliced-bf16 tensor-core engine (levels
-# 0..6): the tensor pipe executes this many times the product's model FLOPs.
-OZ_PAIRS = 26
+# Tensor-pipe activity of k_expm_oz64 from an ncu capture (lindblad3q, 100 of
+# 500 slices): sm__pipe_tensor_cycles_active, % of peak while active.
+TENSOR_ACTIVE_PCT = {("lindblad3q", "mixed", "expm"): 17.3}
 # FP32 operations one df32 complex MAC executes (error-free two_prod / two_sum
 # accumulation) per 8 FLOPs of the FP64 model: the model-FLOP rate a fully
 # busy FP32 pipe could reach on df32 work is the FP32 peak / (DF_OPS / 8).
@@ -882,10 +882,10 @@ def main():
                                    "(K_exp = 8) split by stage"})
         if single and tc_expm:
             roof.update({"pipe": "tensor cores (tcgen05, df products by exact bf16 slicing)",
-                         "tensor_executed_tflops": achieved * OZ_PAIRS / 1e12,
-                         "tensor_executed_frac": achieved * OZ_PAIRS / peak,
-                         "tensor_note": f"each df product is {OZ_PAIRS} bf16 slice-pair products on the tensor "
-                                        "pipe: tensor_executed = achieved model FLOP/s x that count"})
+                         "tensor_pipe_active_pct_ncu": TENSOR_ACTIVE_PCT.get((args.workload, args.precision, dom)),
+                         "tensor_note": "each df product runs 26 bf16 slice-pair products (12 MMAs of N = 128 and "
+                                        "2 of N = 64 per K step group); achieved counts model FLOPs, so frac "
+                                        "is the df-product rate against the bf16 peak"})
         elif args.precision == "mixed" and single and dom in ("expm", "chain_fwd"):
             # df32 stages: each model FLOP costs DF_OPS_PER_CMAC / 8 FP32 operations
             eff = pipe_peak / (DF_OPS_PER_CMAC / 8.0)

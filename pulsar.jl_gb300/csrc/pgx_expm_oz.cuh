@@ -248,6 +248,55 @@ __device__ __forceinline__ void store_own(float4* own, int mat, const float (&h)
     own[(16 * mat + cp) * kWorkers + threadIdx.x] = make_float4(h[2 * cp], lo[2 * cp], h[2 * cp + 1], lo[2 * cp + 1]);
 }
 
+// Shared-memory carve-up, TMEM, barriers and the engine state of a CTA of the
+// sliced engine's kernels (kExpmThreads threads, kExpmSmem dynamic bytes).
+struct CtaStatic {
+  uint32_t tmem;
+  uint64_t bar[4];
+  float red[16];
+  int cmd[2];
+};
+__device__ __forceinline__ void engine_setup(Engine& g, uint8_t* smem_raw, CtaStatic& st) {
+  const uint32_t pad = (tc::kSmemAlign - (tc::smem_u32(smem_raw) & (tc::kSmemAlign - 1))) & (tc::kSmemAlign - 1);
+  g.bsl = smem_raw + pad;
+  g.abuf = g.bsl + kSlices * kBSlice;
+  g.ci = reinterpret_cast<float2*>(g.abuf + 2 * kASlice);
+  g.red = st.red;
+  g.cmd = st.cmd;
+  g.par = 0;
+  g.seq = 0;
+  g.abort = false;
+  g.eph[0] = g.eph[1] = 0;
+  g.pend[0] = g.pend[1] = 0;
+  for (int b = 0; b < 2; ++b) {
+    g.full[b] = tc::smem_u32(&st.bar[b]);
+    g.empty[b] = tc::smem_u32(&st.bar[2 + b]);
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(&st.tmem, tc::kTmemCols);
+  if (threadIdx.x == 0)
+    for (int b = 0; b < 4; ++b) tc::mbar_init(tc::smem_u32(&st.bar[b]));
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  g.tmem = st.tmem;
+}
+// Workers: stop the issuer, then (bounded) let the groups in flight finish.
+__device__ __forceinline__ void workers_finish(Engine& g) {
+  wsync();
+  if (threadIdx.x == 0) hand_over(g, -1);
+  drain(g, 0);
+  drain(g, 1);
+}
+// Every thread: frees TMEM once workers and issuer are done.
+__device__ __forceinline__ void engine_teardown(Engine& g) {
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(g.tmem, tc::kTmemCols);
+  }
+}
+
 }  // namespace oz
 
 // Flag of the tensor-core expm: a completion wait gave up (its units are
@@ -291,35 +340,10 @@ constexpr size_t kExpmPrepSmem = (size_t)Lay<64, kSwzExpm>::SIZE * sizeof(float4
 // 168 registers per thread.
 __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, WorkDev w) {
   using namespace oz;
-  using L = Lay<64, kSwzExpm>;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bar[4];
-  __shared__ float s_red[16];
-  __shared__ int s_cmd[2];
-  const uint32_t pad = (tc::kSmemAlign - (tc::smem_u32(smem_raw) & (tc::kSmemAlign - 1))) & (tc::kSmemAlign - 1);
+  __shared__ CtaStatic st;
   Engine g;
-  g.bsl = smem_raw + pad;
-  g.abuf = g.bsl + kSlices * kBSlice;
-  g.ci = reinterpret_cast<float2*>(g.abuf + 2 * kASlice);
-  g.red = s_red;
-  g.cmd = s_cmd;
-  g.par = 0;
-  g.seq = 0;
-  g.abort = false;
-  g.eph[0] = g.eph[1] = 0;
-  g.pend[0] = g.pend[1] = 0;
-  for (int b = 0; b < 2; ++b) {
-    g.full[b] = tc::smem_u32(&s_bar[b]);
-    g.empty[b] = tc::smem_u32(&s_bar[2 + b]);
-  }
-  if (threadIdx.x < 32) tc::tmem_alloc(&s_tmem, tc::kTmemCols);
-  if (threadIdx.x == 0)
-    for (int b = 0; b < 4; ++b) tc::mbar_init(tc::smem_u32(&s_bar[b]));
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  g.tmem = s_tmem;
+  engine_setup(g, smem_raw, st);
   if (threadIdx.x >= kWorkers) {  // the issuing warp
     if (threadIdx.x == kWorkers) issue_loop(g);
     __syncwarp();
@@ -349,7 +373,8 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
       // The products of the unit, at one call site (one copy of the
       // product's code), in place on x:
       //   powers:  B^2 = B B (st 0), B^3 = B^2 B (st 1), B^4 = B^2 B^2 (st 2);
-      //   then x = B^q becomes the right factor and Y = C_{L-1} + c_m B^q;
+      //   then x = B^q becomes the right factor and Y = C_{L-1} + c_m B^q
+      //   (C_{L-1} parked during the last power product);
       //   Horner:  Y <- Y B^q + C_i, i = L-2 .. 0;
       //   squarings: Y <- Y Y.
       const int n_pow = q - 1, n_hor = nL - 1, n_steps = n_pow + n_hor + s;
@@ -375,21 +400,19 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
           if (q == 3) store_own(own, 2, xh, xl);
           eR = stage_right(g, l, xh, xl);
 #pragma unroll
-          for (int cp = 0; cp < 16; ++cp) {
-            df v0, v1;
-            block_pair(nL - 1, q, l.i, l.c0, l.im == 0, own, cp, c_dfcoef, v0, v1);
-            v0 = df_add(v0, df_mul(df{xh[2 * cp], xl[2 * cp]}, c_dfcoef[deg]));
-            v1 = df_add(v1, df_mul(df{xh[2 * cp + 1], xl[2 * cp + 1]}, c_dfcoef[deg]));
-            xh[2 * cp] = v0.hi;
-            xl[2 * cp] = v0.lo;
-            xh[2 * cp + 1] = v1.hi;
-            xl[2 * cp + 1] = v1.lo;
+          for (int c = 0; c < 32; ++c) {  // C_{L-1} was parked during the last power product
+            const float2 a = g.ci[c * kWorkers + threadIdx.x];
+            const df v = df_add(df{a.x, a.y}, df_mul(df{xh[c], xl[c]}, c_dfcoef[deg]));
+            xh[c] = v.hi;
+            xl[c] = v.lo;
           }
         }
         if (st == n_steps) break;
         if (st == 0 || st >= n_pow + n_hor) eR = stage_right(g, l, xh, xl);  // B; or a squaring's Y
-        if (st >= n_pow && st < n_pow + n_hor) {
-          const int i = n_pow + n_hor - 1 - st;
+        // the last power product parks C_{L-1} (B^1 .. B^{q-1} are known), each
+        // Horner step the next block
+        if ((st >= n_pow && st < n_pow + n_hor) || st == n_pow - 1) {
+          const int i = st == n_pow - 1 ? nL - 1 : n_pow + n_hor - 1 - st;
           const auto park = [&] {  // C_i into shared memory while the MMAs run
 #pragma unroll 4
             for (int cp = 0; cp < 16; ++cp) {
@@ -399,7 +422,7 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
               g.ci[(2 * cp + 1) * kWorkers + threadIdx.x] = make_float2(v1.hi, v1.lo);
             }
           };
-          ok = product(g, l, xh, xl, eR, true, park);
+          ok = product(g, l, xh, xl, eR, st != n_pow - 1, park);
         } else {
           ok = product(g, l, xh, xl, eR, false, nop);
         }
@@ -423,19 +446,9 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
       }
       if (threadIdx.x == 0) atomicOr(&g_expm_tc_timeout, 1);
     }
-    // stop the issuer; then, bounded, let the groups in flight finish before
-    // TMEM is freed
-    wsync();
-    if (threadIdx.x == 0) hand_over(g, -1);
-    drain(g, 0);
-    drain(g, 1);
+    workers_finish(g);
   }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    tc::fence_after_sync();
-    tc::tmem_dealloc(g.tmem, tc::kTmemCols);
-  }
+  engine_teardown(g);
 }
 
 // The parallel-in-time forward chain's in-block prefix products at D = 64 on
@@ -450,33 +463,9 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
 __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbDev p, WorkDev w, int store) {
   using namespace oz;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bar[4];
-  __shared__ float s_red[16];
-  __shared__ int s_cmd[2];
-  const uint32_t pad = (tc::kSmemAlign - (tc::smem_u32(smem_raw) & (tc::kSmemAlign - 1))) & (tc::kSmemAlign - 1);
+  __shared__ CtaStatic st;
   Engine g;
-  g.bsl = smem_raw + pad;
-  g.abuf = g.bsl + kSlices * kBSlice;
-  g.ci = reinterpret_cast<float2*>(g.abuf + 2 * kASlice);  // here: the parked U_{k+1}
-  g.red = s_red;
-  g.cmd = s_cmd;
-  g.par = 0;
-  g.seq = 0;
-  g.abort = false;
-  g.eph[0] = g.eph[1] = 0;
-  g.pend[0] = g.pend[1] = 0;
-  for (int b = 0; b < 2; ++b) {
-    g.full[b] = tc::smem_u32(&s_bar[b]);
-    g.empty[b] = tc::smem_u32(&s_bar[2 + b]);
-  }
-  if (threadIdx.x < 32) tc::tmem_alloc(&s_tmem, tc::kTmemCols);
-  if (threadIdx.x == 0)
-    for (int b = 0; b < 4; ++b) tc::mbar_init(tc::smem_u32(&s_bar[b]));
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  g.tmem = s_tmem;
+  engine_setup(g, smem_raw, st);  // g.ci holds the parked U_{k+1}
   if (threadIdx.x >= kWorkers) {
     if (threadIdx.x == kWorkers) issue_loop(g);
     __syncwarp();
@@ -559,17 +548,82 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
       }
       if (threadIdx.x == 0) atomicOr(&g_expm_tc_timeout, 1);
     }
-    wsync();
-    if (threadIdx.x == 0) hand_over(g, -1);
-    drain(g, 0);
-    drain(g, 1);
+    workers_finish(g);
   }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    tc::fence_after_sync();
-    tc::tmem_dealloc(g.tmem, tc::kTmemCols);
+  engine_teardown(g);
+}
+
+// The parallel-in-time forward chain's combine at D = 64 on the same engine:
+// per member P = I, then for each block b in order pit_pre[b] = P (FP32, when
+// `store`) and P <- T_b P in df (T_0 I = T_0 as is); then the CUDA-core
+// kernel's epilogue (U_total in FP64, the overlap, f and the chain-rule
+// coefficient) on P copied into shared memory.  A CTA that gives up
+// NaN-poisons the objective of its remaining members.
+__global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_combine_oz64(ProbDev p, WorkDev w, int store) {
+  using namespace oz;
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ CtaStatic st;
+  Engine g;
+  engine_setup(g, smem_raw, st);
+  if (threadIdx.x >= kWorkers) {
+    if (threadIdx.x == kWorkers) issue_loop(g);
+    __syncwarp();
+  } else {
+    const Lane l = tc::lane_of();
+    const Team<256> tm{(int)threadIdx.x, 1};           // the workers' barrier
+    float4* Pc = reinterpret_cast<float4*>(g.ci);       // 64 KB: P for the epilogue
+    double2* red = reinterpret_cast<double2*>(g.abuf);  // the epilogue's scratch (idle slice buffers)
+    const auto entry = [&](int c) { return (size_t)(l.i + 64 * (l.c0 + c)); };
+    const auto nop = [] {};
+    int m = blockIdx.x;
+    for (; m < p.n_members; m += gridDim.x) {
+      float xh[32], xl[32], uh[32], ul[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {  // P = I
+        xh[c] = (l.im == 0 && l.i == l.c0 + c) ? 1.f : 0.f;
+        xl[c] = 0.f;
+      }
+      bool ok = true;
+#pragma unroll 1
+      for (int b = 0; b < w.pit_blocks && ok; ++b) {
+        const float4* tot = w.pit_tot + ((size_t)m * w.pit_blocks + b) * 4096;
+        if (store) {
+          float* pre = reinterpret_cast<float*>(w.pit_pre + ((size_t)m * w.pit_blocks + b) * 4096);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) pre[entry(c) * 2 + l.im] = xh[c];
+        }
+        const int eR = b > 0 ? stage_right(g, l, xh, xl) : 0;  // P
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          const float4 v = tot[entry(c)];
+          uh[c] = l.im ? v.y : v.x;
+          ul[c] = l.im ? v.w : v.z;
+        }
+        if (b > 0) ok = product(g, l, uh, ul, eR, false, nop);  // T_b P
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          xh[c] = uh[c];
+          xl[c] = ul[c];
+        }
+      }
+      if (!ok) break;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        float* f = reinterpret_cast<float*>(Pc + entry(c));
+        f[l.im] = xh[c];
+        f[2 + l.im] = xl[c];
+      }
+      wsync();
+      chain_epilogue_mx<64, 256>(tm, p, w, m, Pc, red);
+      wsync();  // P and the scratch are read before the next member reuses them
+    }
+    if (g.abort && threadIdx.x == 0) {
+      for (; m < p.n_members; m += gridDim.x) w.Fm[m] = __longlong_as_double(0x7ff8000000000000LL);
+      atomicOr(&g_expm_tc_timeout, 1);
+    }
+    workers_finish(g);
   }
+  engine_teardown(g);
 }
 
 }  // namespace pgx

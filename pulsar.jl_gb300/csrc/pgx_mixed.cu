@@ -1402,12 +1402,18 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
     const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
     local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
   }
-  const size_t smem_c = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
-  auto combine = k_chainf_combine_mx<D, false>;
-  if constexpr (D == 64 && G::T == 256)
-    if (p.lsym) combine = k_chainf_combine_mx<D, true>;
-  ensure_smem_mx(combine, smem_c);
-  combine<<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
+  if (D == 64 && expm_team == kTeamTensor) {
+    ensure_smem_mx(k_chainf_combine_oz64, oz::kExpmSmem);
+    k_chainf_combine_oz64<<<p.n_members < li.num_sms ? p.n_members : li.num_sms, oz::kExpmThreads,
+                            oz::kExpmSmem, li.stream>>>(p, w, store);
+  } else {
+    const size_t smem_c = (size_t)G::TPC * (2 * D * D + G::T) * sizeof(float4);
+    auto combine = k_chainf_combine_mx<D, false>;
+    if constexpr (D == 64 && G::T == 256)
+      if (p.lsym) combine = k_chainf_combine_mx<D, true>;
+    ensure_smem_mx(combine, smem_c);
+    combine<<<(p.n_members + G::TPC - 1) / G::TPC, G::THREADS, smem_c, li.stream>>>(p, w, store);
+  }
   *li.launches += 2;
   if (store && p.n_t > w.pit_len) {
     if constexpr (D == 64) {  // tensor cores (pgx_fix_tc.cuh)

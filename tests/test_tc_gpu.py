@@ -330,3 +330,40 @@ def test_tc_expm_lindblad_and_state_targets(pg):
     F2, _ = ps.eval(u1)
     ps.close()
     assert abs(F1 - F2) <= 1e-11, (F1, F2)
+
+
+def test_tc_expm_and_chains_f_only_evaluation_matches(pg):
+    """An F-only evaluation (no prefix stores, as the optimisers' line
+    searches run) through the tensor-core expm and chain kernels gives the F
+    of the full evaluation, bit for bit."""
+    prob, u0 = fx.lindblad_3q(n_t=60, n_draws=3)
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    F_full, _ = p.eval(u0)
+    F_only, G = p.eval(u0, want_grad=False)
+    p.close()
+    assert G is None and F_only == F_full
+
+
+def test_context_released_by_its_last_problem():
+    """Closing a context while problems still point to it only marks it
+    closing; the last problem's destruction releases it (a fresh process, so
+    the check does not depend on other tests' contexts)."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    code = (
+        "import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+        "import numpy as np, __graft_entry__ as ge\n"
+        "pg = ge.load_package()\n"
+        "from test_parity_gpu import random_gate_problem, to_gpu\n"
+        "ctx = pg.Context(0)\n"
+        "prob, u0 = random_gate_problem(np.random.default_rng(2), 4, n_t=4, n_members=2)\n"
+        "ps = [to_gpu(pg, prob, 'exact', ctx=ctx) for _ in range(2)]\n"
+        "F0, _ = ps[0].eval(np.zeros((2, 4)))\n"
+        "ctx.close()\n"
+        "F1, _ = ps[1].eval(np.zeros((2, 4)))\n"
+        "assert F1 == F0\n"
+        "ps[0].close(); ps[1].close(); print('ok')\n" % (str(root), str(root / "tests")))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.stdout[-500:], r.stderr[-2000:])

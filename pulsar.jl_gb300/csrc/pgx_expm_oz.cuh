@@ -252,7 +252,7 @@ __device__ __forceinline__ void store_own(float4* own, int mat, const float (&h)
 // sliced engine's kernels (kExpmThreads threads, kExpmSmem dynamic bytes).
 struct CtaStatic {
   uint32_t tmem;
-  uint64_t bar[4];
+  uint64_t bar[5];  // full[2], empty[2], and the chain kernels' operand copies
   float red[16];
   int cmd[2];
 };
@@ -274,11 +274,30 @@ __device__ __forceinline__ void engine_setup(Engine& g, uint8_t* smem_raw, CtaSt
   }
   if (threadIdx.x < 32) tc::tmem_alloc(&st.tmem, tc::kTmemCols);
   if (threadIdx.x == 0)
-    for (int b = 0; b < 4; ++b) tc::mbar_init(tc::smem_u32(&st.bar[b]));
+    for (int b = 0; b < 5; ++b) tc::mbar_init(tc::smem_u32(&st.bar[b]));
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   g.tmem = st.tmem;
+}
+
+// The chain kernels' next left factor (one 64 KB df matrix, contiguous in
+// HBM) into g.ci by two bulk copies (TMA) on barrier `mbar`; issued by worker
+// 0 once every worker has read the previous one.
+__device__ __forceinline__ void fetch_left(Engine& g, uint32_t mbar, const float4* src) {
+  tc::mbar_expect_tx(mbar, 65536u);
+  tc::tma_bulk_copy(tc::smem_u32(g.ci), src, 32768u, mbar);
+  tc::tma_bulk_copy(tc::smem_u32(g.ci) + 32768u, reinterpret_cast<const uint8_t*>(src) + 32768, 32768u, mbar);
+}
+// This worker's values of the fetched matrix (after waiting for the copy).
+__device__ __forceinline__ void read_left(const Engine& g, const Lane& l, float (&h)[32], float (&lo)[32]) {
+  const float4* M = reinterpret_cast<const float4*>(g.ci);
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const float4 v = M[l.i + 64 * (l.c0 + c)];
+    h[c] = l.im ? v.y : v.x;
+    lo[c] = l.im ? v.w : v.z;
+  }
 }
 // Workers: stop the issuer, then (bounded) let the groups in flight finish.
 __device__ __forceinline__ void workers_finish(Engine& g) {
@@ -456,8 +475,8 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_expm_oz64(ProbDev p, Wo
 // P_{k+1} = U_k P_k in df; with `store` the FP32 rounding of every P_k
 // (k0 <= k < k1) for the gradient; the block product P_k1 into pit_tot.
 // P_{k0+1} = U_k0 is taken as is.  Each step stages P_k as the right factor
-// and multiplies U_k (left, this worker's values) into it; U_{k+1} is parked
-// in shared memory while the step's MMAs run.  Same CTA shape, barriers and
+// and multiplies U_k (left, this worker's values) into it; U_{k+1} arrives in
+// shared memory by TMA bulk copies while the step's MMAs run.  Same CTA shape, barriers and
 // bounded waits as k_expm_oz64; a CTA that gives up NaN-poisons the block
 // products of its remaining items.
 __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbDev p, WorkDev w, int store) {
@@ -465,13 +484,16 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
   extern __shared__ uint8_t smem_raw[];
   __shared__ CtaStatic st;
   Engine g;
-  engine_setup(g, smem_raw, st);  // g.ci holds the parked U_{k+1}
+  engine_setup(g, smem_raw, st);  // g.ci receives U_{k+1}
   if (threadIdx.x >= kWorkers) {
     if (threadIdx.x == kWorkers) issue_loop(g);
     __syncwarp();
   } else {
     const Lane l = tc::lane_of();
     const long items = (long)p.n_members * w.pit_blocks;
+    const uint32_t tbar = tc::smem_u32(&st.bar[4]);
+    uint32_t tph = 0;
+    int tpend = 0;  // operand copies issued and not yet waited for
     // this worker's entries e = i + 64 c of a 4096-entry matrix
     const auto entry = [&](int c) { return (size_t)(l.i + 64 * (l.c0 + c)); };
     long it = blockIdx.x;
@@ -493,7 +515,10 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
         xl[c] = l.im ? v.w : v.z;
       }
       bool ok = true;
-      bool parked = false;
+      if (k0 + 1 < k1) {  // U_{k0+1} by TMA
+        if (threadIdx.x == 0) fetch_left(g, tbar, Um + (size_t)(k0 + 1) * 4096);
+        ++tpend;
+      }
 #pragma unroll 1
       for (int k = k0 + 1; k <= k1 && ok; ++k) {  // x holds P_k
         if (store && k < k1)
@@ -501,31 +526,22 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
           for (int c = 0; c < 32; ++c) Pst[((size_t)k * 4096 + entry(c)) * 2 + l.im] = xh[c];
         if (k == k1) break;
         const int eR = stage_right(g, l, xh, xl);  // P_k
-        if (parked) {
-#pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const float2 v = g.ci[c * kWorkers + threadIdx.x];
-            uh[c] = v.x;
-            ul[c] = v.y;
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const float4 v = Um[(size_t)k * 4096 + entry(c)];
-            uh[c] = l.im ? v.y : v.x;
-            ul[c] = l.im ? v.w : v.z;
-          }
+        const bool got = tc::mbar_wait(tbar, tph);  // U_k in shared memory
+        if (wsync_or(!got)) {
+          g.abort = true;
+          ok = false;
+          break;
         }
-        parked = k + 1 < k1;
-        const auto park = [&] {  // U_{k+1} into shared memory while the MMAs run
-          if (k + 1 < k1)
-#pragma unroll 8
-            for (int c = 0; c < 32; ++c) {
-              const float4 v = Um[(size_t)(k + 1) * 4096 + entry(c)];
-              g.ci[c * kWorkers + threadIdx.x] = l.im ? make_float2(v.y, v.w) : make_float2(v.x, v.z);
-            }
+        tph ^= 1;
+        --tpend;
+        read_left(g, l, uh, ul);
+        const auto prefetch = [&] {  // U_{k+1} while the MMAs run: every worker has read U_k
+          if (k + 1 < k1) {
+            if (threadIdx.x == 0) fetch_left(g, tbar, Um + (size_t)(k + 1) * 4096);
+            ++tpend;
+          }
         };
-        ok = product(g, l, uh, ul, eR, false, park);  // U_k P_k
+        ok = product(g, l, uh, ul, eR, false, prefetch);  // U_k P_k
 #pragma unroll
         for (int c = 0; c < 32; ++c) {
           xh[c] = uh[c];
@@ -547,6 +563,7 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
         for (int e = threadIdx.x; e < 4096 * 4; e += kWorkers) tot[e] = nan;
       }
       if (threadIdx.x == 0) atomicOr(&g_expm_tc_timeout, 1);
+      if (tpend > 0) tc::mbar_wait(tbar, tph);  // bounded: the copy in flight lands before the CTA ends
     }
     workers_finish(g);
   }
@@ -555,7 +572,8 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_local_oz64(ProbD
 
 // The parallel-in-time forward chain's combine at D = 64 on the same engine:
 // per member P = I, then for each block b in order pit_pre[b] = P (FP32, when
-// `store`) and P <- T_b P in df (T_0 I = T_0 as is); then the CUDA-core
+// `store`) and P <- T_b P in df (T_0 I = T_0 as is; T_{b+1} arrives by TMA
+// bulk copies while step b's MMAs run); then the CUDA-core
 // kernel's epilogue (U_total in FP64, the overlap, f and the chain-rule
 // coefficient) on P copied into shared memory.  A CTA that gives up
 // NaN-poisons the objective of its remaining members.
@@ -574,7 +592,9 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_combine_oz64(Pro
     float4* Pc = reinterpret_cast<float4*>(g.ci);       // 64 KB: P for the epilogue
     double2* red = reinterpret_cast<double2*>(g.abuf);  // the epilogue's scratch (idle slice buffers)
     const auto entry = [&](int c) { return (size_t)(l.i + 64 * (l.c0 + c)); };
-    const auto nop = [] {};
+    const uint32_t tbar = tc::smem_u32(&st.bar[4]);
+    uint32_t tph = 0;
+    int tpend = 0;  // operand copies issued and not yet waited for
     int m = blockIdx.x;
     for (; m < p.n_members; m += gridDim.x) {
       float xh[32], xl[32], uh[32], ul[32];
@@ -584,22 +604,46 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_combine_oz64(Pro
         xl[c] = 0.f;
       }
       bool ok = true;
+      const float4* Tm = w.pit_tot + (size_t)m * w.pit_blocks * 4096;
+      if (store) {  // pit_pre[0] = I
+        float* pre = reinterpret_cast<float*>(w.pit_pre + (size_t)m * w.pit_blocks * 4096);
+#pragma unroll
+        for (int c = 0; c < 32; ++c) pre[entry(c) * 2 + l.im] = xh[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {  // P = T_0 I = T_0
+        const float4 v = Tm[entry(c)];
+        xh[c] = l.im ? v.y : v.x;
+        xl[c] = l.im ? v.w : v.z;
+      }
+      if (w.pit_blocks > 1) {  // T_1 by TMA
+        if (threadIdx.x == 0) fetch_left(g, tbar, Tm + 4096);
+        ++tpend;
+      }
 #pragma unroll 1
-      for (int b = 0; b < w.pit_blocks && ok; ++b) {
-        const float4* tot = w.pit_tot + ((size_t)m * w.pit_blocks + b) * 4096;
+      for (int b = 1; b < w.pit_blocks && ok; ++b) {
         if (store) {
           float* pre = reinterpret_cast<float*>(w.pit_pre + ((size_t)m * w.pit_blocks + b) * 4096);
 #pragma unroll
           for (int c = 0; c < 32; ++c) pre[entry(c) * 2 + l.im] = xh[c];
         }
-        const int eR = b > 0 ? stage_right(g, l, xh, xl) : 0;  // P
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          const float4 v = tot[entry(c)];
-          uh[c] = l.im ? v.y : v.x;
-          ul[c] = l.im ? v.w : v.z;
+        const int eR = stage_right(g, l, xh, xl);  // P
+        const bool got = tc::mbar_wait(tbar, tph);  // T_b in shared memory
+        if (wsync_or(!got)) {
+          g.abort = true;
+          ok = false;
+          break;
         }
-        if (b > 0) ok = product(g, l, uh, ul, eR, false, nop);  // T_b P
+        tph ^= 1;
+        --tpend;
+        read_left(g, l, uh, ul);
+        const auto prefetch = [&] {  // T_{b+1} while the MMAs run: every worker has read T_b
+          if (b + 1 < w.pit_blocks) {
+            if (threadIdx.x == 0) fetch_left(g, tbar, Tm + (size_t)(b + 1) * 4096);
+            ++tpend;
+          }
+        };
+        ok = product(g, l, uh, ul, eR, false, prefetch);  // T_b P
 #pragma unroll
         for (int c = 0; c < 32; ++c) {
           xh[c] = uh[c];
@@ -615,12 +659,14 @@ __global__ void __launch_bounds__(oz::kExpmThreads, 1) k_chainf_combine_oz64(Pro
       }
       wsync();
       chain_epilogue_mx<64, 256>(tm, p, w, m, Pc, red);
+      tc::fence_smem_to_async();  // these writes to g.ci before the next member's copies into it
       wsync();  // P and the scratch are read before the next member reuses them
     }
     if (g.abort && threadIdx.x == 0) {
       for (; m < p.n_members; m += gridDim.x) w.Fm[m] = __longlong_as_double(0x7ff8000000000000LL);
       atomicOr(&g_expm_tc_timeout, 1);
     }
+    if (g.abort && tpend > 0) tc::mbar_wait(tbar, tph);  // bounded: the copy in flight lands first
     workers_finish(g);
   }
   engine_teardown(g);

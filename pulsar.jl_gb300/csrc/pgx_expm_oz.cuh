@@ -175,9 +175,8 @@ __device__ __forceinline__ bool product(Engine& g, const Lane& l, float (&h)[32]
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     float Lv[kExpmLevels][8];
-#pragma unroll
-    for (int lv = 0; lv < kExpmLevels; ++lv)
-      tmem_ld8(g.tmem + l.lane_addr + (uint32_t)(64 * lv + l.c0 + 8 * q), Lv[lv]);
+    static_assert(kExpmLevels == 7, "one load batch per level set");
+    tmem_ld8x7(g.tmem + l.lane_addr + (uint32_t)(l.c0 + 8 * q), Lv);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       float L[kExpmLevels];

@@ -158,6 +158,89 @@ __device__ __forceinline__ void mm1(const Team<T>& tm, C* out, const C* A, const
   mm<D, T, false, SW>(tm, out, A, B, (const C*)nullptr, (const C*)nullptr, EpiNone{});
 }
 
+// One pass over k of the product pair below: Q always, P when WITH_P.
+template <int D, int T, int SW, bool WITH_P, class C, class EpiP, class EpiQ>
+__device__ __forceinline__ void mm_pair_pass(const Team<T>& tm, C* outP, C* outQ, const C* A, const C* dA,
+                                             const C* Bm, const C* dBm, EpiP epiP, EpiQ epiQ) {
+  using BK = Blocking<D, T>;
+  using L = Lay<D, SW>;
+  constexpr int RB = BK::RB, CB = BK::CB;
+  const bool active = tm.lane < BK::ACTIVE;
+  const int rb = tm.lane % BK::NR, cb = tm.lane / BK::NR;
+  C p[RB][CB], q[RB][CB];
+#pragma unroll
+  for (int i = 0; i < RB; ++i)
+#pragma unroll
+    for (int j = 0; j < CB; ++j) {
+      p[i][j] = czero<C>();
+      q[i][j] = czero<C>();
+    }
+  if (active) {
+#pragma unroll 1
+    for (int k = 0; k < D; ++k) {
+      C a[RB], da[RB], b[CB], db[CB];
+#pragma unroll
+      for (int i = 0; i < RB; ++i) {
+        const int e = L::idx(rb + BK::NR * i, k);
+        a[i] = A[e];
+        da[i] = dA[e];
+      }
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int e = L::idx(k, cb + BK::NCB * j);
+        b[j] = Bm[e];
+        db[j] = dBm[e];
+      }
+#pragma unroll
+      for (int i = 0; i < RB; ++i)
+#pragma unroll
+        for (int j = 0; j < CB; ++j) {
+          q[i][j] = cmac(q[i][j], da[i], b[j]);
+          q[i][j] = cmac(q[i][j], a[i], db[j]);
+          if constexpr (WITH_P) p[i][j] = cmac(p[i][j], a[i], b[j]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int r = rb + BK::NR * i, c = cb + BK::NCB * j, e = L::idx(r, c);
+        if constexpr (WITH_P) p[i][j] = epiP(e, r, c, p[i][j]);
+        q[i][j] = epiQ(e, r, c, q[i][j]);
+      }
+  }
+  tm.sync();
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int e = L::idx(rb + BK::NR * i, cb + BK::NCB * j);
+        if constexpr (WITH_P) outP[e] = p[i][j];
+        outQ[e] = q[i][j];
+      }
+  }
+  tm.sync();
+}
+
+// The product pair of a Frechet step: P = A Bm and Q = dA Bm + A dBm (the
+// derivative of A Bm along dA, dBm), then epiP / epiQ as in mm; outputs may
+// alias inputs.  Q adds dA Bm before A dBm at every k, on every path, so the
+// result does not depend on the team size.  With at most 8 outputs per lane
+// both products run in one pass over k that loads A[., k] and Bm[k, .] once
+// for both; beyond that the registers allow only Q's pass and then P's (outQ
+// never aliases A or Bm, which are all that P reads).
+template <int D, int T, int SW, class C, class EpiP, class EpiQ>
+__device__ __forceinline__ void mm_frechet(const Team<T>& tm, C* outP, C* outQ, const C* A, const C* dA,
+                                           const C* Bm, const C* dBm, EpiP epiP, EpiQ epiQ) {
+  if constexpr (Blocking<D, T>::NE <= 8) {
+    mm_pair_pass<D, T, SW, true>(tm, outP, outQ, A, dA, Bm, dBm, epiP, epiQ);
+  } else {
+    mm_pair_pass<D, T, SW, false>(tm, outP, outQ, A, dA, Bm, dBm, epiP, epiQ);
+    mm<D, T, false, SW>(tm, outP, A, Bm, (const C*)nullptr, (const C*)nullptr, epiP);
+  }
+}
+
 template <int D, int T, class C>
 __device__ __forceinline__ void copy_mat(const Team<T>& tm, C* dst, const C* src) {
   for (int e = tm.lane; e < D * D; e += T) dst[e] = src[e];
@@ -351,8 +434,7 @@ template <class C, int D, int S = D * D> struct Work2 {
 // q = 4, in six matrices instead of ten.
 template <int D, int T, int SW = 0, class C, int S, class R>
 __device__ void taylor_exp_frechet2(const Team<T>& tm, const Work2<C, D, S>& w, int m, int s, const R* invf) {
-  mm1<D, T, SW>(tm, w.X, w.B, w.B);
-  mm<D, T, true, SW>(tm, w.dX, w.B, w.dB, w.dB, w.B, EpiNone{});
+  mm_frechet<D, T, SW>(tm, w.X, w.dX, w.B, w.dB, w.B, w.dB, EpiNone{}, EpiNone{});
   const int L = m / 2;
   for (int q = tm.lane; q < D * D; q += T) {
     const int r = q % D, c = q / D, e = Lay<D, SW>::idx(r, c);
@@ -365,18 +447,17 @@ __device__ void taylor_exp_frechet2(const Team<T>& tm, const Work2<C, D, S>& w, 
   for (int i = L - 2; i >= 0; --i) {
     const C* B = w.B;
     const C* dB = w.dB;
-    mm<D, T, true, SW>(tm, w.dY, w.dX, w.Y, w.X, w.dY,
-                       [=](int e, int, int, C v) { return cadd(v, cscale(dB[e], invf[2 * i + 1])); });
-    mm<D, T, false, SW>(tm, w.Y, w.X, w.Y, (const C*)nullptr, (const C*)nullptr, [=](int e, int r, int c, C v) {
-      C t = cadd(v, cscale(B[e], invf[2 * i + 1]));
-      if (r == c) t.x += invf[2 * i];
-      return t;
-    });
+    // Y <- X Y + C_i and dY <- dX Y + X dY + dC_i (both from the old Y, dY)
+    mm_frechet<D, T, SW>(
+        tm, w.Y, w.dY, w.X, w.dX, w.Y, w.dY,
+        [=](int e, int r, int c, C v) {
+          C t = cadd(v, cscale(B[e], invf[2 * i + 1]));
+          if (r == c) t.x += invf[2 * i];
+          return t;
+        },
+        [=](int e, int, int, C v) { return cadd(v, cscale(dB[e], invf[2 * i + 1])); });
   }
-  for (int k = 0; k < s; ++k) {
-    mm<D, T, true, SW>(tm, w.dY, w.Y, w.dY, w.dY, w.Y, EpiNone{});
-    mm1<D, T, SW>(tm, w.Y, w.Y, w.Y);
-  }
+  for (int k = 0; k < s; ++k) mm_frechet<D, T, SW>(tm, w.Y, w.dY, w.Y, w.dY, w.Y, w.dY, EpiNone{}, EpiNone{});
 }
 
 }  // namespace pgx

@@ -677,14 +677,25 @@ __device__ __forceinline__ void load_hi(const Team<T>& tm, float2* dst, const fl
   }
 }
 
+// Teams of the backward chain's in-block suffixes.  They run on a side
+// stream beside the df forward prefixes, so the fewest SMs serve them best:
+// one warp per (member, block) chain at D = 16 (spin-4 evaluation 20.68 ->
+// 20.82 M units/s against T = 256; T = 64 and 128 were slower).
+template <int D> struct SufCfg {
+  static constexpr int T = (D == 16) ? 32 : Cfg<D>::T;
+  static constexpr int TPC = (D <= 8) ? Cfg<D>::TPC : (T >= 256 ? 1 : 256 / T);
+  static constexpr int THREADS = T * TPC;
+};
+
 template <int D>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainb_local_mx(ProbDev p, WorkDev w) {
-  using G = Cfg<D>;
+__global__ void __launch_bounds__(SufCfg<D>::THREADS) k_chainb_local_mx(ProbDev p, WorkDev w) {
+  using G = SufCfg<D>;
   constexpr int T = G::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* smem = reinterpret_cast<float2*>(smem_raw);
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
+  Team<T> tm{(int)(threadIdx.x % T)};
+  tm.bar = (T > 32 && G::TPC > 1) ? 1 + team : 0;
   float2* R = smem + (size_t)team * 2 * D * D;
   float2* Ub = R + D * D;
   const long items = (long)p.n_members * w.pit_blocks;
@@ -1446,7 +1457,7 @@ cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Launch
 // forward chain runs.
 template <int D>
 static cudaError_t do_chain_bwd_local_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li) {
-  using G = Cfg<D>;
+  using G = SufCfg<D>;
   const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float2);
   ensure_smem_mx(k_chainb_local_mx<D>, smem_l);
   const int grid_l = grid_for(k_chainb_local_mx<D>, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC,

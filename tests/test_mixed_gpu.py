@@ -181,6 +181,27 @@ def test_autotune_keeps_results_bit_identical(pg, d):
     p.close()
 
 
+@pytest.mark.parametrize("d,teams", [(16, (32, 64, 128, 256)), (32, (128, 256)), (64, (256, 512))])
+def test_gradient_team_sizes_bit_identical(pg, d, teams):
+    """Every CUDA-core gradient team gives the same bits: the Frechet product
+    pairs run in one pass over k up to 8 outputs per lane (d = 16 at T = 32,
+    d = 64 at T = 512) and in two passes beyond (d = 64 at T = 256), with the
+    same order of terms."""
+    rng = np.random.default_rng(900 + d)
+    prob, u0 = random_gate_problem(rng, d, n_t=8, n_members=3, dt=0.3 / np.sqrt(d))
+    p = to_gpu(pg, prob, "exact", precision="mixed")
+    ref = None
+    for t in teams:
+        p.set_teams(grad=t)
+        assert p.teams[1] == t
+        F, G = p.eval(u0)
+        if ref is None:
+            ref = (F, G)
+        else:
+            assert F == ref[0] and np.array_equal(G, ref[1]), t
+    p.close()
+
+
 MODES = ("ref_grape", "ref_mr", "exact")
 
 

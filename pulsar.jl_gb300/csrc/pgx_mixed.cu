@@ -428,15 +428,26 @@ __global__ void __launch_bounds__(kRefThreads) k_refine_unitary_mx(ProbDev p, Wo
 //           consumes P in FP32).
 // LSYM (D = 64, Hermiticity-preserving superoperators): the prefix products
 // keep half of each product (mm_df_lsym).
+// Teams of the in-block prefixes.  At D = 16, 64-thread teams (2 x 2
+// blocks, 79 registers: 12 teams per SM) over about 7 (member, block) chains
+// per SM (the runtime's block count) balance the SMs better than one
+// 256-thread team per chain: spin-4 20.85 -> 21.08 M units/s.
+template <int D> struct PreCfg {
+  static constexpr int T = (D == 16) ? 64 : Cfg<D>::T;
+  static constexpr int TPC = (D <= 8) ? Cfg<D>::TPC : (T >= 256 ? 1 : 256 / T);
+  static constexpr int THREADS = T * TPC;
+};
+
 template <int D, bool LSYM>
-__global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_local_mx(ProbDev p, WorkDev w, int store) {
-  using G = Cfg<D>;
+__global__ void __launch_bounds__(PreCfg<D>::THREADS) k_chainf_local_mx(ProbDev p, WorkDev w, int store) {
+  using G = PreCfg<D>;
   constexpr int T = G::T;
   constexpr int NE = (D * D + T - 1) / T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float4* smem = reinterpret_cast<float4*>(smem_raw);
   const int team = threadIdx.x / T;
-  const Team<T> tm{(int)(threadIdx.x % T)};
+  Team<T> tm{(int)(threadIdx.x % T)};
+  tm.bar = (T > 32 && G::TPC > 1) ? 1 + team : 0;
   float4* Pc = smem + (size_t)team * (2 * D * D);
   float4* Ub = Pc + D * D;
   const long items = (long)p.n_members * w.pit_blocks;
@@ -1407,13 +1418,14 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
     k_chainf_local_oz64<<<items < li.num_sms ? (int)items : li.num_sms, oz::kExpmThreads, oz::kExpmSmem,
                           li.stream>>>(p, w, store);
   } else {
-    const size_t smem_l = (size_t)G::TPC * 2 * D * D * sizeof(float4);
+    using PC = PreCfg<D>;
+    const size_t smem_l = (size_t)PC::TPC * 2 * D * D * sizeof(float4);
     auto local = k_chainf_local_mx<D, false>;
-    if constexpr (D == 64 && G::T == 256)
+    if constexpr (D == 64 && PC::T == 256)
       if (p.lsym) local = k_chainf_local_mx<D, true>;
     ensure_smem_mx(local, smem_l);
-    const int grid_l = grid_for(local, G::THREADS, smem_l, (long)p.n_members * w.pit_blocks, G::TPC, li.num_sms, 0);
-    local<<<grid_l, G::THREADS, smem_l, li.stream>>>(p, w, store);
+    const int grid_l = grid_for(local, PC::THREADS, smem_l, (long)p.n_members * w.pit_blocks, PC::TPC, li.num_sms, 0);
+    local<<<grid_l, PC::THREADS, smem_l, li.stream>>>(p, w, store);
   }
   if (D == 64 && expm_team == kTeamTensor) {
     ensure_smem_mx(k_chainf_combine_oz64, oz::kExpmSmem);

@@ -345,13 +345,15 @@ static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
 }
 
 // Blocks of the parallel-in-time mixed gate chain: enough (member, block)
-// teams to fill the GPU (about 4 teams of 256 threads per SM, 16 warp-teams at
-// Dp <= 8), blocks of at least 8 slices; 1 = the sequential chain.
+// chains to fill the GPU without a second wave of the prefix kernel (about 4
+// teams of 256 threads per SM from D = 32, 7 of the 12 64-thread teams an SM
+// holds at D = 16, 16 warp-teams at Dp <= 8), blocks of at least 8 slices;
+// 1 = the sequential chain.
 static void pit_shape(const pgx_problem_desc* d, int Dp, int num_sms, int* blocks, int* len) {
   *blocks = 1;
   *len = d->n_slices;
   if (d->precision != PGX_PREC_MIXED || d->target != PGX_TARGET_GATE) return;
-  const long target = (long)(Dp <= 8 ? 16 : 4) * num_sms;
+  const long target = (long)(Dp <= 8 ? 16 : Dp == 16 ? 7 : 4) * num_sms;
   long b = (target + d->n_members - 1) / d->n_members;
   b = std::min<long>(b, std::max(1, d->n_slices / 8));
   if (b <= 1) return;

@@ -239,3 +239,64 @@ def test_frechet_spectral_matches_scipy():
     L1 = mb.frechet_exp(A, E, (H, dt))
     L2 = mb.frechet_exp(A, E)
     assert np.max(np.abs(L1 - L2)) < 1e-12 * max(1.0, np.max(np.abs(L2)))
+
+
+# --- test/Physics/PhysicsValidation.jl (textbook results) -----------------------
+# The pulse sequences below are the reference tests' own; PHYS_* build them
+# once for these oracle checks and for the device checks in
+# tests/test_physics_kats_gpu.py.
+
+RABI_OMEGA = 2 * np.pi * 1e5                                   # :285
+ECHO_T_FREE = 5e-6                                            # :55
+ECHO_DOMEGA = (0.0, 1e3, 5e3, -3e3, 10e3)                     # :54
+
+
+def phys_rabi(theta: float):
+    """One slice of H = Omega sigma_x / 2 for the pulse area theta (:284-308):
+    a state-transfer problem |0> -> |1>, square fidelity = P1."""
+    prob = mb.Problem(drifts=np.zeros((1, 2, 2), complex), controls=(SX / 2)[None],
+                      dt=np.array([theta / RABI_OMEGA]), target="states", fidelity="square",
+                      states_init=np.array([[1, 0]], complex), states_target=np.array([[0, 1]], complex))
+    return prob, np.array([[RABI_OMEGA]])
+
+
+def phys_echo(domega: float):
+    """pi/2 - free - pi - free - pi/2 about x, free precession domega sigma_z,
+    each interval T_free (:50-73), as five slices with controls (sigma_x,
+    sigma_z); square fidelity |<1|psi>|^2 = P1."""
+    T = ECHO_T_FREE
+    u = np.array([[np.pi / 4 / T, 0.0, np.pi / 2 / T, 0.0, np.pi / 4 / T],
+                  [0.0, domega, 0.0, domega, 0.0]])
+    prob = mb.Problem(drifts=np.zeros((1, 2, 2), complex), controls=np.stack([SX, SZ]), dt=np.full(5, T),
+                      target="states", fidelity="square", states_init=np.array([[1, 0]], complex),
+                      states_target=np.array([[0, 1]], complex))
+    return prob, u
+
+
+def test_pi_pulse_and_two_half_pi_pulses_flip_the_qubit():     # :24-48
+    psi0 = np.array([1, 0], complex)
+    out = rs.expm_neg_i(np.pi / 2 * SX, 1.0) @ psi0
+    assert abs(out[0]) ** 2 < 1e-10 and abs(abs(out[1]) ** 2 - 1) < 1e-10
+    Uh = rs.expm_neg_i(np.pi / 4 * SX, 1.0)
+    out2 = Uh @ (Uh @ psi0)
+    assert abs(out2[0]) ** 2 < 1e-10 and abs(abs(out2[1]) ** 2 - 1) < 1e-10
+
+
+def test_x_rotation_is_the_not_gate():                         # :104-106
+    U = rs.expm_neg_i(np.pi / 2 * SX, 1.0)
+    assert abs(rs.gate_fidelity(U, SX) - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("theta,p1", [(np.pi, 1.0), (2 * np.pi, 0.0), (np.pi / 2, 0.5)])
+def test_rabi_populations(theta, p1):                          # :280-308
+    prob, u = phys_rabi(theta)
+    F, _ = mb.eval_problem(prob, u, want_grad=False)
+    assert abs(F - p1) < 1e-10
+
+
+def test_spin_echo_refocuses_every_offset():                   # :50-73
+    F0 = mb.eval_problem(*phys_echo(0.0), want_grad=False)[0]
+    assert abs(F0) < 1e-10  # a net 2 pi rotation about x: back in |0>
+    for dw in ECHO_DOMEGA[1:]:
+        F = mb.eval_problem(*phys_echo(dw), want_grad=False)[0]
+        assert abs(F - F0) < 1e-6

@@ -309,3 +309,25 @@ def test_drift_ramp_mixed_and_validation(pg, ctx):
             p.set_drift_ramp(ops + 1j * np.eye(16), mo, tau)     # not Hermitian
         assert e.value.status == 1
         p.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ensemble_aggregators_reference_samples(pg, precision):
+    """EnsembleTests.jl:33-62 on the device: four qubits whose gate fidelities
+    to the identity are the reference test's samples 0.9, 0.8, 0.7, 0.6 (an x
+    rotation by theta has F = cos^2(theta / 2)), aggregated by :mean,
+    :worst_case and :cvar with alpha = 0.5."""
+    samples = np.array([0.9, 0.8, 0.7, 0.6])
+    theta = 2 * np.arccos(np.sqrt(samples))
+    sx = np.array([[0, 1], [1, 0]], complex)
+    systems = [pg.quantum_system(np.zeros((2, 2), complex), [t * sx / 2]) for t in theta]
+    cs = pg.ControlSequence(np.ones((1, 1)), 1.0)
+    tgt = pg.unitary_target(np.eye(2, dtype=complex))
+    got = {}
+    for agg in ("mean", "worst_case", "cvar"):
+        obj = pg.build_ensemble_from_systems(systems, tgt, cs, aggregator=agg, precision=precision, cvar_alpha=0.5)
+        got[agg] = obj.value(np.ones(1))
+    assert abs(got["mean"] - samples.mean()) < 1e-12
+    assert abs(got["worst_case"] - 0.6) < 1e-12
+    assert abs(got["cvar"] - (0.6 + 0.7) / 2) < 1e-12
+    assert got["worst_case"] <= got["cvar"] <= got["mean"] + 1e-12

@@ -300,3 +300,17 @@ def test_spin_echo_refocuses_every_offset():                   # :50-73
     for dw in ECHO_DOMEGA[1:]:
         F = mb.eval_problem(*phys_echo(dw), want_grad=False)[0]
         assert abs(F - F0) < 1e-6
+
+
+# --- test/Algorithms/EnsembleTests.jl "aggregator correctness" (:33-62) ------
+
+def test_ensemble_aggregators_on_synthetic_samples():
+    offsets = [0.9, 0.8, 0.7, 0.6]
+    grads = [np.array([1.0, 0.0]) for _ in offsets]
+    F_m, G_m = rs.aggregate(offsets, grads, "mean")
+    F_wc, G_wc = rs.aggregate(offsets, grads, "worst_case")
+    F_cv, _ = rs.aggregate(offsets, grads, "cvar", 0.5)
+    assert abs(F_m - sum(offsets) / 4) < 1e-15 and np.allclose(G_m, [1.0, 0.0])
+    assert F_wc == min(offsets) and np.allclose(G_wc, [1.0, 0.0])
+    assert abs(F_cv - (0.6 + 0.7) / 2) < 1e-15
+    assert F_wc <= F_cv <= F_m + 1e-12

@@ -187,6 +187,10 @@ bool tc_kernels_used(const ProbDev& p);
 int mixed_variants(const ProbDev& p, int kernel, int* out);
 int mixed_admitted(const ProbDev& p, int kernel, int* out);
 int mixed_default_team(const ProbDev& p, int kernel);
+// (member, block) prefix chains of the mixed gate chain that the GPU holds at
+// once (the CUDA-core prefix kernel at its occupancy on the current device,
+// times num_sms); 0 when Dp has no such kernel here (Dp > 32).
+long chain_prefix_capacity(int Dp, int num_sms);
 // The df expm over the items of n mixed problems of padded dimension Dp = 2
 // (the only one batches share; device tables ps, ws; problem i's members x
 // slices items start at first[i], a multiple of expm_small_align(Dp);

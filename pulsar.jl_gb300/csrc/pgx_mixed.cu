@@ -15,6 +15,7 @@
 //              table) and traces; results accumulated as FP64.
 // F therefore carries df (~1e-13 per product) rounding; G carries FP32
 // (~1e-6 relative) rounding.
+#include <atomic>
 #include <type_traits>
 
 #include "pgx_df.cuh"
@@ -1462,6 +1463,35 @@ static cudaError_t do_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const Lau
 cudaError_t launch_chain_fwd_mx(const ProbDev& p, const WorkDev& w, const LaunchInfo& li, bool store) {
   PGX_DISPATCH_MX(p.Dp, return do_chain_fwd_mx<D_>(p, w, li, store));
   return cudaSuccess;
+}
+
+// Prefix teams one SM holds (queried once per dimension; the same on every
+// device of one architecture).
+template <int D>
+static long prefix_teams_per_sm() {
+  static std::atomic<int> cached{-1};
+  int n = cached.load(std::memory_order_relaxed);
+  if (n < 0) {
+    using PC = PreCfg<D>;
+    const size_t smem = (size_t)PC::TPC * 2 * D * D * sizeof(float4);  // <= 32 KB up to D = 32
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chainf_local_mx<D, false>, PC::THREADS, smem) !=
+        cudaSuccess)
+      return 0;
+    n = per_sm * PC::TPC;
+    cached.store(n, std::memory_order_relaxed);
+  }
+  return n;
+}
+long chain_prefix_capacity(int Dp, int num_sms) {
+  switch (Dp) {
+    case 2: return prefix_teams_per_sm<2>() * num_sms;
+    case 4: return prefix_teams_per_sm<4>() * num_sms;
+    case 8: return prefix_teams_per_sm<8>() * num_sms;
+    case 16: return prefix_teams_per_sm<16>() * num_sms;
+    case 32: return prefix_teams_per_sm<32>() * num_sms;
+    default: return 0;
+  }
 }
 
 // In-block suffix products of the parallel-in-time backward chain.  They need

@@ -345,16 +345,20 @@ static Sizes sizes_of(const pgx_problem_desc* d, int Dp, int num_sms) {
 }
 
 // Blocks of the parallel-in-time mixed gate chain: enough (member, block)
-// chains to fill the GPU without a second wave of the prefix kernel (about 4
-// teams of 256 threads per SM from D = 32, 7 of the 12 64-thread teams an SM
-// holds at D = 16, 16 warp-teams at Dp <= 8), blocks of at least 8 slices;
-// 1 = the sequential chain.
+// chains to fill the GPU (about 4 teams of 256 threads per SM from D = 32, 7
+// of the 12 64-thread teams an SM holds at D = 16, 16 warp-teams at
+// Dp <= 8), but never more than the prefix kernel holds at once, and blocks
+// of at least 8 slices; 1 = the sequential chain.
 static void pit_shape(const pgx_problem_desc* d, int Dp, int num_sms, int* blocks, int* len) {
   *blocks = 1;
   *len = d->n_slices;
   if (d->precision != PGX_PREC_MIXED || d->target != PGX_TARGET_GATE) return;
   const long target = (long)(Dp <= 8 ? 16 : Dp == 16 ? 7 : 4) * num_sms;
   long b = (target + d->n_members - 1) / d->n_members;
+  // never more chains than the prefix kernel holds at once: the rest would
+  // run as a second wave of whole chains
+  const long cap = pgx::chain_prefix_capacity(Dp, num_sms);
+  if (cap > 0) b = std::min<long>(b, std::max<long>(1, cap / d->n_members));
   b = std::min<long>(b, std::max(1, d->n_slices / 8));
   if (b <= 1) return;
   const int L = (int)((d->n_slices + b - 1) / b);

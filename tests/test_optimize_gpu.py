@@ -132,3 +132,26 @@ def test_compute_fidelity_and_gradient_api(pg):
     Uo = rs.compute_total_propagator(rs.compute_propagators(
         rs.build_total_hamiltonian(rs.QuantumSystem(H, Hc), rs.ControlSequence.from_controls(u0, 0.05)), 0.05))
     assert np.max(np.abs(pg.propagate(pg.quantum_system(H, Hc), pg.ControlSequence.from_controls(u0, 0.05)) - Uo)) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["convergence", "monotone", "gradient_vanishes", "x_gate", "cnot", "improves",
+                                  "long_pulse"])
+def test_grape_reference_cases_on_device(pg, name, precision):
+    """The runs of the reference's GRAPETests.jl through grape_optimize on the
+    device: each passes the reference test's own assertions, and in FP64
+    follows the oracle's loop (iteration count, F history)."""
+    from test_oracle_kats import _oracle_grape, grape_case_checks, grape_cases
+
+    (H, Hc), (kind, T), u, dt, kw = grape_cases()[name]
+    sys_g = pg.quantum_system(H, Hc)
+    tgt = pg.state_target(T) if kind == "state" else pg.unitary_target(T)
+    cs = pg.ControlSequence.from_controls(u, dt)
+    F0 = pg.compute_fidelity(sys_g, cs, tgt)
+    r = pg.grape_optimize(sys_g, tgt, cs, pg.GRAPEConfig(precision=precision, **kw))
+    grape_case_checks(name, r, F0)
+    if precision == "fp64":
+        ro, Fo0 = _oracle_grape(name)
+        assert abs(F0 - Fo0) < 1e-12
+        assert r.n_iterations == ro.n_iterations
+        _hist_close(r.fidelity_history, ro.fidelity_history, 1e-9)

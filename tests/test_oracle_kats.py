@@ -372,3 +372,80 @@ def test_inept_antiphase_and_grape_improvement():
     F0 = rs.compute_fidelity(sys_, cs, tgt)
     r = rs.grape_optimize(sys_, tgt, cs, rs.GRAPEConfig(max_iter=200))
     assert r.fidelity > F0
+
+
+# --- test/Algorithms/GRAPETests.jl (:20-288) -----------------------------------
+# Resonant qubit with 1 MHz Rabi drives, and a ZZ-coupled qubit pair; the
+# reference's seeds are MersenneTwister streams, these numpy's.  GRAPE_CASES
+# feeds these oracle checks and the device runs in tests/test_optimize_gpu.py:
+# name -> (system, target, u [n_c, n_t], dt, GRAPEConfig keywords).
+
+def grape_qubit():                                             # :20-30
+    return np.zeros((2, 2), complex), [2 * np.pi * 1e6 * SX, 2 * np.pi * 1e6 * SY]
+
+
+def grape_two_qubit():                                         # :35-53
+    ZI, IZ, ZZ = np.kron(SZ, I2), np.kron(I2, SZ), np.kron(SZ, SZ)
+    H = 2 * np.pi * (80e3 * ZI + 60e3 * IZ + 50e3 * ZZ)
+    Hc = [2 * np.pi * 1e6 * np.kron(SX, I2), 2 * np.pi * 1e6 * np.kron(SY, I2),
+          2 * np.pi * 1e6 * np.kron(I2, SX), 2 * np.pi * 1e6 * np.kron(I2, SY)]
+    return H, Hc
+
+
+CNOT = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], complex)
+KET1 = np.array([0, 1], complex)
+
+
+def grape_cases():
+    r = np.random.default_rng
+    return {
+        "convergence": (grape_qubit(), ("state", KET1), 0.1 * r(42).standard_normal((2, 100)), 1e-7,
+                        dict(max_iter=500, convergence_tol=1e-9)),                        # :59-85
+        "monotone": (grape_qubit(), ("state", KET1), 0.05 * r(7).standard_normal((2, 50)), 1e-7,
+                     dict(max_iter=200)),                                                 # :88-113
+        "gradient_vanishes": (grape_qubit(), ("state", KET1), 0.1 * r(11).standard_normal((2, 80)), 1e-7,
+                              dict(max_iter=600, convergence_tol=1e-10)),                 # :116-138
+        "x_gate": (grape_qubit(), ("gate", SX), 0.1 * r(55).standard_normal((2, 100)), 1e-7,
+                   dict(max_iter=600, convergence_tol=1e-9)),                             # :181-195
+        "cnot": (grape_two_qubit(), ("gate", CNOT), 0.02 * r(33).standard_normal((4, 120)), 5e-8,
+                 dict(max_iter=1000, convergence_tol=1e-8)),                              # :198-224
+        "improves": (grape_qubit(), ("state", KET1), 0.001 * r(999).standard_normal((2, 30)), 1e-7,
+                     dict(max_iter=50)),                                                  # :227-243
+        "long_pulse": (grape_qubit(), ("state", KET1), 0.05 * r(123).standard_normal((2, 500)), 2e-8,
+                       dict(max_iter=200)),                                               # :271-290
+    }
+
+
+def grape_case_checks(name, r, F0):
+    """The reference test's assertions on a result r (F0: the start's F)."""
+    hist = np.asarray(r.fidelity_history)
+    if name == "convergence":
+        assert r.fidelity > 0.99 and (r.converged or r.n_iterations == 500)
+        assert np.all(np.diff(hist) >= -1e-8)
+    elif name == "monotone":
+        assert np.all(np.diff(hist) >= -1e-8)
+    elif name == "gradient_vanishes":
+        assert r.gradient_norm_history[-1] < 1e-3
+    elif name == "x_gate":
+        assert r.fidelity > 0.99
+    elif name == "cnot":
+        assert r.fidelity > 0.95
+    elif name == "improves":
+        assert r.fidelity > F0
+    elif name == "long_pulse":
+        assert np.isfinite(r.fidelity) and 0.0 <= r.fidelity <= 1.0 + 1e-10
+
+
+def _oracle_grape(name):
+    (H, Hc), (kind, T), u, dt, kw = grape_cases()[name]
+    sys_ = rs.QuantumSystem(H, Hc)
+    tgt = rs.state_target(T) if kind == "state" else rs.unitary_target(T)
+    cs = rs.ControlSequence(np.ascontiguousarray(u.T), dt)
+    return rs.grape_optimize(sys_, tgt, cs, rs.GRAPEConfig(**kw)), rs.compute_fidelity(sys_, cs, tgt)
+
+
+@pytest.mark.parametrize("name", ["convergence", "monotone", "gradient_vanishes", "x_gate", "cnot", "improves",
+                                  "long_pulse"])
+def test_grape_reference_cases(name):
+    r, F0 = _oracle_grape(name)
+    grape_case_checks(name, r, F0)

@@ -533,7 +533,8 @@ __global__ void __launch_bounds__(Cfg<D>::THREADS) k_chainf_combine_mx(ProbDev p
 // HBM into padded shared memory (each entry is read D times by the product).
 // The products are bound by their shared-memory operand loads, so the teams
 // give each lane 8 outputs (2 x 4 blocks) up to D = 32: at D = 16, T = 32
-// runs the spin-4 evaluation 3 % faster than 2 x 2 blocks at T = 64.
+// runs the spin-4 evaluation 3 % faster than 2 x 2 blocks at T = 64; at
+// D = 32, 16 outputs per lane (T = 64) were 0.5 % slower.
 template <int D> struct FixCfg {
   static constexpr int T = (D <= 16) ? 32 : (D == 32) ? 128 : 256;
   static constexpr int TPC = (T >= 256) ? 1 : 256 / T;
@@ -692,9 +693,10 @@ __device__ __forceinline__ void load_hi(const Team<T>& tm, float2* dst, const fl
 // Teams of the backward chain's in-block suffixes.  They run on a side
 // stream beside the df forward prefixes, so the fewest SMs serve them best:
 // one warp per (member, block) chain at D = 16 (spin-4 evaluation 20.68 ->
-// 20.82 M units/s against T = 256; T = 64 and 128 were slower).
+// 20.82 M units/s against T = 256; T = 64 and 128 were slower).  At D = 32
+// 64-thread teams were 1 % slower than 256 on the largest uneven problems.
 template <int D> struct SufCfg {
-  static constexpr int T = (D == 16) ? 32 : Cfg<D>::T;
+  static constexpr int T = (D == 16) ? 32 : (D == 32) ? 256 : Cfg<D>::T;
   static constexpr int TPC = (D <= 8) ? Cfg<D>::TPC : (T >= 256 ? 1 : 256 / T);
   static constexpr int THREADS = T * TPC;
 };

@@ -328,6 +328,33 @@ __device__ int g_expm_tc_timeout;
 // then imaginary part, column-major) in the unit's U slot, which the expm
 // overwrites with exp(A_k) at the end.  Memory-bound work at full occupancy,
 // kept out of the one-CTA-per-SM tensor-core kernel.
+// FP32 1-norm of the prologue's 64 x 64 df matrix by all 256 threads (x
+// 1.00001, as norm1f): thread t sums rows 16 (t % 4) .. + 15 of column t / 4,
+// the four partial sums of a column meet by two xor shuffles (every lane of
+// the four ends with the same sum), and the largest column comes from warp
+// and block maxima.  red: 8 floats.
+__device__ __forceinline__ float prep_norm1_64(const float4* A, float* red) {
+  using L = Lay<64, kSwzExpm>;
+  const int t = threadIdx.x, c = t >> 2, r0 = (t & 3) * 16;
+  float s = 0.f;
+#pragma unroll 4
+  for (int r = r0; r < r0 + 16; ++r) {
+    const float4 a = A[L::idx(r, c)];
+    s += sqrtf(fmaf(a.x, a.x, a.y * a.y));
+  }
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, o));
+  if ((t & 31) == 0) red[t >> 5] = s;
+  __syncthreads();
+  float best = red[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i) best = fmaxf(best, red[i]);
+  __syncthreads();  // red is the degree choice's scratch next
+  return best * 1.00001f;
+}
+
 __global__ void __launch_bounds__(256) k_expm_prep_oz64(ProbDev p, WorkDev w) {
   using L = Lay<64, kSwzExpm>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -339,7 +366,7 @@ __global__ void __launch_bounds__(256) k_expm_prep_oz64(ProbDev p, WorkDev w) {
     const int m = (int)(it / p.n_t), k = (int)(it % p.n_t);
     build_A_df<64, 256, kSwzExpm>(tm, p, w, m, k, A);
     tm.sync();
-    const float nrm = norm1f<64, 256, kSwzExpm>(tm, A, red);
+    const float nrm = prep_norm1_64(A, red);
     const int pk = choose_expm_df<256>(tm, nrm, 64, false, reinterpret_cast<int*>(red));
     const float sc = ldexpf(1.f, -((pk >> 8) & 63));
     float2* out = reinterpret_cast<float2*>(w.U) + (size_t)it * 8192;
